@@ -1,0 +1,462 @@
+"""Benchmark of the geomjax sampler hot path on one GB300 (or N replicas).
+
+Workload (default, ``--workload logreg``): Bayesian logistic regression,
+X ∈ R^{1000×25} iid N(0,1) float32, β* ~ N(0, I), y ~ Bernoulli(σ(Xβ*)),
+prior N(0, 100·I), RMHMC (implicit midpoint, fixed-point tol 1e-6, at most
+100 iterations) with the Fisher metric XᵀΛX + I/100, 4096 chains, 8 steps of
+0.05 per transition, mixed precision (FP32 state, split-BF16 tcgen05
+contractions, FP64 Cholesky / log det / accept).  Synthetic seeded data;
+the reference publishes no dataset for this path.
+
+A "step" is one transition of every chain.  ``value`` = leapfrog steps/s =
+chains × integration steps × timed transitions / device seconds, with the
+inputs (z, u) already resident; L2 is flushed (256 MB write) between timed
+transitions.  ``e2e`` times the same transitions through the public API
+with host buffers: H2D of z and u from pinned memory, the step, D2H of the
+new positions and accept flags, every transition.
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+reference itself is JAX, which is not installed here, so its float64 NumPy
+restatement (``oracle/``) is timed on a bounded sample of chains.
+
+Multi-GPU: chains are independent, so N ranks run N replicas with their own
+chains (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "min-ESS/s and leapfrog steps/s, batched mixed-precision vs plain FP64 CUDA, 1 GB300"
+
+WORKLOADS = {
+    "logreg": dict(name="logistic_regression_N1000_d25_rmhmc_fisher_4096chains", N=1000, d=25,
+                   C=4096, L=8, h=0.05, sampler="rmhmc"),
+    "monge": dict(name="funnel_D100_lmcmonge_alpha1_8192chains", D=100, C=8192, L=16, h=0.02,
+                  sampler="lmcmonge"),
+}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+                for n, v in zip(names, s[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except Exception:
+                pass
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args, wl):
+    import numpy as np
+    import torch
+
+    import geomjax_gb300 as gj
+    from geomjax_gb300 import _lib as L
+    from geomjax_gb300.data import logreg_data
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    C, Lsteps, h = wl["C"], wl["L"], wl["h"]
+    if wl["sampler"] == "rmhmc":
+        X, y = logreg_data(wl["N"], wl["d"], seed=0)
+        target = gj.logistic_regression(X, y, precision="mixed", device=dev)
+        kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path)
+        d = wl["d"]
+        extra = {}
+        state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
+    else:
+        d = wl["D"]
+        target = gj.funnel(D=d, precision="mixed", device=dev)
+        kern = gj.lmcmonge.build_kernel()
+        extra = dict(alpha2=1.0, inverse_mass=torch.ones(d, device=dev))
+        state = gj.lmcmonge.init(torch.ones(C, d), target)
+    K, W = args.steps, args.warmup
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    Z = torch.randn(K + W, C, d, generator=gen, device=dev, dtype=target.dtype)
+    U = torch.rand(K + W, C, generator=gen, device=dev, dtype=torch.float64)
+    info = kern.new_info(C, d, target, dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    # warm-up
+    for i in range(W):
+        kern.step_inplace(target, state, Z[i], U[i], info, h, Lsteps, **extra)
+    torch.cuda.synchronize()
+    ctx = kern.context(target, C)
+    trace = torch.empty(K, C, d, dtype=target.dtype, device=dev)
+    acc_sum = torch.zeros(C, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    stats = np.zeros(5, dtype=np.int64)
+    import ctypes
+
+    buf = (ctypes.c_int64 * 5)()
+    clocks = ClockSampler(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for i in range(K):
+        flush.zero_()
+        evs[i][0].record(stream)
+        kern.step_inplace(target, state, Z[W + i], U[W + i], info, h, Lsteps, **extra)
+        evs[i][1].record(stream)
+        trace[i].copy_(state.position)
+        acc_sum += info["acceptance_rate"]
+        n = ctx.lib.gj_stats(ctx.h, buf, 5)
+        stats += np.array(buf[:5], dtype=np.int64)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    # dominant-kernel timing: the same transitions with CUDA events around every
+    # GEMM launch (profiling switches the batched path to its host-driven loop)
+    prof = np.zeros(5, dtype=np.int64)
+    if wl["sampler"] == "rmhmc":
+        L.check(ctx.lib.gj_profile(ctx.h, 1))
+        for i in range(min(K, 3)):
+            flush.zero_()
+            kern.step_inplace(target, state, Z[W + i], U[W + i], info, h, Lsteps, **extra)
+            ctx.lib.gj_stats(ctx.h, buf, 5)
+            prof += np.array(buf[:5], dtype=np.int64)
+        L.check(ctx.lib.gj_profile(ctx.h, 0))
+        torch.cuda.synchronize()
+    dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    dev_s = _barrier_max(dev_s, ws)
+    steps_per_s = ws * C * Lsteps * K / dev_s
+    ess = gj.effective_sample_size(trace, chain_axis=1, sample_axis=0)
+    min_ess = float(torch.min(ess).item())
+    # --- e2e through the public API with host buffers
+    Zh = torch.empty(C, d, dtype=target.dtype).pin_memory()
+    Uh = torch.empty(C, dtype=torch.float64).pin_memory()
+    Ph = torch.empty(C, d, dtype=target.dtype).pin_memory()
+    Ah = torch.empty(C, dtype=torch.uint8).pin_memory()
+    g2 = torch.Generator().manual_seed(99 + rank)
+    Zd = torch.empty(C, d, dtype=target.dtype, device=dev)
+    Ud = torch.empty(C, dtype=torch.float64, device=dev)
+    Zh.copy_(torch.randn(C, d, generator=g2).to(target.dtype))
+    Uh.copy_(torch.rand(C, generator=g2, dtype=torch.float64))
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(K, 10))
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        Zd.copy_(Zh, non_blocking=True)
+        Ud.copy_(Uh, non_blocking=True)
+        kern.step_inplace(target, state, Zd, Ud, info, h, Lsteps, **extra)
+        Ph.copy_(state.position, non_blocking=True)
+        Ah.copy_(info["is_accepted"], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = _barrier_max(time.perf_counter() - t0, ws)
+    e2e = ws * C * Lsteps * e2e_steps / e2e_s
+    h2d = Zh.numel() * Zh.element_size() + Uh.numel() * 8
+    d2h = Ph.numel() * Ph.element_size() + Ah.numel()
+    peaks, src = _peaks()
+    roof = None
+    if wl["sampler"] == "rmhmc" and prof[4] > 0:
+        achieved = prof[3] / (prof[4] * 1e-9) / 1e12  # TFLOP/s over the GEMM launches
+        peak = float(peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"]))
+        roof = {"bound": "tensor", "kernel": "gemm_tc_kernel (split-BF16 tcgen05)",
+                "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{src} bf16 sustained",
+                "traffic": None,
+                "gemm_ms_per_transition": round(prof[4] * 1e-6 / min(K, 3), 3),
+                "gemm_launches_per_transition": int(prof[1] // min(K, 3)),
+                "evals_per_transition": round(prof[0] / min(K, 3), 2)}
+    out = {
+        "metric": METRIC, "value": round(steps_per_s, 1), "unit": "leapfrog steps/s",
+        "n_gpus": ws, "steps": K, "warmup": W, "ms_per_step": round(1e3 * dev_s / K, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
+                   "step_size": h, "precision": "mixed", "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "min_ess_per_s": round(ws * min_ess / dev_s, 2), "min_ess": round(min_ess, 2),
+        "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
+        "e2e": {"value": round(e2e, 1), "unit": "leapfrog steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(K * (prof[1] + prof[2]) // max(1, min(K, 3))) if wl["sampler"] == "rmhmc" else K,
+        "roofline": roof, "clocks": clk, "wall_s": round(t_wall, 3),
+    }
+    return out
+
+
+def run_plain_fp64(args, wl):
+    """The plain per-chain FP64 CUDA form of the same workload: one thread
+    per chain, every vector and the metric algebra in float64.  For the
+    dense-Fisher workload it runs on a bounded sample of chains (each chain
+    costs O(N·d²) FP64 per map evaluation)."""
+    import torch
+
+    import geomjax_gb300 as gj
+    from geomjax_gb300.data import logreg_data
+
+    dev = torch.device("cuda", _dist()[2])
+    Lsteps, h = wl["L"], wl["h"]
+    if wl["sampler"] == "rmhmc":
+        C = min(wl["C"], 256)
+        X, y = logreg_data(wl["N"], wl["d"], seed=0)
+        target = gj.logistic_regression(X, y, precision="fp64", device=dev)
+        kern = gj.rmhmc.build_kernel()
+        d = wl["d"]
+        extra = {}
+        state = gj.rmhmc.init(0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(0),
+                                                 dtype=torch.float64), target)
+        K = 2
+    else:
+        C = wl["C"]
+        d = wl["D"]
+        target = gj.funnel(D=d, precision="fp64", device=dev)
+        kern = gj.lmcmonge.build_kernel()
+        extra = dict(alpha2=1.0, inverse_mass=torch.ones(d, dtype=torch.float64, device=dev))
+        state = gj.lmcmonge.init(torch.ones(C, d, dtype=torch.float64), target)
+        K = args.steps
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4321)
+    info = kern.new_info(C, d, target, dev)
+    W = 1 if wl["sampler"] == "rmhmc" else args.warmup
+    for i in range(W):
+        kern.step_inplace(target, state, torch.randn(C, d, generator=gen, device=dev, dtype=torch.float64),
+                          torch.rand(C, generator=gen, device=dev, dtype=torch.float64), info, h, Lsteps,
+                          **extra)
+    trace = torch.empty(K, C, d, dtype=torch.float64, device=dev)
+    Z = torch.randn(K, C, d, generator=gen, device=dev, dtype=torch.float64)
+    U = torch.rand(K, C, generator=gen, device=dev, dtype=torch.float64)
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    torch.cuda.synchronize()
+    for i in range(K):
+        evs[i][0].record(stream)
+        kern.step_inplace(target, state, Z[i], U[i], info, h, Lsteps, **extra)
+        evs[i][1].record(stream)
+        trace[i].copy_(state.position)
+    torch.cuda.synchronize()
+    dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    out = {"value": round(C * Lsteps * K / dev_s, 1), "unit": "leapfrog steps/s", "chains": C,
+           "transitions": K, "ms_per_step": round(1e3 * dev_s / K, 3),
+           "form": "one thread per chain, float64 throughout"}
+    if K >= 4:
+        ess = gj.effective_sample_size(trace, chain_axis=1, sample_axis=0)
+        out["min_ess_per_s"] = round(float(torch.min(ess).item()) / dev_s, 2)
+    return out
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    """The float64 oracle on the host cores, on a bounded sample of chains."""
+    import numpy as np
+
+    from oracle import lmcmonge as O_monge
+    from oracle import rmhmc as O_rm
+    from oracle import targets as OT
+
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    rng = np.random.Generator(np.random.PCG64(0))
+    if wl["sampler"] == "rmhmc":
+        X, y = OT.make_logreg_data(wl["N"], wl["d"], seed=0)
+        ot = OT.LogisticRegression(X, y)
+        d = wl["d"]
+
+        def run(C):
+            q = rng.standard_normal((C, d)) * 0.01
+            s = O_rm.init(ot, q)
+            t = time.perf_counter()
+            O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
+            return time.perf_counter() - t
+    else:
+        d = wl["D"]
+        ot = OT.Funnel(D=d)
+
+        def run(C):
+            s = O_monge.init(ot, np.ones((C, d)))
+            t = time.perf_counter()
+            O_monge.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], np.ones(d),
+                           wl["L"], alpha2=1.0)
+            return time.perf_counter() - t
+    C = 8
+    t = run(C)
+    while t < budget_s / 4 and C < wl["C"]:
+        C = min(wl["C"], C * 4)
+        t = run(C)
+    return {"value": round(C * wl["L"] / t, 2), "unit": "leapfrog steps/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{C} chains x 1 transition x {wl['L']} steps of the same workload, "
+                      f"float64 NumPy oracle ({t:.1f} s)"}
+
+
+def run_reference(args, wl):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return None
+    import numpy as np
+
+    from oracle import lmcmonge as O_monge
+    from oracle import rmhmc as O_rm
+    from oracle import targets as OT
+
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    rng = np.random.Generator(np.random.PCG64(0))
+    if wl["sampler"] == "rmhmc":
+        X, y = OT.make_logreg_data(wl["N"], wl["d"], seed=0)
+        ot = OT.LogisticRegression(X, y)
+        d = wl["d"]
+        C = 16
+        s = O_rm.init(ot, rng.standard_normal((C, d)) * 0.01)
+
+        def step(s):
+            s2, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
+            return s2
+    else:
+        d = wl["D"]
+        ot = OT.Funnel(D=d)
+        C = 256
+        s = O_monge.init(ot, np.ones((C, d)))
+
+        def step(s):
+            s2, _ = O_monge.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"],
+                                   np.ones(d), wl["L"], alpha2=1.0)
+            return s2
+    for _ in range(max(1, min(args.warmup, 2))):
+        s = step(s)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = step(s)
+    dt = time.perf_counter() - t0
+    v = C * wl["L"] * args.steps / dt
+    return {
+        "metric": METRIC, "value": round(v, 2), "unit": "leapfrog steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": wl["name"], "chains_sampled": C, "integration_steps": wl["L"],
+                   "step_size": wl["h"]},
+        "cpu_baseline": {"value": round(v, 2), "unit": "leapfrog steps/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{C} chains per step (JAX reference not installable; float64 "
+                                   f"NumPy restatement in oracle/)"},
+        "e2e": {"value": round(v, 2), "unit": "leapfrog steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="logreg", choices=sorted(WORKLOADS))
+    ap.add_argument("--logreg-path", default="tcgen05", choices=["auto", "simt", "tcgen05", "per_chain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 per-chain arm")
+    ap.add_argument("--chains", type=int, default=None, help="override the chain count (small cases)")
+    args = ap.parse_args()
+    wl = dict(WORKLOADS[args.workload])
+    if args.chains:
+        wl["C"] = args.chains
+        wl["name"] = wl["name"].rsplit("_", 1)[0] + f"_{args.chains}chains"
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        out = run_reference(args, wl)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    out = run_ours(args, wl)
+    if rank == 0:
+        if not args.no_plain:
+            out["plain_fp64"] = run_plain_fp64(args, wl)
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(wl)
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,19 @@
+"""geomjax_gb300 — GB300-native (sm_103a) sampler hot path of geomjax.
+
+RMHMC (implicit midpoint / generalized leapfrog), LMC with a dense metric and
+LMC on a Monge patch, over registered device target families, batched over
+many chains.  The compute path is the CUDA library built by
+``geomjax_gb300.build``; there is no CPU fallback.
+"""
+from .base import (AdaptationAlgorithm, AdaptationResults, Draws, LMCInfo, LMCState, RMHMCInfo,
+                   RMHMCState, SamplingAlgorithm)
+from .diagnostics import effective_sample_size, ess, potential_scale_reduction, rhat
+from .samplers import Kernel, lmc, lmcmonge, rmhmc
+from .targets import funnel, hierarchical_gaussian, logistic_regression
+
+__all__ = [
+    "AdaptationAlgorithm", "AdaptationResults", "Draws", "LMCInfo", "LMCState", "RMHMCInfo",
+    "RMHMCState", "SamplingAlgorithm", "Kernel", "rmhmc", "lmc", "lmcmonge", "funnel",
+    "logistic_regression", "hierarchical_gaussian", "effective_sample_size", "ess",
+    "potential_scale_reduction", "rhat",
+]

@@ -1,0 +1,204 @@
+"""Host-side adaptation loops driving the device kernels.
+
+Restates the reference's Stan-style warm-up:
+* ``dual_averaging`` (``optimizers/dual_averaging.py:53-129``) and its
+  step-size wrapper (``adaptation/step_size.py:65-150``);
+* ``welford_covariance`` (``adaptation/mass_matrix.py:159-260``) and the
+  regularised ``mass_matrix_adaptation`` final step (``:131-154``);
+* ``build_schedule`` (``adaptation/window_adaptation.py:360-450``);
+* ``window_adaptation`` (``window_adaptation.py:245-357``) and
+  ``step_size_adaptation`` (``adaptation/step_size_adaptation.py:100-203``).
+
+Batching: the reference adapts one chain (users vmap it).  Here all chains
+of a context share one step size (the kernels take a scalar step size): the
+dual-averaging statistic is the mean acceptance probability over chains and
+the Welford estimator pools every chain's position.  The reference's
+``window_adaptation`` passes the adapted inverse mass matrix as the 5th
+positional kernel argument (``window_adaptation.py:303-310``), which only
+fits the LMC-Monge kernel (``lmcmonge/lmc.py:156``); for ``rmhmc`` / ``lmc``
+(whose 5th argument is the metric) only the step size is adapted, as
+``step_size_adaptation`` does.
+"""
+from __future__ import annotations
+
+import math
+from typing import NamedTuple
+
+import torch
+
+from .base import AdaptationAlgorithm, AdaptationResults
+from .samplers import lmc, lmcmonge, rmhmc
+
+
+class DualAveragingState(NamedTuple):
+    log_step_size: float
+    log_step_size_avg: float
+    step: int
+    avg_error: float
+    mu: float
+
+
+def dual_averaging_init(initial_step_size: float) -> DualAveragingState:
+    """dual_averaging.py:87-99: μ = log(10·ε₀)."""
+    return DualAveragingState(math.log(initial_step_size), 0.0, 1, 0.0,
+                              math.log(10.0 * initial_step_size))
+
+
+def dual_averaging_update(s: DualAveragingState, gradient: float, t0=10, gamma=0.05,
+                          kappa=0.75) -> DualAveragingState:
+    """dual_averaging.py:101-123 (``gradient`` = target − acceptance)."""
+    reg = s.step + t0
+    eta = s.step ** (-kappa)
+    avg_error = (1.0 - 1.0 / reg) * s.avg_error + gradient / reg
+    log_x = s.mu - (math.sqrt(s.step) / gamma) * avg_error
+    log_x_avg = eta * s.log_step_size + (1.0 - eta) * s.log_step_size_avg
+    return DualAveragingState(log_x, log_x_avg, s.step + 1, avg_error, s.mu)
+
+
+class WelfordState(NamedTuple):
+    mean: torch.Tensor
+    m2: torch.Tensor
+    count: int
+
+
+def welford_init(d, diagonal=True, device="cpu"):
+    z = torch.zeros(d, dtype=torch.float64, device=device)
+    return WelfordState(z, z.clone() if diagonal else torch.zeros(d, d, dtype=torch.float64,
+                                                                  device=device), 0)
+
+
+def welford_update(s: WelfordState, value: torch.Tensor) -> WelfordState:
+    """mass_matrix.py:206-230, one sample per call; a [C, d] batch is folded
+    in row by row (the pooled estimator over chains)."""
+    value = value.double()
+    if value.ndim == 1:
+        value = value[None]
+    mean, m2, n = s.mean, s.m2, s.count
+    for x in value:
+        n += 1
+        delta = x - mean
+        mean = mean + delta / n
+        upd = x - mean
+        m2 = m2 + (delta * upd if m2.ndim == 1 else torch.outer(upd, delta))
+    return WelfordState(mean, m2, n)
+
+
+def welford_covariance(s: WelfordState):
+    """mass_matrix.py:232-260: covariance = m2 / (n − 1)."""
+    return s.m2 / (s.count - 1), s.count, s.mean
+
+
+def regularized_inverse_mass(s: WelfordState):
+    """mass_matrix.py:131-154 (Stan's shrinkage)."""
+    cov, n, mean = welford_covariance(s)
+    scaled = (n / (n + 5.0)) * cov
+    shrink = 1e-3 * (5.0 / (n + 5.0))
+    if scaled.ndim == 1:
+        return scaled + shrink
+    return scaled + shrink * torch.eye(mean.shape[0], dtype=scaled.dtype, device=scaled.device)
+
+
+def build_schedule(num_steps: int, initial_buffer_size=75, final_buffer_size=50,
+                   first_window_size=25):
+    """window_adaptation.py:360-450; list of (stage, is_middle_window_end)."""
+    schedule = []
+    if num_steps < 20:
+        return [(0, False)] * num_steps
+    if initial_buffer_size + first_window_size + final_buffer_size > num_steps:
+        initial_buffer_size = int(0.15 * num_steps)
+        final_buffer_size = int(0.1 * num_steps)
+        first_window_size = num_steps - initial_buffer_size - final_buffer_size
+    schedule += [(0, False)] * (initial_buffer_size - 1)
+    schedule.append((0, False))
+    final_buffer_start = num_steps - final_buffer_size
+    next_size = first_window_size
+    next_start = initial_buffer_size
+    while next_start < final_buffer_start:
+        cur_start, cur_size = next_start, next_size
+        if 3 * cur_size <= final_buffer_start - cur_start:
+            next_size = 2 * cur_size
+        else:
+            cur_size = final_buffer_start - cur_start
+        next_start = cur_start + cur_size
+        schedule += [(1, False)] * (next_start - 1 - cur_start)
+        schedule.append((1, True))
+    schedule += [(0, False)] * (num_steps - 1 - final_buffer_start)
+    schedule.append((0, False))
+    return schedule
+
+
+def _kernel_and_init(algorithm):
+    if algorithm is rmhmc or algorithm is lmc or algorithm is lmcmonge:
+        return algorithm.build_kernel(), algorithm.init
+    raise ValueError("algorithm must be geomjax_gb300.rmhmc, lmc or lmcmonge")
+
+
+def window_adaptation(algorithm, target, is_mass_matrix_diagonal=True, initial_step_size=1.0,
+                      target_acceptance_rate=0.80, progress_bar=False, **extra_parameters):
+    """window_adaptation.py:245-357.  ``extra_parameters``: at least
+    ``num_integration_steps``; ``alpha2`` for lmcmonge."""
+    kernel, init = _kernel_and_init(algorithm)
+    adapt_mass = algorithm is lmcmonge
+    if adapt_mass and not is_mass_matrix_diagonal:
+        raise ValueError("the Monge metric takes a diagonal inverse mass matrix")
+    L = int(extra_parameters.pop("num_integration_steps"))
+
+    def run(rng_key, position, num_steps: int = 1000):
+        gen = rng_key if isinstance(rng_key, torch.Generator) else \
+            torch.Generator(device=target.device).manual_seed(int(rng_key))
+        state = init(position, target)
+        d = target.dim
+        da = dual_averaging_init(initial_step_size)
+        step_size = initial_step_size
+        wf = welford_init(d, True, target.device)
+        inv_mass = torch.ones(d, dtype=target.dtype, device=target.device)
+        infos = []
+        for stage, is_end in build_schedule(num_steps):
+            kw = dict(alpha2=extra_parameters.get("alpha2", 0.001),
+                      inverse_mass_matrix=inv_mass) if adapt_mass else {}
+            state, info = kernel(gen, state, target, step_size, L, **kw)
+            acc = float(info.acceptance_rate.mean().item())
+            infos.append(acc)
+            if stage == 1 and adapt_mass:
+                wf = welford_update(wf, state.position)
+            da = dual_averaging_update(da, target_acceptance_rate - acc)
+            step_size = math.exp(da.log_step_size)
+            if is_end:  # slow_final (window_adaptation.py:174-190)
+                if adapt_mass and wf.count > 1:
+                    inv_mass = regularized_inverse_mass(wf).to(target.dtype)
+                    wf = welford_init(d, True, target.device)
+                da = dual_averaging_init(math.exp(da.log_step_size_avg))
+                step_size = math.exp(da.log_step_size)
+        params = {"step_size": math.exp(da.log_step_size_avg), "num_integration_steps": L,
+                  **extra_parameters}
+        if adapt_mass:
+            params["inverse_mass_matrix"] = inv_mass
+        return AdaptationResults(state, params), infos
+
+    return AdaptationAlgorithm(run)
+
+
+def step_size_adaptation(algorithm, target, initial_step_size=1.0, target_acceptance_rate=0.80,
+                         progress_bar=False, lower_bound=1e-3, **extra_parameters):
+    """adaptation/step_size_adaptation.py:100-203."""
+    kernel, init = _kernel_and_init(algorithm)
+    L = int(extra_parameters.pop("num_integration_steps"))
+
+    def run(rng_key, position, num_steps: int = 1000):
+        gen = rng_key if isinstance(rng_key, torch.Generator) else \
+            torch.Generator(device=target.device).manual_seed(int(rng_key))
+        state = init(position, target)
+        da = dual_averaging_init(initial_step_size)
+        step_size = initial_step_size
+        infos = []
+        for _ in range(num_steps):
+            state, info = kernel(gen, state, target, step_size, L, **extra_parameters)
+            acc = float(info.acceptance_rate.mean().item())
+            infos.append(acc)
+            da = dual_averaging_update(da, target_acceptance_rate - acc)
+            step_size = math.exp(da.log_step_size)
+        params = {"step_size": max(math.exp(da.log_step_size_avg), lower_bound),
+                  "num_integration_steps": L, **extra_parameters}
+        return AdaptationResults(state, params), infos
+
+    return AdaptationAlgorithm(run)

@@ -1,0 +1,362 @@
+// extern "C" boundary (include/geomjax_gb300.h): argument checks, context,
+// dispatch to the per-chain kernels, the warp-per-chain LMC-Monge kernel and
+// the batched dense-Fisher logistic-regression RMHMC pipeline.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "chain_kernels.cuh"
+#include "logreg_batched.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, const char* a = "") {
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), fmt, a);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return GJ_OK;
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  g_last_error = buf;
+  return GJ_ECUDA;
+}
+
+int check_target(const gj_target* t, int precision) {
+  if (!t) return fail(GJ_EINVAL, "target is NULL");
+  if (precision != GJ_FP64 && precision != GJ_MIXED) return fail(GJ_EINVAL, "bad precision");
+  if (t->dim < 1) return fail(GJ_EINVAL, "dim must be >= 1");
+  switch (t->family) {
+    case GJ_FUNNEL:
+      if (t->dim < 2) return fail(GJ_EINVAL, "funnel needs dim >= 2");
+      if (t->metric != GJ_METRIC_DIAG_FISHER && t->metric != GJ_METRIC_PULLBACK &&
+          t->metric != GJ_METRIC_IDENTITY)
+        return fail(GJ_EINVAL, "funnel metric must be diag, pullback or identity");
+      if (!(t->p0 > 0)) return fail(GJ_EINVAL, "funnel sigma must be > 0");
+      break;
+    case GJ_LOGREG:
+      if (t->n_data < 1 || !t->X || !t->y) return fail(GJ_EINVAL, "logreg needs X[N, d] and y[N]");
+      if (t->metric != GJ_METRIC_DENSE_FISHER && t->metric != GJ_METRIC_IDENTITY)
+        return fail(GJ_EINVAL, "logreg metric must be dense Fisher or identity");
+      if (!(t->p0 > 0)) return fail(GJ_EINVAL, "logreg prior variance must be > 0");
+      break;
+    case GJ_HIERGAUSS:
+      if (t->n_data < 1 || t->dim != t->n_data + 2 || !t->y || !t->s)
+        return fail(GJ_EINVAL, "hierarchical Gaussian needs dim = J + 2, y[J], sigma[J]");
+      if (t->metric != GJ_METRIC_DENSE_FISHER && t->metric != GJ_METRIC_IDENTITY)
+        return fail(GJ_EINVAL, "hier metric must be dense Fisher or identity");
+      if (!(t->p0 > 0) || !(t->p1 > 0)) return fail(GJ_EINVAL, "hier scales must be > 0");
+      break;
+    default:
+      return fail(GJ_EINVAL, "unknown target family");
+  }
+  return GJ_OK;
+}
+
+int check_state(const gj_chain_state* s, int C, bool need_vol) {
+  if (!s || !s->position || !s->logdensity_grad || !s->logdensity)
+    return fail(GJ_EINVAL, "chain state has a NULL array");
+  if (s->num_chains != C) return fail(GJ_EINVAL, "state.num_chains differs from the context's");
+  if (need_vol && !s->volume_adjustment)
+    return fail(GJ_EINVAL, "LMC state needs volume_adjustment");
+  return GJ_OK;
+}
+
+int check_params(const gj_step_params* p) {
+  if (!p) return fail(GJ_EINVAL, "params is NULL");
+  if (p->num_integration_steps < 0) return fail(GJ_EINVAL, "num_integration_steps < 0");
+  if (!(p->step_size == p->step_size)) return fail(GJ_EINVAL, "step_size is NaN");
+  if (p->max_iters < 0) return fail(GJ_EINVAL, "max_iters < 0");
+  return GJ_OK;
+}
+
+}  // namespace
+
+struct gj_ctx {
+  gj_target target;
+  int sampler;
+  int precision;
+  int C;
+  int logreg_path;  // GJ_OPT_LOGREG_PATH
+  int tpb;
+  int profile;
+  int loop_mode;  // GJ_OPT_LOOP
+  int chol_fp64;  // GJ_OPT_CHOL_FP64
+  gj::LogregBatched* lb;
+};
+
+extern "C" {
+
+int32_t gj_version(void) { return 100; }
+
+const char* gj_last_error(void) { return g_last_error.c_str(); }
+
+int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
+                  int32_t num_chains, gj_ctx** out) {
+  if (!out) return fail(GJ_EINVAL, "out is NULL");
+  *out = nullptr;
+  int st = check_target(target, precision);
+  if (st) return st;
+  if (sampler < GJ_SAMPLER_RMHMC || sampler > GJ_SAMPLER_LMCMONGE)
+    return fail(GJ_EINVAL, "bad sampler");
+  if (num_chains < 1) return fail(GJ_EINVAL, "num_chains must be >= 1");
+  gj_ctx* c = new (std::nothrow) gj_ctx();
+  if (!c) return fail(GJ_ENOMEM, "host allocation failed");
+  c->target = *target;
+  c->sampler = sampler;
+  c->precision = precision;
+  c->C = num_chains;
+  c->logreg_path = 0;
+  c->tpb = 64;
+  c->profile = 0;
+  c->loop_mode = 0;
+  c->chol_fp64 = 1;
+  c->lb = nullptr;
+  *out = c;
+  return GJ_OK;
+}
+
+int32_t gj_destroy(gj_ctx* ctx) {
+  if (!ctx) return GJ_OK;
+  if (ctx->lb) gj::logreg_batched_destroy(ctx->lb);
+  delete ctx;
+  return GJ_OK;
+}
+
+int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  if (key == GJ_OPT_LOGREG_PATH) {
+    if (value < 0 || value > 3) return fail(GJ_EINVAL, "logreg path must be 0..3");
+    ctx->logreg_path = (int)value;
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_LOOP) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "loop mode must be 0 (graph) or 1 (host)");
+    ctx->loop_mode = (int)value;
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_CHOL_FP64) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "factorisation precision flag must be 0 or 1");
+    ctx->chol_fp64 = (int)value;
+    if (ctx->lb) gj::logreg_batched_set_chol_fp64(ctx->lb, ctx->chol_fp64);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_THREADS_PER_BLOCK) {
+    if (value < 32 || value > 1024 || (value % 32)) return fail(GJ_EINVAL, "bad threads per block");
+    ctx->tpb = (int)value;
+    return GJ_OK;
+  }
+  return fail(GJ_EINVAL, "unknown option");
+}
+
+int32_t gj_init(gj_ctx* ctx, gj_chain_state* s, void* stream) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  int st = check_state(s, ctx->C, false);
+  if (st) return st;
+  const gj::TargetDev t = gj::to_dev(ctx->target);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (ctx->precision == GJ_FP64)
+    e = gj::launch_logdensity_grad<double>(t, (const double*)s->position, s->logdensity,
+                                           (double*)s->logdensity_grad, s->volume_adjustment,
+                                           ctx->C, cs);
+  else
+    e = gj::launch_logdensity_grad<float>(t, (const float*)s->position, s->logdensity,
+                                          (float*)s->logdensity_grad, s->volume_adjustment,
+                                          ctx->C, cs);
+  return cuda_status(e, "gj_init");
+}
+
+int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, const void* z,
+                      const double* u, gj_info* info, void* stream) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  if (ctx->sampler != GJ_SAMPLER_RMHMC) return fail(GJ_EINVAL, "context is not an RMHMC context");
+  int st = check_params(p);
+  if (!st) st = check_state(s, ctx->C, false);
+  if (st) return st;
+  if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
+  if (p->integrator != GJ_IMPLICIT_MIDPOINT && p->integrator != GJ_GENERALIZED_LEAPFROG)
+    return fail(GJ_EINVAL, "bad integrator");
+  const gj::TargetDev t = gj::to_dev(ctx->target);
+  const gj::StepDev sp = gj::to_dev(*p);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  // dense-Fisher logistic regression in mixed precision: batched pipeline
+  if (ctx->precision == GJ_MIXED && t.family == GJ_LOGREG && t.metric == GJ_METRIC_DENSE_FISHER &&
+      ctx->logreg_path != 3) {
+    if (p->integrator != GJ_IMPLICIT_MIDPOINT)
+      return fail(GJ_ENOTSUP, "the batched logistic-regression path implements the implicit midpoint");
+    if (!ctx->lb) {
+      int rc = gj::logreg_batched_create(t, ctx->C, &ctx->lb);
+      if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+      gj::logreg_batched_set_profile(ctx->lb, ctx->profile);
+      gj::logreg_batched_set_chol_fp64(ctx->lb, ctx->chol_fp64);
+    }
+    const int gemm = (ctx->logreg_path == 1) ? 1 : 2;
+    // host-driven loop while profiling (events around each GEMM) or on request
+    const bool graph = ctx->loop_mode == 0 && !ctx->profile;
+    int rc = graph ? gj::logreg_batched_rmhmc_step_graph(ctx->lb, sp, (float*)s->position,
+                                                         (float*)s->logdensity_grad, s->logdensity,
+                                                         (const float*)z, u,
+                                                         gj::to_dev<float>(info), gemm, cs)
+                   : gj::logreg_batched_rmhmc_step(ctx->lb, sp, (float*)s->position,
+                                                   (float*)s->logdensity_grad, s->logdensity,
+                                                   (const float*)z, u, gj::to_dev<float>(info),
+                                                   gemm, cs);
+    if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+    return GJ_OK;
+  }
+  if (t.d > 32) return fail(GJ_ENOTSUP, "per-chain RMHMC supports d <= 32");
+  cudaError_t e;
+  if (ctx->precision == GJ_FP64)
+    e = gj::launch_rmhmc_chain<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
+                                       s->logdensity, (const double*)z, u,
+                                       gj::to_dev<double>(info), ctx->C, ctx->tpb, cs);
+  else
+    e = gj::launch_rmhmc_chain<float>(t, sp, (float*)s->position, (float*)s->logdensity_grad,
+                                      s->logdensity, (const float*)z, u, gj::to_dev<float>(info),
+                                      ctx->C, ctx->tpb, cs);
+  return cuda_status(e, "gj_rmhmc_step");
+}
+
+int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, const void* z,
+                    const double* u, gj_info* info, void* stream) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  if (ctx->sampler != GJ_SAMPLER_LMC) return fail(GJ_EINVAL, "context is not an LMC context");
+  int st = check_params(p);
+  if (!st) st = check_state(s, ctx->C, true);
+  if (st) return st;
+  if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
+  const gj::TargetDev t = gj::to_dev(ctx->target);
+  if (t.d > 32) return fail(GJ_ENOTSUP, "dense LMC supports d <= 32");
+  const gj::StepDev sp = gj::to_dev(*p);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (ctx->precision == GJ_FP64)
+    e = gj::launch_lmc_chain<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
+                                     s->logdensity, s->volume_adjustment, (const double*)z, u,
+                                     gj::to_dev<double>(info), ctx->C, ctx->tpb, cs);
+  else
+    e = gj::launch_lmc_chain<float>(t, sp, (float*)s->position, (float*)s->logdensity_grad,
+                                    s->logdensity, s->volume_adjustment, (const float*)z, u,
+                                    gj::to_dev<float>(info), ctx->C, ctx->tpb, cs);
+  return cuda_status(e, "gj_lmc_step");
+}
+
+int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, const void* z,
+                         const double* u, gj_info* info, void* stream) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  if (ctx->sampler != GJ_SAMPLER_LMCMONGE)
+    return fail(GJ_EINVAL, "context is not an LMC-Monge context");
+  int st = check_params(p);
+  if (!st) st = check_state(s, ctx->C, true);
+  if (st) return st;
+  if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
+  const gj::TargetDev t = gj::to_dev(ctx->target);
+  const gj::StepDev sp = gj::to_dev(*p);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (ctx->precision == GJ_MIXED && gj::monge_warp_supported(t)) {
+    e = gj::launch_monge_warp(t, sp, (float*)s->position, (float*)s->logdensity_grad,
+                              s->logdensity, s->volume_adjustment, (const float*)z, u,
+                              gj::to_dev<float>(info), ctx->C, cs);
+    return cuda_status(e, "gj_lmcmonge_step");
+  }
+  if (t.d > 128) return fail(GJ_ENOTSUP, "per-chain LMC-Monge supports d <= 128");
+  if (ctx->precision == GJ_FP64)
+    e = gj::launch_monge_chain<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
+                                       s->logdensity, s->volume_adjustment, (const double*)z, u,
+                                       gj::to_dev<double>(info), ctx->C, ctx->tpb, cs);
+  else
+    e = gj::launch_monge_chain<float>(t, sp, (float*)s->position, (float*)s->logdensity_grad,
+                                      s->logdensity, s->volume_adjustment, (const float*)z, u,
+                                      gj::to_dev<float>(info), ctx->C, ctx->tpb, cs);
+  return cuda_status(e, "gj_lmcmonge_step");
+}
+
+int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
+  if (!ctx || !out || n < 0) return fail(GJ_EINVAL, "bad arguments");
+  int64_t v[5] = {0, 0, 0, 0, 0};
+  if (ctx->lb) {
+    const gj::LogregStats s = gj::logreg_batched_stats(ctx->lb);
+    v[0] = s.evals;
+    v[1] = s.gemm_launches;
+    v[2] = s.other_launches;
+    v[3] = (int64_t)s.gemm_flops;
+    v[4] = (int64_t)s.gemm_ns;
+  } else {
+    v[2] = 1;  // the per-chain and warp-per-chain paths launch one kernel per step
+  }
+  const int m = n < 5 ? n : 5;
+  for (int i = 0; i < m; ++i) out[i] = v[i];
+  return m;
+}
+
+int32_t gj_profile(gj_ctx* ctx, int32_t on) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  ctx->profile = on ? 1 : 0;
+  if (ctx->lb) gj::logreg_batched_set_profile(ctx->lb, ctx->profile);
+  return GJ_OK;
+}
+
+int32_t gj_gemm_split_bf16(int32_t impl, int32_t planes, int32_t M, int32_t N, int32_t K,
+                           const float* A, const float* B, float* D, void* stream) {
+  if (impl != 1 && impl != 2) return fail(GJ_EINVAL, "impl must be 1 (SIMT) or 2 (tcgen05)");
+  if (planes != 2 && planes != 3) return fail(GJ_EINVAL, "planes must be 2 or 3");
+  int rc = gj::gemm_split_test(impl, planes, M, N, K, A, B, D, static_cast<cudaStream_t>(stream));
+  if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+  return GJ_OK;
+}
+
+int32_t gj_logdensity_grad(const gj_target* target, int32_t precision, int32_t C, const void* q,
+                           double* ld, void* grad, void* stream) {
+  int st = check_target(target, precision);
+  if (st) return st;
+  if (C < 1 || !q || !ld || !grad) return fail(GJ_EINVAL, "bad arrays");
+  const gj::TargetDev t = gj::to_dev(*target);
+  if (t.d > 128) return fail(GJ_ENOTSUP, "operator kernels support d <= 128");
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = precision == GJ_FP64
+                      ? gj::launch_logdensity_grad<double>(t, (const double*)q, ld, (double*)grad,
+                                                           nullptr, C, cs)
+                      : gj::launch_logdensity_grad<float>(t, (const float*)q, ld, (float*)grad,
+                                                          nullptr, C, cs);
+  return cuda_status(e, "gj_logdensity_grad");
+}
+
+int32_t gj_hvp(const gj_target* target, int32_t precision, int32_t C, const void* q,
+               const void* u, void* out, void* stream) {
+  int st = check_target(target, precision);
+  if (st) return st;
+  if (C < 1 || !q || !u || !out) return fail(GJ_EINVAL, "bad arrays");
+  const gj::TargetDev t = gj::to_dev(*target);
+  if (t.d > 128) return fail(GJ_ENOTSUP, "operator kernels support d <= 128");
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = precision == GJ_FP64
+                      ? gj::launch_hvp<double>(t, (const double*)q, (const double*)u,
+                                               (double*)out, C, cs)
+                      : gj::launch_hvp<float>(t, (const float*)q, (const float*)u, (float*)out, C,
+                                              cs);
+  return cuda_status(e, "gj_hvp");
+}
+
+int32_t gj_metric(const gj_target* target, int32_t precision, int32_t C, const void* q,
+                  void* out, void* stream) {
+  int st = check_target(target, precision);
+  if (st) return st;
+  if (C < 1 || !q || !out) return fail(GJ_EINVAL, "bad arrays");
+  const gj::TargetDev t = gj::to_dev(*target);
+  if (t.d > 32) return fail(GJ_ENOTSUP, "metric operator supports d <= 32");
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = precision == GJ_FP64
+                      ? gj::launch_metric<double>(t, (const double*)q, (double*)out, C, cs)
+                      : gj::launch_metric<float>(t, (const float*)q, (float*)out, C, cs);
+  return cuda_status(e, "gj_metric");
+}
+
+}  // extern "C"

@@ -1,0 +1,743 @@
+// Per-chain kernels: one thread owns one chain for a whole transition.
+//
+// This is the "plain per-chain" form of every sampler and target family
+// (precision float64 or mixed), and the path for small-d targets:
+//   rmhmc_chain_kernel    rmhmc/rmhmc.py:131-174 + rmhmc_proposal :376-440,
+//                          integrators rmhmc/integrators.py:53-156 (implicit
+//                          midpoint) or the generalized leapfrog
+//                          (Girolami & Calderhead 2011, eqs. 16-18)
+//   lmc_chain_kernel      lmcmc/lmc.py:135-180, lmcmc/integrators.py:51-144,
+//                          lmcmc/metrics.py:75-219
+//   monge_chain_kernel    lmcmonge/lmc.py:151-236, lmcmonge/integrators.py:52-194,
+//                          lmcmonge/metrics.py:44-284
+//   operator kernels      value_and_grad, hvp, metric
+// Chain state lives in per-thread arrays of compile-time capacity DMAX
+// (registers / local memory); the metric linear algebra is float64.
+#include "chain_kernels.cuh"
+#include "linalg.cuh"
+#include "targets.cuh"
+
+namespace gj {
+
+// ---------------------------------------------------------------------------
+// factored metric at one position
+// ---------------------------------------------------------------------------
+template <int DMAX>
+struct MetricEval {
+  double L[DMAX * DMAX];     // diag: G_i in L[0..d); dense: Cholesky factor
+  double Ginv[DMAX * DMAX];  // diag: 1/G_i; dense: inverse (when requested)
+  double logdet;
+  bool diag;
+};
+
+template <typename T, int DMAX>
+__device__ __noinline__ void eval_metric(const TargetDev& t, const T* q, MetricEval<DMAX>& M, bool want_inv,
+                            bool* bad) {
+  const int d = t.d;
+  M.diag = metric_is_diag(t.metric);
+  metric<T, DMAX>(t, q, M.L);
+  if (M.diag) {
+    double ld = 0.0;
+    for (int i = 0; i < d; ++i) {
+      if (!(M.L[i] > 0.0)) *bad = true;
+      M.Ginv[i] = 1.0 / M.L[i];
+      ld += log(M.L[i]);
+    }
+    M.logdet = ld;
+    return;
+  }
+  M.logdet = chol_inplace(M.L, d, bad);
+  if (want_inv) {
+    double e[DMAX], y[DMAX];
+    chol_inverse(M.L, d, M.Ginv, e, y);
+  }
+}
+
+// u = G^{-1} p
+template <typename T, int DMAX>
+__device__ __noinline__ void metric_solve(const MetricEval<DMAX>& M, int d, const T* p, double* u) {
+  if (M.diag) {
+    for (int i = 0; i < d; ++i) u[i] = M.Ginv[i] * double(p[i]);
+    return;
+  }
+  double b[DMAX], y[DMAX];
+  for (int i = 0; i < d; ++i) b[i] = double(p[i]);
+  chol_fwd(M.L, d, b, y);
+  chol_bwd(M.L, d, y, u);
+}
+
+// K = ½ pᵀG⁻¹p + ½ log det G + d/2 log 2π  (rmhmc/metrics.py:60-74)
+template <typename T, int DMAX>
+__device__ __noinline__ double kinetic_rm(const MetricEval<DMAX>& M, int d, const T* p) {
+  double quad = 0.0;
+  if (M.diag) {
+    for (int i = 0; i < d; ++i) quad += double(p[i]) * double(p[i]) * M.Ginv[i];
+  } else {
+    double b[DMAX], y[DMAX];
+    for (int i = 0; i < d; ++i) b[i] = double(p[i]);
+    chol_fwd(M.L, d, b, y);
+    for (int i = 0; i < d; ++i) quad += y[i] * y[i];
+  }
+  return 0.5 * quad + 0.5 * M.logdet + 0.5 * d * kLog2Pi;
+}
+
+__device__ __forceinline__ bool fp_continue(int n, int max_iters, double norm, double tol) {
+  return (n < max_iters) && isfinite(norm) && (norm < 1e10) && (norm > tol);
+}
+
+// ---------------------------------------------------------------------------
+// RMHMC integrators
+// ---------------------------------------------------------------------------
+// One evaluation of the implicit-midpoint map (rmhmc/integrators.py:119-142):
+// (qo, po) = (qs + h/2 G(qi)⁻¹pi, ps − h/2 [∂_qK(qi, pi) − ∇ℓ(qi)]).
+template <typename T, int DMAX>
+__device__ __noinline__ void im_map(const TargetDev& t, double hh, const T* qi, const T* pi, const T* qs,
+                       const T* ps, T* qo, T* po, MetricEval<DMAX>& M, bool* bad) {
+  const int d = t.d;
+  T gi[DMAX];
+  logdensity_grad<T>(t, qi, gi);
+  eval_metric<T, DMAX>(t, qi, M, true, bad);
+  double u[DMAX], dK[DMAX];
+  metric_solve<T, DMAX>(M, d, pi, u);
+  kinetic_dq<T>(t, qi, M.Ginv, u, dK);
+  for (int i = 0; i < d; ++i) {
+    qo[i] = T(double(qs[i]) + hh * u[i]);
+    po[i] = T(double(ps[i]) - hh * (dK[i] - double(gi[i])));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ double inf_norm2(const T* a, const T* b, const T* c, const T* e, int d) {
+  double m = 0.0;
+  for (int i = 0; i < d; ++i) {
+    m = fmax(m, fabs(double(a[i]) - double(b[i])));
+    m = fmax(m, fabs(double(c[i]) - double(e[i])));
+  }
+  // NaN must survive the max (jnp.max propagates NaN)
+  for (int i = 0; i < d; ++i)
+    if (isnan(double(a[i]) - double(b[i])) || isnan(double(c[i]) - double(e[i]))) return NAN;
+  return m;
+}
+
+template <typename T>
+__device__ __forceinline__ double inf_norm1(const T* a, const T* b, int d) {
+  double m = 0.0;
+  bool nan = false;
+  for (int i = 0; i < d; ++i) {
+    const double x = double(a[i]) - double(b[i]);
+    nan |= isnan(x);
+    m = fmax(m, fabs(x));
+  }
+  return nan ? NAN : m;
+}
+
+// implicit_midpoint.one_step (rmhmc/integrators.py:116-154): q, p in/out,
+// g, ld out.  Returns the fixed-point iteration count; *conv = success.
+template <typename T, int DMAX>
+__device__ __noinline__ int im_step(const TargetDev& t, const StepDev& sp, T* q, T* p, T* g, double* ld,
+                       MetricEval<DMAX>& M, bool* conv, bool* bad) {
+  const int d = t.d;
+  const double hh = 0.5 * sp.h;
+  T q0[DMAX], p0[DMAX], qc[DMAX], pc[DMAX], qn[DMAX], pn[DMAX];
+  for (int i = 0; i < d; ++i) {
+    q0[i] = q[i];
+    p0[i] = p[i];
+  }
+  im_map<T, DMAX>(t, hh, q0, p0, q0, p0, qn, pn, M, bad);  // eager first eval (:84)
+  double nrm = inf_norm2(qn, q0, pn, p0, d);
+  int it = 0;
+  while (fp_continue(it, sp.max_iters, nrm, sp.tol)) {
+    for (int i = 0; i < d; ++i) {
+      qc[i] = qn[i];
+      pc[i] = pn[i];
+    }
+    im_map<T, DMAX>(t, hh, qc, pc, q0, p0, qn, pn, M, bad);
+    nrm = inf_norm2(qn, qc, pn, pc, d);
+    ++it;
+  }
+  *conv = isfinite(nrm) && nrm <= sp.tol;
+  im_map<T, DMAX>(t, hh, qn, pn, qn, pn, q, p, M, bad);  // explicit half step (:147-148)
+  *ld = logdensity_grad<T>(t, q, g);
+  return it;
+}
+
+// Generalized leapfrog: q, p, g (gradient at q on entry) in/out, ld out.
+template <typename T, int DMAX>
+__device__ __noinline__ int gl_step(const TargetDev& t, const StepDev& sp, T* q, T* p, T* g, double* ld,
+                       MetricEval<DMAX>& M, bool* conv, bool* bad) {
+  const int d = t.d;
+  const double hh = 0.5 * sp.h;
+  T p0[DMAX], q0[DMAX], xc[DMAX], xn[DMAX];
+  double u[DMAX], dK[DMAX], u0[DMAX];
+  for (int i = 0; i < d; ++i) {
+    p0[i] = p[i];
+    q0[i] = q[i];
+  }
+  // (1) p½ = p − h/2 ∂_qH(q, p½): the metric at q is fixed during this solve
+  eval_metric<T, DMAX>(t, q0, M, true, bad);
+  auto pmap = [&](const T* pi, T* po) {
+    metric_solve<T, DMAX>(M, d, pi, u);
+    kinetic_dq<T>(t, q0, M.Ginv, u, dK);
+    for (int i = 0; i < d; ++i) po[i] = T(double(p0[i]) - hh * (dK[i] - double(g[i])));
+  };
+  pmap(p0, xn);
+  double nrm = inf_norm1(xn, p0, d);
+  int it = 0, it_total = 0;
+  while (fp_continue(it, sp.max_iters, nrm, sp.tol)) {
+    for (int i = 0; i < d; ++i) xc[i] = xn[i];
+    pmap(xc, xn);
+    nrm = inf_norm1(xn, xc, d);
+    ++it;
+  }
+  bool ok = isfinite(nrm) && nrm <= sp.tol;
+  it_total += it;
+  for (int i = 0; i < d; ++i) p[i] = xn[i];  // p½
+  metric_solve<T, DMAX>(M, d, p, u0);
+  // (2) q' = q + h/2 [G⁻¹(q) + G⁻¹(q')] p½
+  auto qmap = [&](const T* qi, T* qo) {
+    eval_metric<T, DMAX>(t, qi, M, false, bad);
+    metric_solve<T, DMAX>(M, d, p, u);
+    for (int i = 0; i < d; ++i) qo[i] = T(double(q0[i]) + hh * (u0[i] + u[i]));
+  };
+  qmap(q0, xn);
+  nrm = inf_norm1(xn, q0, d);
+  it = 0;
+  while (fp_continue(it, sp.max_iters, nrm, sp.tol)) {
+    for (int i = 0; i < d; ++i) xc[i] = xn[i];
+    qmap(xc, xn);
+    nrm = inf_norm1(xn, xc, d);
+    ++it;
+  }
+  ok = ok && isfinite(nrm) && nrm <= sp.tol;
+  it_total += it;
+  for (int i = 0; i < d; ++i) q[i] = xn[i];
+  // (3) p' = p½ − h/2 ∂_qH(q', p½)
+  *ld = logdensity_grad<T>(t, q, g);
+  eval_metric<T, DMAX>(t, q, M, true, bad);
+  metric_solve<T, DMAX>(M, d, p, u);
+  kinetic_dq<T>(t, q, M.Ginv, u, dK);
+  for (int i = 0; i < d; ++i) p[i] = T(double(p[i]) - hh * (dK[i] - double(g[i])));
+  *conv = ok;
+  return it_total;
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) rmhmc_chain_kernel(TargetDev t, StepDev sp, T* pos, T* grad,
+                                                          double* logdens, const T* z,
+                                                          const double* uacc, InfoDev<T> info,
+                                                          int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  T q[DMAX], p[DMAX], g[DMAX];
+  for (int i = 0; i < d; ++i) {
+    q[i] = pos[(size_t)c * d + i];
+    g[i] = grad[(size_t)c * d + i];
+  }
+  const double ld0 = logdens[c];
+  bool bad = false;
+  MetricEval<DMAX> M;
+  // momentum p = chol(G)·z or sqrt(G)⊙z (rmhmc/metrics.py:45-58, util.py:83)
+  eval_metric<T, DMAX>(t, q, M, false, &bad);
+  for (int i = 0; i < d; ++i) {
+    if (M.diag) {
+      p[i] = T(sqrt(M.L[i]) * double(z[(size_t)c * d + i]));
+    } else {
+      double s = 0.0;
+      for (int k = 0; k <= i; ++k) s += M.L[i * d + k] * double(z[(size_t)c * d + k]);
+      p[i] = T(s);
+    }
+    if (info.momentum) info.momentum[(size_t)c * d + i] = p[i];
+  }
+  const double H0 = -ld0 + kinetic_rm<T, DMAX>(M, d, p);  // hmc_energy (mcmc/metrics.py:160-166)
+  double ld = ld0;
+  int iters = 0;
+  bool all_conv = true;
+  for (int s = 0; s < sp.L; ++s) {  // static_integration (mcmc/trajectory.py:121-139)
+    bool conv = true;
+    if (sp.integrator == GJ_GENERALIZED_LEAPFROG)
+      iters += gl_step<T, DMAX>(t, sp, q, p, g, &ld, M, &conv, &bad);
+    else
+      iters += im_step<T, DMAX>(t, sp, q, p, g, &ld, M, &conv, &bad);
+    all_conv &= conv;
+  }
+  // flip_momentum (rmhmc.py:443-462) does not change K; H1 at the proposal
+  eval_metric<T, DMAX>(t, q, M, false, &bad);
+  const double H1 = -ld + kinetic_rm<T, DMAX>(M, d, p);
+  const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
+  if (a.accept) {
+    for (int i = 0; i < d; ++i) {
+      pos[(size_t)c * d + i] = q[i];
+      grad[(size_t)c * d + i] = g[i];
+    }
+    logdens[c] = ld;
+  }
+  if (info.acc_rate) info.acc_rate[c] = a.p_acc;
+  if (info.accepted) info.accepted[c] = a.accept;
+  if (info.divergent) info.divergent[c] = a.divergent;
+  if (info.energy) info.energy[c] = H1;
+  if (info.fp_iters) info.fp_iters[c] = iters;
+  if (info.status)
+    info.status[c] = (all_conv ? 0u : GJ_CHAIN_FP_NOT_CONVERGED) |
+                     (isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// dense-metric LMC (lmcmc/*)
+// ---------------------------------------------------------------------------
+// Ω̃(q, v, h) = G + h/2·½(P1 + P2 − P3) (lmcmc/metrics.py:158-179) written
+// into Om; also returns ∇ log det G (lmcmc/metrics.py:181-189) when gld != 0.
+template <typename T, int DMAX>
+__device__ __noinline__ void omega_tilde(const TargetDev& t, const T* q, const double* v, double h,
+                            const double* G, const double* Ginv, bool diag, double* Om,
+                            double* gld) {
+  const int d = t.d;
+  const double c = 0.25 * h;
+  double dG[DMAX * DMAX];
+  for (int i = 0; i < d * d; ++i) Om[i] = 0.0;
+  if (diag) {
+    for (int a = 0; a < d; ++a) Om[a * d + a] = G[a];
+    for (int k = 0; k < d; ++k) {
+      metric_deriv<T>(t, q, k, dG);  // dG[a] = ∂G_a/∂q_k
+      double tr = 0.0;
+      for (int a = 0; a < d; ++a) {
+        Om[a * d + a] += c * dG[a] * v[k];  // P1 = diag(Σ_k ∂_kG_a v_k)
+        Om[a * d + k] += c * dG[a] * v[a];  // P2[a][k] = ∂_kG_a v_a
+        Om[k * d + a] -= c * dG[a] * v[a];  // −P2ᵀ
+        tr += Ginv[a] * dG[a];
+      }
+      if (gld) gld[k] = tr;
+    }
+    return;
+  }
+  for (int i = 0; i < d * d; ++i) Om[i] = G[i];
+  for (int k = 0; k < d; ++k) {
+    metric_deriv<T>(t, q, k, dG);  // dG[a*d+b] = ∂G_ab/∂q_k
+    double tr = 0.0;
+    for (int a = 0; a < d; ++a)
+      for (int b = 0; b < d; ++b) tr += Ginv[a * d + b] * dG[b * d + a];
+    if (gld) gld[k] = tr;
+    for (int l = 0; l < d; ++l) {
+      double s2 = 0.0;
+      for (int i = 0; i < d; ++i) s2 += v[i] * dG[i * d + l];
+      Om[l * d + k] += c * s2;  // P2[l][k] = Σ_i v_i ∂_kG_il
+      for (int j = 0; j < d; ++j) Om[l * d + j] += c * v[k] * dG[j * d + l];  // P1
+    }
+    for (int j = 0; j < d; ++j) {
+      double s3 = 0.0;
+      for (int i = 0; i < d; ++i) s3 += v[i] * dG[i * d + j];
+      Om[k * d + j] -= c * s3;  // P3[k][j] = Σ_i v_i ∂_kG_ij
+    }
+  }
+}
+
+template <int DMAX>
+struct LmcWork {
+  double G[DMAX * DMAX];
+  double Ginv[DMAX * DMAX];
+  double Om[DMAX * DMAX];
+};
+
+// G (symmetrised), its inverse and log det at q
+template <typename T, int DMAX>
+__device__ __noinline__ double lmc_metric(const TargetDev& t, const T* q, LmcWork<DMAX>& W, bool diag,
+                             bool* bad) {
+  const int d = t.d;
+  metric<T, DMAX>(t, q, W.G);
+  if (diag) {
+    double ld = 0.0;
+    for (int i = 0; i < d; ++i) {
+      if (!(W.G[i] > 0.0)) *bad = true;
+      W.Ginv[i] = 1.0 / W.G[i];
+      ld += log(W.G[i]);
+    }
+    return ld;
+  }
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < i; ++j) {
+      const double s = 0.5 * (W.G[i * d + j] + W.G[j * d + i]);
+      W.G[i * d + j] = s;
+      W.G[j * d + i] = s;
+    }
+  for (int i = 0; i < d * d; ++i) W.Om[i] = W.G[i];
+  const double ld = chol_inplace(W.Om, d, bad);
+  double e[DMAX], y[DMAX];
+  chol_inverse(W.Om, d, W.Ginv, e, y);
+  return ld;
+}
+
+// half_step_fn (lmcmc/integrators.py:61-91); v in/out (double), J in/out.
+template <typename T, int DMAX>
+__device__ __noinline__ void lmc_half_step(const TargetDev& t, const T* q, double* v, double* J, const T* g,
+                              double h, LmcWork<DMAX>& W, bool diag, bool* bad) {
+  const int d = t.d;
+  int piv[DMAX];
+  double gld[DMAX], vt[DMAX];
+  lmc_metric<T, DMAX>(t, q, W, diag, bad);
+  omega_tilde<T, DMAX>(t, q, v, h, W.G, W.Ginv, diag, W.Om, gld);
+  *J -= lu_inplace(W.Om, piv, d);
+  for (int i = 0; i < d; ++i) {
+    double gv = 0.0;
+    if (diag) {
+      gv = W.G[i] * v[i];
+    } else {
+      for (int j = 0; j < d; ++j) gv += W.G[i * d + j] * v[j];
+    }
+    const double dphi = -double(g[i]) + 0.5 * gld[i];
+    vt[i] = gv - 0.5 * h * dphi;
+  }
+  lu_solve(W.Om, piv, d, vt);
+  for (int i = 0; i < d; ++i) v[i] = vt[i];
+  omega_tilde<T, DMAX>(t, q, v, -h, W.G, W.Ginv, diag, W.Om, nullptr);
+  *J += lu_inplace(W.Om, piv, d);
+}
+
+// K = −½ log det G + ½ vᵀGv (lmcmc/metrics.py:93-112)
+template <int DMAX>
+__device__ double lmc_kinetic(const LmcWork<DMAX>& W, int d, double logdet, const double* v,
+                              bool diag) {
+  double quad = 0.0;
+  for (int i = 0; i < d; ++i) {
+    if (diag) {
+      quad += W.G[i] * v[i] * v[i];
+    } else {
+      double s = 0.0;
+      for (int j = 0; j < d; ++j) s += W.G[i * d + j] * v[j];
+      quad += v[i] * s;
+    }
+  }
+  return -0.5 * logdet + 0.5 * quad;
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) lmc_chain_kernel(TargetDev t, StepDev sp, T* pos, T* grad,
+                                                        double* logdens, double* vol,
+                                                        const T* z, const double* uacc,
+                                                        InfoDev<T> info, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  const bool diag = metric_is_diag(t.metric);
+  T q[DMAX], g[DMAX];
+  double v[DMAX];
+  for (int i = 0; i < d; ++i) {
+    q[i] = pos[(size_t)c * d + i];
+    g[i] = grad[(size_t)c * d + i];
+  }
+  const double ld0 = logdens[c];
+  const double J0 = vol[c];
+  bool bad = false;
+  LmcWork<DMAX> W;
+  // velocity v = L^{-T} z (lmcmc/metrics.py:75-91)
+  double logdet = lmc_metric<T, DMAX>(t, q, W, diag, &bad);
+  if (diag) {
+    for (int i = 0; i < d; ++i) v[i] = double(z[(size_t)c * d + i]) / sqrt(W.G[i]);
+  } else {
+    double zz[DMAX];
+    for (int i = 0; i < d; ++i) zz[i] = double(z[(size_t)c * d + i]);
+    chol_bwd(W.Om, d, zz, v);  // W.Om holds the Cholesky factor after lmc_metric
+  }
+  for (int i = 0; i < d; ++i)
+    if (info.momentum) info.momentum[(size_t)c * d + i] = T(v[i]);
+  const double H0 = -ld0 + lmc_kinetic<DMAX>(W, d, logdet, v, diag) - J0;  // lmc_energy
+  double ld = ld0, J = J0;
+  for (int s = 0; s < sp.L; ++s) {  // lan_integrator.one_step (lmcmc/integrators.py:93-144)
+    lmc_half_step<T, DMAX>(t, q, v, &J, g, sp.h, W, diag, &bad);
+    for (int i = 0; i < d; ++i) q[i] = T(double(q[i]) + sp.h * v[i]);
+    ld = logdensity_grad<T>(t, q, g);
+    lmc_half_step<T, DMAX>(t, q, v, &J, g, sp.h, W, diag, &bad);
+  }
+  logdet = lmc_metric<T, DMAX>(t, q, W, diag, &bad);
+  const double H1 = -ld + lmc_kinetic<DMAX>(W, d, logdet, v, diag) - J;
+  const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
+  if (a.accept) {
+    for (int i = 0; i < d; ++i) {
+      pos[(size_t)c * d + i] = q[i];
+      grad[(size_t)c * d + i] = g[i];
+    }
+    logdens[c] = ld;
+    vol[c] = J;
+  }
+  if (info.acc_rate) info.acc_rate[c] = a.p_acc;
+  if (info.accepted) info.accepted[c] = a.accept;
+  if (info.divergent) info.divergent[c] = a.divergent;
+  if (info.energy) info.energy[c] = H1;
+  if (info.fp_iters) info.fp_iters[c] = 0;
+  if (info.status)
+    info.status[c] = (isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// LMC on a Monge patch, one thread per chain (lmcmonge/*)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ double dotd(const T* a, const T* b, int d) {
+  double s = 0.0;
+  for (int i = 0; i < d; ++i) s += double(a[i]) * double(b[i]);
+  return s;
+}
+
+// half_step_omega (lmcmonge/integrators.py:158-194)
+template <typename T, int DMAX>
+__device__ __noinline__ void monge_half(double a2, T* v, double* J, const T* dl, const T* Hv, double L,
+                           const T* dl_ig, const T* Hdl_ig, const T* ig_Hdl_ig, double eps,
+                           int fix, int d) {
+  const double det1 = 1.0 + 0.5 * eps * a2 * dotd(Hv, dl_ig, d);
+  *J -= log(fabs(det1));
+  const double sL = sqrt(L);
+  double dphi_dl = 0.0;
+  for (int i = 0; i < d; ++i) dphi_dl += (-double(dl[i]) + a2 * double(Hdl_ig[i]) / sL) * double(dl_ig[i]);
+  T vt[DMAX];
+  for (int i = 0; i < d; ++i) {
+    const double dphi_ig = -double(dl_ig[i]) + a2 * double(ig_Hdl_ig[i]) / sL;
+    vt[i] = T(double(v[i]) - 0.5 * eps * sL * (dphi_ig - a2 * dphi_dl * double(dl_ig[i])));
+  }
+  double corr = 0.5 * eps * dotd(vt, Hv, d) / det1;
+  if (fix) corr *= a2;
+  for (int i = 0; i < d; ++i) v[i] = T(double(vt[i]) - corr * double(dl_ig[i]));
+  *J += log(fabs(1.0 - 0.5 * eps * a2 * dotd(Hdl_ig, v, d)));
+}
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) monge_chain_kernel(TargetDev t, StepDev sp, T* pos, T* grad,
+                                                          double* logdens, double* vol,
+                                                          const T* z, const double* uacc,
+                                                          InfoDev<T> info, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  const double a2 = sp.alpha2;
+  const T* imv = static_cast<const T*>(sp.inv_mass);
+  T q[DMAX], g[DMAX], v[DMAX], gn[DMAX], dl_ig[DMAX], Hdl[DMAX], igH[DMAX], hv[DMAX], im[DMAX];
+  double slm = 0.0;  // Σ log M
+  for (int i = 0; i < d; ++i) {
+    q[i] = pos[(size_t)c * d + i];
+    g[i] = grad[(size_t)c * d + i];
+    im[i] = imv ? imv[i] : T(1);
+    slm += -log(double(im[i]));
+  }
+  const double ld0 = logdens[c];
+  const double J0 = vol[c];
+  // setup (lmcmonge/lmc.py:177-208)
+  double L = 0.0;
+  for (int i = 0; i < d; ++i) L += double(im[i]) * double(g[i]) * double(g[i]);
+  L = 1.0 + a2 * L;
+  double sL = sqrt(L);
+  for (int i = 0; i < d; ++i) {
+    gn[i] = T(double(g[i]) / sL);
+    dl_ig[i] = im[i] * gn[i];
+  }
+  hvp<T>(t, q, dl_ig, Hdl);
+  for (int i = 0; i < d; ++i) {
+    Hdl[i] = T(double(Hdl[i]) / sL);
+    igH[i] = im[i] * Hdl[i];
+  }
+  // velocity: closed-form factor of diag(M⁻¹) − α² w wᵀ (lmcmonge/metrics.py:155-166)
+  {
+    double suf = 0.0;
+    double tau_next[DMAX];
+    for (int i = d - 1; i >= 0; --i) {
+      const double ui = double(dl_ig[i]) / sqrt(double(im[i]));
+      suf += ui * ui;
+      tau_next[i] = 1.0 / L + a2 * suf - a2 * ui * ui;  // τ_{i+1}
+    }
+    double pre = 0.0;
+    for (int i = 0; i < d; ++i) {
+      const double ui = double(dl_ig[i]) / sqrt(double(im[i]));
+      const double tn = tau_next[i];
+      const double ta = tn + a2 * ui * ui;  // τ_i
+      const double zi = double(z[(size_t)c * d + i]);
+      const double y = sqrt(tn / ta) * zi - a2 * ui * pre;
+      pre += ui * zi / sqrt(ta * tn);
+      v[i] = T(sqrt(double(im[i])) * y);
+      if (info.momentum) info.momentum[(size_t)c * d + i] = v[i];
+    }
+  }
+  hvp<T>(t, q, v, hv);
+  for (int i = 0; i < d; ++i) hv[i] = T(double(hv[i]) / sL);
+  // K (lmcmonge/metrics.py:168-186) and H0 = −ℓ + K − J
+  auto kinetic = [&](double Lc) {
+    double vmv = 0.0;
+    for (int i = 0; i < d; ++i) vmv += double(v[i]) * double(v[i]) / double(im[i]);
+    const double vg = dotd(v, gn, d);
+    return -0.5 * (log(Lc) + slm) + 0.5 * vmv + 0.5 * Lc * a2 * vg * vg;
+  };
+  const double H0 = -ld0 + kinetic(L) - J0;
+  double ld = ld0, J = J0;
+  for (int s = 0; s < sp.L; ++s) {  // lan_integrator.one_step (integrators.py:63-155)
+    monge_half<T, DMAX>(a2, v, &J, gn, hv, L, dl_ig, Hdl, igH, sp.h, sp.alpha2_fix, d);
+    for (int i = 0; i < d; ++i) q[i] = T(double(q[i]) + sp.h * double(v[i]));
+    ld = logdensity_grad<T>(t, q, g);
+    L = 0.0;
+    for (int i = 0; i < d; ++i) L += double(im[i]) * double(g[i]) * double(g[i]);
+    L = 1.0 + a2 * L;
+    sL = sqrt(L);
+    for (int i = 0; i < d; ++i) gn[i] = T(double(g[i]) / sL);
+    hvp<T>(t, q, v, hv);
+    for (int i = 0; i < d; ++i) {
+      hv[i] = T(double(hv[i]) / sL);
+      dl_ig[i] = im[i] * gn[i];
+    }
+    hvp<T>(t, q, dl_ig, Hdl);
+    for (int i = 0; i < d; ++i) {
+      Hdl[i] = T(double(Hdl[i]) / sL);
+      igH[i] = im[i] * Hdl[i];
+    }
+    monge_half<T, DMAX>(a2, v, &J, gn, hv, L, dl_ig, Hdl, igH, sp.h, sp.alpha2_fix, d);
+    hvp<T>(t, q, v, hv);
+    for (int i = 0; i < d; ++i) hv[i] = T(double(hv[i]) / sL);
+  }
+  const double H1 = -ld + kinetic(L) - J;  // flip_velocity leaves K unchanged
+  const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
+  if (a.accept) {
+    for (int i = 0; i < d; ++i) {
+      pos[(size_t)c * d + i] = q[i];
+      grad[(size_t)c * d + i] = T(double(gn[i]) * sL);  // lmc.py:231
+    }
+    logdens[c] = ld;
+    vol[c] = J;
+  }
+  if (info.acc_rate) info.acc_rate[c] = a.p_acc;
+  if (info.accepted) info.accepted[c] = a.accept;
+  if (info.divergent) info.divergent[c] = a.divergent;
+  if (info.energy) info.energy[c] = H1;
+  if (info.fp_iters) info.fp_iters[c] = 0;
+  if (info.status) info.status[c] = isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE;
+}
+
+// ---------------------------------------------------------------------------
+// operator kernels
+// ---------------------------------------------------------------------------
+template <typename T, int DMAX>
+__global__ void logdensity_grad_kernel(TargetDev t, const T* q, double* ld, T* g, double* vol,
+                                       int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  T qq[DMAX], gg[DMAX];
+  for (int i = 0; i < d; ++i) qq[i] = q[(size_t)c * d + i];
+  const double l = logdensity_grad<T>(t, qq, gg);
+  ld[c] = l;
+  for (int i = 0; i < d; ++i) g[(size_t)c * d + i] = gg[i];
+  if (vol) vol[c] = 0.0;
+}
+
+template <typename T, int DMAX>
+__global__ void hvp_kernel(TargetDev t, const T* q, const T* u, T* out, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  T qq[DMAX], uu[DMAX], oo[DMAX];
+  for (int i = 0; i < d; ++i) {
+    qq[i] = q[(size_t)c * d + i];
+    uu[i] = u[(size_t)c * d + i];
+  }
+  hvp<T>(t, qq, uu, oo);
+  for (int i = 0; i < d; ++i) out[(size_t)c * d + i] = oo[i];
+}
+
+template <typename T, int DMAX>
+__global__ void metric_kernel(TargetDev t, const T* q, T* out, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  T qq[DMAX];
+  double G[DMAX * DMAX];
+  for (int i = 0; i < d; ++i) qq[i] = q[(size_t)c * d + i];
+  metric<T, DMAX>(t, qq, G);
+  const int n = metric_is_diag(t.metric) ? d : d * d;
+  for (int i = 0; i < n; ++i) out[(size_t)c * n + i] = T(G[i]);
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+static inline dim3 grid_for(int C, int tpb) { return dim3((C + tpb - 1) / tpb); }
+
+#define GJ_DISPATCH_DMAX(d, MAXD, ...)                  \
+  if ((d) <= 8) {                                        \
+    constexpr int DM = 8;                                \
+    __VA_ARGS__;                                         \
+  } else if ((d) <= 32) {                                \
+    constexpr int DM = 32;                               \
+    __VA_ARGS__;                                         \
+  } else if ((MAXD) >= 128 && (d) <= 128) {              \
+    constexpr int DM = ((MAXD) >= 128 ? 128 : 32);       \
+    __VA_ARGS__;                                         \
+  } else {                                               \
+    return cudaErrorInvalidValue;                        \
+  }
+
+template <typename T>
+cudaError_t launch_rmhmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                               const T* z, const double* u, const InfoDev<T>& info, int C, int tpb,
+                               cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 32, rmhmc_chain_kernel<T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+                                t, sp, pos, grad, ld, z, u, info, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_lmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                             double* vol, const T* z, const double* u, const InfoDev<T>& info,
+                             int C, int tpb, cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 32, lmc_chain_kernel<T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+                                t, sp, pos, grad, ld, vol, z, u, info, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_monge_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                               double* vol, const T* z, const double* u, const InfoDev<T>& info,
+                               int C, int tpb, cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 128, monge_chain_kernel<T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+                                 t, sp, pos, grad, ld, vol, z, u, info, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_logdensity_grad(const TargetDev& t, const T* q, double* ld, T* g, double* vol,
+                                   int C, cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 128, logdensity_grad_kernel<T, DM><<<grid_for(C, 128), 128, 0, st>>>(
+                                 t, q, ld, g, vol, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_hvp(const TargetDev& t, const T* q, const T* u, T* out, int C, cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 128, hvp_kernel<T, DM><<<grid_for(C, 128), 128, 0, st>>>(t, q, u, out, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_metric(const TargetDev& t, const T* q, T* out, int C, cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 32, metric_kernel<T, DM><<<grid_for(C, 128), 128, 0, st>>>(t, q, out, C));
+  return cudaGetLastError();
+}
+
+#define GJ_INST(T)                                                                               \
+  template cudaError_t launch_rmhmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,  \
+                                             const T*, const double*, const InfoDev<T>&, int,   \
+                                             int, cudaStream_t);                                 \
+  template cudaError_t launch_lmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,    \
+                                           double*, const T*, const double*, const InfoDev<T>&, \
+                                           int, int, cudaStream_t);                              \
+  template cudaError_t launch_monge_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,  \
+                                             double*, const T*, const double*,                  \
+                                             const InfoDev<T>&, int, int, cudaStream_t);         \
+  template cudaError_t launch_logdensity_grad<T>(const TargetDev&, const T*, double*, T*,        \
+                                                 double*, int, cudaStream_t);                    \
+  template cudaError_t launch_hvp<T>(const TargetDev&, const T*, const T*, T*, int,              \
+                                     cudaStream_t);                                              \
+  template cudaError_t launch_metric<T>(const TargetDev&, const T*, T*, int, cudaStream_t);
+
+// compiled once per precision (GJ_CHAIN_PREC = 1: float, 2: double) so the
+// two halves build in parallel
+#if !defined(GJ_CHAIN_PREC) || GJ_CHAIN_PREC == 1
+GJ_INST(float)
+#endif
+#if !defined(GJ_CHAIN_PREC) || GJ_CHAIN_PREC == 2
+GJ_INST(double)
+#endif
+
+}  // namespace gj

@@ -1,0 +1,34 @@
+// Host launchers of the per-chain kernels (chain_kernels.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace gj {
+
+template <typename T>
+cudaError_t launch_rmhmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                               const T* z, const double* u, const InfoDev<T>& info, int C, int tpb,
+                               cudaStream_t st);
+template <typename T>
+cudaError_t launch_lmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                             double* vol, const T* z, const double* u, const InfoDev<T>& info,
+                             int C, int tpb, cudaStream_t st);
+template <typename T>
+cudaError_t launch_monge_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
+                               double* vol, const T* z, const double* u, const InfoDev<T>& info,
+                               int C, int tpb, cudaStream_t st);
+template <typename T>
+cudaError_t launch_logdensity_grad(const TargetDev& t, const T* q, double* ld, T* g, double* vol,
+                                   int C, cudaStream_t st);
+template <typename T>
+cudaError_t launch_hvp(const TargetDev& t, const T* q, const T* u, T* out, int C, cudaStream_t st);
+template <typename T>
+cudaError_t launch_metric(const TargetDev& t, const T* q, T* out, int C, cudaStream_t st);
+
+// warp-per-chain LMC-Monge (monge_warp.cu), float32 state
+cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,
+                              double* ld, double* vol, const float* z, const double* u,
+                              const InfoDev<float>& info, int C, cudaStream_t st);
+bool monge_warp_supported(const TargetDev& t);
+
+}  // namespace gj

@@ -1,0 +1,152 @@
+// Shared device/host helpers for the geomjax_gb300 kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/geomjax_gb300.h"
+
+namespace gj {
+
+constexpr double kLog2Pi = 1.8378770664093454835606594728112;
+
+// Device-side view of a gj_target (passed by value to kernels).
+struct TargetDev {
+  int family;
+  int metric;
+  int d;
+  int n;
+  const void* X;
+  const void* y;
+  const void* s;
+  double p0;
+  double p1;
+};
+
+inline TargetDev to_dev(const gj_target& t) {
+  TargetDev r;
+  r.family = t.family;
+  r.metric = t.metric;
+  r.d = t.dim;
+  r.n = t.n_data;
+  r.X = t.X;
+  r.y = t.y;
+  r.s = t.s;
+  r.p0 = t.p0;
+  r.p1 = t.p1;
+  return r;
+}
+
+// Step parameters in device-friendly form.
+struct StepDev {
+  double h;
+  int L;
+  int integrator;
+  int max_iters;
+  double tol;
+  double div_threshold;
+  double alpha2;
+  const void* inv_mass;
+  int alpha2_fix;
+};
+
+inline StepDev to_dev(const gj_step_params& p) {
+  StepDev s;
+  s.h = p.step_size;
+  s.L = p.num_integration_steps;
+  s.integrator = p.integrator;
+  s.max_iters = p.max_iters;
+  s.tol = p.tol;
+  s.div_threshold = p.divergence_threshold;
+  s.alpha2 = p.alpha2;
+  s.inv_mass = p.inverse_mass;
+  s.alpha2_fix = p.alpha2_fix;
+  return s;
+}
+
+// Output pointers of one transition.
+template <typename T>
+struct InfoDev {
+  double* acc_rate;
+  uint8_t* accepted;
+  uint8_t* divergent;
+  double* energy;
+  int32_t* fp_iters;
+  uint8_t* status;
+  T* momentum;
+};
+
+template <typename T>
+inline InfoDev<T> to_dev(const gj_info* i) {
+  InfoDev<T> r{};
+  if (i) {
+    r.acc_rate = i->acceptance_rate;
+    r.accepted = i->is_accepted;
+    r.divergent = i->is_divergent;
+    r.energy = i->energy;
+    r.fp_iters = i->fp_iters;
+    r.status = i->status;
+    r.momentum = static_cast<T*>(i->momentum);
+  }
+  return r;
+}
+
+// Metropolis accept of mcmc/proposal.py:87-121,168-185 in float64:
+// w = H0 - H1 (NaN -> -inf), p = min(e^w, 1), accept = u < p.
+struct AcceptOut {
+  double w;
+  double p_acc;
+  bool accept;
+  bool divergent;
+};
+
+__device__ __forceinline__ AcceptOut metropolis(double H0, double H1, double u, double div_thr) {
+  AcceptOut a;
+  double w = H0 - H1;
+  if (isnan(w)) w = -INFINITY;
+  a.w = w;
+  a.p_acc = fmin(exp(w), 1.0);
+  a.accept = u < a.p_acc;
+  a.divergent = -w > div_thr;
+  return a;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T dexp(T x);
+template <>
+__device__ __forceinline__ float dexp<float>(float x) { return expf(x); }
+template <>
+__device__ __forceinline__ double dexp<double>(double x) { return exp(x); }
+
+template <typename T>
+__device__ __forceinline__ T dlog1pexp(T a) {  // log(1 + e^a), stable
+  return a > T(0) ? a + log1p(exp(-a)) : log1p(exp(a));
+}
+
+template <typename T>
+__device__ __forceinline__ T dsigmoid(T a) {
+  return T(1) / (T(1) + exp(-a));
+}
+
+}  // namespace gj

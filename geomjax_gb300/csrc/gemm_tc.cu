@@ -1,0 +1,337 @@
+// tcgen05 implementation of the split-BF16 contraction (gemm.cuh) for sm_103a.
+//
+// One CTA computes one 128 x 128 output tile D = A·Bᵀ (both operands K-major):
+//   warp 0      TMA producer: per 64-wide K chunk, one 128 x 64 BF16 box per
+//               plane of A and of B (128B-swizzled) into a 3-stage (two
+//               planes) or 2-stage (three planes) ring
+//   warp 1      allocates 128 TMEM columns; one elected thread issues
+//               tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M = N = 128,
+//               K = 16): the plane products A_i·B_j with i + j < planes per
+//               K step, and tcgen05.commit frees each stage / signals the
+//               accumulator
+//   warps 2-5   epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes
+//               32·(w%4) .. +31 = output rows), per-element epilogue
+// Every mbarrier wait is bounded; on timeout the kernel records an error code
+// in *err and skips the rest of its work, releasing TMEM before exit.
+#include <cuda.h>
+
+#include <cstring>
+
+#include "gemm.cuh"
+
+namespace gj {
+
+struct TcOperand {
+  CUtensorMap map;
+  SplitMat s;
+};
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int TILE_BYTES = 128 * BK * 2;          // one 128 x 64 BF16 box
+constexpr int TMEM_COLS = 128;
+// NPL planes per operand: a stage holds NPL A boxes and NPL B boxes
+template <int NPL>
+struct Cfg {
+  static constexpr int STAGES = NPL == 2 ? 3 : 2;
+  static constexpr int STAGE_BYTES = 2 * NPL * TILE_BYTES;
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+};
+constexpr long long WAIT_LIMIT = 1ll << 26;       // polls before giving up
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// bounded wait on the phase with the given parity; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (i > 64) __nanosleep(32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+      "%4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// K-major, 128B-swizzled shared-memory matrix descriptor (sm_100 format):
+// start>>4 in [0,14), LBO>>4 in [16,30) (unused for swizzled K-major, 1),
+// SBO>>4 in [32,46) = 1024 B between 8-row swizzle atoms, version 1 in
+// [46,48), layout type 2 (SWIZZLE_128B) in [61,64).
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// instruction descriptor, kind::f16: D = F32 (bit 4), A = B = BF16 (bits 7, 10),
+// both K-major, N>>3 at [17,23), M>>4 at [24,29)
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int NPL>
+__global__ void __launch_bounds__(192, 1)
+    gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err) {
+  constexpr int STAGES = Cfg<NPL>::STAGES;
+  constexpr int STAGE_BYTES = Cfg<NPL>::STAGE_BYTES;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned tile ring (required by the 128B swizzle), then barriers
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accum = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int KB = (K + BK - 1) / BK;
+
+  if (warp == 0 && lane == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < KB; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1)) {
+          atomicExch(err, 1);
+          break;
+        }
+        unsigned char* st = base + s * STAGE_BYTES;
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        const int x = kb * BK;
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+          tma_load_2d(st + q * TILE_BYTES, &mapA, &full[s], x, q * rpadA + m0);
+          tma_load_2d(st + (NPL + q) * TILE_BYTES, &mapB, &full[s], x, q * rpadB + n0);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int kb = 0; kb < KB && ok; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!mbar_wait(&full[s], ph)) {
+          atomicExch(err, 2);
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
+        uint64_t da[NPL], db[NPL];
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+          da[q] = make_desc(sa + q * TILE_BYTES);
+          db[q] = make_desc(sa + (NPL + q) * TILE_BYTES);
+        }
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          const uint64_t adv = (uint64_t)((k * 32) >> 4);  // 16 BF16 = 32 B along K
+          // plane products with i + j <= NPL - 1 (the dropped ones are below
+          // the last plane's resolution)
+          mma_bf16(tmem, da[0] + adv, db[0] + adv, (kb > 0 || k > 0) ? 1u : 0u);
+          mma_bf16(tmem, da[0] + adv, db[1] + adv, 1u);
+          mma_bf16(tmem, da[1] + adv, db[0] + adv, 1u);
+          if (NPL == 3) {
+            mma_bf16(tmem, da[0] + adv, db[NPL - 1] + adv, 1u);
+            mma_bf16(tmem, da[1] + adv, db[1] + adv, 1u);
+            mma_bf16(tmem, da[NPL - 1] + adv, db[0] + adv, 1u);
+          }
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(accum);  // also completes when nothing was issued
+    }
+  } else {
+    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    const int q = warp & 3;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(accum, 0));
+    if (!ok && lane == 0) atomicExch(err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && KB > 0) {
+      const int m = m0 + q * 32 + lane;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        if (n0 + c0 >= N) break;  // warp-uniform
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+        if (m < M) {
+          float v[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+          epi_row32(epi, m, n0 + c0, N, v);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+bool tc_available() {
+  int dev = 0, major = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess)
+    return false;
+  return major == 10 && get_encode() != nullptr;
+}
+
+TcOperand* tc_operand_create(const SplitMat& s, int, const char** err) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) {
+    *err = "cuTensorMapEncodeTiled unavailable";
+    return nullptr;
+  }
+  if ((s.ld % 64) || (s.rpad % 128) || (reinterpret_cast<uintptr_t>(s.p) & 15) ||
+      (s.planes != 2 && s.planes != 3)) {
+    *err = "split matrix not padded for TMA";
+    return nullptr;
+  }
+  TcOperand* op = new TcOperand();
+  op->s = s;
+  cuuint64_t dims[2] = {(cuuint64_t)s.ld, (cuuint64_t)s.planes * s.rpad};
+  cuuint64_t strides[1] = {(cuuint64_t)s.ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, 128u};
+  cuuint32_t estr[2] = {1u, 1u};
+  CUresult r = enc(&op->map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s.p, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    *err = "cuTensorMapEncodeTiled failed";
+    delete op;
+    return nullptr;
+  }
+  return op;
+}
+
+void tc_operand_destroy(TcOperand* op) { delete op; }
+
+cudaError_t gemm_tc_prepare() {
+  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       Cfg<2>::SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(gemm_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<3>::SMEM_BYTES);
+}
+
+cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                    cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+  // every box must lie inside the padded planes
+  if (g.M > a->s.rpad || g.N > b->s.rpad || g.K > a->s.ld || g.K > b->s.ld ||
+      a->s.planes != b->s.planes)
+    return cudaErrorInvalidValue;
+  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
+  if (a->s.planes == 3)
+    gemm_tc_kernel<3><<<grid, 192, Cfg<3>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
+                                                            g.M, g.N, g.K, g.epi, err);
+  else
+    gemm_tc_kernel<2><<<grid, 192, Cfg<2>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
+                                                            g.M, g.N, g.K, g.epi, err);
+  return cudaGetLastError();
+}
+
+}  // namespace gj

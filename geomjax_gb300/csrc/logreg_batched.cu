@@ -1,0 +1,1035 @@
+// Batched dense-Fisher logistic-regression RMHMC (implicit midpoint) over all
+// chains at once, mixed precision.
+//
+// Reference path: rmhmc/rmhmc.py:131-174 (kernel), rmhmc/integrators.py:53-156
+// (fixed-point implicit midpoint), rmhmc/metrics.py:42-127 (Gaussian
+// kinetic energy, Cholesky momentum, solve), mcmc/proposal.py:87-185
+// (accept).  The reference differentiates K through the Cholesky of the
+// user's metric; for the Fisher metric G = XᵀΛX + I/s² of logistic
+// regression the same derivative is, per chain,
+//     ∂K/∂β_k = ½ Σ_n Λ'_n x_nk [x_nᵀG⁻¹x_n − (x_nᵀu)²],  u = G⁻¹p.
+//
+// One fixed-point map evaluation for all C chains is five contractions over
+// the data, each one a split-BF16 GEMM with FP32 accumulation (gemm.cuh):
+//   (1) A = Q Xᵀ            [C x N]  epilogue: σ, Λ, Λ', r1 = y − σ
+//   (2) Gvec = Λ Zᵀ          [C x P]  Gram, Z_n = upper triangle of x_n x_nᵀ
+//   (3) per-chain FP64 Cholesky of G = Gvec + I/s², u = G⁻¹p, log det G,
+//       G⁻¹ packed as Z-coefficients (FP32, split to BF16)
+//   (4) S = U Xᵀ            [C x N]  s_cn = x_nᵀu_c
+//   (5) W = Ginv Zᵀ          [C x N]  epilogue: r2 = Λ'(w − s²)
+//   (6) [∇ℓ | 2∂K] = [r1; r2] X      [2C x d]
+//   (7) update: (q, p) ← (q0 + h/2·u, p0 − h/2·(∂K − ∇ℓ)), ∞-norm in FP64,
+//       per-chain convergence exactly as the vmapped lax.while_loop.
+// Z and X are constants of the target, staged once as split-BF16 planes.
+// FP64 is used for the metric Cholesky, log det and solves, the fixed-point
+// norm and the Hamiltonian difference; the log density at the proposal is
+// evaluated per chain in FP32 with an FP64 sum.
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "chain_kernels.cuh"
+#include "gemm.cuh"
+#include "logreg_batched.cuh"
+
+namespace gj {
+
+namespace {
+thread_local std::string g_err;
+
+inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
+
+enum CholMode : int { CH_DRAW = 0, CH_EVAL = 1, CH_ENERGY = 2 };
+enum UpdMode : int { UP_FP0 = 0, UP_FPN = 1, UP_EXPLICIT = 2 };
+
+// ---------------------------------------------------------------------------
+// constants: X and Z = vech(x xᵀ) as split-BF16 planes
+// ---------------------------------------------------------------------------
+__global__ void build_consts_kernel(const float* X, int N, int d, int P, SplitMat Xb, SplitMat XTb,
+                                    SplitMat Zb, SplitMat Zt) {
+  const int n = blockIdx.x;
+  if (n >= N) return;
+  const float* x = X + (size_t)n * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    split_store(Xb, n, j, x[j]);
+    split_store(XTb, j, n, x[j]);
+  }
+  for (int idx = threadIdx.x; idx < P; idx += blockDim.x) {
+    // idx -> (j, k), j <= k, row-major over the upper triangle
+    int j = 0, rem = idx;
+    while (rem >= d - j) {
+      rem -= d - j;
+      ++j;
+    }
+    const int k = j + rem;
+    const float zz = x[j] * x[k];
+    split_store(Zb, n, idx, zz);
+    split_store(Zt, idx, n, zz);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-chain metric factorisation (one warp per chain, shared memory)
+// ---------------------------------------------------------------------------
+struct CholArgs {
+  int mode, C, d, P;
+  double prior_inv;
+  const float* Gv;
+  int gv_ld;
+  const float* z;      // DRAW
+  double* p0;          // DRAW: p0 := L z
+  double* pc;          // current momentum (FP64 iterate; DRAW writes it)
+  double* u;           // [C, d] G⁻¹p (FP64)
+  SplitMat Ub;         // split U for (4)
+  SplitMat Giv;        // split packed G⁻¹ for (5)
+  double* logdet;      // [C]
+  double* quad;        // [C] ||L⁻¹p||² (DRAW: ||z||²)
+  const uint8_t* active;  // EVAL: skip inactive chains (may be NULL)
+  uint8_t* bad;        // [C] non-SPD flag (sticky)
+  float* mom_info;     // DRAW: info.momentum (may be NULL)
+};
+
+template <typename F>  // factorisation type: double (default) or float
+__global__ void chol_kernel(CholArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int c = blockIdx.x * nwarps + warp;
+  const int d = a.d;
+  F* L = reinterpret_cast<F*>(smem_raw) + (size_t)warp * (d * d + 2 * d);
+  F* y = L + d * d;
+  F* xv = y + d;
+  float* Li = reinterpret_cast<float*>(reinterpret_cast<F*>(smem_raw) + (size_t)nwarps * (d * d + 2 * d)) +
+              (size_t)warp * d * d;
+  if (c >= a.C) return;
+  if (a.mode == CH_EVAL && a.active && !a.active[c]) return;
+  // unpack G = Gvec + I/s²
+  for (int idx = lane; idx < a.P; idx += 32) {
+    int j = 0, rem = idx;
+    while (rem >= d - j) {
+      rem -= d - j;
+      ++j;
+    }
+    const int k = j + rem;
+    F g = F(a.Gv[(size_t)c * a.gv_ld + idx]);
+    if (j == k) g += F(a.prior_inv);
+    L[k * d + j] = g;  // lower triangle
+  }
+  __syncwarp();
+  // left-looking Cholesky, lanes over rows
+  bool bad = false;
+  double logdet = 0.0;
+  for (int j = 0; j < d; ++j) {
+    F s = 0;
+    for (int k = lane; k < j; k += 32) s += L[j * d + k] * L[j * d + k];
+    s = warp_sum(s);
+    F djj = L[j * d + j] - s;
+    if (!(djj > F(0))) {
+      bad = true;
+      djj = F(NAN);
+    }
+    const F ljj = sqrt(djj);
+    logdet += 2.0 * log(double(ljj));
+    __syncwarp();
+    if (lane == 0) L[j * d + j] = ljj;
+    const F inv = F(1) / ljj;
+    for (int i = j + 1 + lane; i < d; i += 32) {
+      F t = L[i * d + j];
+      for (int k = 0; k < j; ++k) t -= L[i * d + k] * L[j * d + k];
+      L[i * d + j] = t * inv;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    a.logdet[c] = logdet;
+    if (bad) a.bad[c] = 1;
+  }
+  // right-hand side: DRAW p = L z (and y = L⁻¹p = z); otherwise y = L⁻¹ p
+  if (a.mode == CH_DRAW) {
+    for (int i = lane; i < d; i += 32) y[i] = F(a.z[(size_t)c * d + i]);
+    __syncwarp();
+    double zz = 0.0;
+    for (int i = lane; i < d; i += 32) {
+      F s = 0;
+      for (int k = 0; k <= i; ++k) s += L[i * d + k] * y[k];
+      a.p0[(size_t)c * d + i] = double(s);
+      a.pc[(size_t)c * d + i] = double(s);
+      if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(s);
+      zz += double(y[i]) * double(y[i]);
+    }
+    zz = warp_sum(zz);
+    if (lane == 0) a.quad[c] = zz;
+  } else {
+    // forward substitution, one row at a time, lane-parallel dot products
+    for (int i = 0; i < d; ++i) {
+      F s = 0;
+      for (int k = lane; k < i; k += 32) s += L[i * d + k] * y[k];
+      s = warp_sum(s);
+      if (lane == 0) y[i] = (F(a.pc[(size_t)c * d + i]) - s) / L[i * d + i];
+      __syncwarp();
+    }
+    if (a.mode == CH_ENERGY) {
+      double q = 0.0;
+      for (int i = lane; i < d; i += 32) q += double(y[i]) * double(y[i]);
+      q = warp_sum(q);
+      if (lane == 0) a.quad[c] = q;
+      return;
+    }
+  }
+  __syncwarp();
+  // u = L⁻ᵀ y (backward substitution)
+  for (int i = d - 1; i >= 0; --i) {
+    F s = 0;
+    for (int k = i + 1 + lane; k < d; k += 32) s += L[k * d + i] * xv[k];
+    s = warp_sum(s);
+    if (lane == 0) xv[i] = (y[i] - s) / L[i * d + i];
+    __syncwarp();
+  }
+  for (int i = lane; i < d; i += 32) {
+    a.u[(size_t)c * d + i] = double(xv[i]);
+    split_store(a.Ub, c, i, float(xv[i]));
+  }
+  // L⁻¹ in FP32 (column per lane), then G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients
+  for (int col = lane; col < d; col += 32) {
+    Li[col * d + col] = float(F(1) / L[col * d + col]);
+    for (int i = col + 1; i < d; ++i) {
+      float s = 0.f;
+      for (int k = col; k < i; ++k) s += float(L[i * d + k]) * Li[k * d + col];
+      Li[i * d + col] = -s / float(L[i * d + i]);
+    }
+  }
+  __syncwarp();
+  for (int idx = lane; idx < a.P; idx += 32) {
+    int j = 0, rem = idx;
+    while (rem >= d - j) {
+      rem -= d - j;
+      ++j;
+    }
+    const int k = j + rem;
+    float s = 0.f;
+    for (int m = k; m < d; ++m) s += Li[m * d + j] * Li[m * d + k];
+    split_store(a.Giv, c, idx, (j == k) ? s : 2.f * s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fixed-point update (one thread per chain)
+// ---------------------------------------------------------------------------
+struct UpdArgs {
+  int mode, C, d;
+  double hh, prior_inv, tol;
+  int max_iters;
+  const StepDev* spd;  // when set (graph path), h / tol / max_iters are read from it
+  const float* Gout;  // [2C, ldo]
+  int ldo;
+  const double* u;
+  double *q0, *p0, *qc, *pc;  // FP64 fixed-point iterates
+  float* qf;                  // FP32 copy of the position after each step
+  double* norm;
+  int* iters;
+  int* iters_total;
+  uint8_t* active;
+  uint8_t* notconv;
+  SplitMat Qb;
+  int* n_active;
+};
+
+__global__ void update_kernel(UpdArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.C) return;
+  if (a.mode == UP_FPN && !a.active[c]) return;
+  const int d = a.d;
+  const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
+  const double tol = a.spd ? a.spd->tol : a.tol;
+  const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
+  const double* qs = (a.mode == UP_EXPLICIT) ? a.qc : a.q0;
+  const double* ps = (a.mode == UP_EXPLICIT) ? a.pc : a.p0;
+  double nrm = 0.0;
+  bool nan = false;
+  for (int i = 0; i < d; ++i) {
+    const size_t o = (size_t)c * d + i;
+    const double q = a.qc[o];
+    const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
+    const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
+    const double qn = qs[o] + hh * a.u[o];
+    const double pn = ps[o] - hh * (dK - g);
+    const double e1 = qn - q, e2 = pn - a.pc[o];
+    nan |= isnan(e1) || isnan(e2);
+    nrm = fmax(nrm, fmax(fabs(e1), fabs(e2)));
+    a.qc[o] = qn;
+    a.pc[o] = pn;
+    split_store(a.Qb, c, i, float(qn));
+    if (a.mode == UP_EXPLICIT) {
+      a.q0[o] = qn;
+      a.p0[o] = pn;
+      a.qf[o] = float(qn);
+    }
+  }
+  if (a.mode == UP_EXPLICIT) return;
+  if (nan) nrm = NAN;
+  const int it = (a.mode == UP_FP0) ? 0 : a.iters[c] + 1;
+  a.iters[c] = it;
+  a.norm[c] = nrm;
+  const bool act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
+  a.active[c] = act;
+  if (a.mode == UP_FPN) a.iters_total[c] += 1;
+  if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
+  if (act) atomicAdd(a.n_active, 1);
+}
+
+__global__ void begin_kernel(int C, int d, const float* pos, double* q0, double* qc, float* qf,
+                             SplitMat Qb, int* iters_total, uint8_t* notconv, uint8_t* bad) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  for (int i = 0; i < d; ++i) {
+    const float q = pos[(size_t)c * d + i];
+    q0[(size_t)c * d + i] = q;
+    qc[(size_t)c * d + i] = q;
+    qf[(size_t)c * d + i] = q;
+    split_store(Qb, c, i, q);
+  }
+  iters_total[c] = 0;
+  notconv[c] = 0;
+  bad[c] = 0;
+}
+
+__global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q,
+                              const double* logdet0, const double* ld1, const double* quad1,
+                              const double* logdet1, const double* uacc, double div_thr,
+                              const StepDev* spd,
+                              const float* qf, const float* g1, float* pos, float* grad,
+                              double* logdens, InfoDev<float> info, const int* iters_total,
+                              const uint8_t* notconv, const uint8_t* bad) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const double cst = 0.5 * d * kLog2Pi;
+  // K = ½pᵀG⁻¹p + ½ log det G + d/2 log 2π (rmhmc/metrics.py:60-74)
+  const double H0 = -ld0[c] + 0.5 * H0q[c] + 0.5 * logdet0[c] + cst;
+  const double H1 = -ld1[c] + 0.5 * quad1[c] + 0.5 * logdet1[c] + cst;
+  const AcceptOut a = metropolis(H0, H1, uacc[c], spd ? spd->div_threshold : div_thr);
+  if (a.accept) {
+    for (int i = 0; i < d; ++i) {
+      pos[(size_t)c * d + i] = qf[(size_t)c * d + i];
+      grad[(size_t)c * d + i] = g1[(size_t)c * d + i];
+    }
+    logdens[c] = ld1[c];
+  }
+  if (info.acc_rate) info.acc_rate[c] = a.p_acc;
+  if (info.accepted) info.accepted[c] = a.accept;
+  if (info.divergent) info.divergent[c] = a.divergent;
+  if (info.energy) info.energy[c] = H1;
+  if (info.fp_iters) info.fp_iters[c] = iters_total[c];
+  if (info.status)
+    info.status[c] = (notconv[c] ? GJ_CHAIN_FP_NOT_CONVERGED : 0u) |
+                     (isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE) | (bad[c] ? GJ_CHAIN_NOT_SPD : 0u);
+}
+
+// Sets the WHILE condition of the fixed-point loop node: iterate while a
+// chain is active, at most max_iters + 1 body executions per solve.
+__global__ void loop_cond_kernel(cudaGraphConditionalHandle h, const int* n_active, int* trips,
+                                 const StepDev* spd) {
+  const int t = *trips;
+  *trips = t + 1;
+  const bool more = (*n_active > 0) && (t <= spd->max_iters);
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+template <typename Tp>
+Tp* dalloc(size_t n, std::vector<void*>& owned, bool* ok) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(Tp) + 256) != cudaSuccess) {
+    *ok = false;
+    return nullptr;
+  }
+  cudaMemset(p, 0, n * sizeof(Tp) + 256);
+  owned.push_back(p);
+  return static_cast<Tp*>(p);
+}
+
+}  // namespace
+
+struct LogregBatched {
+  TargetDev t;
+  int C, N, d, P, dpad, Npad, Pp;
+  std::vector<void*> owned;
+  // constants
+  SplitMat Xb, XTb, Zb, Zt;
+  // per-chain buffers
+  SplitMat Qb, Ub, Lam, Giv, Rb;
+  float *Lp, *S, *Gv, *Gout;
+  double *q0, *p0, *qc, *pc;
+  float *qf, *gnew;
+  double *u, *norm, *logdet0, *quad0, *logdet1, *quad1, *ldnew;
+  int *iters, *iters_total, *n_active_d;
+  int* n_active_h;  // pinned
+  uint8_t *active, *notconv, *bad;
+  int* tc_err;
+  TcOperand *tXb, *tXTb, *tZb, *tZt, *tQb, *tUb, *tLam, *tGiv, *tRb;
+  bool tc_ok;
+  int chol_fp64;
+  int prof;
+  // graph path: device step parameters, staging buffers, captured graph
+  StepDev* spd;
+  StepDev* sp_host;  // pinned
+  float *pos_s, *grad_s, *z_s, *mom_s;
+  double *ld_s, *u_s, *acc_s, *energy_s;
+  uint8_t *accepted_s, *divergent_s, *status_s;
+  int* fpit_s;
+  int* trips;
+  cudaStream_t cap_main, cap_body;
+  cudaGraphExec_t gexec;
+  int g_L, g_impl, g_chol;
+  std::vector<cudaEvent_t> ev;
+  size_t ev_used;
+  LogregStats stats;
+};
+
+const char* logreg_batched_error() { return g_err.c_str(); }
+
+LogregStats logreg_batched_stats(const LogregBatched* lb) { return lb->stats; }
+void logreg_batched_set_chol_fp64(LogregBatched* lb, int on) { lb->chol_fp64 = on; }
+void logreg_batched_set_profile(LogregBatched* lb, int on) { lb->prof = on; }
+
+static SplitMat make_split(LogregBatched* lb, int rows, int kdim, int planes, bool* ok) {
+  SplitMat s;
+  s.rows = rows;
+  s.kdim = kdim;
+  s.ld = roundup(kdim, 64);
+  s.rpad = roundup(rows, 128);
+  s.planes = planes;
+  s.p = dalloc<bf16>((size_t)planes * s.rpad * s.ld, lb->owned, ok);
+  return s;
+}
+
+void logreg_batched_destroy(LogregBatched* lb) {
+  if (!lb) return;
+  TcOperand* ops[] = {lb->tXb, lb->tXTb, lb->tZb, lb->tZt, lb->tQb,
+                      lb->tUb, lb->tLam, lb->tGiv, lb->tRb};
+  for (TcOperand* o : ops)
+    if (o) tc_operand_destroy(o);
+  for (void* p : lb->owned) cudaFree(p);
+  for (cudaEvent_t e : lb->ev) cudaEventDestroy(e);
+  if (lb->gexec) cudaGraphExecDestroy(lb->gexec);
+  if (lb->cap_main) cudaStreamDestroy(lb->cap_main);
+  if (lb->cap_body) cudaStreamDestroy(lb->cap_body);
+  if (lb->sp_host) cudaFreeHost(lb->sp_host);
+  if (lb->n_active_h) cudaFreeHost(lb->n_active_h);
+  delete lb;
+}
+
+int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
+  *out = nullptr;
+  if (t.d > 128) {
+    g_err = "batched logistic-regression path supports d <= 128";
+    return GJ_ENOTSUP;
+  }
+  LogregBatched* lb = new LogregBatched();
+  lb->t = t;
+  lb->C = C;
+  lb->N = t.n;
+  lb->d = t.d;
+  lb->P = t.d * (t.d + 1) / 2;
+  lb->chol_fp64 = 1;
+  lb->prof = 0;
+  lb->ev_used = 0;
+  lb->gexec = nullptr;
+  lb->g_L = lb->g_impl = lb->g_chol = -1;
+  lb->cap_main = lb->cap_body = nullptr;
+  lb->sp_host = nullptr;
+  lb->stats = LogregStats{};
+  bool ok = true;
+  const int N = lb->N, d = lb->d, P = lb->P;
+  // Operands whose rounding feeds the fixed-point map at first order (Xβ,
+  // x_nᵀu and the gradient contraction) use three planes, so the map is
+  // FP32-smooth and converges to the absolute tolerance; the Gram and trace
+  // operands enter through G⁻¹ only and use two.
+  lb->Xb = make_split(lb, N, d, 3, &ok);
+  lb->XTb = make_split(lb, d, N, 3, &ok);
+  lb->Zb = make_split(lb, N, P, 2, &ok);
+  lb->Zt = make_split(lb, P, N, 2, &ok);
+  lb->Qb = make_split(lb, C, d, 3, &ok);
+  lb->Ub = make_split(lb, C, d, 3, &ok);
+  lb->Lam = make_split(lb, C, N, 2, &ok);
+  lb->Giv = make_split(lb, C, P, 2, &ok);
+  lb->Rb = make_split(lb, 2 * C, N, 3, &ok);
+  lb->dpad = roundup(d, 8);
+  lb->Npad = roundup(N, 8);
+  lb->Pp = roundup(P, 8);
+  lb->Lp = dalloc<float>((size_t)C * lb->Npad, lb->owned, &ok);
+  lb->S = dalloc<float>((size_t)C * lb->Npad, lb->owned, &ok);
+  lb->Gv = dalloc<float>((size_t)C * lb->Pp, lb->owned, &ok);
+  lb->Gout = dalloc<float>((size_t)2 * C * lb->dpad, lb->owned, &ok);
+  lb->q0 = dalloc<double>((size_t)C * d, lb->owned, &ok);
+  lb->p0 = dalloc<double>((size_t)C * d, lb->owned, &ok);
+  lb->qc = dalloc<double>((size_t)C * d, lb->owned, &ok);
+  lb->pc = dalloc<double>((size_t)C * d, lb->owned, &ok);
+  lb->qf = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->gnew = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->u = dalloc<double>((size_t)C * d, lb->owned, &ok);
+  lb->norm = dalloc<double>(C, lb->owned, &ok);
+  lb->logdet0 = dalloc<double>(C, lb->owned, &ok);
+  lb->quad0 = dalloc<double>(C, lb->owned, &ok);
+  lb->logdet1 = dalloc<double>(C, lb->owned, &ok);
+  lb->quad1 = dalloc<double>(C, lb->owned, &ok);
+  lb->ldnew = dalloc<double>(C, lb->owned, &ok);
+  lb->iters = dalloc<int>(C, lb->owned, &ok);
+  lb->iters_total = dalloc<int>(C, lb->owned, &ok);
+  lb->n_active_d = dalloc<int>(1, lb->owned, &ok);
+  lb->active = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->notconv = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->bad = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->tc_err = dalloc<int>(1, lb->owned, &ok);
+  lb->spd = dalloc<StepDev>(1, lb->owned, &ok);
+  lb->pos_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->grad_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->z_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->mom_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->ld_s = dalloc<double>(C, lb->owned, &ok);
+  lb->u_s = dalloc<double>(C, lb->owned, &ok);
+  lb->acc_s = dalloc<double>(C, lb->owned, &ok);
+  lb->energy_s = dalloc<double>(C, lb->owned, &ok);
+  lb->accepted_s = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->divergent_s = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->status_s = dalloc<uint8_t>(C, lb->owned, &ok);
+  lb->fpit_s = dalloc<int>(C, lb->owned, &ok);
+  lb->trips = dalloc<int>(1, lb->owned, &ok);
+  if (cudaMallocHost(&lb->sp_host, sizeof(StepDev)) != cudaSuccess) ok = false;
+  if (cudaStreamCreateWithFlags(&lb->cap_main, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+  if (cudaStreamCreateWithFlags(&lb->cap_body, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+  if (cudaMallocHost(&lb->n_active_h, sizeof(int)) != cudaSuccess) ok = false;
+  if (!ok) {
+    g_err = "device allocation failed in the batched logistic-regression context";
+    logreg_batched_destroy(lb);
+    return GJ_ENOMEM;
+  }
+  build_consts_kernel<<<N, 128>>>(static_cast<const float*>(t.X), N, d, P, lb->Xb, lb->XTb, lb->Zb,
+                                  lb->Zt);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    g_err = std::string("building logistic-regression constants: ") + cudaGetErrorString(e);
+    logreg_batched_destroy(lb);
+    return GJ_ECUDA;
+  }
+  {
+    const int warps = d <= 32 ? 4 : 1;
+    const int smax = (int)((size_t)warps * ((d * d + 2 * d) * sizeof(double) + (size_t)d * d * sizeof(float)));
+    cudaError_t a1 = cudaFuncSetAttribute(chol_kernel<double>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaError_t a2 = cudaFuncSetAttribute(chol_kernel<float>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (a1 != cudaSuccess || a2 != cudaSuccess) {
+      g_err = "metric factorisation needs more shared memory than the device allows";
+      logreg_batched_destroy(lb);
+      return GJ_ENOTSUP;
+    }
+  }
+  lb->tc_ok = false;
+  if (tc_available() && gemm_tc_prepare() == cudaSuccess) {
+    const char* err = nullptr;
+    lb->tXb = tc_operand_create(lb->Xb, 0, &err);
+    lb->tXTb = tc_operand_create(lb->XTb, 0, &err);
+    lb->tZb = tc_operand_create(lb->Zb, 0, &err);
+    lb->tZt = tc_operand_create(lb->Zt, 0, &err);
+    lb->tQb = tc_operand_create(lb->Qb, 0, &err);
+    lb->tUb = tc_operand_create(lb->Ub, 0, &err);
+    lb->tLam = tc_operand_create(lb->Lam, 0, &err);
+    lb->tGiv = tc_operand_create(lb->Giv, 0, &err);
+    lb->tRb = tc_operand_create(lb->Rb, 0, &err);
+    lb->tc_ok = lb->tXb && lb->tXTb && lb->tZb && lb->tZt && lb->tQb && lb->tUb && lb->tLam &&
+                lb->tGiv && lb->tRb;
+  }
+  *out = lb;
+  return GJ_OK;
+}
+
+namespace {
+
+struct Runner {
+  LogregBatched* lb;
+  int impl;
+  cudaStream_t st;
+  cudaError_t err = cudaSuccess;
+  const StepDev* spd = nullptr;  // graph path: step parameters in device memory
+
+  void gemm(const SplitMat& A, const TcOperand* ta, const SplitMat& B, const TcOperand* tb, int M,
+            int N, int K, const Epi& e) {
+    if (err != cudaSuccess) return;
+    GemmArgs g;
+    g.A = A;
+    g.B = B;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.epi = e;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (lb->prof) {
+      while (lb->ev.size() < lb->ev_used + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) break;
+        lb->ev.push_back(e);
+      }
+      if (lb->ev.size() >= lb->ev_used + 2) {
+        e0 = lb->ev[lb->ev_used];
+        e1 = lb->ev[lb->ev_used + 1];
+        lb->ev_used += 2;
+        cudaEventRecord(e0, st);
+      }
+    }
+    if (impl == 2)
+      err = gemm_tc(g, ta, tb, lb->tc_err, st);
+    else
+      err = gemm_simt(g, st);
+    if (e1) cudaEventRecord(e1, st);
+    lb->stats.gemm_launches++;
+    lb->stats.gemm_flops += 2.0 * M * N * K;
+  }
+  void check(cudaError_t e) {
+    if (err == cudaSuccess) err = e;
+    lb->stats.other_launches++;
+  }
+
+  // metric at the current iterate: (1) and (2)
+  void metric_gram() {
+    LogregBatched& L = *lb;
+    Epi e{};
+    e.mode = EPI_SIGMOID;
+    e.y = static_cast<const float*>(L.t.y);
+    e.lam = L.Lam;
+    e.lp = L.Lp;
+    e.lp_ld = L.Npad;
+    e.r = L.Rb;
+    gemm(L.Qb, L.tQb, L.Xb, L.tXb, L.C, L.N, L.d, e);
+    Epi g{};
+    g.mode = EPI_STORE;
+    g.D = L.Gv;
+    g.ldd = L.Pp;
+    gemm(L.Lam, L.tLam, L.Zt, L.tZt, L.C, L.P, L.N, g);
+  }
+
+  void chol(int mode, const float* z, double* logdet, double* quad, float* mom_info,
+            bool only_active = false) {
+    LogregBatched& L = *lb;
+    CholArgs a{};
+    a.mode = mode;
+    a.C = L.C;
+    a.d = L.d;
+    a.P = L.P;
+    a.prior_inv = 1.0 / L.t.p0;
+    a.Gv = L.Gv;
+    a.gv_ld = L.Pp;
+    a.z = z;
+    a.p0 = L.p0;
+    a.pc = L.pc;
+    a.u = L.u;
+    a.Ub = L.Ub;
+    a.Giv = L.Giv;
+    a.logdet = logdet;
+    a.quad = quad;
+    a.active = only_active ? L.active : nullptr;
+    a.bad = L.bad;
+    a.mom_info = mom_info;
+    const int d = L.d;
+    const int warps = d <= 32 ? 4 : 1;
+    const size_t fsz = L.chol_fp64 ? sizeof(double) : sizeof(float);
+    const size_t smem = (size_t)warps * ((d * d + 2 * d) * fsz + (size_t)d * d * sizeof(float));
+    const dim3 grid((L.C + warps - 1) / warps);
+    // the dynamic shared-memory limit was raised at context creation
+    if (L.chol_fp64)
+      chol_kernel<double><<<grid, 32 * warps, smem, st>>>(a);
+    else
+      chol_kernel<float><<<grid, 32 * warps, smem, st>>>(a);
+    check(cudaGetLastError());
+  }
+
+  // (4)-(6) after the factorisation
+  void trace_grad() {
+    LogregBatched& L = *lb;
+    Epi s{};
+    s.mode = EPI_STORE;
+    s.D = L.S;
+    s.ldd = L.Npad;
+    gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
+    Epi w{};
+    w.mode = EPI_TRACE;
+    w.S = L.S;
+    w.s_ld = L.Npad;
+    w.lp = L.Lp;
+    w.lp_ld = L.Npad;
+    w.r = L.Rb;
+    w.r_off = L.C;
+    gemm(L.Giv, L.tGiv, L.Zb, L.tZb, L.C, L.N, L.P, w);
+    Epi o{};
+    o.mode = EPI_STORE;
+    o.D = L.Gout;
+    o.ldd = L.dpad;
+    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
+  }
+
+  void update(int mode, const StepDev& sp) {
+    LogregBatched& L = *lb;
+    UpdArgs a{};
+    a.mode = mode;
+    a.C = L.C;
+    a.d = L.d;
+    a.hh = 0.5 * sp.h;
+    a.prior_inv = 1.0 / L.t.p0;
+    a.tol = sp.tol;
+    a.max_iters = sp.max_iters;
+    a.Gout = L.Gout;
+    a.ldo = L.dpad;
+    a.u = L.u;
+    a.q0 = L.q0;
+    a.p0 = L.p0;
+    a.qc = L.qc;
+    a.pc = L.pc;
+    a.qf = L.qf;
+    a.norm = L.norm;
+    a.iters = L.iters;
+    a.iters_total = L.iters_total;
+    a.active = L.active;
+    a.notconv = L.notconv;
+    a.Qb = L.Qb;
+    a.n_active = L.n_active_d;
+    a.spd = spd;
+    update_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(a);
+    check(cudaGetLastError());
+  }
+};
+
+}  // namespace
+
+int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
+                              double* logdens, const float* z, const double* u,
+                              const InfoDev<float>& info, int gemm_impl, cudaStream_t st) {
+  if (gemm_impl == 2 && !lb->tc_ok) {
+    g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
+    return GJ_ENOTSUP;
+  }
+  lb->stats = LogregStats{};
+  lb->ev_used = 0;
+  Runner R{lb, gemm_impl, st};
+  const int C = lb->C, d = lb->d;
+  begin_kernel<<<(C + 127) / 128, 128, 0, st>>>(C, d, pos, lb->q0, lb->qc, lb->qf, lb->Qb,
+                                                 lb->iters_total, lb->notconv, lb->bad);
+  R.check(cudaGetLastError());
+  for (int s = 0; s < sp.L; ++s) {
+    // fixed-point evaluation #0 (rmhmc/integrators.py:84); at s == 0 it also
+    // draws p = chol(G(q0))·z (rmhmc/metrics.py:45-58)
+    R.metric_gram();
+    if (s == 0)
+      R.chol(CH_DRAW, z, lb->logdet0, lb->quad0, info.momentum);
+    else
+      R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
+    R.trace_grad();
+    R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
+    R.update(UP_FP0, sp);
+    int guard = 0;
+    for (;;) {
+      R.check(cudaMemcpyAsync(lb->n_active_h, lb->n_active_d, sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+      R.check(cudaStreamSynchronize(st));
+      if (R.err != cudaSuccess) break;
+      if (*lb->n_active_h == 0 || guard > sp.max_iters + 1) break;
+      ++guard;
+      R.metric_gram();
+      R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
+      R.trace_grad();
+      R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
+      R.update(UP_FPN, sp);
+      lb->stats.evals++;
+    }
+    lb->stats.evals++;
+    // explicit half step from the midpoint (rmhmc/integrators.py:147-148)
+    R.metric_gram();
+    R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
+    R.trace_grad();
+    R.update(UP_EXPLICIT, sp);
+    lb->stats.evals++;
+  }
+  if (sp.L == 0) {
+    // no trajectory: draw the momentum anyway for H0 = H1
+    R.metric_gram();
+    R.chol(CH_DRAW, z, lb->logdet0, lb->quad0, info.momentum);
+  }
+  // energy at the proposal: metric, log det, ||L⁻¹p||², ℓ and ∇ℓ (FP32, FP64 sum)
+  R.metric_gram();
+  R.chol(CH_ENERGY, nullptr, lb->logdet1, lb->quad1, nullptr);
+  R.check(launch_logdensity_grad<float>(lb->t, lb->qf, lb->ldnew, lb->gnew, nullptr, C, st));
+  accept_kernel<<<(C + 127) / 128, 128, 0, st>>>(
+      C, d, logdens, lb->quad0, lb->logdet0, lb->ldnew, lb->quad1, lb->logdet1, u,
+      sp.div_threshold, nullptr, lb->qf, lb->gnew, pos, grad, logdens, info, lb->iters_total,
+      lb->notconv,
+      lb->bad);
+  R.check(cudaGetLastError());
+  if (R.err == cudaSuccess && lb->prof && lb->ev_used) {
+    R.check(cudaStreamSynchronize(st));
+    double ns = 0.0;
+    for (size_t i = 0; i + 1 < lb->ev_used; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, lb->ev[i], lb->ev[i + 1]) == cudaSuccess) ns += 1e6 * ms;
+    }
+    lb->stats.gemm_ns = ns;
+  }
+  if (R.err != cudaSuccess) {
+    g_err = std::string("batched logistic-regression step: ") + cudaGetErrorString(R.err);
+    return GJ_ECUDA;
+  }
+  if (gemm_impl == 2) {
+    int herr = 0;
+    if (cudaMemcpyAsync(&herr, lb->tc_err, sizeof(int), cudaMemcpyDeviceToHost, st) ==
+            cudaSuccess &&
+        cudaStreamSynchronize(st) == cudaSuccess && herr != 0) {
+      g_err = "tcgen05 GEMM wait timed out (code " + std::to_string(herr) + ")";
+      cudaMemsetAsync(lb->tc_err, 0, sizeof(int), st);
+      return GJ_ECUDA;
+    }
+  }
+  return GJ_OK;
+}
+
+namespace {
+
+__global__ void set_step_kernel(StepDev* dst, StepDev v) { *dst = v; }
+
+int graph_fail(const char* what, cudaError_t e) {
+  g_err = std::string("graph capture (") + what + "): " + cudaGetErrorString(e);
+  return GJ_ECUDA;
+}
+
+// Capture one whole transition (all L steps, each fixed-point solve a
+// conditional WHILE node) into lb->gexec.  The graph reads and writes the
+// context's staging buffers; step parameters come from lb->spd.
+int build_graph(LogregBatched* lb, int L, int impl) {
+  if (lb->gexec) {
+    cudaGraphExecDestroy(lb->gexec);
+    lb->gexec = nullptr;
+  }
+  const int C = lb->C, d = lb->d;
+  cudaStream_t s = lb->cap_main;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return graph_fail("begin", e);
+  Runner R{lb, impl, s};
+  R.spd = lb->spd;
+  begin_kernel<<<(C + 127) / 128, 128, 0, s>>>(C, d, lb->pos_s, lb->q0, lb->qc, lb->qf, lb->Qb,
+                                                lb->iters_total, lb->notconv, lb->bad);
+  StepDev dummy{};
+  for (int st = 0; st < L && R.err == cudaSuccess; ++st) {
+    R.metric_gram();
+    if (st == 0)
+      R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
+    else
+      R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
+    R.trace_grad();
+    R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), s));
+    R.update(UP_FP0, dummy);
+    R.check(cudaMemsetAsync(lb->trips, 0, sizeof(int), s));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) break;
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) break;
+    loop_cond_kernel<<<1, 1, 0, s>>>(h, lb->n_active_d, lb->trips, lb->spd);
+    e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) break;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) break;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) break;
+    e = cudaStreamBeginCaptureToGraph(lb->cap_body, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) break;
+    Runner B{lb, impl, lb->cap_body};
+    B.spd = lb->spd;
+    B.metric_gram();
+    B.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
+    B.trace_grad();
+    B.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), lb->cap_body));
+    B.update(UP_FPN, dummy);
+    loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
+    B.check(cudaGetLastError());
+    cudaGraph_t bout = nullptr;
+    e = cudaStreamEndCapture(lb->cap_body, &bout);
+    if (e == cudaSuccess && B.err != cudaSuccess) e = B.err;
+    if (e != cudaSuccess) break;
+    R.metric_gram();
+    R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
+    R.trace_grad();
+    R.update(UP_EXPLICIT, dummy);
+  }
+  if (L == 0) {
+    R.metric_gram();
+    R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
+  }
+  R.metric_gram();
+  R.chol(CH_ENERGY, nullptr, lb->logdet1, lb->quad1, nullptr);
+  R.check(launch_logdensity_grad<float>(lb->t, lb->qf, lb->ldnew, lb->gnew, nullptr, C, s));
+  InfoDev<float> inf{};
+  inf.acc_rate = lb->acc_s;
+  inf.accepted = lb->accepted_s;
+  inf.divergent = lb->divergent_s;
+  inf.energy = lb->energy_s;
+  inf.fp_iters = lb->fpit_s;
+  inf.status = lb->status_s;
+  inf.momentum = nullptr;
+  accept_kernel<<<(C + 127) / 128, 128, 0, s>>>(
+      C, d, lb->ld_s, lb->quad0, lb->logdet0, lb->ldnew, lb->quad1, lb->logdet1, lb->u_s, 0.0,
+      lb->spd, lb->qf, lb->gnew, lb->pos_s, lb->grad_s, lb->ld_s, inf, lb->iters_total,
+      lb->notconv, lb->bad);
+  R.check(cudaGetLastError());
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return graph_fail("conditional node", e);
+  }
+  if (e2 != cudaSuccess) return graph_fail("end", e2);
+  if (R.err != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return graph_fail("kernels", R.err);
+  }
+  e = cudaGraphInstantiate(&lb->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    lb->gexec = nullptr;
+    return graph_fail("instantiate", e);
+  }
+  lb->g_L = L;
+  lb->g_impl = impl;
+  lb->g_chol = lb->chol_fp64;
+  return GJ_OK;
+}
+
+template <typename Tp>
+void copy_out(Tp* dst, const Tp* src, size_t n, cudaStream_t st, cudaError_t* err) {
+  if (!dst || *err != cudaSuccess) return;
+  *err = cudaMemcpyAsync(dst, src, n * sizeof(Tp), cudaMemcpyDeviceToDevice, st);
+}
+
+}  // namespace
+
+int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
+                                    double* logdens, const float* z, const double* u,
+                                    const InfoDev<float>& info, int gemm_impl, cudaStream_t st) {
+  if (gemm_impl == 2 && !lb->tc_ok) {
+    g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
+    return GJ_ENOTSUP;
+  }
+  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64) {
+    // the capture streams must not see unfinished work of the caller's stream
+    cudaStreamSynchronize(st);
+    const int rc = build_graph(lb, sp.L, gemm_impl);
+    if (rc) return rc;
+  }
+  const int C = lb->C, d = lb->d;
+  lb->stats = LogregStats{};
+  set_step_kernel<<<1, 1, 0, st>>>(lb->spd, sp);
+  cudaError_t e = cudaGetLastError();
+  copy_out(lb->pos_s, pos, (size_t)C * d, st, &e);
+  copy_out(lb->grad_s, grad, (size_t)C * d, st, &e);
+  copy_out(lb->ld_s, logdens, (size_t)C, st, &e);
+  copy_out(lb->z_s, z, (size_t)C * d, st, &e);
+  copy_out(lb->u_s, u, (size_t)C, st, &e);
+  if (e == cudaSuccess) e = cudaGraphLaunch(lb->gexec, st);
+  copy_out(pos, lb->pos_s, (size_t)C * d, st, &e);
+  copy_out(grad, lb->grad_s, (size_t)C * d, st, &e);
+  copy_out(logdens, lb->ld_s, (size_t)C, st, &e);
+  copy_out(info.acc_rate, lb->acc_s, (size_t)C, st, &e);
+  copy_out(info.accepted, lb->accepted_s, (size_t)C, st, &e);
+  copy_out(info.divergent, lb->divergent_s, (size_t)C, st, &e);
+  copy_out(info.energy, lb->energy_s, (size_t)C, st, &e);
+  copy_out(info.fp_iters, lb->fpit_s, (size_t)C, st, &e);
+  copy_out(info.status, lb->status_s, (size_t)C, st, &e);
+  copy_out(info.momentum, lb->mom_s, (size_t)C * d, st, &e);
+  if (e != cudaSuccess) {
+    g_err = std::string("graph step: ") + cudaGetErrorString(e);
+    return GJ_ECUDA;
+  }
+  lb->stats.other_launches = 1;  // one graph launch (its kernels are counted by the caller)
+  return GJ_OK;
+}
+
+static __global__ void split_rows_kernel(const float* X, int R, int K, SplitMat S) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)R * K) return;
+  split_store(S, (int)(i / K), (int)(i % K), X[i]);
+}
+
+int gemm_split_test(int impl, int planes, int M, int N, int K, const float* A, const float* B,
+                    float* D, cudaStream_t st) {
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !D || (planes != 2 && planes != 3)) {
+    g_err = "bad GEMM test arguments";
+    return GJ_EINVAL;
+  }
+  LogregBatched tmp;
+  bool ok = true;
+  SplitMat a = make_split(&tmp, M, K, planes, &ok);
+  SplitMat b = make_split(&tmp, N, K, planes, &ok);
+  int* err = dalloc<int>(1, tmp.owned, &ok);
+  int rc = GJ_OK;
+  if (!ok) {
+    g_err = "device allocation failed";
+    rc = GJ_ENOMEM;
+  }
+  TcOperand *ta = nullptr, *tb = nullptr;
+  if (!rc) {
+    cudaDeviceSynchronize();  // the scratch memsets run on the legacy stream
+    split_rows_kernel<<<(unsigned)(((size_t)M * K + 255) / 256), 256, 0, st>>>(A, M, K, a);
+    split_rows_kernel<<<(unsigned)(((size_t)N * K + 255) / 256), 256, 0, st>>>(B, N, K, b);
+    GemmArgs g;
+    g.A = a;
+    g.B = b;
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.epi = Epi{};
+    g.epi.mode = EPI_STORE;
+    g.epi.D = D;
+    g.epi.ldd = N;
+    cudaError_t e = cudaSuccess;
+    if (impl == 2) {
+      const char* msg = "tcgen05 unavailable";
+      if (tc_available() && gemm_tc_prepare() == cudaSuccess) {
+        ta = tc_operand_create(a, 0, &msg);
+        tb = tc_operand_create(b, 0, &msg);
+      }
+      if (!ta || !tb) {
+        g_err = msg;
+        rc = GJ_ENOTSUP;
+      } else {
+        e = gemm_tc(g, ta, tb, err, st);
+      }
+    } else {
+      e = gemm_simt(g, st);
+    }
+    if (!rc) {
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      int herr = 0;
+      if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        g_err = std::string("GEMM test: ") + cudaGetErrorString(e);
+        rc = GJ_ECUDA;
+      } else if (herr) {
+        g_err = "tcgen05 GEMM wait timed out (code " + std::to_string(herr) + ")";
+        rc = GJ_ECUDA;
+      }
+    }
+  }
+  if (ta) tc_operand_destroy(ta);
+  if (tb) tc_operand_destroy(tb);
+  for (void* p : tmp.owned) cudaFree(p);
+  tmp.owned.clear();
+  return rc;
+}
+
+}  // namespace gj

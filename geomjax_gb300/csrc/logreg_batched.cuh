@@ -1,0 +1,48 @@
+// Batched dense-Fisher logistic-regression RMHMC (implicit midpoint), mixed
+// precision.  See logreg_batched.cu.
+#pragma once
+
+#include "common.cuh"
+
+namespace gj {
+
+struct LogregBatched;
+
+int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out);
+void logreg_batched_destroy(LogregBatched* lb);
+const char* logreg_batched_error();
+
+// gemm_impl: 1 = SIMT FP32 GEMM over the BF16 hi/lo planes, 2 = tcgen05.
+// chol_fp64: 1 = metric Cholesky / solves in float64 (default), 0 = float32.
+int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
+                              double* logdens, const float* z, const double* u,
+                              const InfoDev<float>& info, int gemm_impl, cudaStream_t st);
+
+// Same transition as one CUDA-graph launch: every fixed-point solve is a
+// conditional WHILE node driven by the device-side count of active chains
+// (no host synchronisation inside the step).  The graph is captured on the
+// first call and again when the number of steps, the GEMM implementation or
+// the factorisation precision changes; step size, tolerance, iteration cap
+// and divergence threshold are read from device memory at run time.
+int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
+                                    double* logdens, const float* z, const double* u,
+                                    const InfoDev<float>& info, int gemm_impl, cudaStream_t st);
+
+// Last-step statistics of the batched path (host-side counters).
+struct LogregStats {
+  long long evals;           // fixed-point map evaluations issued (all chains)
+  long long gemm_launches;   // GEMM kernels launched
+  long long other_launches;  // other kernels launched
+  double gemm_flops;         // algorithmic flops of the GEMMs issued
+  double gemm_ns;            // GPU time of the GEMM launches (profiling on)
+};
+LogregStats logreg_batched_stats(const LogregBatched* lb);
+void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);
+void logreg_batched_set_profile(LogregBatched* lb, int on);
+
+// D[M, N] = A[M, K]·B[N, K]ᵀ through the split-BF16 GEMM `impl` (test hook;
+// allocates scratch and synchronises the stream).
+int gemm_split_test(int impl, int planes, int M, int N, int K, const float* A, const float* B,
+                    float* D, cudaStream_t st);
+
+}  // namespace gj

@@ -1,0 +1,205 @@
+/*
+ * geomjax_gb300 — C ABI of the GB300-native sampler hot path.
+ *
+ * Every entry point replaces one call of the reference's pure-function kernel
+ * API (williwilliams3/geomjax, Python/JAX):
+ *
+ *   gj_rmhmc_step     replaces kernel(rng_key, state, logdensity_fn, step_size,
+ *                      metric_fn, num_integration_steps)
+ *                      geomjax/rmhmc/rmhmc.py:131-174 (+ rmhmc_proposal :376-440)
+ *   gj_lmcmonge_step  replaces kernel(rng_key, state, logdensity_fn, step_size,
+ *                      inverse_mass_matrix, num_integration_steps, alpha2)
+ *                      geomjax/lmcmonge/lmc.py:151-236 (+ lmc_proposal :472-536)
+ *   gj_lmc_step       replaces kernel(rng_key, state, logdensity_fn, step_size,
+ *                      metric_fn, num_integration_steps)
+ *                      geomjax/lmcmc/lmc.py:135-180 (+ lmc_proposal :411-476)
+ *   gj_init           replaces init(position, logdensity_fn)
+ *                      geomjax/rmhmc/rmhmc.py:96-98, lmcmonge/lmc.py:101-109,
+ *                      lmcmc/lmc.py:98-101 (value_and_grad at the position)
+ *   gj_logdensity_grad / gj_hvp / gj_metric
+ *                      the operators the reference obtains by autodiff of the
+ *                      user's logdensity_fn / metric_fn:
+ *                      jax.value_and_grad (rmhmc/integrators.py:111),
+ *                      util.hvp = jvp(grad f) (util.py:120-121),
+ *                      metric_fn (rmhmc/metrics.py:42-58)
+ *
+ * The reference's user-supplied Python callables become a registered device
+ * target family (gj_target).  The reference draws its randomness from a JAX
+ * key (key_momentum -> normal, key_integrator -> bernoulli,
+ * rmhmc/rmhmc.py:158-161, mcmc/proposal.py:178); here the caller passes the
+ * standard normals z[C, d] and the uniforms u[C] explicitly, and the accept
+ * is u < min(exp(H0 - H1), 1) exactly as jax.random.bernoulli.
+ *
+ * Conventions
+ *   - All array pointers are DEVICE pointers owned by the caller; row-major,
+ *     chains first: position[C, d].  Per-chain scalars are float64.
+ *   - precision GJ_FP64: every vector is float64 ("plain FP64 form").
+ *     precision GJ_MIXED: vectors and target data are float32; FP64 is kept
+ *     for the metric Cholesky/log-det/solves, the fixed-point convergence
+ *     norm and the Hamiltonian difference.
+ *   - Calls are stream-ordered on `stream` (a cudaStream_t, NULL = legacy
+ *     default stream) and never synchronise the host, except where a
+ *     comment says so.  A context is not thread-safe: one host thread per
+ *     context.
+ *   - Return value: a gj_status.  Numerical trouble never raises: it shows up
+ *     per chain (NaN energy -> rejected, divergence flag, fixed-point
+ *     non-convergence bit in gj_info.status), as in the reference.
+ */
+#ifndef GEOMJAX_GB300_H
+#define GEOMJAX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GJ_OK = 0,
+  GJ_EINVAL = 1,   /* bad shape / pointer / enum value */
+  GJ_ENOTSUP = 2,  /* combination not built (e.g. dense metric above the size limit) */
+  GJ_ECUDA = 3,    /* a CUDA runtime call failed; see gj_last_error() */
+  GJ_ENOMEM = 4
+} gj_status;
+
+typedef enum { GJ_FUNNEL = 1, GJ_LOGREG = 2, GJ_HIERGAUSS = 3 } gj_family;
+
+typedef enum {
+  GJ_METRIC_DIAG_FISHER = 1,  /* funnel: diag(e^-v .., 1/s^2 + (D-1)/2) */
+  GJ_METRIC_DENSE_FISHER = 2, /* logreg: X^T Lambda X + I/s^2 ; hier: arrowhead Fisher */
+  GJ_METRIC_PULLBACK = 3,     /* funnel: J^-T J^-1 (examples/funnel/main.py:41-54) */
+  GJ_METRIC_IDENTITY = 4      /* G = I (tests/test_samplers.py:25) */
+} gj_metric_kind;
+
+typedef enum { GJ_FP64 = 0, GJ_MIXED = 1 } gj_precision;
+
+typedef enum { GJ_IMPLICIT_MIDPOINT = 0, GJ_GENERALIZED_LEAPFROG = 1 } gj_integrator;
+
+typedef enum { GJ_SAMPLER_RMHMC = 0, GJ_SAMPLER_LMC = 1, GJ_SAMPLER_LMCMONGE = 2 } gj_sampler;
+
+/* per-chain status bits (gj_info.status) */
+#define GJ_CHAIN_FP_NOT_CONVERGED 0x1u /* a fixed-point solve stopped without reaching tol */
+#define GJ_CHAIN_NONFINITE 0x2u        /* the proposal energy was NaN/Inf */
+#define GJ_CHAIN_NOT_SPD 0x4u          /* a metric Cholesky met a non-positive pivot */
+
+/* A registered target family plus its data (device pointers). */
+typedef struct {
+  int32_t family;  /* gj_family */
+  int32_t metric;  /* gj_metric_kind */
+  int32_t dim;     /* d */
+  int32_t n_data;  /* logreg: N rows of X; hier: J groups; funnel: 0 */
+  const void* X;   /* logreg: X[N, d] (float32 for GJ_MIXED, float64 for GJ_FP64) */
+  const void* y;   /* logreg: labels[N]; hier: observations y[J] (same dtype as X) */
+  const void* s;   /* hier: observation scales sigma[J] (same dtype); else NULL */
+  double p0;       /* funnel: sigma (3); logreg: prior variance (100); hier: mu scale */
+  double p1;       /* hier: v scale; otherwise unused */
+} gj_target;
+
+/* Chain state (device pointers).  Dtype of position/grad follows precision. */
+typedef struct {
+  void* position;            /* [C, d] */
+  void* logdensity_grad;     /* [C, d] */
+  double* logdensity;        /* [C] */
+  double* volume_adjustment; /* [C] LMC / LMC-Monge only (may be NULL for RMHMC) */
+  int32_t num_chains;        /* C */
+} gj_chain_state;
+
+/* Per-transition information (device pointers, each may be NULL). */
+typedef struct {
+  double* acceptance_rate; /* [C] min(exp(H0 - H1), 1) */
+  uint8_t* is_accepted;    /* [C] */
+  uint8_t* is_divergent;   /* [C] -(H0 - H1) > divergence_threshold */
+  double* energy;          /* [C] H1, the proposal's energy */
+  int32_t* fp_iters;       /* [C] fixed-point iterations summed over the trajectory */
+  uint8_t* status;         /* [C] GJ_CHAIN_* bits */
+  void* momentum;          /* [C, d] the drawn momentum (RMHMC) or velocity (LMC) */
+} gj_info;
+
+typedef struct {
+  double step_size;
+  int32_t num_integration_steps;
+  int32_t integrator;          /* gj_integrator (RMHMC) */
+  int32_t max_iters;           /* fixed-point iteration cap (reference default 100) */
+  double tol;                  /* fixed-point tolerance (reference default 1e-6) */
+  double divergence_threshold; /* reference default 1000 */
+  double alpha2;               /* LMC-Monge alpha^2 (reference default 0.001) */
+  const void* inverse_mass;    /* LMC-Monge diagonal inverse mass [d] (state dtype); NULL = ones */
+  int32_t alpha2_fix;          /* LMC-Monge: 1 = multiply the Sherman-Morrison correction by
+                                  alpha^2 (the reference omits it, lmcmonge/integrators.py:186-189) */
+  int32_t reserved;
+} gj_step_params;
+
+typedef struct gj_ctx gj_ctx;
+
+/* Version and last error message of the calling thread. */
+int32_t gj_version(void);
+const char* gj_last_error(void);
+
+/* A context binds one target, sampler and precision to a chain count and owns
+ * the device workspaces of the batched paths.  It allocates device memory
+ * (cudaMalloc) at creation and on the first step that needs a workspace;
+ * gj_destroy frees it.  The target's data pointers must outlive the context. */
+int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
+                  int32_t num_chains, gj_ctx** out);
+int32_t gj_destroy(gj_ctx* ctx);
+
+/* Selects the implementation of the dense-Fisher logistic-regression RMHMC
+ * path in GJ_MIXED: 0 = automatic (batched tensor-core pipeline),
+ * 1 = batched pipeline with the SIMT FP32 GEMM, 2 = batched pipeline with the
+ * tcgen05 BF16 hi/lo GEMM, 3 = per-chain kernel. */
+int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
+#define GJ_OPT_LOGREG_PATH 1
+#define GJ_OPT_THREADS_PER_BLOCK 2
+/* batched path loop driver: 0 = one CUDA-graph launch per transition with
+ * conditional WHILE nodes for the fixed-point solves (default), 1 = host
+ * loop that reads the active-chain count back after every iteration */
+#define GJ_OPT_LOOP 3
+/* batched path metric factorisation: 1 = float64 Cholesky / log det /
+ * solves (default), 0 = float32 */
+#define GJ_OPT_CHOL_FP64 4
+
+/* value_and_grad of the log density at state->position; zeroes
+ * volume_adjustment when present. */
+int32_t gj_init(gj_ctx* ctx, gj_chain_state* state, void* stream);
+
+int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_state* state,
+                      const void* z, const double* u, gj_info* info, void* stream);
+int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_state* state,
+                         const void* z, const double* u, gj_info* info, void* stream);
+int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_state* state,
+                    const void* z, const double* u, gj_info* info, void* stream);
+
+/* Counters of the last step on this context: out[0] fixed-point map
+ * evaluations, out[1] GEMM launches, out[2] other kernel launches,
+ * out[3] algorithmic GEMM flops, out[4] GPU time of the GEMM launches in
+ * nanoseconds (only while profiling is on).  Returns the number written
+ * (<= n).  No counterpart in the reference (measurement only). */
+int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n);
+/* 1 = bracket every GEMM launch with CUDA events so gj_stats reports their
+ * GPU time (the step then synchronises at its end); 0 = off (default).
+ * No counterpart in the reference (measurement only). */
+int32_t gj_profile(gj_ctx* ctx, int32_t on);
+
+/* Test hook of the batched contraction (no counterpart in the reference):
+ * D[M, N] = A[M, K] · B[N, K]ᵀ for float32 device arrays A, B, D, computed
+ * from `planes` (2 or 3) split-BF16 planes per operand with FP32
+ * accumulation by impl 1 (SIMT) or impl 2 (tcgen05).  Allocates and frees
+ * device scratch; synchronises the stream. */
+int32_t gj_gemm_split_bf16(int32_t impl, int32_t planes, int32_t M, int32_t N, int32_t K,
+                           const float* A, const float* B, float* D, void* stream);
+
+/* Operator-level entry points (no context).  q, grad, u, out: [C, d];
+ * logdensity: [C] float64; metric_out: [C, d] (diagonal metrics) or
+ * [C, d, d] (dense), dtype of the precision. */
+int32_t gj_logdensity_grad(const gj_target* target, int32_t precision, int32_t num_chains,
+                           const void* q, double* logdensity, void* grad, void* stream);
+int32_t gj_hvp(const gj_target* target, int32_t precision, int32_t num_chains, const void* q,
+               const void* u, void* out, void* stream);
+int32_t gj_metric(const gj_target* target, int32_t precision, int32_t num_chains,
+                  const void* q, void* metric_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEOMJAX_GB300_H */

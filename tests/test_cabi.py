@@ -1,0 +1,92 @@
+"""The C-ABI library loads and exports every symbol the header declares; host
+argument checks reject bad inputs without touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from geomjax_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_symbols():
+    text = open(os.path.join(ROOT, "include", "geomjax_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int32_t|const char\*)\s+(gj_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_header_symbol():
+    lib = L.load()
+    syms = _header_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(lib, s), s
+        assert s in L.SIGNATURES, f"{s} has no ctypes signature"
+
+
+def test_version_and_error_strings():
+    lib = L.load()
+    assert lib.gj_version() >= 100
+    assert isinstance(lib.gj_last_error(), bytes)
+
+
+def test_struct_layouts_match_c(tmp_path):
+    """ctypes layouts equal the C compiler's (offsetof / sizeof of the header)."""
+    import shutil
+    import subprocess
+
+    ours = (ctypes.sizeof(L.GjTarget), L.GjStepParams.tol.offset, L.GjStepParams.inverse_mass.offset,
+            ctypes.sizeof(L.GjStepParams), ctypes.sizeof(L.GjChainState), ctypes.sizeof(L.GjInfo))
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        assert ours == (56, 24, 48, 64, 40, 56)
+        return
+    src = tmp_path / "off.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "geomjax_gb300.h"\n'
+        'int main(){printf("%zu %zu %zu %zu %zu %zu", sizeof(gj_target), offsetof(gj_step_params,tol),'
+        ' offsetof(gj_step_params,inverse_mass), sizeof(gj_step_params), sizeof(gj_chain_state),'
+        ' sizeof(gj_info));}\n')
+    exe = tmp_path / "off"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = tuple(int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                               check=True).stdout.split())
+    assert got == ours
+
+
+def test_argument_checks_without_gpu():
+    lib = L.load()
+    h = ctypes.c_void_p()
+    bad = L.GjTarget(99, 1, 2, 0, None, None, None, 3.0, 0.0)
+    assert lib.gj_create(ctypes.byref(bad), 0, 0, 4, ctypes.byref(h)) == L.GJ_EINVAL
+    assert b"family" in lib.gj_last_error()
+    t = L.GjTarget(L.GJ_FUNNEL, L.GJ_METRIC_DIAG_FISHER, 1, 0, None, None, None, 3.0, 0.0)
+    assert lib.gj_create(ctypes.byref(t), 0, 0, 4, ctypes.byref(h)) == L.GJ_EINVAL
+    t = L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 5, 10, None, None, None, 100.0, 0.0)
+    assert lib.gj_create(ctypes.byref(t), 0, 1, 4, ctypes.byref(h)) == L.GJ_EINVAL
+    t = L.GjTarget(L.GJ_FUNNEL, L.GJ_METRIC_DIAG_FISHER, 3, 0, None, None, None, 3.0, 0.0)
+    assert lib.gj_create(ctypes.byref(t), 7, 0, 4, ctypes.byref(h)) == L.GJ_EINVAL
+    assert lib.gj_create(ctypes.byref(t), 0, 0, 0, ctypes.byref(h)) == L.GJ_EINVAL
+    # a valid context is pure host state until the first step
+    assert lib.gj_create(ctypes.byref(t), 0, 0, 4, ctypes.byref(h)) == L.GJ_OK
+    st = L.GjChainState(None, None, None, None, 4)
+    p = L.GjStepParams(0.1, 10, 0, 100, 1e-6, 1000.0, 0.0, None, 0, 0)
+    assert lib.gj_rmhmc_step(h, ctypes.byref(p), ctypes.byref(st), None, None, None, None) == L.GJ_EINVAL
+    assert lib.gj_lmc_step(h, ctypes.byref(p), ctypes.byref(st), None, None, None, None) == L.GJ_EINVAL
+    p.num_integration_steps = -1
+    assert lib.gj_set_option(h, 999, 0) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_LOGREG_PATH, 9) == L.GJ_EINVAL
+    assert lib.gj_gemm_split_bf16(3, 2, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
+    assert lib.gj_gemm_split_bf16(1, 4, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
+    assert lib.gj_destroy(h) == L.GJ_OK
+
+
+def test_no_cpu_fallback():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import geomjax_gb300 as gj
+
+    with pytest.raises(L.GeomjaxError):
+        gj.funnel(D=2, precision="fp64", device="cpu").logdensity_and_grad([[0.0, 0.0]])
