@@ -7,6 +7,7 @@
 #include <string>
 
 #include "chain_kernels.cuh"
+#include "gemm.cuh"
 #include "logreg_batched.cuh"
 
 namespace {

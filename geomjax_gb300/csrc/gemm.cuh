@@ -6,6 +6,7 @@
 // a SIMT FP32 kernel (gemm_simt.cu) and the tcgen05/TMA kernel (gemm_tc.cu).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -59,12 +60,19 @@ struct Epi {
   const float* S;
   int s_ld;
   int r_off;
+  // EPI_SIGMOID, when set: ld_acc[m] += Σ_n [y_n a − log(1 + e^a)] (FP64 sum)
+  double* ld_acc;
 };
+
+__device__ __forceinline__ float softplus(float a) {
+  return a > 0.f ? a + log1pf(__expf(-a)) : log1pf(__expf(a));
+}
 
 __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
   if (e.mode == EPI_STORE) {
     e.D[(size_t)m * e.ldd + n] = v;
   } else if (e.mode == EPI_SIGMOID) {
+    if (e.ld_acc) atomicAdd(&e.ld_acc[m], double(e.y[n] * v - softplus(v)));
     const float sg = 1.f / (1.f + __expf(-v));
     const float lam = sg * (1.f - sg);
     split_store(e.lam, m, n, lam);
@@ -105,6 +113,16 @@ __device__ __forceinline__ void split_store8(const SplitMat& s, int r, int k, co
 // element-wise otherwise.
 __device__ __forceinline__ void epi_row32(const Epi& e, int m, int n0, int N, const float* v) {
   const bool full = n0 + 32 <= N;
+  if (e.mode == EPI_SIGMOID && e.ld_acc) {
+    double acc = 0.0;
+    for (int j = 0; j < 32; ++j)
+      if (n0 + j < N) acc += double(e.y[n0 + j] * v[j] - softplus(v[j]));
+    atomicAdd(&e.ld_acc[m], acc);
+    Epi e2 = e;
+    e2.ld_acc = nullptr;
+    epi_row32(e2, m, n0, N, v);
+    return;
+  }
   if (!full || (e.mode == EPI_STORE && (e.ldd & 3)) ||
       (e.mode != EPI_STORE && ((e.lp_ld & 3) || (e.mode == EPI_TRACE && (e.s_ld & 3))))) {
     for (int j = 0; j < 32; ++j)
@@ -158,12 +176,18 @@ struct GemmArgs {
 cudaError_t gemm_simt(const GemmArgs& g, cudaStream_t st);
 
 // tcgen05 path: tensor maps are built once per operand buffer.
-struct TcOperand;  // opaque (holds a CUtensorMap)
+struct TcOperand {
+  CUtensorMap map;
+  SplitMat s;
+};
+// Encodes the operand's tensor map in place (no allocation); false on error.
+bool tc_operand_init(TcOperand* op, const SplitMat& s, const char** err);
 TcOperand* tc_operand_create(const SplitMat& s, int box_rows, const char** err);
 void tc_operand_destroy(TcOperand* op);
 bool tc_available();
 cudaError_t gemm_tc_prepare();  // raises the kernel's shared-memory limit (call before capture)
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
+
 
 }  // namespace gj

@@ -21,11 +21,6 @@
 
 namespace gj {
 
-struct TcOperand {
-  CUtensorMap map;
-  SplitMat s;
-};
-
 namespace {
 
 constexpr int BM = 128, BN = 128, BK = 64;
@@ -279,18 +274,17 @@ bool tc_available() {
   return major == 10 && get_encode() != nullptr;
 }
 
-TcOperand* tc_operand_create(const SplitMat& s, int, const char** err) {
+bool tc_operand_init(TcOperand* op, const SplitMat& s, const char** err) {
   EncodeTiledFn enc = get_encode();
   if (!enc) {
     *err = "cuTensorMapEncodeTiled unavailable";
-    return nullptr;
+    return false;
   }
   if ((s.ld % 64) || (s.rpad % 128) || (reinterpret_cast<uintptr_t>(s.p) & 15) ||
       (s.planes != 2 && s.planes != 3)) {
     *err = "split matrix not padded for TMA";
-    return nullptr;
+    return false;
   }
-  TcOperand* op = new TcOperand();
   op->s = s;
   cuuint64_t dims[2] = {(cuuint64_t)s.ld, (cuuint64_t)s.planes * s.rpad};
   cuuint64_t strides[1] = {(cuuint64_t)s.ld * 2};
@@ -301,6 +295,14 @@ TcOperand* tc_operand_create(const SplitMat& s, int, const char** err) {
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     *err = "cuTensorMapEncodeTiled failed";
+    return false;
+  }
+  return true;
+}
+
+TcOperand* tc_operand_create(const SplitMat& s, int, const char** err) {
+  TcOperand* op = new TcOperand();
+  if (!tc_operand_init(op, s, err)) {
     delete op;
     return nullptr;
   }

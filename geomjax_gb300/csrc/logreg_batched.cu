@@ -89,6 +89,16 @@ struct CholArgs {
   float* mom_info;     // DRAW: info.momentum (may be NULL)
 };
 
+// Shared-memory layout per CTA: the packed lower-triangle pair table
+// (column-major: (i, k) for k = 0.., i = k..d-1) used to spread triangle
+// updates over lanes, then per warp the factor L (d x d, F), two F vectors,
+// and L⁻¹ (d x d, float).
+__host__ __device__ inline size_t chol_smem_bytes(int d, int warps, size_t fsz) {
+  const size_t pairs = (size_t)d * (d + 1) / 2;
+  const size_t tab = ((pairs * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
+  return tab + (size_t)warps * (((size_t)d * d + 2 * d) * fsz + (size_t)d * d * sizeof(float));
+}
+
 template <typename F>  // factorisation type: double (default) or float
 __global__ void chol_kernel(CholArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -96,15 +106,28 @@ __global__ void chol_kernel(CholArgs a) {
   const int nwarps = blockDim.x >> 5;
   const int c = blockIdx.x * nwarps + warp;
   const int d = a.d;
-  F* L = reinterpret_cast<F*>(smem_raw) + (size_t)warp * (d * d + 2 * d);
+  const int P = a.P;
+  uint16_t* tab = reinterpret_cast<uint16_t*>(smem_raw);  // tab[2t] = i, tab[2t+1] = k
+  const size_t tabb = (((size_t)P * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
+  F* L = reinterpret_cast<F*>(smem_raw + tabb) + (size_t)warp * (d * d + 2 * d);
   F* y = L + d * d;
   F* xv = y + d;
-  float* Li = reinterpret_cast<float*>(reinterpret_cast<F*>(smem_raw) + (size_t)nwarps * (d * d + 2 * d)) +
+  float* Li = reinterpret_cast<float*>(reinterpret_cast<F*>(smem_raw + tabb) +
+                                       (size_t)nwarps * (d * d + 2 * d)) +
               (size_t)warp * d * d;
+  // column-major pair table (all threads of the CTA)
+  for (int t = threadIdx.x; t < d; t += blockDim.x) {
+    int off = t * d - t * (t - 1) / 2;  // start of column t
+    for (int i = t; i < d; ++i, ++off) {
+      tab[2 * off] = (uint16_t)i;
+      tab[2 * off + 1] = (uint16_t)t;
+    }
+  }
+  __syncthreads();
   if (c >= a.C) return;
   if (a.mode == CH_EVAL && a.active && !a.active[c]) return;
-  // unpack G = Gvec + I/s²
-  for (int idx = lane; idx < a.P; idx += 32) {
+  // unpack G = Gvec + I/s² (Gvec is row-major over the upper triangle)
+  for (int idx = lane; idx < P; idx += 32) {
     int j = 0, rem = idx;
     while (rem >= d - j) {
       rem -= d - j;
@@ -116,56 +139,60 @@ __global__ void chol_kernel(CholArgs a) {
     L[k * d + j] = g;  // lower triangle
   }
   __syncwarp();
-  // left-looking Cholesky, lanes over rows
+  // right-looking Cholesky: scale column j, then the trailing triangle
+  // (i, k), j < k <= i, spread over the lanes through the pair table
   bool bad = false;
   double logdet = 0.0;
+  int col_start = 0;  // packed offset of column j
   for (int j = 0; j < d; ++j) {
-    F s = 0;
-    for (int k = lane; k < j; k += 32) s += L[j * d + k] * L[j * d + k];
-    s = warp_sum(s);
-    F djj = L[j * d + j] - s;
+    F djj = L[j * d + j];
     if (!(djj > F(0))) {
       bad = true;
       djj = F(NAN);
     }
     const F ljj = sqrt(djj);
     logdet += 2.0 * log(double(ljj));
+    const F inv = F(1) / ljj;
     __syncwarp();
     if (lane == 0) L[j * d + j] = ljj;
-    const F inv = F(1) / ljj;
-    for (int i = j + 1 + lane; i < d; i += 32) {
-      F t = L[i * d + j];
-      for (int k = 0; k < j; ++k) t -= L[i * d + k] * L[j * d + k];
-      L[i * d + j] = t * inv;
+    for (int i = j + 1 + lane; i < d; i += 32) L[i * d + j] *= inv;
+    __syncwarp();
+    const int tstart = col_start + (d - j);  // first pair of column j + 1
+    for (int t = tstart + lane; t < P; t += 32) {
+      const int i = tab[2 * t], k = tab[2 * t + 1];
+      L[i * d + k] -= L[i * d + j] * L[k * d + j];
     }
+    col_start = tstart;
     __syncwarp();
   }
   if (lane == 0) {
     a.logdet[c] = logdet;
     if (bad) a.bad[c] = 1;
   }
-  // right-hand side: DRAW p = L z (and y = L⁻¹p = z); otherwise y = L⁻¹ p
+  // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
+  // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
     for (int i = lane; i < d; i += 32) y[i] = F(a.z[(size_t)c * d + i]);
     __syncwarp();
     double zz = 0.0;
     for (int i = lane; i < d; i += 32) {
-      F s = 0;
-      for (int k = 0; k <= i; ++k) s += L[i * d + k] * y[k];
-      a.p0[(size_t)c * d + i] = double(s);
-      a.pc[(size_t)c * d + i] = double(s);
-      if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(s);
+      F sacc = 0;
+      for (int k = 0; k <= i; ++k) sacc += L[i * d + k] * y[k];
+      a.p0[(size_t)c * d + i] = double(sacc);
+      a.pc[(size_t)c * d + i] = double(sacc);
+      if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
       zz += double(y[i]) * double(y[i]);
     }
     zz = warp_sum(zz);
     if (lane == 0) a.quad[c] = zz;
   } else {
-    // forward substitution, one row at a time, lane-parallel dot products
-    for (int i = 0; i < d; ++i) {
-      F s = 0;
-      for (int k = lane; k < i; k += 32) s += L[i * d + k] * y[k];
-      s = warp_sum(s);
-      if (lane == 0) y[i] = (F(a.pc[(size_t)c * d + i]) - s) / L[i * d + i];
+    for (int i = lane; i < d; i += 32) y[i] = F(a.pc[(size_t)c * d + i]);
+    __syncwarp();
+    for (int j = 0; j < d; ++j) {
+      const F yj = y[j] / L[j * d + j];
+      __syncwarp();
+      if (lane == 0) y[j] = yj;
+      for (int i = j + 1 + lane; i < d; i += 32) y[i] -= L[i * d + j] * yj;
       __syncwarp();
     }
     if (a.mode == CH_ENERGY) {
@@ -177,38 +204,45 @@ __global__ void chol_kernel(CholArgs a) {
     }
   }
   __syncwarp();
-  // u = L⁻ᵀ y (backward substitution)
-  for (int i = d - 1; i >= 0; --i) {
-    F s = 0;
-    for (int k = i + 1 + lane; k < d; k += 32) s += L[k * d + i] * xv[k];
-    s = warp_sum(s);
-    if (lane == 0) xv[i] = (y[i] - s) / L[i * d + i];
+  // u = L⁻ᵀ y, column-oriented backward substitution
+  for (int i = lane; i < d; i += 32) xv[i] = y[i];
+  __syncwarp();
+  for (int j = d - 1; j >= 0; --j) {
+    const F xj = xv[j] / L[j * d + j];
+    __syncwarp();
+    if (lane == 0) xv[j] = xj;
+    for (int i = lane; i < j; i += 32) xv[i] -= L[j * d + i] * xj;
     __syncwarp();
   }
   for (int i = lane; i < d; i += 32) {
     a.u[(size_t)c * d + i] = double(xv[i]);
     split_store(a.Ub, c, i, float(xv[i]));
   }
-  // L⁻¹ in FP32 (column per lane), then G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients
-  for (int col = lane; col < d; col += 32) {
-    Li[col * d + col] = float(F(1) / L[col * d + col]);
-    for (int i = col + 1; i < d; ++i) {
-      float s = 0.f;
-      for (int k = col; k < i; ++k) s += float(L[i * d + k]) * Li[k * d + col];
-      Li[i * d + col] = -s / float(L[i * d + i]);
-    }
-  }
+  // L⁻¹ in FP32: forward substitution of the identity, all columns at once
+  for (int t = lane; t < d * d; t += 32) Li[t] = ((t / d) == (t % d)) ? 1.f : 0.f;
   __syncwarp();
-  for (int idx = lane; idx < a.P; idx += 32) {
+  for (int k = 0; k < d; ++k) {
+    const float ikk = 1.f / float(L[k * d + k]);
+    for (int cc = lane; cc <= k; cc += 32) Li[k * d + cc] *= ikk;
+    __syncwarp();
+    const int w = k + 1, n = (d - k - 1) * w;
+    for (int t = lane; t < n; t += 32) {
+      const int i = k + 1 + t / w, cc = t % w;
+      Li[i * d + cc] -= float(L[i * d + k]) * Li[k * d + cc];
+    }
+    __syncwarp();
+  }
+  // G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients (row-major upper triangle)
+  for (int idx = lane; idx < P; idx += 32) {
     int j = 0, rem = idx;
     while (rem >= d - j) {
       rem -= d - j;
       ++j;
     }
     const int k = j + rem;
-    float s = 0.f;
-    for (int m = k; m < d; ++m) s += Li[m * d + j] * Li[m * d + k];
-    split_store(a.Giv, c, idx, (j == k) ? s : 2.f * s);
+    float sacc = 0.f;
+    for (int m = k; m < d; ++m) sacc += Li[m * d + j] * Li[m * d + k];
+    split_store(a.Giv, c, idx, (j == k) ? sacc : 2.f * sacc);
   }
 }
 
@@ -234,8 +268,10 @@ struct UpdArgs {
   int* n_active;
 };
 
+// one warp per chain, lanes over coordinates
 __global__ void update_kernel(UpdArgs a) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= a.C) return;
   if (a.mode == UP_FPN && !a.active[c]) return;
   const int d = a.d;
@@ -246,7 +282,7 @@ __global__ void update_kernel(UpdArgs a) {
   const double* ps = (a.mode == UP_EXPLICIT) ? a.pc : a.p0;
   double nrm = 0.0;
   bool nan = false;
-  for (int i = 0; i < d; ++i) {
+  for (int i = lane; i < d; i += 32) {
     const size_t o = (size_t)c * d + i;
     const double q = a.qc[o];
     const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
@@ -266,6 +302,9 @@ __global__ void update_kernel(UpdArgs a) {
     }
   }
   if (a.mode == UP_EXPLICIT) return;
+  nrm = warp_max(nrm);
+  nan = __any_sync(0xffffffffu, nan);
+  if (lane != 0) return;
   if (nan) nrm = NAN;
   const int it = (a.mode == UP_FP0) ? 0 : a.iters[c] + 1;
   a.iters[c] = it;
@@ -293,26 +332,31 @@ __global__ void begin_kernel(int C, int d, const float* pos, double* q0, double*
   bad[c] = 0;
 }
 
+// Accept: H = −ℓ + ½pᵀG⁻¹p + ½ log det G + d/2 log 2π (rmhmc/metrics.py:60-74,
+// mcmc/metrics.py:160-166), ℓ at the proposal = data row sums + the prior.
 __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q,
-                              const double* logdet0, const double* ld1, const double* quad1,
+                              const double* logdet0, const double* ldsum, const double* quad1,
                               const double* logdet1, const double* uacc, double div_thr,
-                              const StepDev* spd,
-                              const float* qf, const float* g1, float* pos, float* grad,
+                              const StepDev* spd, double prior_var, const double* qc,
+                              const float* Gout, int ldo, float* pos, float* grad,
                               double* logdens, InfoDev<float> info, const int* iters_total,
                               const uint8_t* notconv, const uint8_t* bad) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const double cst = 0.5 * d * kLog2Pi;
-  // K = ½pᵀG⁻¹p + ½ log det G + d/2 log 2π (rmhmc/metrics.py:60-74)
+  double qq = 0.0;
+  for (int i = 0; i < d; ++i) qq += qc[(size_t)c * d + i] * qc[(size_t)c * d + i];
+  const double ld1 = ldsum[c] - 0.5 * qq / prior_var - 0.5 * d * (kLog2Pi + log(prior_var));
   const double H0 = -ld0[c] + 0.5 * H0q[c] + 0.5 * logdet0[c] + cst;
-  const double H1 = -ld1[c] + 0.5 * quad1[c] + 0.5 * logdet1[c] + cst;
+  const double H1 = -ld1 + 0.5 * quad1[c] + 0.5 * logdet1[c] + cst;
   const AcceptOut a = metropolis(H0, H1, uacc[c], spd ? spd->div_threshold : div_thr);
   if (a.accept) {
     for (int i = 0; i < d; ++i) {
-      pos[(size_t)c * d + i] = qf[(size_t)c * d + i];
-      grad[(size_t)c * d + i] = g1[(size_t)c * d + i];
+      const double q = qc[(size_t)c * d + i];
+      pos[(size_t)c * d + i] = float(q);
+      grad[(size_t)c * d + i] = float(double(Gout[(size_t)c * ldo + i]) - q / prior_var);
     }
-    logdens[c] = ld1[c];
+    logdens[c] = ld1;
   }
   if (info.acc_rate) info.acc_rate[c] = a.p_acc;
   if (info.accepted) info.accepted[c] = a.accept;
@@ -512,7 +556,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   }
   {
     const int warps = d <= 32 ? 4 : 1;
-    const int smax = (int)((size_t)warps * ((d * d + 2 * d) * sizeof(double) + (size_t)d * d * sizeof(float)));
+    const int smax = (int)chol_smem_bytes(d, warps, sizeof(double));
     cudaError_t a1 = cudaFuncSetAttribute(chol_kernel<double>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     cudaError_t a2 = cudaFuncSetAttribute(chol_kernel<float>,
@@ -588,11 +632,13 @@ struct Runner {
     lb->stats.other_launches++;
   }
 
-  // metric at the current iterate: (1) and (2)
-  void metric_gram() {
+  // metric at the current iterate: (1) and (2); with ld_acc the Xβ epilogue
+  // also sums the data log likelihood per chain
+  void metric_gram(double* ld_acc = nullptr) {
     LogregBatched& L = *lb;
     Epi e{};
     e.mode = EPI_SIGMOID;
+    e.ld_acc = ld_acc;
     e.y = static_cast<const float*>(L.t.y);
     e.lam = L.Lam;
     e.lp = L.Lp;
@@ -631,7 +677,7 @@ struct Runner {
     const int d = L.d;
     const int warps = d <= 32 ? 4 : 1;
     const size_t fsz = L.chol_fp64 ? sizeof(double) : sizeof(float);
-    const size_t smem = (size_t)warps * ((d * d + 2 * d) * fsz + (size_t)d * d * sizeof(float));
+    const size_t smem = chol_smem_bytes(d, warps, fsz);
     const dim3 grid((L.C + warps - 1) / warps);
     // the dynamic shared-memory limit was raised at context creation
     if (L.chol_fp64)
@@ -665,6 +711,28 @@ struct Runner {
     gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
   }
 
+  // energy at the proposal: ℓ row sums, Gram, log det and ||L⁻¹p||², ∇ℓ
+  void energy() {
+    LogregBatched& L = *lb;
+    check(cudaMemsetAsync(L.ldnew, 0, sizeof(double) * L.C, st));
+    metric_gram(L.ldnew);
+    chol(CH_ENERGY, nullptr, L.logdet1, L.quad1, nullptr);
+    Epi o{};
+    o.mode = EPI_STORE;
+    o.D = L.Gout;
+    o.ldd = L.dpad;
+    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, L.C, L.d, L.N, o);
+  }
+
+  void accept(const double* ld0, const double* u, double div_thr, float* pos, float* grad,
+              double* logdens, const InfoDev<float>& info) {
+    LogregBatched& L = *lb;
+    accept_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(
+        L.C, L.d, ld0, L.quad0, L.logdet0, L.ldnew, L.quad1, L.logdet1, u, div_thr, spd,
+        L.t.p0, L.qc, L.Gout, L.dpad, pos, grad, logdens, info, L.iters_total, L.notconv, L.bad);
+    check(cudaGetLastError());
+  }
+
   void update(int mode, const StepDev& sp) {
     LogregBatched& L = *lb;
     UpdArgs a{};
@@ -691,7 +759,7 @@ struct Runner {
     a.Qb = L.Qb;
     a.n_active = L.n_active_d;
     a.spd = spd;
-    update_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(a);
+    update_kernel<<<(unsigned)(((size_t)L.C * 32 + 255) / 256), 256, 0, st>>>(a);
     check(cudaGetLastError());
   }
 };
@@ -751,16 +819,9 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
     R.metric_gram();
     R.chol(CH_DRAW, z, lb->logdet0, lb->quad0, info.momentum);
   }
-  // energy at the proposal: metric, log det, ||L⁻¹p||², ℓ and ∇ℓ (FP32, FP64 sum)
-  R.metric_gram();
-  R.chol(CH_ENERGY, nullptr, lb->logdet1, lb->quad1, nullptr);
-  R.check(launch_logdensity_grad<float>(lb->t, lb->qf, lb->ldnew, lb->gnew, nullptr, C, st));
-  accept_kernel<<<(C + 127) / 128, 128, 0, st>>>(
-      C, d, logdens, lb->quad0, lb->logdet0, lb->ldnew, lb->quad1, lb->logdet1, u,
-      sp.div_threshold, nullptr, lb->qf, lb->gnew, pos, grad, logdens, info, lb->iters_total,
-      lb->notconv,
-      lb->bad);
-  R.check(cudaGetLastError());
+  // energy at the proposal (3-plane Xβ row sums, Gram, log det, ∇ℓ) and accept
+  R.energy();
+  R.accept(logdens, u, sp.div_threshold, pos, grad, logdens, info);
   if (R.err == cudaSuccess && lb->prof && lb->ev_used) {
     R.check(cudaStreamSynchronize(st));
     double ns = 0.0;
@@ -871,9 +932,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
     R.metric_gram();
     R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
   }
-  R.metric_gram();
-  R.chol(CH_ENERGY, nullptr, lb->logdet1, lb->quad1, nullptr);
-  R.check(launch_logdensity_grad<float>(lb->t, lb->qf, lb->ldnew, lb->gnew, nullptr, C, s));
+  R.energy();
   InfoDev<float> inf{};
   inf.acc_rate = lb->acc_s;
   inf.accepted = lb->accepted_s;
@@ -882,11 +941,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
   inf.fp_iters = lb->fpit_s;
   inf.status = lb->status_s;
   inf.momentum = nullptr;
-  accept_kernel<<<(C + 127) / 128, 128, 0, s>>>(
-      C, d, lb->ld_s, lb->quad0, lb->logdet0, lb->ldnew, lb->quad1, lb->logdet1, lb->u_s, 0.0,
-      lb->spd, lb->qf, lb->gnew, lb->pos_s, lb->grad_s, lb->ld_s, inf, lb->iters_total,
-      lb->notconv, lb->bad);
-  R.check(cudaGetLastError());
+  R.accept(lb->ld_s, lb->u_s, 0.0, lb->pos_s, lb->grad_s, lb->ld_s, inf);
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(s, &g);
   if (e != cudaSuccess) {

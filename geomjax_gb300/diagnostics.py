@@ -15,7 +15,8 @@ import torch
 
 
 def _next_fast_len(n: int) -> int:
-    """Smallest 2^a 3^b 5^c >= n (scipy.fftpack.next_fast_len)."""
+    """Smallest 2^a 3^b 5^c >= n (scipy.fftpack.next_fast_len, which the
+    reference imports at diagnostics.py:18)."""
     best = None
     p5 = 1
     while p5 < 2 * n:
@@ -47,6 +48,8 @@ def effective_sample_size(x, chain_axis=0, sample_axis=1):
     M, N = x.shape[0], x.shape[1]
     if M < 2:
         raise ValueError("effective_sample_size needs two or more chains")
+    if N < 4:
+        raise ValueError("effective_sample_size needs at least four samples per chain")
     mean = x.mean(dim=1, keepdim=True)
     cen = x - mean
     m = _next_fast_len(2 * N)

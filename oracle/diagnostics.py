@@ -10,7 +10,7 @@ initial monotone sequence, τ̂ floored at 1/log10(MN), ESS = MN/τ̂).
 from __future__ import annotations
 
 import numpy as np
-from scipy.fft import next_fast_len
+from scipy.fftpack import next_fast_len  # the reference imports this one (diagnostics.py:18)
 
 
 def potential_scale_reduction(x, chain_axis=0, sample_axis=1):

@@ -57,7 +57,7 @@ def test_gemm_simt(M, N, K, planes):
     D = _run(1, planes, A, B).double()
     exact = A.double() @ B.double().T
     scale = (A.double().abs() @ B.double().abs().T)
-    assert torch.max((D - exact).abs() / scale).item() < (1e-4 if planes == 2 else 1e-6)
+    assert torch.max((D - exact).abs() / scale).item() < (1e-4 if planes == 2 else 4e-6)
 
 
 @pytest.mark.parametrize("planes", [2, 3])
@@ -73,4 +73,5 @@ def test_gemm_tcgen05(M, N, K, planes):
     # same split arithmetic: only FP32 accumulation order differs
     assert torch.max((D - ref).abs() / scale).item() < 2e-6
     exact = A.double() @ B.double().T
-    assert torch.max((D - exact).abs() / scale).item() < (1e-4 if planes == 2 else 1e-6)
+    # three planes: FP32-exact operands, the error is the FP32 accumulation
+    assert torch.max((D - exact).abs() / scale).item() < (1e-4 if planes == 2 else 4e-6)
