@@ -98,6 +98,8 @@ SIGNATURES = {
     "gj_hvp": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                          c_void_p]),
     "gj_metric": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "gj_metric_vjp": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
 }
 
 

@@ -360,4 +360,20 @@ int32_t gj_metric(const gj_target* target, int32_t precision, int32_t C, const v
   return cuda_status(e, "gj_metric");
 }
 
+int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t C, const void* q,
+                      const void* w, void* out, void* stream) {
+  int st = check_target(target, precision);
+  if (st) return st;
+  if (C < 1 || !q || !w || !out) return fail(GJ_EINVAL, "bad arrays");
+  const gj::TargetDev t = gj::to_dev(*target);
+  if (t.d > 32) return fail(GJ_ENOTSUP, "metric adjoint supports d <= 32");
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = precision == GJ_FP64
+                      ? gj::launch_metric_vjp<double>(t, (const double*)q, (const double*)w,
+                                                      (double*)out, C, cs)
+                      : gj::launch_metric_vjp<float>(t, (const float*)q, (const float*)w,
+                                                     (float*)out, C, cs);
+  return cuda_status(e, "gj_metric_vjp");
+}
+
 }  // extern "C"

@@ -649,6 +649,27 @@ __global__ void metric_kernel(TargetDev t, const T* q, T* out, int C) {
   for (int i = 0; i < n; ++i) out[(size_t)c * n + i] = T(G[i]);
 }
 
+// Adjoint of the metric operator: out_k = Σ_ab W_ab ∂G_ab/∂q_k (dense W is
+// d x d; for diagonal metrics W holds the d cotangents of G_a) — the
+// vector-Jacobian product the reference gets from jax.vjp of metric_fn.
+template <typename T, int DMAX>
+__global__ void metric_vjp_kernel(TargetDev t, const T* q, const T* W, T* out, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  const bool diag = metric_is_diag(t.metric);
+  const int nw = diag ? d : d * d;
+  T qq[DMAX];
+  double dG[DMAX * DMAX];
+  for (int i = 0; i < d; ++i) qq[i] = q[(size_t)c * d + i];
+  for (int k = 0; k < d; ++k) {
+    metric_deriv<T>(t, qq, k, dG);
+    double acc = 0.0;
+    for (int i = 0; i < nw; ++i) acc += double(W[(size_t)c * nw + i]) * dG[i];
+    out[(size_t)c * d + k] = T(acc);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
@@ -715,6 +736,13 @@ cudaError_t launch_metric(const TargetDev& t, const T* q, T* out, int C, cudaStr
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out, int C,
+                              cudaStream_t st) {
+  GJ_DISPATCH_DMAX(t.d, 32, metric_vjp_kernel<T, DM><<<grid_for(C, 128), 128, 0, st>>>(t, q, W, out, C));
+  return cudaGetLastError();
+}
+
 #define GJ_INST(T)                                                                               \
   template cudaError_t launch_rmhmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,  \
                                              const T*, const double*, const InfoDev<T>&, int,   \
@@ -729,7 +757,9 @@ cudaError_t launch_metric(const TargetDev& t, const T* q, T* out, int C, cudaStr
                                                  double*, int, cudaStream_t);                    \
   template cudaError_t launch_hvp<T>(const TargetDev&, const T*, const T*, T*, int,              \
                                      cudaStream_t);                                              \
-  template cudaError_t launch_metric<T>(const TargetDev&, const T*, T*, int, cudaStream_t);
+  template cudaError_t launch_metric<T>(const TargetDev&, const T*, T*, int, cudaStream_t);    \
+  template cudaError_t launch_metric_vjp<T>(const TargetDev&, const T*, const T*, T*, int,      \
+                                            cudaStream_t);
 
 // compiled once per precision (GJ_CHAIN_PREC = 1: float, 2: double) so the
 // two halves build in parallel

@@ -24,6 +24,9 @@ template <typename T>
 cudaError_t launch_hvp(const TargetDev& t, const T* q, const T* u, T* out, int C, cudaStream_t st);
 template <typename T>
 cudaError_t launch_metric(const TargetDev& t, const T* q, T* out, int C, cudaStream_t st);
+template <typename T>
+cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out, int C,
+                              cudaStream_t st);
 
 // warp-per-chain LMC-Monge (monge_warp.cu), float32 state
 cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,

@@ -9,8 +9,10 @@
 //               K = 16): the plane products A_i·B_j with i + j < planes per
 //               K step, and tcgen05.commit frees each stage / signals the
 //               accumulator
-//   warps 2-5   epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes
-//               32·(w%4) .. +31 = output rows), per-element epilogue
+//   warps 2-9   epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes
+//               32·(w%4) .. +31 = output rows; the two warps of a lane
+//               quarter take alternate 32-column chunks), staged through
+//               shared memory so every global access is a whole row
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in *err and skips the rest of its work, releasing TMEM before exit.
 #include <cuda.h>
@@ -137,8 +139,103 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Epilogue of one 32 x 32 chunk handled by one warp: lane l holds row
+// m_base + l (v[0..31] = columns n_base..+31).  Values go through a per-warp
+// shared-memory tile (stride 33) so that every global access is a whole row
+// of the chunk written by the 32 lanes together: 128 B per row for FP32,
+// 64 B per BF16 plane — full sectors, no read-modify-write in L2.
+__device__ __forceinline__ void stage_row(float* stg, int lane, const float* v) {
+#pragma unroll
+  for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = v[j];
+  __syncwarp();
+}
+
+__device__ __forceinline__ void load_tile(float* stg, int lane, const float* src, int ld, int m_base,
+                                          int n_base, int M, int N, float* out) {
+  const int n = n_base + lane;
+  float t[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) {  // 32 independent loads in flight per lane
+    const int m = m_base + r;
+    t[r] = (m < M && n < N) ? __ldg(src + (size_t)m * ld + n) : 0.f;
+  }
+#pragma unroll
+  for (int r = 0; r < 32; ++r) stg[r * 33 + lane] = t[r];
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 32; ++j) out[j] = stg[lane * 33 + j];
+  __syncwarp();
+}
+
+__device__ __forceinline__ void store_f32(const float* stg, int lane, float* dst, int ld, int m_base,
+                                          int n_base, int M, int N) {
+  const int n = n_base + lane;
+  if (n < N) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      const int m = m_base + r;
+      if (m < M) dst[(size_t)m * ld + n] = stg[r * 33 + lane];
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void store_split(const float* stg, int lane, const SplitMat& S, int row_off,
+                                            int m_base, int n_base, int M, int N) {
+  const int n = n_base + lane;
+  if (n < N) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      const int m = m_base + r;
+      if (m < M) split_store(S, row_off + m, n, stg[r * 33 + lane]);
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, int m_base, int n_base,
+                                          int M, int N, float* v) {
+  if (e.mode == EPI_STORE) {
+    stage_row(stg, lane, v);
+    store_f32(stg, lane, e.D, e.ldd, m_base, n_base, M, N);
+    return;
+  }
+  if (e.mode == EPI_SIGMOID) {
+    float lp[32], r1[32];
+    double ld = 0.0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int n = n_base + j;
+      const float yv = (n < N) ? e.y[n] : 0.f;
+      const float a = v[j];
+      const float sg = 1.f / (1.f + __expf(-a));
+      if (e.ld_acc && n < N) ld += double(yv * a - softplus(a));
+      v[j] = sg * (1.f - sg);  // Λ
+      lp[j] = v[j] * (1.f - 2.f * sg);
+      r1[j] = yv - sg;
+    }
+    const int m = m_base + lane;
+    if (e.ld_acc && m < M) atomicAdd(&e.ld_acc[m], ld);
+    stage_row(stg, lane, v);
+    store_split(stg, lane, e.lam, 0, m_base, n_base, M, N);
+    stage_row(stg, lane, lp);
+    store_f32(stg, lane, e.lp, e.lp_ld, m_base, n_base, M, N);
+    stage_row(stg, lane, r1);
+    store_split(stg, lane, e.r, 0, m_base, n_base, M, N);
+    return;
+  }
+  // EPI_TRACE: r2 = Λ'(w − s²)
+  float sv[32], lv[32];
+  load_tile(stg, lane, e.S, e.s_ld, m_base, n_base, M, N, sv);
+  load_tile(stg, lane, e.lp, e.lp_ld, m_base, n_base, M, N, lv);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = lv[j] * (v[j] - sv[j] * sv[j]);
+  stage_row(stg, lane, v);
+  store_split(stg, lane, e.r, e.r_off, m_base, n_base, M, N);
+}
+
 template <int NPL>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(320, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err) {
   constexpr int STAGES = Cfg<NPL>::STAGES;
@@ -233,24 +330,26 @@ __global__ void __launch_bounds__(192, 1)
       mma_commit(accum);  // also completes when nothing was issued
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    // epilogue warps 2..9: TMEM lane quarter = warp % 4; the two warps of a
+    // quarter take alternate 32-column chunks
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const bool ok = __all_sync(0xffffffffu, mbar_wait(accum, 0));
     if (!ok && lane == 0) atomicExch(err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok && KB > 0) {
-      const int m = m0 + q * 32 + lane;
+      // the operand ring is free once the accumulator is complete: each
+      // epilogue warp stages its chunks in its own 32 x 33 float tile
+      float* stg = reinterpret_cast<float*>(base) + (warp - 2) * (32 * 33);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = 32 * half; c0 < BN; c0 += 64) {
         if (n0 + c0 >= N) break;  // warp-uniform
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
-        if (m < M) {
-          float v[32];
+        float v[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-          epi_row32(epi, m, n0 + c0, N, v);
-        }
+        for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+        epi_chunk(epi, stg, lane, m0 + q * 32, n0 + c0, M, N, v);
       }
     }
   }
@@ -328,10 +427,10 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
     return cudaErrorInvalidValue;
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
   if (a->s.planes == 3)
-    gemm_tc_kernel<3><<<grid, 192, Cfg<3>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
+    gemm_tc_kernel<3><<<grid, 320, Cfg<3>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
                                                             g.M, g.N, g.K, g.epi, err);
   else
-    gemm_tc_kernel<2><<<grid, 192, Cfg<2>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
+    gemm_tc_kernel<2><<<grid, 320, Cfg<2>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
                                                             g.M, g.N, g.K, g.epi, err);
   return cudaGetLastError();
 }

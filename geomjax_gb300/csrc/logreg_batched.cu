@@ -91,12 +91,34 @@ struct CholArgs {
 
 // Shared-memory layout per CTA: the packed lower-triangle pair table
 // (column-major: (i, k) for k = 0.., i = k..d-1) used to spread triangle
-// updates over lanes, then per warp the factor L (d x d, F), two F vectors,
-// and L⁻¹ (d x d, float).
+// updates over lanes, then per warp the factor L (d x d, F), three F vectors
+// (two work vectors and the reciprocal diagonal), and L⁻¹ (d x d, float).
 __host__ __device__ inline size_t chol_smem_bytes(int d, int warps, size_t fsz) {
   const size_t pairs = (size_t)d * (d + 1) / 2;
   const size_t tab = ((pairs * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
-  return tab + (size_t)warps * (((size_t)d * d + 2 * d) * fsz + (size_t)d * d * sizeof(float));
+  return tab + (size_t)warps * (((size_t)d * d + 3 * d) * fsz + (size_t)d * d * sizeof(float));
+}
+
+// 1/sqrt(a) without a division: the FP32 estimate (relative error < 2^-22)
+// refined by one Newton step x ← x·(3 − a·x²)/2, whose quadratic
+// convergence leaves a relative error below 2^-43.  The sign / range checks
+// run on the FP32 copy to keep the FP64 pipe for arithmetic.  Non-positive
+// or non-finite a gives NaN.
+__device__ __forceinline__ double rsqrt_nr(double a) {
+  const float af = float(a);
+  const float xf = rsqrtf(af);
+  if (!(af > 0.f) || !(xf > 0.f) || isinf(xf) || isinf(af)) {
+    if (!(a > 0.0) || !isfinite(a)) return NAN;
+    return 1.0 / sqrt(a);  // outside the FP32 range
+  }
+  const double x = double(xf);
+  const double ax = a * x;
+  return x * fma(-0.5 * ax, x, 1.5);
+}
+__device__ __forceinline__ float rsqrt_nr(float a) {
+  if (!(a > 0.f) || !isfinite(a)) return NAN;
+  float x = rsqrtf(a);
+  return x * (1.5f - 0.5f * a * x * x);
 }
 
 template <typename F>  // factorisation type: double (default) or float
@@ -109,11 +131,12 @@ __global__ void chol_kernel(CholArgs a) {
   const int P = a.P;
   uint16_t* tab = reinterpret_cast<uint16_t*>(smem_raw);  // tab[2t] = i, tab[2t+1] = k
   const size_t tabb = (((size_t)P * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
-  F* L = reinterpret_cast<F*>(smem_raw + tabb) + (size_t)warp * (d * d + 2 * d);
+  F* L = reinterpret_cast<F*>(smem_raw + tabb) + (size_t)warp * (d * d + 3 * d);
   F* y = L + d * d;
   F* xv = y + d;
+  F* rdiag = xv + d;  // 1 / L_jj
   float* Li = reinterpret_cast<float*>(reinterpret_cast<F*>(smem_raw + tabb) +
-                                       (size_t)nwarps * (d * d + 2 * d)) +
+                                       (size_t)nwarps * (d * d + 3 * d)) +
               (size_t)warp * d * d;
   // column-major pair table (all threads of the CTA)
   for (int t = threadIdx.x; t < d; t += blockDim.x) {
@@ -142,19 +165,24 @@ __global__ void chol_kernel(CholArgs a) {
   // right-looking Cholesky: scale column j, then the trailing triangle
   // (i, k), j < k <= i, spread over the lanes through the pair table
   bool bad = false;
-  double logdet = 0.0;
+  // log det G = log Π pivots, accumulated as mantissa · 2^exponent so that
+  // only one logarithm is taken per chain
+  double pm = 1.0;
+  int pe = 0;
   int col_start = 0;  // packed offset of column j
   for (int j = 0; j < d; ++j) {
-    F djj = L[j * d + j];
-    if (!(djj > F(0))) {
-      bad = true;
-      djj = F(NAN);
-    }
-    const F ljj = sqrt(djj);
-    logdet += 2.0 * log(double(ljj));
-    const F inv = F(1) / ljj;
+    const F djj = L[j * d + j];
+    if (!(djj > F(0))) bad = true;
+    const F inv = rsqrt_nr(djj);  // 1/L_jj
+    const F ljj = djj * inv;
+    int e;
+    pm = frexp(pm * double(djj), &e);
+    pe += e;
     __syncwarp();
-    if (lane == 0) L[j * d + j] = ljj;
+    if (lane == 0) {
+      L[j * d + j] = ljj;
+      rdiag[j] = inv;
+    }
     for (int i = j + 1 + lane; i < d; i += 32) L[i * d + j] *= inv;
     __syncwarp();
     const int tstart = col_start + (d - j);  // first pair of column j + 1
@@ -166,7 +194,7 @@ __global__ void chol_kernel(CholArgs a) {
     __syncwarp();
   }
   if (lane == 0) {
-    a.logdet[c] = logdet;
+    a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
   }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
@@ -189,7 +217,7 @@ __global__ void chol_kernel(CholArgs a) {
     for (int i = lane; i < d; i += 32) y[i] = F(a.pc[(size_t)c * d + i]);
     __syncwarp();
     for (int j = 0; j < d; ++j) {
-      const F yj = y[j] / L[j * d + j];
+      const F yj = y[j] * rdiag[j];
       __syncwarp();
       if (lane == 0) y[j] = yj;
       for (int i = j + 1 + lane; i < d; i += 32) y[i] -= L[i * d + j] * yj;
@@ -208,7 +236,7 @@ __global__ void chol_kernel(CholArgs a) {
   for (int i = lane; i < d; i += 32) xv[i] = y[i];
   __syncwarp();
   for (int j = d - 1; j >= 0; --j) {
-    const F xj = xv[j] / L[j * d + j];
+    const F xj = xv[j] * rdiag[j];
     __syncwarp();
     if (lane == 0) xv[j] = xj;
     for (int i = lane; i < j; i += 32) xv[i] -= L[j * d + i] * xj;
@@ -219,16 +247,17 @@ __global__ void chol_kernel(CholArgs a) {
     split_store(a.Ub, c, i, float(xv[i]));
   }
   // L⁻¹ in FP32: forward substitution of the identity, all columns at once
-  for (int t = lane; t < d * d; t += 32) Li[t] = ((t / d) == (t % d)) ? 1.f : 0.f;
+  // (row k final after scaling; then rows i > k, lanes over i)
+  for (int i = lane; i < d; i += 32)
+    for (int cc = 0; cc < d; ++cc) Li[i * d + cc] = (i == cc) ? 1.f : 0.f;
   __syncwarp();
   for (int k = 0; k < d; ++k) {
-    const float ikk = 1.f / float(L[k * d + k]);
+    const float ikk = float(rdiag[k]);
     for (int cc = lane; cc <= k; cc += 32) Li[k * d + cc] *= ikk;
     __syncwarp();
-    const int w = k + 1, n = (d - k - 1) * w;
-    for (int t = lane; t < n; t += 32) {
-      const int i = k + 1 + t / w, cc = t % w;
-      Li[i * d + cc] -= float(L[i * d + k]) * Li[k * d + cc];
+    for (int i = k + 1 + lane; i < d; i += 32) {
+      const float lik = float(L[i * d + k]);
+      for (int cc = 0; cc <= k; ++cc) Li[i * d + cc] -= lik * Li[k * d + cc];
     }
     __syncwarp();
   }

@@ -198,6 +198,13 @@ int32_t gj_hvp(const gj_target* target, int32_t precision, int32_t num_chains, c
 int32_t gj_metric(const gj_target* target, int32_t precision, int32_t num_chains,
                   const void* q, void* metric_out, void* stream);
 
+/* Adjoint (vector-Jacobian product) of the metric operator:
+ * out[c, k] = Σ_ab W[c, a, b] ∂G_ab/∂q_k at q[c] (W is [C, d] for diagonal
+ * metrics).  Replaces jax.vjp of the user's metric_fn; the adjoints of the
+ * log density and of its gradient are gj_logdensity_grad and gj_hvp. */
+int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_chains,
+                      const void* q, const void* w, void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

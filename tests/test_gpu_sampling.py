@@ -43,38 +43,37 @@ def test_rmhmc_funnel_posterior_moments():
     _mcse_check(tr, 0.0, 9.0, "v")
 
 
-def test_lmcmonge_gaussian_like_moments():
-    """LMC-Monge (mixed) on the hierarchical Gaussian with a single group and
-    tiny observation noise is close to Gaussian in θ_1; checked against a
-    long float64 run of the same kernel family for mean/variance agreement of
-    μ within 2 MCSE of the difference."""
+def test_lmcmonge_mixed_matches_fp64_posterior():
+    """Equal posterior accuracy of the mixed and the plain FP64 LMC-Monge
+    forms on the funnel (D = 10, α² = 1, h = 0.02, 16 steps): the mean and
+    variance of v = θ[D−1] from the two forms agree within 2 Monte Carlo
+    standard errors of their difference (both forms run the same burn-in, so
+    what is compared is the effect of the precision, not mixing)."""
     import geomjax_gb300 as gj
-    from oracle import targets as OT
 
-    y, s = OT.make_hier_data(8, seed=4)
-    C, S = 1024, 200
-    means, vars_, esss = [], [], []
-    for prec in ("mixed", "fp64"):
-        tg = gj.hierarchical_gaussian(y, s, precision=prec)
-        kern = gj.lmcmonge.build_kernel()
+    D, C, S = 10, 2048, 300
+    stats = []
+    for prec, seed in (("mixed", 1), ("fp64", 2)):
+        tg = gj.funnel(D=D, precision=prec)
         dt = torch.float32 if prec == "mixed" else torch.float64
-        st = gj.lmcmonge.init(torch.zeros(C, tg.dim, dtype=dt), tg)
-        im = torch.ones(tg.dim, dtype=dt, device="cuda")
-        gen = torch.Generator(device="cuda").manual_seed(1 if prec == "mixed" else 2)
-        for _ in range(200):
-            st, _ = kern(gen, st, tg, 0.2, 8, alpha2=0.1, inverse_mass_matrix=im)
+        kern = gj.lmcmonge.build_kernel()
+        st = gj.lmcmonge.init(torch.ones(C, D, dtype=dt), tg)
+        im = torch.ones(D, dtype=dt, device="cuda")
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        for _ in range(300):
+            st, _ = kern(gen, st, tg, 0.02, 16, alpha2=1.0, inverse_mass_matrix=im)
         tr = torch.empty(S, C, dtype=torch.float64, device="cuda")
         for i in range(S):
-            st, _ = kern(gen, st, tg, 0.2, 8, alpha2=0.1, inverse_mass_matrix=im)
-            tr[i] = st.position[:, tg.J].double()  # μ
+            st, _ = kern(gen, st, tg, 0.02, 16, alpha2=1.0, inverse_mass_matrix=im)
+            tr[i] = st.position[:, D - 1].double()
         ess = float(gj.ess(tr, chain_axis=1, sample_axis=0).item())
-        means.append(float(tr.mean().item()))
-        vars_.append(float(tr.var().item()))
-        esss.append(ess)
-    se = math.sqrt(vars_[0] / esss[0] + vars_[1] / esss[1])
-    assert abs(means[0] - means[1]) < 2 * se, (means, se)
-    se_v = math.sqrt(2 * vars_[0] ** 2 / esss[0] + 2 * vars_[1] ** 2 / esss[1])
-    assert abs(vars_[0] - vars_[1]) < 2 * se_v, (vars_, se_v)
+        stats.append((float(tr.mean().item()), float(tr.var().item()), ess))
+    (m0, v0, e0), (m1, v1, e1) = stats
+    se = math.sqrt(v0 / e0 + v1 / e1)
+    assert abs(m0 - m1) < 2 * se, stats
+
+    se_v = math.sqrt(2 * v0 ** 2 / e0 + 2 * v1 ** 2 / e1)
+    assert abs(v0 - v1) < 2 * se_v, stats
 
 
 def test_window_adaptation_lmcmonge():
