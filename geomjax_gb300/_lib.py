@@ -93,6 +93,8 @@ SIGNATURES = {
     "gj_profile": (c_int32, [c_void_p, c_int32]),
     "gj_gemm_split_bf16": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p,
                                      c_void_p, c_void_p, c_void_p]),
+    "gj_gemm_split_bf16_noalloc": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32,
+                                             c_void_p, c_void_p, c_void_p, c_void_p]),
     "gj_logdensity_grad": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p,
                                      c_void_p, c_void_p]),
     "gj_hvp": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p,

@@ -31,6 +31,7 @@ UNITS = [
     ("gemm_simt.cu", []),
     ("gemm_tc.cu", []),
     ("capi.cu", []),
+    ("noalloc.cu", []),
 ]
 
 

@@ -314,6 +314,13 @@ int32_t gj_gemm_split_bf16(int32_t impl, int32_t planes, int32_t M, int32_t N, i
   return GJ_OK;
 }
 
+int32_t gj_gemm_split_bf16_noalloc(int32_t impl, int32_t planes, int32_t M, int32_t N, int32_t K,
+                                   const float* A, const float* B, float* D, void* stream) {
+  int rc = gj::gemm_split_noalloc(impl, planes, M, N, K, A, B, D, static_cast<cudaStream_t>(stream));
+  if (rc) return fail(rc, "%s", gj::gemm_noalloc_error());
+  return GJ_OK;
+}
+
 int32_t gj_logdensity_grad(const gj_target* target, int32_t precision, int32_t C, const void* q,
                            double* ld, void* grad, void* stream) {
   int st = check_target(target, precision);

@@ -189,5 +189,11 @@ cudaError_t gemm_tc_prepare();  // raises the kernel's shared-memory limit (call
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
 
+// noalloc.cu: the same contraction with the split planes in a static device
+// array (no cudaMalloc / cudaFree); capacity in BF16 elements.
+int gemm_split_noalloc(int impl, int planes, int M, int N, int K, const float* A, const float* B,
+                       float* D, cudaStream_t st);
+const char* gemm_noalloc_error();
+size_t gemm_noalloc_capacity();
 
 }  // namespace gj

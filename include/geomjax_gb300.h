@@ -188,6 +188,24 @@ int32_t gj_profile(gj_ctx* ctx, int32_t on);
 int32_t gj_gemm_split_bf16(int32_t impl, int32_t planes, int32_t M, int32_t N, int32_t K,
                            const float* A, const float* B, float* D, void* stream);
 
+/* The same contraction as gj_gemm_split_bf16, for callers that cannot
+ * allocate device memory: a JAX/XLA custom call, whose framework has
+ * reserved nearly all device memory for its own pool, or work recorded by
+ * stream capture.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine: its split planes live in one static device array of 8 MiB
+ * (4,194,304 BF16 elements) that every GPU loading the library holds until
+ * the process exits.  Limit: planes * (ceil128(M) + ceil128(N)) * ceil64(K)
+ * <= 4194304, otherwise GJ_EINVAL.  All calls share the array: calls that
+ * overlap on the GPU (other streams or host threads) race on it and must be
+ * serialised by the caller; every call rewrites all of the array it reads.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Synchronises the stream.  No counterpart in
+ * the reference. */
+int32_t gj_gemm_split_bf16_noalloc(int32_t impl, int32_t planes, int32_t M, int32_t N,
+                                   int32_t K, const float* A, const float* B, float* D,
+                                   void* stream);
+
 /* Operator-level entry points (no context).  q, grad, u, out: [C, d];
  * logdensity: [C] float64; metric_out: [C, d] (diagonal metrics) or
  * [C, d, d] (dense), dtype of the precision. */
