@@ -139,7 +139,8 @@ def run_ours(args, wl):
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
         kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path, loop=args.loop,
-                                     cholesky=args.cholesky)
+                                     cholesky=args.cholesky,
+                                     chol_chains_per_warp=args.chol_cpw)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -251,7 +252,8 @@ def run_ours(args, wl):
         "data": "synthetic (seeded)",
         "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
                    "step_size": h, "precision": "mixed", "loop": args.loop,
-                   "cholesky": args.cholesky, "l2": "flushed between timed steps (256 MB write)",
+                   "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
+                   "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
         "min_ess": (round(min_ess, 2) if K >= 4 else None),
@@ -435,6 +437,8 @@ def main():
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="fixed-point loop driver of the batched path (host: profilable by ncu)")
     ap.add_argument("--cholesky", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--chol-cpw", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="chains per warp in the metric factorisation (0 = automatic)")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
     if args.chains:

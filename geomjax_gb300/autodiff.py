@@ -94,3 +94,65 @@ def grad_logdensity(target: Target, q):
 
 def metric(target: Target, q):
     return _Metric.apply(q, target)
+
+
+class _TransitionStats(torch.autograd.Function):
+    """Mean acceptance probability and mean energy error of one generalized-
+    leapfrog RMHMC transition as differentiable functions of the step size h
+    and the metric regulariser λ (logistic regression, float64).  The forward
+    pass runs the tangent kernel once and keeps the 2 x 2 Jacobian of the two
+    means; the backward pass is that Jacobian's transpose times the incoming
+    gradients (exact for the discrete trajectory with fixed iteration
+    counts)."""
+
+    @staticmethod
+    def forward(ctx, h, lam, target, q0, z, nsteps, kp, kq):
+        out = transition_jacobian(target, q0, z, float(h), float(lam), nsteps, kp, kq)
+        ctx.jac = out.mean(dim=0)  # (p, dp/dh, dp/dλ, ΔH, dΔH/dh, dΔH/dλ)
+        return ctx.jac[0].clone(), ctx.jac[3].clone()
+
+    @staticmethod
+    def backward(ctx, gp, gdh):
+        j = ctx.jac
+        gh = gp * j[1] + gdh * j[4]
+        gl = gp * j[2] + gdh * j[5]
+        return gh, gl, None, None, None, None, None, None
+
+
+def transition_stats(target, q0, z, step_size, metric_reg, num_integration_steps, kp=6, kq=6):
+    """(mean p_accept, mean ΔH) of one generalized-leapfrog transition from
+    positions q0 with momentum normals z; differentiable in ``step_size`` and
+    ``metric_reg`` (0-d float64 tensors with requires_grad)."""
+    if target.precision != "fp64" or target.family != L.GJ_LOGREG:
+        raise ValueError("transition_stats needs a float64 logistic-regression target")
+    q0 = torch.as_tensor(q0, dtype=torch.float64).to(target.device).contiguous()
+    z = torch.as_tensor(z, dtype=torch.float64).to(target.device).contiguous()
+    return _TransitionStats.apply(step_size, metric_reg, target, q0, z, num_integration_steps, kp, kq)
+
+
+def transition_values(target, q0, z, step_size, metric_reg, num_integration_steps, kp=6, kq=6):
+    """Per-chain (p_accept, ΔH) without tangents (used for finite differences)."""
+    lib = L.lib()
+    q0 = torch.as_tensor(q0, dtype=torch.float64).to(target.device).contiguous()
+    z = torch.as_tensor(z, dtype=torch.float64).to(target.device).contiguous()
+    out = torch.empty(q0.shape[0], 6, dtype=torch.float64, device=target.device)
+    d = target.descriptor()
+    L.check(lib.gj_logreg_gl_transition_jvp(ctypes.byref(d), q0.shape[0], L.ptr(q0), L.ptr(z),
+                                            float(step_size), float(metric_reg),
+                                            int(num_integration_steps), int(kp), int(kq), 0,
+                                            L.ptr(out), _stream()))
+    return out[:, 0], out[:, 3]
+
+
+def transition_jacobian(target, q0, z, step_size, metric_reg, num_integration_steps, kp=6, kq=6):
+    """Per-chain [C, 6] output of the tangent kernel."""
+    lib = L.lib()
+    q0 = torch.as_tensor(q0, dtype=torch.float64).to(target.device).contiguous()
+    z = torch.as_tensor(z, dtype=torch.float64).to(target.device).contiguous()
+    out = torch.empty(q0.shape[0], 6, dtype=torch.float64, device=target.device)
+    d = target.descriptor()
+    L.check(lib.gj_logreg_gl_transition_jvp(ctypes.byref(d), q0.shape[0], L.ptr(q0), L.ptr(z),
+                                            float(step_size), float(metric_reg),
+                                            int(num_integration_steps), int(kp), int(kq), 1,
+                                            L.ptr(out), _stream()))
+    return out

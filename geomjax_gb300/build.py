@@ -32,6 +32,7 @@ UNITS = [
     ("gemm_tc.cu", []),
     ("capi.cu", []),
     ("noalloc.cu", []),
+    ("traj_jvp.cu", []),
 ]
 
 

@@ -89,6 +89,7 @@ struct gj_ctx {
   int profile;
   int loop_mode;  // GJ_OPT_LOOP
   int chol_fp64;  // GJ_OPT_CHOL_FP64
+  int chol_cpw;   // GJ_OPT_CHOL_CHAINS_PER_WARP
   gj::LogregBatched* lb;
 };
 
@@ -118,6 +119,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->profile = 0;
   c->loop_mode = 0;
   c->chol_fp64 = 1;
+  c->chol_cpw = 0;
   c->lb = nullptr;
   *out = c;
   return GJ_OK;
@@ -146,6 +148,13 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     if (value < 0 || value > 1) return fail(GJ_EINVAL, "factorisation precision flag must be 0 or 1");
     ctx->chol_fp64 = (int)value;
     if (ctx->lb) gj::logreg_batched_set_chol_fp64(ctx->lb, ctx->chol_fp64);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_CHOL_CHAINS_PER_WARP) {
+    if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+      return fail(GJ_EINVAL, "chains per warp must be 0 (automatic), 1, 2, 4 or 8");
+    ctx->chol_cpw = (int)value;
+    if (ctx->lb) gj::logreg_batched_set_chol_cpw(ctx->lb, ctx->chol_cpw);
     return GJ_OK;
   }
   if (key == GJ_OPT_THREADS_PER_BLOCK) {
@@ -197,6 +206,7 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
       if (rc) return fail(rc, "%s", gj::logreg_batched_error());
       gj::logreg_batched_set_profile(ctx->lb, ctx->profile);
       gj::logreg_batched_set_chol_fp64(ctx->lb, ctx->chol_fp64);
+      gj::logreg_batched_set_chol_cpw(ctx->lb, ctx->chol_cpw);
     }
     const int gemm = (ctx->logreg_path == 1) ? 1 : 2;
     // host-driven loop while profiling (events around each GEMM) or on request
@@ -381,6 +391,24 @@ int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t C, con
                       : gj::launch_metric_vjp<float>(t, (const float*)q, (const float*)w,
                                                      (float*)out, C, cs);
   return cuda_status(e, "gj_metric_vjp");
+}
+
+int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const double* q0,
+                                    const double* z, double step_size, double metric_reg,
+                                    int32_t num_integration_steps, int32_t kp, int32_t kq,
+                                    int32_t tangents, double* out, void* stream) {
+  int st = check_target(target, GJ_FP64);
+  if (st) return st;
+  if (target->family != GJ_LOGREG) return fail(GJ_EINVAL, "the differentiated trajectory is for logistic regression");
+  if (target->dim > 16) return fail(GJ_ENOTSUP, "the differentiated trajectory supports d <= 16");
+  if (C < 1 || !q0 || !z || !out || kp < 1 || kq < 1 || num_integration_steps < 0 ||
+      !(metric_reg > 0) || !(step_size == step_size))
+    return fail(GJ_EINVAL, "bad arguments");
+  cudaError_t e = gj::launch_gl_trajectory_jvp(
+      static_cast<const double*>(target->X), static_cast<const double*>(target->y), target->n_data,
+      target->dim, target->p0, C, q0, z, step_size, metric_reg, num_integration_steps, kp, kq,
+      tangents, out, static_cast<cudaStream_t>(stream));
+  return cuda_status(e, "gj_logreg_gl_transition_jvp");
 }
 
 }  // extern "C"

@@ -28,6 +28,12 @@ template <typename T>
 cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out, int C,
                               cudaStream_t st);
 
+// differentiated generalized-leapfrog transition (traj_jvp.cu)
+cudaError_t launch_gl_trajectory_jvp(const double* X, const double* y, int N, int d,
+                                     double prior_var, int C, const double* q0, const double* z,
+                                     double h, double lam, int L, int Kp, int Kq, int tangents,
+                                     double* out, cudaStream_t st);
+
 // warp-per-chain LMC-Monge (monge_warp.cu), float32 state
 cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,
                               double* ld, double* vol, const float* z, const double* u,

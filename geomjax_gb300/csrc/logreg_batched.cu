@@ -24,6 +24,7 @@
 // FP64 is used for the metric Cholesky, log det and solves, the fixed-point
 // norm and the Hamiltonian difference; the log density at the proposal is
 // evaluated per chain in FP32 with an FP64 sum.
+#include <algorithm>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -89,14 +90,58 @@ struct CholArgs {
   float* mom_info;     // DRAW: info.momentum (may be NULL)
 };
 
-// Shared-memory layout per CTA: the packed lower-triangle pair table
-// (column-major: (i, k) for k = 0.., i = k..d-1) used to spread triangle
-// updates over lanes, then per warp the factor L (d x d, F), three F vectors
-// (two work vectors and the reciprocal diagonal), and L⁻¹ (d x d, float).
-__host__ __device__ inline size_t chol_smem_bytes(int d, int warps, size_t fsz) {
+// Chain packing.  The FP64 pipe issues one warp instruction for all 32 lanes
+// whatever the active mask, so the factorisation packs several chains into a
+// warp: a sub-group of `lpc` lanes owns one chain and every pivot, scaling
+// and substitution step serves 32 / lpc chains per instruction.  The factor
+// is held as a packed lower triangle in column-major order,
+// L(i, k) at colstart(k) + i − k with colstart(k) = k·d − k(k−1)/2, which is
+// also the index of the upper-triangle entry (k, i) in the row-major packed
+// Gram output, so unpacking G is a plain copy.
+//
+// Shared memory per CTA: the pair table (packed index t → row i | col k << 16,
+// 4 bytes each), then per chain: L (P F's), y, x, 1/L_jj (d F's each) and
+// L⁻¹ packed like L (P floats).  The per-chain stride is a multiple of 8 bytes
+// that is 4 (mod 16) doubles, so the 4 chains of a half-warp touching
+// consecutive packed entries fall in distinct banks.
+struct CholCfg {
+  int cpw;       // chains per warp
+  int lpc;       // lanes per chain (32 / cpw)
+  int warps;     // warps per CTA
+  size_t stride; // bytes per chain
+  size_t tab;    // bytes of the pair table
+  size_t smem;   // dynamic shared memory per CTA
+};
+
+__host__ __device__ inline size_t chol_table_bytes(int d) {
   const size_t pairs = (size_t)d * (d + 1) / 2;
-  const size_t tab = ((pairs * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
-  return tab + (size_t)warps * (((size_t)d * d + 3 * d) * fsz + (size_t)d * d * sizeof(float));
+  return (pairs * sizeof(uint32_t) + 15) / 16 * 16;
+}
+
+__host__ __device__ inline size_t chol_chain_bytes(int d, size_t fsz) {
+  const size_t pairs = (size_t)d * (d + 1) / 2;
+  size_t b = pairs * fsz + 3 * (size_t)d * fsz + pairs * sizeof(float);
+  size_t w = (b + 7) / 8;  // 8-byte words
+  while (w % 16 != 4) ++w;
+  return w * 8;
+}
+
+// cpw_req: requested chains per warp (1, 2, 4 or 8; 0 = automatic); reduced
+// until a warp's chains fit in 40 KB.  Measured on GB300 at d = 25, 4096
+// chains (leapfrog steps/s of the whole transition): FP64 1.64M / 1.96M /
+// 2.06M / 1.74M and FP32 2.29M / 2.46M / 2.35M / 2.00M for 1 / 2 / 4 / 8
+// chains per warp, so the automatic choice is 4 for FP64 (whose issue slots
+// bound the factorisation) and 2 for FP32 (where latency does).
+inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0) {
+  CholCfg c{};
+  c.stride = chol_chain_bytes(d, fsz);
+  c.tab = chol_table_bytes(d);
+  c.cpw = cpw_req > 0 ? cpw_req : (fsz == sizeof(double) ? 4 : 2);
+  while (c.cpw > 1 && (size_t)c.cpw * c.stride > 40 * 1024) c.cpw >>= 1;
+  c.lpc = 32 / c.cpw;
+  c.warps = c.cpw >= 4 ? 1 : 4 / c.cpw;
+  c.smem = c.tab + (size_t)c.warps * c.cpw * c.stride;
+  return c;
 }
 
 // 1/sqrt(a) without a division: the FP32 estimate (relative error < 2^-22)
@@ -121,158 +166,212 @@ __device__ __forceinline__ float rsqrt_nr(float a) {
   return x * (1.5f - 0.5f * a * x * x);
 }
 
-template <typename F>  // factorisation type: double (default) or float
-__global__ void chol_kernel(CholArgs a) {
+__device__ __forceinline__ int colstart(int k, int d) { return k * d - (k * (k - 1)) / 2; }
+
+// sum over the LPC lanes of a sub-group (LPC a power of two, sub-groups aligned)
+template <int LPC>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = LPC >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename F, int LPC>  // factorisation type (double / float), lanes per chain
+__global__ void chol_kernel(CholArgs a, int stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int CPW = 32 / LPC;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
-  const int c = blockIdx.x * nwarps + warp;
+  const int sub = lane / LPC, sl = lane % LPC;
+  const int c = (blockIdx.x * nwarps + warp) * CPW + sub;
   const int d = a.d;
   const int P = a.P;
-  uint16_t* tab = reinterpret_cast<uint16_t*>(smem_raw);  // tab[2t] = i, tab[2t+1] = k
-  const size_t tabb = (((size_t)P * 2 * sizeof(uint16_t)) + 15) / 16 * 16;
-  F* L = reinterpret_cast<F*>(smem_raw + tabb) + (size_t)warp * (d * d + 3 * d);
-  F* y = L + d * d;
+  uint32_t* tab = reinterpret_cast<uint32_t*>(smem_raw);
+  unsigned char* base = smem_raw + chol_table_bytes(d) + (size_t)(warp * CPW + sub) * stride;
+  F* L = reinterpret_cast<F*>(base);  // packed lower, column-major
+  F* y = L + P;
   F* xv = y + d;
   F* rdiag = xv + d;  // 1 / L_jj
-  float* Li = reinterpret_cast<float*>(reinterpret_cast<F*>(smem_raw + tabb) +
-                                       (size_t)nwarps * (d * d + 3 * d)) +
-              (size_t)warp * d * d;
-  // column-major pair table (all threads of the CTA)
-  for (int t = threadIdx.x; t < d; t += blockDim.x) {
-    int off = t * d - t * (t - 1) / 2;  // start of column t
-    for (int i = t; i < d; ++i, ++off) {
-      tab[2 * off] = (uint16_t)i;
-      tab[2 * off + 1] = (uint16_t)t;
-    }
+  float* Li = reinterpret_cast<float*>(rdiag + d);  // L⁻¹, packed like L
+  for (int k = threadIdx.x; k < d; k += blockDim.x) {
+    int off = colstart(k, d);
+    for (int i = k; i < d; ++i, ++off) tab[off] = (uint32_t)i | ((uint32_t)k << 16);
   }
   __syncthreads();
-  if (c >= a.C) return;
-  if (a.mode == CH_EVAL && a.active && !a.active[c]) return;
-  // unpack G = Gvec + I/s² (Gvec is row-major over the upper triangle)
-  for (int idx = lane; idx < P; idx += 32) {
-    int j = 0, rem = idx;
-    while (rem >= d - j) {
-      rem -= d - j;
-      ++j;
+  const bool live = c < a.C && !(a.mode == CH_EVAL && a.active && !a.active[c]);
+  if (__all_sync(0xffffffffu, !live)) return;  // uniform per warp
+  // G = Gvec + I/s²: the packed layouts coincide; idle slots get the identity
+  for (int t = sl; t < P; t += LPC) {
+    const uint32_t ik = tab[t];
+    const bool diag = (ik & 0xffffu) == (ik >> 16);
+    F g;
+    if (live) {
+      g = F(a.Gv[(size_t)c * a.gv_ld + t]);
+      if (diag) g += F(a.prior_inv);
+    } else {
+      g = diag ? F(1) : F(0);
     }
-    const int k = j + rem;
-    F g = F(a.Gv[(size_t)c * a.gv_ld + idx]);
-    if (j == k) g += F(a.prior_inv);
-    L[k * d + j] = g;  // lower triangle
+    L[t] = g;
   }
   __syncwarp();
-  // right-looking Cholesky: scale column j, then the trailing triangle
-  // (i, k), j < k <= i, spread over the lanes through the pair table
+  // right-looking Cholesky; log det G = log Π pivots, accumulated as
+  // mantissa · 2^exponent so that one logarithm is taken per chain
   bool bad = false;
-  // log det G = log Π pivots, accumulated as mantissa · 2^exponent so that
-  // only one logarithm is taken per chain
   double pm = 1.0;
   int pe = 0;
-  int col_start = 0;  // packed offset of column j
+  int cj = 0;  // colstart(j)
   for (int j = 0; j < d; ++j) {
-    const F djj = L[j * d + j];
+    const F djj = L[cj];
     if (!(djj > F(0))) bad = true;
     const F inv = rsqrt_nr(djj);  // 1/L_jj
-    const F ljj = djj * inv;
     int e;
     pm = frexp(pm * double(djj), &e);
     pe += e;
     __syncwarp();
-    if (lane == 0) {
-      L[j * d + j] = ljj;
+    if (sl == 0) {
+      L[cj] = djj * inv;
       rdiag[j] = inv;
     }
-    for (int i = j + 1 + lane; i < d; i += 32) L[i * d + j] *= inv;
+    for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
     __syncwarp();
-    const int tstart = col_start + (d - j);  // first pair of column j + 1
-    for (int t = tstart + lane; t < P; t += 32) {
-      const int i = tab[2 * t], k = tab[2 * t + 1];
-      L[i * d + k] -= L[i * d + j] * L[k * d + j];
+    // trailing triangle: column j is read-only here and disjoint from the
+    // entries written, so the iterations' loads may be issued together
+    const int cn = cj + (d - j);  // colstart(j + 1)
+    const F* __restrict__ colj = L + cj - j;  // colj[i] = L(i, j)
+    F* __restrict__ tr = L;
+#pragma unroll 4
+    for (int t = cn + sl; t < P; t += LPC) {
+      const uint32_t ik = tab[t];
+      tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
     }
-    col_start = tstart;
+    cj = cn;
     __syncwarp();
   }
-  if (lane == 0) {
+  if (sl == 0 && live) {
     a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
   }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
   // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
-    for (int i = lane; i < d; i += 32) y[i] = F(a.z[(size_t)c * d + i]);
+    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
     __syncwarp();
     double zz = 0.0;
-    for (int i = lane; i < d; i += 32) {
+    for (int i = sl; i < d; i += LPC) {
       F sacc = 0;
-      for (int k = 0; k <= i; ++k) sacc += L[i * d + k] * y[k];
-      a.p0[(size_t)c * d + i] = double(sacc);
-      a.pc[(size_t)c * d + i] = double(sacc);
-      if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
+      int ck = 0;
+      for (int k = 0; k <= i; ++k) {
+        sacc += L[ck + i - k] * y[k];
+        ck += d - k;
+      }
+      if (live) {
+        a.p0[(size_t)c * d + i] = double(sacc);
+        a.pc[(size_t)c * d + i] = double(sacc);
+        if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
+      }
       zz += double(y[i]) * double(y[i]);
     }
-    zz = warp_sum(zz);
-    if (lane == 0) a.quad[c] = zz;
+    zz = group_sum<LPC>(zz);
+    if (sl == 0 && live) a.quad[c] = zz;
   } else {
-    for (int i = lane; i < d; i += 32) y[i] = F(a.pc[(size_t)c * d + i]);
+    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
     __syncwarp();
+    int cs = 0;
     for (int j = 0; j < d; ++j) {
       const F yj = y[j] * rdiag[j];
       __syncwarp();
-      if (lane == 0) y[j] = yj;
-      for (int i = j + 1 + lane; i < d; i += 32) y[i] -= L[i * d + j] * yj;
+      if (sl == 0) y[j] = yj;
+      for (int i = j + 1 + sl; i < d; i += LPC) y[i] -= L[cs + i - j] * yj;
+      cs += d - j;
       __syncwarp();
     }
     if (a.mode == CH_ENERGY) {
       double q = 0.0;
-      for (int i = lane; i < d; i += 32) q += double(y[i]) * double(y[i]);
-      q = warp_sum(q);
-      if (lane == 0) a.quad[c] = q;
+      for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
+      q = group_sum<LPC>(q);
+      if (sl == 0 && live) a.quad[c] = q;
       return;
     }
   }
   __syncwarp();
-  // u = L⁻ᵀ y, column-oriented backward substitution
-  for (int i = lane; i < d; i += 32) xv[i] = y[i];
+  // u = L⁻ᵀ y, column-oriented backward substitution (row j of L is
+  // L(j, i) at colstart(i) + j − i)
+  for (int i = sl; i < d; i += LPC) xv[i] = y[i];
   __syncwarp();
   for (int j = d - 1; j >= 0; --j) {
     const F xj = xv[j] * rdiag[j];
     __syncwarp();
-    if (lane == 0) xv[j] = xj;
-    for (int i = lane; i < j; i += 32) xv[i] -= L[j * d + i] * xj;
+    if (sl == 0) xv[j] = xj;
+    for (int i = sl; i < j; i += LPC) xv[i] -= L[colstart(i, d) + j - i] * xj;
     __syncwarp();
   }
-  for (int i = lane; i < d; i += 32) {
-    a.u[(size_t)c * d + i] = double(xv[i]);
-    split_store(a.Ub, c, i, float(xv[i]));
+  if (live) {
+    for (int i = sl; i < d; i += LPC) {
+      a.u[(size_t)c * d + i] = double(xv[i]);
+      split_store(a.Ub, c, i, float(xv[i]));
+    }
   }
-  // L⁻¹ in FP32: forward substitution of the identity, all columns at once
-  // (row k final after scaling; then rows i > k, lanes over i)
-  for (int i = lane; i < d; i += 32)
-    for (int cc = 0; cc < d; ++cc) Li[i * d + cc] = (i == cc) ? 1.f : 0.f;
+  // L⁻¹ in FP32 by forward substitution of the identity, all columns at
+  // once: row k is final once scaled, then rows i > k are reduced by it
+  for (int t = sl; t < P; t += LPC) {
+    const uint32_t ik = tab[t];
+    Li[t] = (ik & 0xffffu) == (ik >> 16) ? 1.f : 0.f;
+  }
   __syncwarp();
+  int ck = 0;  // colstart(k)
   for (int k = 0; k < d; ++k) {
     const float ikk = float(rdiag[k]);
-    for (int cc = lane; cc <= k; cc += 32) Li[k * d + cc] *= ikk;
+    for (int cc = sl; cc <= k; cc += LPC) Li[colstart(cc, d) + k - cc] *= ikk;
     __syncwarp();
-    for (int i = k + 1 + lane; i < d; i += 32) {
-      const float lik = float(L[i * d + k]);
-      for (int cc = 0; cc <= k; ++cc) Li[i * d + cc] -= lik * Li[k * d + cc];
+    for (int i = k + 1 + sl; i < d; i += LPC) {
+      const float lik = float(L[ck + i - k]);
+      int cc0 = 0;  // colstart(cc)
+      for (int cc = 0; cc <= k; ++cc) {
+        Li[cc0 + i - cc] -= lik * Li[cc0 + k - cc];
+        cc0 += d - cc;
+      }
     }
+    ck += d - k;
     __syncwarp();
   }
-  // G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients (row-major upper triangle)
-  for (int idx = lane; idx < P; idx += 32) {
-    int j = 0, rem = idx;
-    while (rem >= d - j) {
-      rem -= d - j;
-      ++j;
-    }
-    const int k = j + rem;
+  // G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients (row-major upper triangle, whose
+  // index for (k, i), k <= i, is the packed index t of (i, k)); the
+  // off-diagonal coefficients are doubled
+  if (!live) return;
+  for (int t = sl; t < P; t += LPC) {
+    const uint32_t ik = tab[t];
+    const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+    const float* li = Li + colstart(i, d) - i;  // li[m] = L⁻¹(m, i)
+    const float* lk = Li + colstart(k, d) - k;  // lk[m] = L⁻¹(m, k)
     float sacc = 0.f;
-    for (int m = k; m < d; ++m) sacc += Li[m * d + j] * Li[m * d + k];
-    split_store(a.Giv, c, idx, (j == k) ? sacc : 2.f * sacc);
+    for (int m = i; m < d; ++m) sacc += lk[m] * li[m];
+    split_store(a.Giv, c, t, (i == k) ? sacc : 2.f * sacc);
   }
+}
+
+template <typename F>
+void chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, cudaStream_t st) {
+  const int th = 32 * cf.warps;
+  switch (cf.lpc) {
+    case 4: chol_kernel<F, 4><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
+    case 8: chol_kernel<F, 8><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
+    case 16: chol_kernel<F, 16><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
+    default: chol_kernel<F, 32><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
+  }
+}
+
+template <typename F>
+cudaError_t chol_set_smem(int smax) {
+  cudaError_t e = cudaSuccess, r;
+  r = cudaFuncSetAttribute(chol_kernel<F, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+  if (r != cudaSuccess) e = r;
+  r = cudaFuncSetAttribute(chol_kernel<F, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+  if (r != cudaSuccess) e = r;
+  r = cudaFuncSetAttribute(chol_kernel<F, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+  if (r != cudaSuccess) e = r;
+  r = cudaFuncSetAttribute(chol_kernel<F, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+  if (r != cudaSuccess) e = r;
+  return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -440,6 +539,7 @@ struct LogregBatched {
   TcOperand *tXb, *tXTb, *tZb, *tZt, *tQb, *tUb, *tLam, *tGiv, *tRb;
   bool tc_ok;
   int chol_fp64;
+  int chol_cpw;  // chains per warp in the factorisation (0 = automatic)
   int prof;
   // graph path: device step parameters, staging buffers, captured graph
   StepDev* spd;
@@ -461,6 +561,7 @@ const char* logreg_batched_error() { return g_err.c_str(); }
 
 LogregStats logreg_batched_stats(const LogregBatched* lb) { return lb->stats; }
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on) { lb->chol_fp64 = on; }
+void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw) { lb->chol_cpw = cpw; }
 void logreg_batched_set_profile(LogregBatched* lb, int on) { lb->prof = on; }
 
 static SplitMat make_split(LogregBatched* lb, int rows, int kdim, int planes, bool* ok) {
@@ -503,6 +604,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->d = t.d;
   lb->P = t.d * (t.d + 1) / 2;
   lb->chol_fp64 = 1;
+  lb->chol_cpw = 0;
   lb->prof = 0;
   lb->ev_used = 0;
   lb->gexec = nullptr;
@@ -584,12 +686,15 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
     return GJ_ECUDA;
   }
   {
-    const int warps = d <= 32 ? 4 : 1;
-    const int smax = (int)chol_smem_bytes(d, warps, sizeof(double));
-    cudaError_t a1 = cudaFuncSetAttribute(chol_kernel<double>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-    cudaError_t a2 = cudaFuncSetAttribute(chol_kernel<float>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    // the largest layout any chains-per-warp choice can ask for: the table
+    // plus 4 chains, or one chain of a 40 KB+ stride
+    size_t smax = 0;
+    for (int cpw = 1; cpw <= 8; cpw *= 2) {
+      smax = std::max(smax, chol_config(d, sizeof(double), cpw).smem);
+      smax = std::max(smax, chol_config(d, sizeof(float), cpw).smem);
+    }
+    cudaError_t a1 = chol_set_smem<double>((int)smax);
+    cudaError_t a2 = chol_set_smem<float>((int)smax);
     if (a1 != cudaSuccess || a2 != cudaSuccess) {
       g_err = "metric factorisation needs more shared memory than the device allows";
       logreg_batched_destroy(lb);
@@ -703,16 +808,15 @@ struct Runner {
     a.active = only_active ? L.active : nullptr;
     a.bad = L.bad;
     a.mom_info = mom_info;
-    const int d = L.d;
-    const int warps = d <= 32 ? 4 : 1;
-    const size_t fsz = L.chol_fp64 ? sizeof(double) : sizeof(float);
-    const size_t smem = chol_smem_bytes(d, warps, fsz);
-    const dim3 grid((L.C + warps - 1) / warps);
+    const CholCfg cf =
+        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw);
+    const int per_cta = cf.warps * cf.cpw;
+    const dim3 grid((L.C + per_cta - 1) / per_cta);
     // the dynamic shared-memory limit was raised at context creation
     if (L.chol_fp64)
-      chol_kernel<double><<<grid, 32 * warps, smem, st>>>(a);
+      chol_launch<double>(cf, grid, a, st);
     else
-      chol_kernel<float><<<grid, 32 * warps, smem, st>>>(a);
+      chol_launch<float>(cf, grid, a, st);
     check(cudaGetLastError());
   }
 
@@ -990,7 +1094,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
   }
   lb->g_L = L;
   lb->g_impl = impl;
-  lb->g_chol = lb->chol_fp64;
+  lb->g_chol = lb->chol_fp64 * 16 + lb->chol_cpw;
   return GJ_OK;
 }
 
@@ -1009,7 +1113,7 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
     g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
     return GJ_ENOTSUP;
   }
-  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64) {
+  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64 * 16 + lb->chol_cpw) {
     // the capture streams must not see unfinished work of the caller's stream
     cudaStreamSynchronize(st);
     const int rc = build_graph(lb, sp.L, gemm_impl);

@@ -38,6 +38,8 @@ struct LogregStats {
 };
 LogregStats logreg_batched_stats(const LogregBatched* lb);
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);
+// chains per warp in the metric factorisation: 1, 2, 4, 8 or 0 (automatic)
+void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw);
 void logreg_batched_set_profile(LogregBatched* lb, int on);
 
 // D[M, N] = A[M, K]·B[N, K]ᵀ through the split-BF16 GEMM `impl` (test hook;

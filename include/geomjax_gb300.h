@@ -157,6 +157,11 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
 /* batched path metric factorisation: 1 = float64 Cholesky / log det /
  * solves (default), 0 = float32 */
 #define GJ_OPT_CHOL_FP64 4
+/* batched path metric factorisation: chains sharing one warp (1, 2, 4 or 8;
+ * 0 = automatic).  The factorisation's FP64 instructions issue once per warp
+ * whatever the lanes in use, so packing chains divides its FP64 work, while
+ * fewer warps hide less latency. */
+#define GJ_OPT_CHOL_CHAINS_PER_WARP 5
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */
@@ -222,6 +227,22 @@ int32_t gj_metric(const gj_target* target, int32_t precision, int32_t num_chains
  * log density and of its gradient are gj_logdensity_grad and gj_hvp. */
 int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_chains,
                       const void* q, const void* w, void* out, void* stream);
+
+/* Derivatives of one RMHMC transition with the generalized leapfrog, for a
+ * GJ_LOGREG target with float64 data: with respect to the step size h and
+ * the metric regulariser λ (G = XᵀΛX + λI; the prior variance stays
+ * target->p0), by forward-mode tangent propagation through the whole
+ * discrete trajectory.  Each fixed-point half step runs exactly kp (momentum)
+ * / kq (position) iterations so the differentiated map is fixed.  q0, z:
+ * [C, d] float64 start positions and momentum normals.  out[C, 6] =
+ * (p_accept, ∂p_accept/∂h, ∂p_accept/∂λ, ΔH = H1 − H0, ∂ΔH/∂h, ∂ΔH/∂λ);
+ * tangents = 0 computes the values only (the tangent slots are zero).
+ * d <= 16.  Replaces the reference's jax.jacfwd through a trajectory
+ * (adaptation/chees_adaptation_lmcmonge.py:497-519). */
+int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t num_chains, const double* q0,
+                                    const double* z, double step_size, double metric_reg,
+                                    int32_t num_integration_steps, int32_t kp, int32_t kq,
+                                    int32_t tangents, double* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,21 @@ def test_argument_checks_without_gpu():
     p.num_integration_steps = -1
     assert lib.gj_set_option(h, 999, 0) == L.GJ_EINVAL
     assert lib.gj_set_option(h, L.GJ_OPT_LOGREG_PATH, 9) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_CHOL_CHAINS_PER_WARP, 3) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_CHOL_CHAINS_PER_WARP, 16) == L.GJ_EINVAL
+    for v in (0, 1, 2, 4, 8):
+        assert lib.gj_set_option(h, L.GJ_OPT_CHOL_CHAINS_PER_WARP, v) == L.GJ_OK
+    # the differentiated transition checks its arguments on the host
+    assert lib.gj_logreg_gl_transition_jvp(None, 1, None, None, 0.1, 0.5, 1, 2, 2, 1, None,
+                                           None) == L.GJ_EINVAL
+    tl = L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 20, 10, 1, 1, None, 100.0, 0.0)
+    assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 2, 2, 1, 1,
+                                           None) == L.GJ_ENOTSUP
+    tl.dim = 5
+    assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, -1.0, 1, 2, 2, 1, 1,
+                                           None) == L.GJ_EINVAL
+    assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 0, 2, 1, 1,
+                                           None) == L.GJ_EINVAL
     assert lib.gj_gemm_split_bf16(3, 2, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
     assert lib.gj_gemm_split_bf16(1, 4, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
     assert lib.gj_destroy(h) == L.GJ_OK

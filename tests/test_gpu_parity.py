@@ -244,20 +244,24 @@ def test_accept_agreement_monge_funnel100():
     assert agree / total >= 0.999
 
 
-@pytest.mark.parametrize("path,loop,chol", [("simt", "host", "fp64"), ("tcgen05", "host", "fp64"),
-                                             ("tcgen05", "graph", "fp64"), ("simt", "graph", "fp64"),
-                                             ("tcgen05", "graph", "fp32")])
-def test_logreg_batched_per_step(path, loop, chol):
+@pytest.mark.parametrize("path,loop,chol,d,C", [
+    ("simt", "host", "fp64", 9, 160), ("tcgen05", "host", "fp64", 9, 160),
+    ("tcgen05", "graph", "fp64", 9, 160), ("simt", "graph", "fp64", 9, 160),
+    ("tcgen05", "graph", "fp32", 9, 160),
+    # 8 chains share a warp in the factorisation at d = 9; at d = 40 two do,
+    # and 37 chains leave a ragged last warp
+    ("tcgen05", "graph", "fp64", 40, 37), ("tcgen05", "host", "fp32", 40, 37)])
+def test_logreg_batched_per_step(path, loop, chol, d, C):
     """The batched dense-Fisher path (split-BF16 contractions, FP64 fixed-point
     iterates, FP64 or FP32 factorisation, host-driven loop or one CUDA-graph
     launch) against the oracle: per-step positions over 10 steps within 1e-5."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
-    kw = dict(N=300, d=9, seed=3)
+    kw = dict(N=300 if d < 32 else 500, d=d, seed=3)
     ot = oracle_target("logreg", **kw)
     dt = device_target("logreg", "mixed", **kw)
-    C, h, L = 160, 0.05, 10
+    h, L = 0.05, 10
     q0 = start_positions(ot.dim, C, seed=1, scale=0.2).astype(np.float32).astype(np.float64)
     z, _ = normals(C, ot.dim, 2, np.float32)
     u = -np.ones(C)
@@ -271,10 +275,10 @@ def test_logreg_batched_per_step(path, loop, chol):
         assert e < 1e-5, f"step {step}: {e}"
     assert rel_err(_np(info.energy), oinfo.energy) < 1e-4
     # iteration counts over the 10 solves agree up to solves whose norm lands
-    # next to the tolerance (FP32-level rounding of the map); no solve may run
-    # away towards max_iters
+    # next to the tolerance (FP32-level rounding of the map, more of it at
+    # larger d); no solve may run away towards max_iters
     diff = np.abs(_np(info.fixed_point_iters) - oinfo.fixed_point_iters)
-    assert diff.max() <= 10 and diff.mean() < 2.5, (diff.max(), diff.mean())
+    assert diff.max() <= 10 and diff.mean() < (2.5 if d < 32 else 5.0), (diff.max(), diff.mean())
 
 
 def test_logreg_batched_accept_and_graph_reuse():
