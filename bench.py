@@ -38,6 +38,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "min-ESS/s and leapfrog steps/s, batched mixed-precision vs plain FP64 CUDA, 1 GB300"
 
+# DRAM bytes (read + write) per GEMM launch on the default logistic-regression
+# workload (4096 chains), averaged over the five GEMMs of one map evaluation,
+# from one ncu capture (profiles/gemm_tc_and_chol_logreg_N1000_d25_C4096_ncu.md).
+# Reported only for that chain count.
+NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 24.2e6}
+
 WORKLOADS = {
     "logreg": dict(name="logistic_regression_N1000_d25_rmhmc_fisher_4096chains", N=1000, d=25,
                    C=4096, L=8, h=0.05, sampler="rmhmc"),
@@ -241,7 +247,8 @@ def run_ours(args, wl):
         roof = {"bound": "tensor", "kernel": "gemm_tc_kernel (split-BF16 tcgen05)",
                 "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                 "frac": round(achieved / peak, 4), "peak_source": f"{src} bf16 sustained",
-                "traffic": None,
+                "traffic": NCU_TRAFFIC_PER_GEMM_LAUNCH.get((wl["name"], C)),
+                "traffic_unit": "bytes per GEMM launch (ncu dram read + write)",
                 "gemm_ms_per_transition": round(prof[4] * 1e-6 / min(K, 3), 3),
                 "gemm_launches_per_transition": int(prof[1] // min(K, 3)),
                 "evals_per_transition": round(prof[0] / min(K, 3), 2)}
