@@ -141,6 +141,7 @@ def run_ours(args, wl):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     C, Lsteps, h = wl["C"], wl["L"], wl["h"]
+    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else 1))
     if wl["sampler"] == "rmhmc":
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
@@ -260,6 +261,7 @@ def run_ours(args, wl):
         "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
                    "step_size": h, "precision": "mixed", "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
+                   "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
@@ -444,6 +446,10 @@ def main():
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="fixed-point loop driver of the batched path (host: profilable by ncu)")
     ap.add_argument("--cholesky", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--gemm-tile-n", type=int, default=128, choices=[64, 128],
+                    help="tcgen05 GEMM output tile width for N > 64")
+    ap.add_argument("--gemm-one-cta", action="store_true",
+                    help="deeper operand ring, one CTA per SM")
     ap.add_argument("--chol-cpw", type=int, default=0, choices=[0, 1, 2, 4, 8],
                     help="chains per warp in the metric factorisation (0 = automatic)")
     args = ap.parse_args()

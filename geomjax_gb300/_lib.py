@@ -101,6 +101,7 @@ SIGNATURES = {
     "gj_hvp": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                          c_void_p]),
     "gj_metric": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "gj_set_gemm_tiling": (c_int32, [c_int32, c_int32]),
     "gj_logreg_gl_transition_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_void_p, c_void_p,
                                               c_double, c_double, c_int32, c_int32, c_int32,
                                               c_int32, c_void_p, c_void_p]),

@@ -177,7 +177,9 @@ cudaError_t gemm_simt(const GemmArgs& g, cudaStream_t st);
 
 // tcgen05 path: tensor maps are built once per operand buffer.
 struct TcOperand {
-  CUtensorMap map;
+  CUtensorMap map;    // 64 x 128-row boxes (A operands, B with 128-wide tiles)
+  CUtensorMap map64;  // 64 x 64-row boxes (B with 64-wide tiles)
+  CUtensorMap map32;  // 64 x 32-row boxes (B with 32-wide tiles)
   SplitMat s;
 };
 // Encodes the operand's tensor map in place (no allocation); false on error.
@@ -186,6 +188,10 @@ TcOperand* tc_operand_create(const SplitMat& s, int box_rows, const char** err);
 void tc_operand_destroy(TcOperand* op);
 bool tc_available();
 cudaError_t gemm_tc_prepare();  // raises the kernel's shared-memory limit (call before capture)
+// Process-wide tile policy: bn_wide = 64 or 128 for N > 64; two_ctas = 1
+// limits the operand ring so that two CTAs share an SM.  Takes effect for
+// launches (and graph captures) made after the call.
+void gemm_tc_set_tuning(int bn_wide, int two_ctas);
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
 

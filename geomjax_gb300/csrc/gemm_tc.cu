@@ -17,6 +17,7 @@
 // in *err and skips the rest of its work, releasing TMEM before exit.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "gemm.cuh"
@@ -25,15 +26,21 @@ namespace gj {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int TILE_BYTES = 128 * BK * 2;          // one 128 x 64 BF16 box
-constexpr int TMEM_COLS = 128;
-// NPL planes per operand: a stage holds NPL A boxes and NPL B boxes
-template <int NPL>
+constexpr int BM = 128, BK = 64;
+constexpr int A_TILE_BYTES = BM * BK * 2;         // one 128 x 64 BF16 box
+// NPL planes per operand, BN output columns per CTA (32, 64 or 128): a stage
+// holds NPL A boxes (128 x 64) and NPL B boxes (BN x 64)
+template <int NPL, int BN>
 struct Cfg {
-  static constexpr int STAGES = NPL == 2 ? 3 : 2;
-  static constexpr int STAGE_BYTES = 2 * NPL * TILE_BYTES;
-  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+  static constexpr int B_TILE_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = NPL * (A_TILE_BYTES + B_TILE_BYTES);
+  // up to 4 stages within the 227 KB a CTA may use
+  static constexpr int FIT = (227 * 1024 - 1024 - 256) / STAGE_BYTES;
+  static constexpr int MAX_STAGES = FIT < 4 ? FIT : 4;
+  static constexpr int TMEM_COLS = BN < 32 ? 32 : BN;
+  static constexpr int IDESC = (1 << 4) | (1 << 7) | (1 << 10) | ((BN >> 3) << 17) |
+                               ((BM >> 4) << 24);
+  static constexpr int smem(int stages) { return stages * STAGE_BYTES + 1024 + 256; }
 };
 constexpr long long WAIT_LIMIT = 1ll << 26;       // polls before giving up
 
@@ -106,16 +113,14 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-// instruction descriptor, kind::f16: D = F32 (bit 4), A = B = BF16 (bits 7, 10),
-// both K-major, N>>3 at [17,23), M>>4 at [24,29)
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+// instruction descriptor (Cfg::IDESC), kind::f16: D = F32 (bit 4), A = B = BF16
+// (bits 7, 10), both K-major, N>>3 at [17,23), M>>4 at [24,29)
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -139,107 +144,117 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Epilogue of one 32 x 32 chunk handled by one warp: lane l holds row
-// m_base + l (v[0..31] = columns n_base..+31).  Values go through a per-warp
-// shared-memory tile (stride 33) so that every global access is a whole row
-// of the chunk written by the 32 lanes together: 128 B per row for FP32,
-// 64 B per BF16 plane — full sectors, no read-modify-write in L2.
+// Epilogue of one 32 x 32 chunk handled by one warp.  The accumulator rows
+// (lane l holds row m_base + l, v[0..31] = columns n_base..+31) are staged
+// once in the warp's shared-memory tile (stride 33: conflict-free both ways),
+// then read back as row segments: in pass it (0..3) lane l takes row
+// 8·it + l/4, columns 8·(l%4) .. +7.  Each lane then works on 8 consecutive
+// values of one row, so every global access is 16 bytes per lane (one row
+// of the chunk = 4 lanes) and few registers stay live.
 __device__ __forceinline__ void stage_row(float* stg, int lane, const float* v) {
 #pragma unroll
   for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = v[j];
   __syncwarp();
 }
 
-__device__ __forceinline__ void load_tile(float* stg, int lane, const float* src, int ld, int m_base,
-                                          int n_base, int M, int N, float* out) {
-  const int n = n_base + lane;
-  float t[32];
-#pragma unroll
-  for (int r = 0; r < 32; ++r) {  // 32 independent loads in flight per lane
-    const int m = m_base + r;
-    t[r] = (m < M && n < N) ? __ldg(src + (size_t)m * ld + n) : 0.f;
-  }
-#pragma unroll
-  for (int r = 0; r < 32; ++r) stg[r * 33 + lane] = t[r];
-  __syncwarp();
-#pragma unroll
-  for (int j = 0; j < 32; ++j) out[j] = stg[lane * 33 + j];
-  __syncwarp();
+__device__ __forceinline__ bool aligned16(const void* p, int ld) {
+  return ((reinterpret_cast<uintptr_t>(p) & 15) == 0) && ((ld & 3) == 0);
 }
 
-__device__ __forceinline__ void store_f32(const float* stg, int lane, float* dst, int ld, int m_base,
-                                          int n_base, int M, int N) {
-  const int n = n_base + lane;
-  if (n < N) {
+__device__ __forceinline__ void load8(const float* src, int n, int N, bool vec, float* out) {
+  if (vec) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(src));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(src) + 1);
+    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+  } else {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
-      const int m = m_base + r;
-      if (m < M) dst[(size_t)m * ld + n] = stg[r * 33 + lane];
-    }
+    for (int k = 0; k < 8; ++k) out[k] = (n + k < N) ? __ldg(src + k) : 0.f;
   }
-  __syncwarp();
 }
 
-__device__ __forceinline__ void store_split(const float* stg, int lane, const SplitMat& S, int row_off,
-                                            int m_base, int n_base, int M, int N) {
-  const int n = n_base + lane;
-  if (n < N) {
+__device__ __forceinline__ void store8(float* dst, int n, int N, bool vec, const float* x) {
+  if (vec) {
+    reinterpret_cast<float4*>(dst)[0] = make_float4(x[0], x[1], x[2], x[3]);
+    reinterpret_cast<float4*>(dst)[1] = make_float4(x[4], x[5], x[6], x[7]);
+  } else {
 #pragma unroll
-    for (int r = 0; r < 32; ++r) {
-      const int m = m_base + r;
-      if (m < M) split_store(S, row_off + m, n, stg[r * 33 + lane]);
-    }
+    for (int k = 0; k < 8; ++k)
+      if (n + k < N) dst[k] = x[k];
   }
-  __syncwarp();
+}
+
+__device__ __forceinline__ void split8(const SplitMat& S, int row, int n, int N, bool full,
+                                       const float* x) {
+  if (full) {
+    split_store8(S, row, n, x);  // plane rows are 128-byte aligned, n a multiple of 8
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (n + k < N) split_store(S, row, n + k, x[k]);
+  }
 }
 
 __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, int m_base, int n_base,
-                                          int M, int N, float* v) {
-  if (e.mode == EPI_STORE) {
-    stage_row(stg, lane, v);
-    store_f32(stg, lane, e.D, e.ldd, m_base, n_base, M, N);
-    return;
-  }
-  if (e.mode == EPI_SIGMOID) {
-    float lp[32], r1[32];
-    double ld = 0.0;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int n = n_base + j;
-      const float yv = (n < N) ? e.y[n] : 0.f;
-      const float a = v[j];
-      const float sg = 1.f / (1.f + __expf(-a));
-      if (e.ld_acc && n < N) ld += double(yv * a - softplus(a));
-      v[j] = sg * (1.f - sg);  // Λ
-      lp[j] = v[j] * (1.f - 2.f * sg);
-      r1[j] = yv - sg;
-    }
-    const int m = m_base + lane;
-    if (e.ld_acc && m < M) atomicAdd(&e.ld_acc[m], ld);
-    stage_row(stg, lane, v);
-    store_split(stg, lane, e.lam, 0, m_base, n_base, M, N);
-    stage_row(stg, lane, lp);
-    store_f32(stg, lane, e.lp, e.lp_ld, m_base, n_base, M, N);
-    stage_row(stg, lane, r1);
-    store_split(stg, lane, e.r, 0, m_base, n_base, M, N);
-    return;
-  }
-  // EPI_TRACE: r2 = Λ'(w − s²)
-  float sv[32], lv[32];
-  load_tile(stg, lane, e.S, e.s_ld, m_base, n_base, M, N, sv);
-  load_tile(stg, lane, e.lp, e.lp_ld, m_base, n_base, M, N, lv);
-#pragma unroll
-  for (int j = 0; j < 32; ++j) v[j] = lv[j] * (v[j] - sv[j] * sv[j]);
+                                          int M, int N, const float* v) {
   stage_row(stg, lane, v);
-  store_split(stg, lane, e.r, e.r_off, m_base, n_base, M, N);
+  const int cc = (lane & 3) * 8;
+  const int n = n_base + cc;
+  const bool full = n + 8 <= N;
+#pragma unroll 1
+  for (int it = 0; it < 4; ++it) {
+    const int rr = it * 8 + (lane >> 2);
+    const int m = m_base + rr;
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = stg[rr * 33 + cc + k];
+    if (e.mode == EPI_STORE) {
+      if (m < M) store8(e.D + (size_t)m * e.ldd + n, n, N, full && aligned16(e.D, e.ldd), a);
+    } else if (e.mode == EPI_SIGMOID) {
+      float yv[8], lam[8], lp[8], r1[8];
+      load8(e.y + n, n, N, full && aligned16(e.y, 0), yv);
+      double ld = 0.0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float sg = __fdividef(1.f, 1.f + __expf(-a[k]));
+        lam[k] = sg * (1.f - sg);
+        lp[k] = lam[k] * (1.f - 2.f * sg);
+        r1[k] = yv[k] - sg;
+        if (e.ld_acc && n + k < N) ld += double(yv[k] * a[k] - softplus(a[k]));
+      }
+      if (m < M) {
+        split8(e.lam, m, n, N, full, lam);
+        store8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lp);
+        split8(e.r, m, n, N, full, r1);
+      }
+      if (e.ld_acc) {  // the 4 lanes of a row, then one atomic per row and chunk
+        ld += __shfl_xor_sync(0xffffffffu, ld, 1);
+        ld += __shfl_xor_sync(0xffffffffu, ld, 2);
+        if ((lane & 3) == 0 && m < M) atomicAdd(&e.ld_acc[m], ld);
+      }
+    } else {  // EPI_TRACE: r2 = Λ'(w − s²)
+      if (m < M) {
+        float sv[8], lv[8], r2[8];
+        load8(e.S + (size_t)m * e.s_ld + n, n, N, full && aligned16(e.S, e.s_ld), sv);
+        load8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r2[k] = lv[k] * (a[k] - sv[k] * sv[k]);
+        split8(e.r, e.r_off + m, n, N, full, r2);
+      }
+    }
+  }
+  __syncwarp();  // the tile is reused by the warp's next chunk
 }
 
-template <int NPL>
-__global__ void __launch_bounds__(320, 1)
+// STAGES (run time, 1 .. Cfg::MAX_STAGES) is the depth of the operand ring,
+// chosen by the host so that two CTAs share an SM where that fits.
+template <int NPL, int BN>
+__global__ void __launch_bounds__(320, 2)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err) {
-  constexpr int STAGES = Cfg<NPL>::STAGES;
-  constexpr int STAGE_BYTES = Cfg<NPL>::STAGE_BYTES;
+                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err, int STAGES) {
+  using C = Cfg<NPL, BN>;
+  constexpr int STAGE_BYTES = C::STAGE_BYTES;
+  constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned tile ring (required by the 128B swizzle), then barriers
   unsigned char* base = reinterpret_cast<unsigned char*>(
@@ -287,8 +302,9 @@ __global__ void __launch_bounds__(320, 1)
         const int x = kb * BK;
 #pragma unroll
         for (int q = 0; q < NPL; ++q) {
-          tma_load_2d(st + q * TILE_BYTES, &mapA, &full[s], x, q * rpadA + m0);
-          tma_load_2d(st + (NPL + q) * TILE_BYTES, &mapB, &full[s], x, q * rpadB + n0);
+          tma_load_2d(st + q * A_TILE_BYTES, &mapA, &full[s], x, q * rpadA + m0);
+          tma_load_2d(st + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES, &mapB, &full[s], x,
+                      q * rpadB + n0);
         }
       }
     }
@@ -308,21 +324,22 @@ __global__ void __launch_bounds__(320, 1)
         uint64_t da[NPL], db[NPL];
 #pragma unroll
         for (int q = 0; q < NPL; ++q) {
-          da[q] = make_desc(sa + q * TILE_BYTES);
-          db[q] = make_desc(sa + (NPL + q) * TILE_BYTES);
+          da[q] = make_desc(sa + q * A_TILE_BYTES);
+          db[q] = make_desc(sa + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES);
         }
+        constexpr uint32_t ID = (uint32_t)C::IDESC;
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
           const uint64_t adv = (uint64_t)((k * 32) >> 4);  // 16 BF16 = 32 B along K
           // plane products with i + j <= NPL - 1 (the dropped ones are below
           // the last plane's resolution)
-          mma_bf16(tmem, da[0] + adv, db[0] + adv, (kb > 0 || k > 0) ? 1u : 0u);
-          mma_bf16(tmem, da[0] + adv, db[1] + adv, 1u);
-          mma_bf16(tmem, da[1] + adv, db[0] + adv, 1u);
+          mma_bf16(tmem, da[0] + adv, db[0] + adv, ID, (kb > 0 || k > 0) ? 1u : 0u);
+          mma_bf16(tmem, da[0] + adv, db[1] + adv, ID, 1u);
+          mma_bf16(tmem, da[1] + adv, db[0] + adv, ID, 1u);
           if (NPL == 3) {
-            mma_bf16(tmem, da[0] + adv, db[NPL - 1] + adv, 1u);
-            mma_bf16(tmem, da[1] + adv, db[1] + adv, 1u);
-            mma_bf16(tmem, da[NPL - 1] + adv, db[0] + adv, 1u);
+            mma_bf16(tmem, da[0] + adv, db[NPL - 1] + adv, ID, 1u);
+            mma_bf16(tmem, da[1] + adv, db[1] + adv, ID, 1u);
+            mma_bf16(tmem, da[NPL - 1] + adv, db[0] + adv, ID, 1u);
           }
         }
         mma_commit(&empty[s]);
@@ -387,14 +404,20 @@ bool tc_operand_init(TcOperand* op, const SplitMat& s, const char** err) {
   op->s = s;
   cuuint64_t dims[2] = {(cuuint64_t)s.ld, (cuuint64_t)s.planes * s.rpad};
   cuuint64_t strides[1] = {(cuuint64_t)s.ld * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, 128u};
   cuuint32_t estr[2] = {1u, 1u};
-  CUresult r = enc(&op->map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s.p, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    *err = "cuTensorMapEncodeTiled failed";
-    return false;
+  // boxes of 64 K-elements by 128, 64 and 32 rows (A tiles and the B tiles
+  // of the three tile widths)
+  CUtensorMap* maps[3] = {&op->map, &op->map64, &op->map32};
+  const cuuint32_t rows[3] = {128u, 64u, 32u};
+  for (int i = 0; i < 3; ++i) {
+    cuuint32_t box[2] = {(cuuint32_t)BK, rows[i]};
+    CUresult r = enc(maps[i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s.p, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      *err = "cuTensorMapEncodeTiled failed";
+      return false;
+    }
   }
   return true;
 }
@@ -410,12 +433,71 @@ TcOperand* tc_operand_create(const SplitMat& s, int, const char** err) {
 
 void tc_operand_destroy(TcOperand* op) { delete op; }
 
+namespace {
+
+template <int NPL, int BN>
+cudaError_t set_smem_limit() {
+  return cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<NPL, BN>::smem(Cfg<NPL, BN>::MAX_STAGES));
+}
+
+}  // namespace
+
 cudaError_t gemm_tc_prepare() {
-  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       Cfg<2>::SMEM_BYTES);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(gemm_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<3>::SMEM_BYTES);
+  cudaError_t e = cudaSuccess;
+  const cudaError_t r[6] = {set_smem_limit<2, 32>(), set_smem_limit<2, 64>(),
+                            set_smem_limit<2, 128>(), set_smem_limit<3, 32>(),
+                            set_smem_limit<3, 64>(), set_smem_limit<3, 128>()};
+  for (cudaError_t x : r)
+    if (x != cudaSuccess) e = x;
+  return e;
+}
+
+namespace {
+
+// Tile and pipeline choice.  BN: the narrowest of 32 / 64 covering N, else
+// 128 (or 64 when asked).  Stages: as many as the K blocks need (at most
+// MAX_STAGES), cut back towards the shared memory that lets two CTAs share
+// an SM but never below two stages when there are several K blocks (one
+// stage would serialise every TMA load with its MMAs).
+struct TcTuning {
+  int bn_wide = 128;       // tile width for N > 64
+  int two_ctas = 1;        // prefer two CTAs per SM
+};
+TcTuning g_tune;
+
+constexpr int kTwoCtaSmem = 113 * 1024;
+
+template <int NPL, int BN>
+cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                      cudaStream_t st) {
+  using C = Cfg<NPL, BN>;
+  const int kb = (g.K + BK - 1) / BK;
+  int ns = std::max(1, std::min(C::MAX_STAGES, kb));
+  if (g_tune.two_ctas)  // keep two stages when there is more than one K block
+    while (ns > 2 && C::smem(ns) > kTwoCtaSmem) --ns;
+  else
+    ns = std::min(ns, 3);
+  const CUtensorMap& mb = BN == 128 ? b->map : (BN == 64 ? b->map64 : b->map32);
+  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
+  gemm_tc_kernel<NPL, BN><<<grid, 320, C::smem(ns), st>>>(a->map, mb, a->s.rpad, b->s.rpad, g.M,
+                                                           g.N, g.K, g.epi, err, ns);
+  return cudaGetLastError();
+}
+
+template <int NPL>
+cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                             cudaStream_t st) {
+  if (g.N <= 32) return launch_tc<NPL, 32>(g, a, b, err, st);
+  if (g.N <= 64 || g_tune.bn_wide == 64) return launch_tc<NPL, 64>(g, a, b, err, st);
+  return launch_tc<NPL, 128>(g, a, b, err, st);
+}
+
+}  // namespace
+
+void gemm_tc_set_tuning(int bn_wide, int two_ctas) {
+  g_tune.bn_wide = bn_wide == 64 ? 64 : 128;
+  g_tune.two_ctas = two_ctas ? 1 : 0;
 }
 
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
@@ -425,14 +507,8 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
   if (g.M > a->s.rpad || g.N > b->s.rpad || g.K > a->s.ld || g.K > b->s.ld ||
       a->s.planes != b->s.planes)
     return cudaErrorInvalidValue;
-  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
-  if (a->s.planes == 3)
-    gemm_tc_kernel<3><<<grid, 320, Cfg<3>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
-                                                            g.M, g.N, g.K, g.epi, err);
-  else
-    gemm_tc_kernel<2><<<grid, 320, Cfg<2>::SMEM_BYTES, st>>>(a->map, b->map, a->s.rpad, b->s.rpad,
-                                                            g.M, g.N, g.K, g.epi, err);
-  return cudaGetLastError();
+  return a->s.planes == 3 ? launch_tc_planes<3>(g, a, b, err, st)
+                          : launch_tc_planes<2>(g, a, b, err, st);
 }
 
 }  // namespace gj

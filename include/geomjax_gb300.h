@@ -228,6 +228,13 @@ int32_t gj_metric(const gj_target* target, int32_t precision, int32_t num_chains
 int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_chains,
                       const void* q, const void* w, void* out, void* stream);
 
+/* Process-wide tile policy of the tcgen05 split-BF16 GEMMs: output tile
+ * width for N > 64 (64 or 128; narrower N always takes 32 or 64) and whether
+ * the operand ring is cut back so that two CTAs share an SM (1, default) or
+ * kept up to three stages (0).  Applies to launches and CUDA-graph captures
+ * made after the call (a context's captured graph keeps its tiles). */
+int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm);
+
 /* Derivatives of one RMHMC transition with the generalized leapfrog, for a
  * GJ_LOGREG target with float64 data: with respect to the step size h and
  * the metric regulariser λ (G = XᵀΛX + λI; the prior variance stays
