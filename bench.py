@@ -147,7 +147,8 @@ def run_ours(args, wl):
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
         kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path, loop=args.loop,
                                      cholesky=args.cholesky,
-                                     chol_chains_per_warp=args.chol_cpw)
+                                     chol_chains_per_warp=args.chol_cpw,
+                                     chain_groups=args.groups)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -261,7 +262,7 @@ def run_ours(args, wl):
         "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
                    "step_size": h, "precision": "mixed", "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
-                   "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
+                   "chain_groups": args.groups or "auto", "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
@@ -450,6 +451,8 @@ def main():
                     help="tcgen05 GEMM output tile width for N > 64")
     ap.add_argument("--gemm-one-cta", action="store_true",
                     help="deeper operand ring, one CTA per SM")
+    ap.add_argument("--groups", type=int, default=0,
+                    help="chain groups on concurrent streams (0 = automatic)")
     ap.add_argument("--chol-cpw", type=int, default=0, choices=[0, 1, 2, 4, 8],
                     help="chains per warp in the metric factorisation (0 = automatic)")
     args = ap.parse_args()

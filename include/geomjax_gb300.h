@@ -162,6 +162,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * whatever the lanes in use, so packing chains divides its FP64 work, while
  * fewer warps hide less latency. */
 #define GJ_OPT_CHOL_CHAINS_PER_WARP 5
+/* batched path: independent chain groups (1 .. 8; 0 = automatic = 1).  In
+ * graph mode each group's transition is its own CUDA graph on its own
+ * stream, forked from and joined to the caller's stream, so that one group's
+ * FP64 factorisation may overlap another group's GEMMs.  Results are
+ * bit-identical for any group count. */
+#define GJ_OPT_CHAIN_GROUPS 6
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */
