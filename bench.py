@@ -49,6 +49,8 @@ WORKLOADS = {
                    C=4096, L=8, h=0.05, sampler="rmhmc"),
     "monge": dict(name="funnel_D100_lmcmonge_alpha1_8192chains", D=100, C=8192, L=16, h=0.02,
                   sampler="lmcmonge"),
+    "uneven": dict(name="uneven_logreg_2048posteriors_N200-5000_d8-128_64chains", B=2048, C=64,
+                   L=8, h=0.05, sampler="batch"),
 }
 
 
@@ -276,6 +278,100 @@ def run_ours(args, wl):
     return out
 
 
+def run_batch(args, wl):
+    """Uneven batch: B logistic-regression posteriors with N and d
+    log-uniform in [200, 5000] and [8, 128], C chains each, one transition =
+    every posterior's CUDA graph on a pool of streams."""
+    import numpy as np
+    import torch
+
+    from geomjax_gb300 import _lib as L
+    from geomjax_gb300.batch import PosteriorBatch
+    from geomjax_gb300.data import logreg_data, uneven_logreg_batch
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B, C, Lsteps, h = wl["B"], wl["C"], wl["L"], wl["h"]
+    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else 1))
+    Ns, ds = uneven_logreg_batch(B, seed=rank)
+    t_setup = time.perf_counter()
+    data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
+    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev)
+    del data
+    g0 = torch.Generator().manual_seed(rank)
+    state = pb.init([0.01 * torch.randn(C, int(d), generator=g0) for d in ds])
+    n = int(pb.offsets[-1])
+    K, W = args.steps, args.warmup
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    Z = torch.randn(K + W, n, generator=gen, device=dev, dtype=torch.float32)
+    U = torch.rand(K + W, B * C, generator=gen, device=dev, dtype=torch.float64)
+    info = pb.new_info()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for i in range(W):
+        pb.step_inplace(state, Z[i], U[i], info, h, Lsteps)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    acc_sum = torch.zeros(B * C, dtype=torch.float64, device=dev)
+    clocks = ClockSampler(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for i in range(K):
+        flush.zero_()
+        evs[i][0].record(stream)
+        pb.step_inplace(state, Z[W + i], U[W + i], info, h, Lsteps)
+        evs[i][1].record(stream)
+        acc_sum += info["acceptance_rate"]
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    dev_s = _barrier_max(sum(a.elapsed_time(b) for a, b in evs) / 1e3, ws)
+    steps_per_s = ws * B * C * Lsteps * K / dev_s
+    # e2e: host draws in, positions and accept flags out, every transition
+    Zh = torch.randn(n, generator=torch.Generator().manual_seed(9)).pin_memory()
+    Uh = torch.rand(B * C, dtype=torch.float64, generator=torch.Generator().manual_seed(8)).pin_memory()
+    Ph = torch.empty(n, dtype=torch.float32).pin_memory()
+    Ah = torch.empty(B * C, dtype=torch.uint8).pin_memory()
+    Zd, Ud = torch.empty_like(Zh, device=dev), torch.empty_like(Uh, device=dev)
+    e2e_steps = max(1, min(K, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        Zd.copy_(Zh, non_blocking=True)
+        Ud.copy_(Uh, non_blocking=True)
+        pb.step_inplace(state, Zd, Ud, info, h, Lsteps)
+        Ph.copy_(state.position, non_blocking=True)
+        Ah.copy_(info["is_accepted"], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = _barrier_max(time.perf_counter() - t0, ws)
+    return {
+        "metric": "leapfrog steps/s over all chains of an uneven posterior batch, 1 GB300",
+        "value": round(steps_per_s, 1), "unit": "leapfrog steps/s", "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": round(1e3 * dev_s / K, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["name"], "posteriors": B, "chains_per_posterior": C,
+                   "integration_steps": Lsteps, "step_size": h, "streams": args.streams,
+                   "mean_N": float(np.mean(Ns)), "mean_d": float(np.mean(ds)),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
+        "e2e": {"value": round(ws * B * C * Lsteps * e2e_steps / e2e_s, 1), "unit": "leapfrog steps/s",
+                "h2d_bytes_per_step": int(Zh.numel() * 4 + Uh.numel() * 8),
+                "d2h_bytes_per_step": int(Ph.numel() * 4 + Ah.numel())},
+        "graph_launches": B * K, "setup_s": round(t_setup, 1), "clocks": clk,
+        "wall_s": round(t_wall, 3),
+    }
+
+
 def run_plain_fp64(args, wl):
     """The plain per-chain FP64 CUDA form of the same workload: one thread
     per chain, every vector and the metric algebra in float64.  For the
@@ -400,6 +496,29 @@ def run_reference(args, wl):
         def step(s):
             s2, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
             return s2
+    elif wl["sampler"] == "batch":
+        # a bounded sample of the uneven batch: 8 chains of each of the first
+        # four posteriors, one after another as the reference would run them
+        from geomjax_gb300.data import uneven_logreg_batch
+
+        Ns, ds = uneven_logreg_batch(wl["B"], seed=0)
+        C = 8
+        posts = []
+        for i in range(4):
+            X, y = OT.make_logreg_data(int(Ns[i]), int(ds[i]), seed=1000 + i)
+            ot_i = OT.LogisticRegression(X, y)
+            posts.append((ot_i, int(ds[i]), O_rm.init(ot_i, rng.standard_normal((C, int(ds[i]))) * 0.01)))
+        C = 8 * len(posts)
+
+        def step(s):
+            out = []
+            for ot_i, d_i, s_i in s:
+                s2, _ = O_rm.kernel(ot_i, s_i, rng.standard_normal((8, d_i)), rng.random(8),
+                                    wl["h"], wl["L"])
+                out.append((ot_i, d_i, s2))
+            return out
+
+        s = posts
     else:
         d = wl["D"]
         ot = OT.Funnel(D=d)
@@ -453,6 +572,8 @@ def main():
                     help="deeper operand ring, one CTA per SM")
     ap.add_argument("--groups", type=int, default=0,
                     help="chain groups on concurrent streams (0 = automatic)")
+    ap.add_argument("--streams", type=int, default=16, help="stream pool of the uneven batch")
+    ap.add_argument("--posteriors", type=int, default=None, help="override the uneven batch size")
     ap.add_argument("--chol-cpw", type=int, default=0, choices=[0, 1, 2, 4, 8],
                     help="chains per warp in the metric factorisation (0 = automatic)")
     args = ap.parse_args()
@@ -460,6 +581,9 @@ def main():
     if args.chains:
         wl["C"] = args.chains
         wl["name"] = wl["name"].rsplit("_", 1)[0] + f"_{args.chains}chains"
+    if args.posteriors and "B" in wl:
+        wl["B"] = args.posteriors
+        wl["name"] = wl["name"].replace("2048posteriors", f"{args.posteriors}posteriors")
     ws, rank, local = _dist()
     if args.impl == "reference":
         out = run_reference(args, wl)
@@ -472,6 +596,11 @@ def main():
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if wl["sampler"] == "batch":
+        out = run_batch(args, wl)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return
     out = run_ours(args, wl)
     if rank == 0:
         if not args.no_plain:

@@ -102,6 +102,11 @@ SIGNATURES = {
                          c_void_p]),
     "gj_metric": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     "gj_set_gemm_tiling": (c_int32, [c_int32, c_int32]),
+    "gj_batch_create": (c_int32, [c_void_p, c_int32, c_int32, c_int32, POINTER(c_void_p)]),
+    "gj_batch_destroy": (c_int32, [c_void_p]),
+    "gj_batch_set_option": (c_int32, [c_void_p, c_int32, c_int64]),
+    "gj_batch_rmhmc_step": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p]),
     "gj_logreg_gl_transition_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_void_p, c_void_p,
                                               c_double, c_double, c_int32, c_int32, c_int32,
                                               c_int32, c_void_p, c_void_p]),

@@ -521,6 +521,140 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const do
   return cuda_status(e, "gj_logreg_gl_transition_jvp");
 }
 
+// ---------------------------------------------------------------------------
+// batches of independent dense-Fisher logistic-regression posteriors
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct gj_batch {
+  int B, C, S;
+  std::vector<gj::LogregBatched*> lbs;
+  std::vector<int> dims;
+  std::vector<size_t> pos_off;  // [B + 1] offsets of each posterior's [C, d_b] block
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork;
+};
+
+namespace {
+
+void batch_free(gj_batch* b) {
+  for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_destroy(lb);
+  for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
+                        int32_t chains_per_posterior, int32_t num_streams, gj_batch** out) {
+  if (!out) return fail(GJ_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (!targets || num_posteriors < 1) return fail(GJ_EINVAL, "need at least one target");
+  if (chains_per_posterior < 1) return fail(GJ_EINVAL, "chains_per_posterior must be >= 1");
+  if (num_streams < 1 || num_streams > 64) return fail(GJ_EINVAL, "num_streams must be 1..64");
+  for (int b = 0; b < num_posteriors; ++b) {
+    const gj_target& t = targets[b];
+    int st = check_target(&t, GJ_MIXED);
+    if (st) return st;
+    if (t.family != GJ_LOGREG || t.metric != GJ_METRIC_DENSE_FISHER)
+      return fail(GJ_EINVAL, "a batch holds dense-Fisher logistic-regression targets");
+    if (t.dim > 128) return fail(GJ_ENOTSUP, "batched logistic regression supports d <= 128");
+  }
+  gj_batch* b = new (std::nothrow) gj_batch();
+  if (!b) return fail(GJ_ENOMEM, "host allocation failed");
+  b->B = num_posteriors;
+  b->C = chains_per_posterior;
+  b->S = num_streams < num_posteriors ? num_streams : num_posteriors;
+  b->fork = nullptr;
+  b->pos_off.push_back(0);
+  for (int i = 0; i < num_posteriors; ++i) {
+    gj::LogregBatched* lb = nullptr;
+    const int rc = gj::logreg_batched_create(gj::to_dev(targets[i]), b->C, &lb);
+    if (rc) {
+      const std::string msg = gj::logreg_batched_error();
+      batch_free(b);
+      return fail(rc, "%s", msg.c_str());
+    }
+    b->lbs.push_back(lb);
+    b->dims.push_back(targets[i].dim);
+    b->pos_off.push_back(b->pos_off.back() + (size_t)b->C * targets[i].dim);
+  }
+  bool ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int s = 0; s < b->S && ok; ++s) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) b->streams.push_back(st);
+    ok = ok && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) b->joins.push_back(ev);
+  }
+  if (!ok) {
+    batch_free(b);
+    return fail(GJ_ECUDA, "stream or event creation failed");
+  }
+  *out = b;
+  return GJ_OK;
+}
+
+int32_t gj_batch_destroy(gj_batch* b) {
+  if (b) batch_free(b);
+  return GJ_OK;
+}
+
+int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
+  if (!b) return fail(GJ_EINVAL, "batch is NULL");
+  if (key == GJ_OPT_CHOL_FP64) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "factorisation precision flag must be 0 or 1");
+    for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_chol_fp64(lb, (int)value);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_CHOL_CHAINS_PER_WARP) {
+    if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+      return fail(GJ_EINVAL, "chains per warp must be 0 (automatic), 1, 2, 4 or 8");
+    for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_chol_cpw(lb, (int)value);
+    return GJ_OK;
+  }
+  return fail(GJ_EINVAL, "unknown batch option");
+}
+
+int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state* s,
+                            const float* z, const double* u, gj_info* info, void* stream) {
+  if (!b) return fail(GJ_EINVAL, "batch is NULL");
+  int st = check_params(p);
+  if (!st) st = check_state(s, b->B * b->C, false);
+  if (st) return st;
+  if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
+  if (p->integrator != GJ_IMPLICIT_MIDPOINT)
+    return fail(GJ_ENOTSUP, "the batched logistic-regression path implements the implicit midpoint");
+  const gj::StepDev sp = gj::to_dev(*p);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const gj::InfoDev<float> inf = gj::to_dev<float>(info);
+  if (cudaEventRecord(b->fork, cs) != cudaSuccess) return fail(GJ_ECUDA, "event record failed");
+  for (int k = 0; k < b->S; ++k)
+    if (cudaStreamWaitEvent(b->streams[k], b->fork, 0) != cudaSuccess)
+      return fail(GJ_ECUDA, "stream wait failed");
+  for (int i = 0; i < b->B; ++i) {
+    const size_t po = b->pos_off[i], co = (size_t)i * b->C;
+    gj::InfoDev<float> ig = info_offset(inf, co, 0);
+    if (inf.momentum) ig.momentum = inf.momentum + po;
+    const int rc = gj::logreg_batched_rmhmc_step_graph(
+        b->lbs[i], sp, (float*)s->position + po, (float*)s->logdensity_grad + po,
+        s->logdensity + co, z + po, u + co, ig, 2, b->streams[i % b->S]);
+    if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+  }
+  for (int k = 0; k < b->S; ++k) {
+    if (cudaEventRecord(b->joins[k], b->streams[k]) != cudaSuccess ||
+        cudaStreamWaitEvent(cs, b->joins[k], 0) != cudaSuccess)
+      return fail(GJ_ECUDA, "event join failed");
+  }
+  return GJ_OK;
+}
+
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm) {
   if (tile_n_wide != 64 && tile_n_wide != 128) return fail(GJ_EINVAL, "tile width must be 64 or 128");
   if (two_ctas_per_sm != 0 && two_ctas_per_sm != 1) return fail(GJ_EINVAL, "two_ctas_per_sm must be 0 or 1");

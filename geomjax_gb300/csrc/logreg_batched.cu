@@ -140,6 +140,8 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0) {
   while (c.cpw > 1 && (size_t)c.cpw * c.stride > 40 * 1024) c.cpw >>= 1;
   c.lpc = 32 / c.cpw;
   c.warps = c.cpw >= 4 ? 1 : 4 / c.cpw;
+  // as many of those warps as fit 200 KB (large d: one warp of one chain)
+  while (c.warps > 1 && c.tab + (size_t)c.warps * c.cpw * c.stride > 200 * 1024) --c.warps;
   c.smem = c.tab + (size_t)c.warps * c.cpw * c.stride;
   return c;
 }
@@ -686,15 +688,22 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
     return GJ_ECUDA;
   }
   {
-    // the largest layout any chains-per-warp choice can ask for: the table
-    // plus 4 chains, or one chain of a 40 KB+ stride
+    // the largest layout any chains-per-warp choice can ask for.  The
+    // kernel attribute is process-wide and shared by every context, so it
+    // only ever grows (a context for a small d must not lower the limit a
+    // larger context's captured launches rely on).
+    static size_t s_chol_smem = 0;
     size_t smax = 0;
     for (int cpw = 1; cpw <= 8; cpw *= 2) {
       smax = std::max(smax, chol_config(d, sizeof(double), cpw).smem);
       smax = std::max(smax, chol_config(d, sizeof(float), cpw).smem);
     }
-    cudaError_t a1 = chol_set_smem<double>((int)smax);
-    cudaError_t a2 = chol_set_smem<float>((int)smax);
+    cudaError_t a1 = cudaSuccess, a2 = cudaSuccess;
+    if (smax > s_chol_smem) {
+      a1 = chol_set_smem<double>((int)smax);
+      a2 = chol_set_smem<float>((int)smax);
+      if (a1 == cudaSuccess && a2 == cudaSuccess) s_chol_smem = smax;
+    }
     if (a1 != cudaSuccess || a2 != cudaSuccess) {
       g_err = "metric factorisation needs more shared memory than the device allows";
       logreg_batched_destroy(lb);

@@ -234,6 +234,30 @@ int32_t gj_metric(const gj_target* target, int32_t precision, int32_t num_chains
 int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_chains,
                       const void* q, const void* w, void* out, void* stream);
 
+/* ---- batches of independent posteriors ----------------------------------
+ * A batch holds B dense-Fisher logistic-regression posteriors of any sizes
+ * (n_data and dim may differ; dim <= 128), each sampled by C RMHMC chains
+ * through the batched mixed-precision pipeline (implicit midpoint).  Every
+ * posterior's transition is one CUDA graph; the graphs are spread
+ * round-robin over num_streams streams forked from and joined to the
+ * caller's stream, so many small posteriors fill the GPU together.
+ * The reference samples one posterior per kernel call; a batch is the
+ * vmapped loop over posteriors a user would write around it.
+ *
+ * Layout: per-chain scalars (logdensity, u, info arrays but momentum) are
+ * [B*C], posterior b's chains at rows [b*C, (b+1)*C).  Vectors (position,
+ * logdensity_grad, z, info.momentum) are ragged: posterior b's [C, d_b]
+ * block starts at C * (d_0 + ... + d_{b-1}).  state->num_chains = B*C.
+ * Targets' X and y must stay valid while the batch lives. */
+typedef struct gj_batch gj_batch;
+int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
+                        int32_t chains_per_posterior, int32_t num_streams, gj_batch** out);
+int32_t gj_batch_destroy(gj_batch* batch);
+/* GJ_OPT_CHOL_FP64 and GJ_OPT_CHOL_CHAINS_PER_WARP, for every posterior */
+int32_t gj_batch_set_option(gj_batch* batch, int32_t key, int64_t value);
+int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_chain_state* state,
+                            const float* z, const double* u, gj_info* info, void* stream);
+
 /* Process-wide tile policy of the tcgen05 split-BF16 GEMMs: output tile
  * width for N > 64 (64 or 128; narrower N always takes 32 or 64) and whether
  * the operand ring is cut back so that two CTAs share an SM (1, default) or

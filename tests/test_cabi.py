@@ -84,6 +84,21 @@ def test_argument_checks_without_gpu():
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 9) == L.GJ_EINVAL
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 2) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(96, 1) == L.GJ_EINVAL
+    # batch creation checks its arguments before touching the GPU
+    bh = ctypes.c_void_p()
+    assert lib.gj_batch_create(None, 1, 64, 4, ctypes.byref(bh)) == L.GJ_EINVAL
+    tl = (L.GjTarget * 2)(L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 5, 10, 1, 1, None,
+                                     100.0, 0.0),
+                          L.GjTarget(L.GJ_FUNNEL, L.GJ_METRIC_DIAG_FISHER, 3, 0, None, None, None,
+                                     3.0, 0.0))
+    tp = ctypes.cast(tl, ctypes.c_void_p)
+    assert lib.gj_batch_create(tp, 0, 64, 4, ctypes.byref(bh)) == L.GJ_EINVAL
+    assert lib.gj_batch_create(tp, 1, 0, 4, ctypes.byref(bh)) == L.GJ_EINVAL
+    assert lib.gj_batch_create(tp, 1, 64, 0, ctypes.byref(bh)) == L.GJ_EINVAL
+    assert lib.gj_batch_create(tp, 2, 64, 4, ctypes.byref(bh)) == L.GJ_EINVAL  # a funnel
+    tl[0].dim = 200
+    assert lib.gj_batch_create(tp, 1, 64, 4, ctypes.byref(bh)) == L.GJ_ENOTSUP
+    assert lib.gj_batch_destroy(None) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(128, 2) == L.GJ_EINVAL
     # the differentiated transition checks its arguments on the host
     assert lib.gj_logreg_gl_transition_jvp(None, 1, None, None, 0.1, 0.5, 1, 2, 2, 1, None,

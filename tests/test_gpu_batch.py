@@ -1,0 +1,90 @@
+"""Batches of uneven logistic-regression posteriors (``gj_batch_*``): every
+posterior's chains follow the oracle step by step, and the batch (graphs on
+a stream pool) is bit-identical to running each posterior on its own."""
+import numpy as np
+import pytest
+
+from tests.helpers import normals, rel_err, start_positions
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+# the largest d first: a later, smaller context must not lower the
+# process-wide shared-memory limit the larger one's launches need
+SIZES = [(220, 110), (200, 8), (350, 21), (260, 40)]
+C = 64
+
+
+def _data():
+    from geomjax_gb300.data import logreg_data
+
+    return [logreg_data(N, d, seed=10 + i) for i, (N, d) in enumerate(SIZES)]
+
+
+def _starts():
+    return [start_positions(d, C, seed=20 + i, scale=0.2).astype(np.float32).astype(np.float64)
+            for i, (_, d) in enumerate(SIZES)]
+
+
+def _draws(seed):
+    zs, us = [], []
+    for i, (_, d) in enumerate(SIZES):
+        z, u = normals(C, d, seed + i, np.float32)
+        zs.append(z)
+        us.append(u)
+    return zs, us
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def test_batch_matches_oracle_per_posterior():
+    from geomjax_gb300.base import Draws
+    from geomjax_gb300.batch import PosteriorBatch
+    from oracle import rmhmc as O_rm
+    from oracle import targets as OT
+
+    data = _data()
+    pb = PosteriorBatch(data, C, num_streams=3)
+    q0 = _starts()
+    zs, _ = _draws(7)
+    us = [-np.ones(C) for _ in SIZES]  # accept every proposal: compare trajectories
+    h = 0.05
+    for L in (1, 4):
+        st = pb.init(q0)
+        st, info = pb.step(Draws(np.concatenate([z.ravel() for z in zs]), np.concatenate(us)), st,
+                           h, L)
+        for b, (X, y) in enumerate(data):
+            ot = OT.LogisticRegression(X, y, prior_var=100.0)
+            traj = []
+            _, oi = O_rm.kernel(ot, O_rm.init(ot, q0[b]), zs[b], us[b], h, L, trajectory=traj)
+            e = rel_err(_np(pb.positions(st, b)), traj[-1].position)
+            assert e < 1e-5, (b, L, e)
+            eb = _np(info.energy)[b * C:(b + 1) * C]
+            assert rel_err(eb, oi.energy) < 1e-4, (b, L)
+
+
+def test_batch_bitwise_equals_single_posterior_runs():
+    import geomjax_gb300 as gj
+    from geomjax_gb300.base import Draws
+    from geomjax_gb300.batch import PosteriorBatch
+
+    data = _data()
+    pb = PosteriorBatch(data, C, num_streams=4)
+    q0 = _starts()
+    zs, us = _draws(11)
+    st = pb.init(q0)
+    st, info = pb.step(Draws(np.concatenate([z.ravel() for z in zs]), np.concatenate(us)), st,
+                       0.05, 6)
+    kern = gj.rmhmc.build_kernel(loop="graph")
+    for b, (X, y) in enumerate(data):
+        t = gj.logistic_regression(X, y, precision="mixed")
+        s1, i1 = kern(Draws(zs[b], us[b]), gj.rmhmc.init(q0[b], t), t, 0.05, 6)
+        np.testing.assert_array_equal(_np(pb.positions(st, b)), _np(s1.position))
+        np.testing.assert_array_equal(_np(st.logdensity)[b * C:(b + 1) * C], _np(s1.logdensity))
+        np.testing.assert_array_equal(_np(info.is_accepted)[b * C:(b + 1) * C],
+                                      _np(i1.is_accepted))
+        np.testing.assert_array_equal(_np(info.fixed_point_iters)[b * C:(b + 1) * C],
+                                      _np(i1.fixed_point_iters))
