@@ -510,7 +510,10 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const do
   int st = check_target(target, GJ_FP64);
   if (st) return st;
   if (target->family != GJ_LOGREG) return fail(GJ_EINVAL, "the differentiated trajectory is for logistic regression");
-  if (target->dim > 16) return fail(GJ_ENOTSUP, "the differentiated trajectory supports d <= 16");
+  if (target->dim > 64) return fail(GJ_ENOTSUP, "the differentiated trajectory supports d <= 64");
+  if (gj::gl_trajectory_smem(target->dim, (int)target->n_data, tangents) > 227 * 1024)
+    return fail(GJ_ENOTSUP, "the differentiated trajectory's per-chain shared memory exceeds 227 KB "
+                            "(d = 64 allows N <= 2000 with tangents)");
   if (C < 1 || !q0 || !z || !out || kp < 1 || kq < 1 || num_integration_steps < 0 ||
       !(metric_reg > 0) || !(step_size == step_size))
     return fail(GJ_EINVAL, "bad arguments");

@@ -28,7 +28,9 @@ template <typename T>
 cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out, int C,
                               cudaStream_t st);
 
-// differentiated generalized-leapfrog transition (traj_jvp.cu)
+// differentiated generalized-leapfrog transition (traj_jvp.cu); shared
+// memory per chain (one CTA) for d, N
+size_t gl_trajectory_smem(int d, int N, int tangents);
 cudaError_t launch_gl_trajectory_jvp(const double* X, const double* y, int N, int d,
                                      double prior_var, int C, const double* q0, const double* z,
                                      double h, double lam, int L, int Kp, int Kq, int tangents,

@@ -274,7 +274,10 @@ int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm);
  * [C, d] float64 start positions and momentum normals.  out[C, 6] =
  * (p_accept, ∂p_accept/∂h, ∂p_accept/∂λ, ΔH = H1 − H0, ∂ΔH/∂h, ∂ΔH/∂λ);
  * tangents = 0 computes the values only (the tangent slots are zero).
- * d <= 16.  Replaces the reference's jax.jacfwd through a trajectory
+ * One CTA per chain holds the chain's factor, vectors and per-datum arrays
+ * in shared memory: d <= 64, and (d(d+1)/2 + 10d + 3N + 256)·24 bytes plus a
+ * 16-row tile of X must fit 227 KB (N <= 2000 at d = 64; GJ_ENOTSUP beyond).
+ * Replaces the reference's jax.jacfwd through a trajectory
  * (adaptation/chees_adaptation_lmcmonge.py:497-519). */
 int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t num_chains, const double* q0,
                                     const double* z, double step_size, double metric_reg,

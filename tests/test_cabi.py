@@ -103,9 +103,13 @@ def test_argument_checks_without_gpu():
     # the differentiated transition checks its arguments on the host
     assert lib.gj_logreg_gl_transition_jvp(None, 1, None, None, 0.1, 0.5, 1, 2, 2, 1, None,
                                            None) == L.GJ_EINVAL
-    tl = L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 20, 10, 1, 1, None, 100.0, 0.0)
+    tl = L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 80, 10, 1, 1, None, 100.0, 0.0)
     assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 2, 2, 1, 1,
                                            None) == L.GJ_ENOTSUP
+    tl.dim, tl.n_data = 64, 5000  # the per-chain shared memory would exceed 227 KB
+    assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 2, 2, 1, 1,
+                                           None) == L.GJ_ENOTSUP
+    tl.n_data = 10
     tl.dim = 5
     assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, -1.0, 1, 2, 2, 1, 1,
                                            None) == L.GJ_EINVAL

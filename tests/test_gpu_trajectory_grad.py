@@ -99,6 +99,40 @@ def test_rejects_unsupported():
     tg = device_target("logreg", "mixed", N=N, d=D)
     with pytest.raises(ValueError):
         AD.transition_stats(tg, *_inputs(C=4), 0.1, 0.5, 2)
-    big = device_target("logreg", "fp64", N=40, d=20)
+    big = device_target("logreg", "fp64", N=40, d=70)
     with pytest.raises(L.GeomjaxError):
-        AD.transition_values(big, np.zeros((2, 20)), np.zeros((2, 20)), 0.1, 0.5, 1)
+        AD.transition_values(big, np.zeros((2, 70)), np.zeros((2, 70)), 0.1, 0.5, 1)
+
+
+def test_full_size_config_tangents_match_central_differences():
+    """The config's size: N = 2000, d = 64, L = 20 generalized-leapfrog steps
+    (here on 32 chains; the cost per chain does not depend on the chain
+    count).  ∂ΔH/∂h at the config's λ = 1/100, and ∂ΔH/∂λ at λ = 50, against
+    central differences (relative step 1e-4, float64), normwise 1e-4.  At
+    λ = 1/100 the regulariser is 2e-5 of G's scale (≈ 500·I), so ∂ΔH/∂λ is
+    below the float64 resolution of H ≈ 10³ and is only checked finite."""
+    from geomjax_gb300 import autodiff as AD
+    from geomjax_gb300.data import logreg_data
+
+    import geomjax_gb300 as gj
+
+    X, y = logreg_data(2000, 64, seed=0)
+    tg = gj.logistic_regression(X, y, precision="fp64")
+    Cc = 32
+    rng = np.random.default_rng(5)
+    q0 = 0.05 * rng.standard_normal((Cc, 64))
+    z = rng.standard_normal((Cc, 64))
+    h, e, L = 0.02, 1e-4, 20
+
+    def dH(hh, ll):
+        return AD.transition_values(tg, q0, z, hh, ll, L)[1].cpu().numpy()
+
+    lam = 0.01
+    J = AD.transition_jacobian(tg, q0, z, h, lam, L).cpu().numpy()
+    assert np.all(np.isfinite(J))
+    fd_h = (dH(h * (1 + e), lam) - dH(h * (1 - e), lam)) / (2 * e * h)
+    assert _normwise(J[:, 4], fd_h) < 1e-4
+    lam = 50.0
+    J = AD.transition_jacobian(tg, q0, z, h, lam, L).cpu().numpy()
+    fd_l = (dH(h, lam * (1 + e)) - dH(h, lam * (1 - e))) / (2 * e * lam)
+    assert _normwise(J[:, 5], fd_l) < 1e-4
