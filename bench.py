@@ -42,13 +42,15 @@ METRIC = "min-ESS/s and leapfrog steps/s, batched mixed-precision vs plain FP64 
 # workload (4096 chains), averaged over the five GEMMs of one map evaluation,
 # from one ncu capture (profiles/gemm_tc_and_chol_logreg_N1000_d25_C4096_ncu.md).
 # Reported only for that chain count.
-NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 24.2e6}
+NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 24.0e6}
 
 WORKLOADS = {
     "logreg": dict(name="logistic_regression_N1000_d25_rmhmc_fisher_4096chains", N=1000, d=25,
                    C=4096, L=8, h=0.05, sampler="rmhmc"),
     "monge": dict(name="funnel_D100_lmcmonge_alpha1_8192chains", D=100, C=8192, L=16, h=0.02,
                   sampler="lmcmonge"),
+    "trajectory_grad": dict(name="logistic_regression_N2000_d64_gl20_dh_dlambda_1024chains", N=2000,
+                            d=64, C=1024, L=20, h=0.02, lam=0.01, sampler="jvp"),
     "uneven": dict(name="uneven_logreg_2048posteriors_N200-5000_d8-128_64chains", B=2048, C=64,
                    L=8, h=0.05, sampler="batch"),
 }
@@ -372,6 +374,62 @@ def run_batch(args, wl):
     }
 
 
+def run_jvp(args, wl):
+    """Differentiated trajectory: per chain, p_accept and ΔH of one
+    generalized-leapfrog transition of L steps with their derivatives with
+    respect to the step size and the metric regulariser (float64 forward
+    mode), through gj_logreg_gl_transition_jvp."""
+    import torch
+
+    from geomjax_gb300 import autodiff as AD
+    from geomjax_gb300.data import logreg_data
+
+    import geomjax_gb300 as gj
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    X, y = logreg_data(wl["N"], wl["d"], seed=0)
+    tg = gj.logistic_regression(X, y, precision="fp64", device=dev)
+    C, d = wl["C"], wl["d"]
+    g0 = torch.Generator().manual_seed(rank)
+    q0 = (0.05 * torch.randn(C, d, generator=g0, dtype=torch.float64)).to(dev)
+    z = torch.randn(C, d, generator=g0, dtype=torch.float64).to(dev)
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        AD.transition_jacobian(tg, q0, z, wl["h"], wl["lam"], wl["L"])
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    for i in range(K):
+        evs[i][0].record(stream)
+        J = AD.transition_jacobian(tg, q0, z, wl["h"], wl["lam"], wl["L"])
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev_s = _barrier_max(sum(a.elapsed_time(b) for a, b in evs) / 1e3, ws)
+    t0 = time.perf_counter()
+    Jh = AD.transition_jacobian(tg, q0, z, wl["h"], wl["lam"], wl["L"]).cpu()
+    e2e_s = time.perf_counter() - t0
+    return {
+        "metric": "differentiated leapfrog steps/s (d/dh and d/dlambda, float64 forward mode), 1 GB300",
+        "value": round(ws * C * wl["L"] * K / dev_s, 1), "unit": "leapfrog steps/s", "n_gpus": ws,
+        "steps": K, "warmup": W, "ms_per_step": round(1e3 * dev_s / K, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (dual numbers, 2 tangents)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["name"], "chains": C, "integration_steps": wl["L"],
+                   "step_size": wl["h"], "metric_regulariser": wl["lam"],
+                   "fixed_point_evaluations": "6 momentum + 6 position per step"},
+        "mean_dDeltaH_dh": float(Jh[:, 4].mean()), "mean_dDeltaH_dlambda": float(Jh[:, 5].mean()),
+        "mean_p_accept": float(Jh[:, 0].mean()),
+        "e2e": {"value": round(ws * C * wl["L"] / e2e_s, 1), "unit": "leapfrog steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(Jh.numel() * 8)},
+        "gpu_launches": K, "clocks": clk,
+    }
+
+
 def run_plain_fp64(args, wl):
     """The plain per-chain FP64 CUDA form of the same workload: one thread
     per chain, every vector and the metric algebra in float64.  For the
@@ -442,6 +500,9 @@ def cpu_baseline(wl, budget_s=12.0):
 
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     rng = np.random.Generator(np.random.PCG64(0))
+    if wl["sampler"] == "jvp":
+        return {"impl": "reference", "unavailable": "the reference differentiates trajectories with "
+                "JAX autodiff, and JAX is not installable here; the float64 oracle has no derivative"}
     if wl["sampler"] == "rmhmc":
         X, y = OT.make_logreg_data(wl["N"], wl["d"], seed=0)
         ot = OT.LogisticRegression(X, y)
@@ -596,8 +657,8 @@ def main():
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if wl["sampler"] == "batch":
-        out = run_batch(args, wl)
+    if wl["sampler"] in ("batch", "jvp"):
+        out = run_batch(args, wl) if wl["sampler"] == "batch" else run_jvp(args, wl)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
