@@ -33,6 +33,10 @@ import sys
 import threading
 import time
 
+# hardware work queues for the stream pool of posterior batches (read when
+# the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 

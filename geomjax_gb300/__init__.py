@@ -4,7 +4,18 @@ RMHMC (implicit midpoint / generalized leapfrog), LMC with a dense metric and
 LMC on a Monge patch, over registered device target families, batched over
 many chains.  The compute path is the CUDA library built by
 ``geomjax_gb300.build``; there is no CPU fallback.
+
+Importing the package before CUDA is initialised sets
+``CUDA_DEVICE_MAX_CONNECTIONS`` to 32 unless the environment already sets
+it.  Batches of posteriors run one CUDA graph per posterior on a pool of
+streams; with the driver's default of 8 hardware queues those streams share
+queues, and 64 posteriors of 64 chains overlapped 3.7x instead of 13x on
+GB300.
 """
+import os as _os
+
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 from .base import (AdaptationAlgorithm, AdaptationResults, Draws, LMCInfo, LMCState, RMHMCInfo,
                    RMHMCState, SamplingAlgorithm)
 from .diagnostics import effective_sample_size, ess, potential_scale_reduction, rhat

@@ -14,6 +14,10 @@ State layout (device tensors):
 * ``logdensity``: float64 [B*C].
 
 ``positions(state, b)`` returns posterior b's [C, d_b] view.
+
+The graphs overlap only as far as the device's hardware work queues allow:
+importing ``geomjax_gb300`` before CUDA starts sets
+``CUDA_DEVICE_MAX_CONNECTIONS=32`` unless the environment sets it.
 """
 from __future__ import annotations
 

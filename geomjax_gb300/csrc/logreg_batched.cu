@@ -398,52 +398,58 @@ struct UpdArgs {
   int* n_active;
 };
 
-// one warp per chain, lanes over coordinates
+// one warp per chain, lanes over coordinates.  *n_active is only a flag
+// (> 0 while some chain iterates): one plain store per block that has an
+// active chain, instead of an atomic per chain on one address.
 __global__ void update_kernel(UpdArgs a) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (c >= a.C) return;
-  if (a.mode == UP_FPN && !a.active[c]) return;
-  const int d = a.d;
-  const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
-  const double tol = a.spd ? a.spd->tol : a.tol;
-  const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
-  const double* qs = (a.mode == UP_EXPLICIT) ? a.qc : a.q0;
-  const double* ps = (a.mode == UP_EXPLICIT) ? a.pc : a.p0;
-  double nrm = 0.0;
-  bool nan = false;
-  for (int i = lane; i < d; i += 32) {
-    const size_t o = (size_t)c * d + i;
-    const double q = a.qc[o];
-    const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
-    const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
-    const double qn = qs[o] + hh * a.u[o];
-    const double pn = ps[o] - hh * (dK - g);
-    const double e1 = qn - q, e2 = pn - a.pc[o];
-    nan |= isnan(e1) || isnan(e2);
-    nrm = fmax(nrm, fmax(fabs(e1), fabs(e2)));
-    a.qc[o] = qn;
-    a.pc[o] = pn;
-    split_store(a.Qb, c, i, float(qn));
-    if (a.mode == UP_EXPLICIT) {
-      a.q0[o] = qn;
-      a.p0[o] = pn;
-      a.qf[o] = float(qn);
+  bool act = false;
+  if (c < a.C && !(a.mode == UP_FPN && !a.active[c])) {  // warp-uniform
+    const int d = a.d;
+    const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
+    const double tol = a.spd ? a.spd->tol : a.tol;
+    const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
+    const double* qs = (a.mode == UP_EXPLICIT) ? a.qc : a.q0;
+    const double* ps = (a.mode == UP_EXPLICIT) ? a.pc : a.p0;
+    double nrm = 0.0;
+    bool nan = false;
+    for (int i = lane; i < d; i += 32) {
+      const size_t o = (size_t)c * d + i;
+      const double q = a.qc[o];
+      const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
+      const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
+      const double qn = qs[o] + hh * a.u[o];
+      const double pn = ps[o] - hh * (dK - g);
+      const double e1 = qn - q, e2 = pn - a.pc[o];
+      nan |= isnan(e1) || isnan(e2);
+      nrm = fmax(nrm, fmax(fabs(e1), fabs(e2)));
+      a.qc[o] = qn;
+      a.pc[o] = pn;
+      split_store(a.Qb, c, i, float(qn));
+      if (a.mode == UP_EXPLICIT) {
+        a.q0[o] = qn;
+        a.p0[o] = pn;
+        a.qf[o] = float(qn);
+      }
+    }
+    if (a.mode != UP_EXPLICIT) {
+      nrm = warp_max(nrm);
+      nan = __any_sync(0xffffffffu, nan);
+      if (nan) nrm = NAN;
+      const int it = (a.mode == UP_FP0) ? 0 : a.iters[c] + 1;
+      act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
+      if (lane == 0) {
+        a.iters[c] = it;
+        a.norm[c] = nrm;
+        a.active[c] = act;
+        if (a.mode == UP_FPN) a.iters_total[c] += 1;
+        if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
+      }
     }
   }
-  if (a.mode == UP_EXPLICIT) return;
-  nrm = warp_max(nrm);
-  nan = __any_sync(0xffffffffu, nan);
-  if (lane != 0) return;
-  if (nan) nrm = NAN;
-  const int it = (a.mode == UP_FP0) ? 0 : a.iters[c] + 1;
-  a.iters[c] = it;
-  a.norm[c] = nrm;
-  const bool act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
-  a.active[c] = act;
-  if (a.mode == UP_FPN) a.iters_total[c] += 1;
-  if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
-  if (act) atomicAdd(a.n_active, 1);
+  if (a.mode == UP_EXPLICIT) return;  // uniform over the grid
+  if (__syncthreads_or(act) && threadIdx.x == 0) *a.n_active = 1;
 }
 
 __global__ void begin_kernel(int C, int d, const float* pos, double* q0, double* qc, float* qf,
