@@ -53,6 +53,8 @@ WORKLOADS = {
                    C=4096, L=8, h=0.05, sampler="rmhmc"),
     "monge": dict(name="funnel_D100_lmcmonge_alpha1_8192chains", D=100, C=8192, L=16, h=0.02,
                   sampler="lmcmonge"),
+    "funnel2d": dict(name="funnel_D2_rmhmc_diag_fisher_gl10_fp64_4chains", D=2, C=4, L=10, h=0.1,
+                     max_iters=6, sampler="rmhmc_funnel"),
     "trajectory_grad": dict(name="logistic_regression_N2000_d64_gl20_dh_dlambda_1024chains", N=2000,
                             d=64, C=1024, L=20, h=0.02, lam=0.01, sampler="jvp"),
     "uneven": dict(name="uneven_logreg_2048posteriors_N200-5000_d8-128_64chains", B=2048, C=64,
@@ -160,6 +162,12 @@ def run_ours(args, wl):
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
+    elif wl["sampler"] == "rmhmc_funnel":
+        d = wl["D"]
+        target = gj.funnel(D=d, metric="diag", precision="fp64", device=dev)
+        kern = gj.rmhmc.build_kernel(integrator="generalized_leapfrog", max_iters=wl["max_iters"])
+        extra = {}
+        state = gj.rmhmc.init(torch.ones(C, d, dtype=torch.float64), target)
     else:
         d = wl["D"]
         target = gj.funnel(D=d, precision="mixed", device=dev)
@@ -265,10 +273,12 @@ def run_ours(args, wl):
     out = {
         "metric": METRIC, "value": round(steps_per_s, 1), "unit": "leapfrog steps/s",
         "n_gpus": ws, "steps": K, "warmup": W, "ms_per_step": round(1e3 * dev_s / K, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3+f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"rmhmc": "f32+bf16x3+f64", "rmhmc_funnel": "f64"}.get(wl["sampler"], "f32"),
         "data": "synthetic (seeded)",
         "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
-                   "step_size": h, "precision": "mixed", "loop": args.loop,
+                   "step_size": h, "precision": "fp64" if wl["sampler"] == "rmhmc_funnel" else "mixed",
+                   "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
                    "chain_groups": args.groups or "auto", "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
                    "l2": "flushed between timed steps (256 MB write)",
@@ -504,9 +514,6 @@ def cpu_baseline(wl, budget_s=12.0):
 
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     rng = np.random.Generator(np.random.PCG64(0))
-    if wl["sampler"] == "jvp":
-        return {"impl": "reference", "unavailable": "the reference differentiates trajectories with "
-                "JAX autodiff, and JAX is not installable here; the float64 oracle has no derivative"}
     if wl["sampler"] == "rmhmc":
         X, y = OT.make_logreg_data(wl["N"], wl["d"], seed=0)
         ot = OT.LogisticRegression(X, y)
@@ -518,6 +525,17 @@ def cpu_baseline(wl, budget_s=12.0):
             t = time.perf_counter()
             O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
             return time.perf_counter() - t
+    elif wl["sampler"] == "rmhmc_funnel":
+        ot = OT.Funnel(D=wl["D"], metric="diag")
+        d = wl["D"]
+
+        def run(C):
+            s = O_rm.init(ot, np.ones((C, d)))
+            t = time.perf_counter()
+            for _ in range(50):
+                s, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"],
+                                   wl["L"], integrator="generalized_leapfrog", max_iters=wl["max_iters"])
+            return (time.perf_counter() - t) / 50
     else:
         d = wl["D"]
         ot = OT.Funnel(D=d)
@@ -551,7 +569,19 @@ def run_reference(args, wl):
 
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     rng = np.random.Generator(np.random.PCG64(0))
-    if wl["sampler"] == "rmhmc":
+    if wl["sampler"] == "jvp":
+        return {"impl": "reference", "unavailable": "the reference differentiates trajectories with "
+                "JAX autodiff, and JAX is not installable here; the float64 oracle has no derivative"}
+    if wl["sampler"] == "rmhmc_funnel":
+        ot = OT.Funnel(D=wl["D"], metric="diag")
+        d, C = wl["D"], wl["C"]
+        s = O_rm.init(ot, np.ones((C, d)))
+
+        def step(s):
+            s2, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"],
+                                integrator="generalized_leapfrog", max_iters=wl["max_iters"])
+            return s2
+    elif wl["sampler"] == "rmhmc":
         X, y = OT.make_logreg_data(wl["N"], wl["d"], seed=0)
         ot = OT.LogisticRegression(X, y)
         d = wl["d"]
@@ -668,7 +698,7 @@ def main():
         return
     out = run_ours(args, wl)
     if rank == 0:
-        if not args.no_plain:
+        if not args.no_plain and wl["sampler"] != "rmhmc_funnel":  # that one is FP64 already
             out["plain_fp64"] = run_plain_fp64(args, wl)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(wl)
