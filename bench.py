@@ -158,7 +158,7 @@ def run_ours(args, wl):
         kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path, loop=args.loop,
                                      cholesky=args.cholesky,
                                      chol_chains_per_warp=args.chol_cpw,
-                                     chain_groups=args.groups)
+                                     chain_groups=args.groups, pdl=args.pdl)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -280,7 +280,7 @@ def run_ours(args, wl):
                    "step_size": h, "precision": "fp64" if wl["sampler"] == "rmhmc_funnel" else "mixed",
                    "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
-                   "chain_groups": args.groups or "auto", "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
+                   "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
@@ -665,6 +665,8 @@ def main():
                     help="tcgen05 GEMM output tile width for N > 64")
     ap.add_argument("--gemm-one-cta", action="store_true",
                     help="deeper operand ring, one CTA per SM")
+    ap.add_argument("--pdl", action="store_true",
+                    help="launch the batched pipeline's kernels with programmatic dependent launch")
     ap.add_argument("--groups", type=int, default=0,
                     help="chain groups on concurrent streams (0 = automatic)")
     ap.add_argument("--streams", type=int, default=16, help="stream pool of the uneven batch")

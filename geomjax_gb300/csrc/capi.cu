@@ -92,6 +92,7 @@ struct gj_ctx {
   int chol_fp64;  // GJ_OPT_CHOL_FP64
   int chol_cpw;   // GJ_OPT_CHOL_CHAINS_PER_WARP
   int groups;     // GJ_OPT_CHAIN_GROUPS (0 = automatic)
+  int pdl;        // GJ_OPT_PDL
   // batched dense-Fisher path: one context per chain group; in graph mode
   // the groups' transitions run on their own streams, forked from and joined
   // to the caller's stream by events, so one group's factorisation can share
@@ -155,6 +156,7 @@ int ensure_groups(gj_ctx* ctx, const gj::TargetDev& t) {
     gj::logreg_batched_set_profile(lb, ctx->profile);
     gj::logreg_batched_set_chol_fp64(lb, ctx->chol_fp64);
     gj::logreg_batched_set_chol_cpw(lb, ctx->chol_cpw);
+    gj::logreg_batched_set_pdl(lb, ctx->pdl);
     ctx->lbs.push_back(lb);
   }
   if (G > 1) {
@@ -208,6 +210,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->chol_fp64 = 1;
   c->chol_cpw = 0;
   c->groups = 0;
+  c->pdl = 0;
   *out = c;
   return GJ_OK;
 }
@@ -242,6 +245,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
       return fail(GJ_EINVAL, "chains per warp must be 0 (automatic), 1, 2, 4 or 8");
     ctx->chol_cpw = (int)value;
     for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_chol_cpw(lb, ctx->chol_cpw);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_PDL) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "PDL flag must be 0 or 1");
+    ctx->pdl = (int)value;
+    for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_pdl(lb, ctx->pdl);
     return GJ_OK;
   }
   if (key == GJ_OPT_CHAIN_GROUPS) {

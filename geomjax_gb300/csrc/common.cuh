@@ -149,4 +149,36 @@ __device__ __forceinline__ T dsigmoid(T a) {
   return T(1) / (T(1) + exp(-a));
 }
 
+// Programmatic dependent launch.  A kernel launched with the PDL attribute
+// may start while its predecessor in the stream (or graph) still runs: it
+// must call pdl_wait() before touching global memory that other kernels
+// read or write; pdl_wait() returns at once in a kernel launched without the
+// attribute.  pdl_trigger() lets the successor's CTAs be scheduled; they are
+// scheduled only once every CTA of this grid has triggered or exited, so a
+// waiting successor never holds resources that this grid still needs.
+// Kernels trigger late (after their main work): a trigger on entry let the
+// successor's CTAs take SM slots the grid's own later waves needed.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t st, Args... args) {
+  if (!pdl) {
+    kernel<<<grid, block, smem, st>>>(args...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace gj

@@ -171,6 +171,7 @@ struct GemmArgs {
   SplitMat B;  // N x K
   int M, N, K;
   Epi epi;
+  bool pdl = false;  // tcgen05 path: launch as a programmatic dependent
 };
 
 cudaError_t gemm_simt(const GemmArgs& g, cudaStream_t st);

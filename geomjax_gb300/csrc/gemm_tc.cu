@@ -287,6 +287,9 @@ __global__ void __launch_bounds__(320, 2)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  // barriers and TMEM are set up; the operands and epilogue inputs come from
+  // the preceding kernels
+  pdl_wait();
 
   if (warp == 0) {
     if (lane == 0) {
@@ -370,6 +373,9 @@ __global__ void __launch_bounds__(320, 2)
       }
     }
   }
+  // the successor may be scheduled once every CTA is this far (its CTAs then
+  // fill the SMs of this grid's finishing last wave)
+  pdl_trigger();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
@@ -480,9 +486,8 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
     ns = std::min(ns, 3);
   const CUtensorMap& mb = BN == 128 ? b->map : (BN == 64 ? b->map64 : b->map32);
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
-  gemm_tc_kernel<NPL, BN><<<grid, 320, C::smem(ns), st>>>(a->map, mb, a->s.rpad, b->s.rpad, g.M,
-                                                           g.N, g.K, g.epi, err, ns);
-  return cudaGetLastError();
+  return launch_k(g.pdl, gemm_tc_kernel<NPL, BN>, grid, dim3(320), (size_t)C::smem(ns), st, a->map,
+                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns);
 }
 
 template <int NPL>

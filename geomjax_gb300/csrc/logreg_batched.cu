@@ -200,6 +200,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     for (int i = k; i < d; ++i, ++off) tab[off] = (uint32_t)i | ((uint32_t)k << 16);
   }
   __syncthreads();
+  pdl_wait();
   const bool live = c < a.C && !(a.mode == CH_EVAL && a.active && !a.active[c]);
   if (__all_sync(0xffffffffu, !live)) return;  // uniform per warp
   // G = Gvec + I/s²: the packed layouts coincide; idle slots get the identity
@@ -249,6 +250,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     cj = cn;
     __syncwarp();
   }
+  pdl_trigger();  // the factorisation is done; the successor may be scheduled
   if (sl == 0 && live) {
     a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
@@ -352,13 +354,15 @@ __global__ void chol_kernel(CholArgs a, int stride) {
 }
 
 template <typename F>
-void chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, cudaStream_t st) {
-  const int th = 32 * cf.warps;
+cudaError_t chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, bool pdl,
+                        cudaStream_t st) {
+  const dim3 th(32 * cf.warps);
+  const int stride = (int)cf.stride;
   switch (cf.lpc) {
-    case 4: chol_kernel<F, 4><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
-    case 8: chol_kernel<F, 8><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
-    case 16: chol_kernel<F, 16><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
-    default: chol_kernel<F, 32><<<grid, th, cf.smem, st>>>(a, (int)cf.stride); break;
+    case 4: return launch_k(pdl, chol_kernel<F, 4>, grid, th, cf.smem, st, a, stride);
+    case 8: return launch_k(pdl, chol_kernel<F, 8>, grid, th, cf.smem, st, a, stride);
+    case 16: return launch_k(pdl, chol_kernel<F, 16>, grid, th, cf.smem, st, a, stride);
+    default: return launch_k(pdl, chol_kernel<F, 32>, grid, th, cf.smem, st, a, stride);
   }
 }
 
@@ -402,6 +406,7 @@ struct UpdArgs {
 // (> 0 while some chain iterates): one plain store per block that has an
 // active chain, instead of an atomic per chain on one address.
 __global__ void update_kernel(UpdArgs a) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   bool act = false;
@@ -477,6 +482,7 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
                               const float* Gout, int ldo, float* pos, float* grad,
                               double* logdens, InfoDev<float> info, const int* iters_total,
                               const uint8_t* notconv, const uint8_t* bad) {
+  pdl_wait();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const double cst = 0.5 * d * kLog2Pi;
@@ -506,11 +512,15 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
 
 // Sets the WHILE condition of the fixed-point loop node: iterate while a
 // chain is active, at most max_iters + 1 body executions per solve.
-__global__ void loop_cond_kernel(cudaGraphConditionalHandle h, const int* n_active, int* trips,
+// The flag is cleared here for the next body, so the body holds only
+// kernels (programmatic dependencies chain kernel to kernel).
+__global__ void loop_cond_kernel(cudaGraphConditionalHandle h, int* n_active, int* trips,
                                  const StepDev* spd) {
+  pdl_wait();
   const int t = *trips;
   *trips = t + 1;
   const bool more = (*n_active > 0) && (t <= spd->max_iters);
+  *n_active = 0;
   cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
@@ -548,6 +558,7 @@ struct LogregBatched {
   bool tc_ok;
   int chol_fp64;
   int chol_cpw;  // chains per warp in the factorisation (0 = automatic)
+  int pdl;       // launch the pipeline's kernels as programmatic dependents
   int prof;
   // graph path: device step parameters, staging buffers, captured graph
   StepDev* spd;
@@ -570,6 +581,7 @@ const char* logreg_batched_error() { return g_err.c_str(); }
 LogregStats logreg_batched_stats(const LogregBatched* lb) { return lb->stats; }
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on) { lb->chol_fp64 = on; }
 void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw) { lb->chol_cpw = cpw; }
+void logreg_batched_set_pdl(LogregBatched* lb, int on) { lb->pdl = on; }
 void logreg_batched_set_profile(LogregBatched* lb, int on) { lb->prof = on; }
 
 static SplitMat make_split(LogregBatched* lb, int rows, int kdim, int planes, bool* ok) {
@@ -613,6 +625,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->P = t.d * (t.d + 1) / 2;
   lb->chol_fp64 = 1;
   lb->chol_cpw = 0;
+  lb->pdl = 0;
   lb->prof = 0;
   lb->ev_used = 0;
   lb->gexec = nullptr;
@@ -754,6 +767,7 @@ struct Runner {
     g.N = N;
     g.K = K;
     g.epi = e;
+    g.pdl = lb->pdl != 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (lb->prof) {
       while (lb->ev.size() < lb->ev_used + 2) {
@@ -828,11 +842,8 @@ struct Runner {
     const int per_cta = cf.warps * cf.cpw;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
     // the dynamic shared-memory limit was raised at context creation
-    if (L.chol_fp64)
-      chol_launch<double>(cf, grid, a, st);
-    else
-      chol_launch<float>(cf, grid, a, st);
-    check(cudaGetLastError());
+    check(L.chol_fp64 ? chol_launch<double>(cf, grid, a, L.pdl, st)
+                      : chol_launch<float>(cf, grid, a, L.pdl, st));
   }
 
   // (4)-(6) after the factorisation
@@ -907,8 +918,8 @@ struct Runner {
     a.Qb = L.Qb;
     a.n_active = L.n_active_d;
     a.spd = spd;
-    update_kernel<<<(unsigned)(((size_t)L.C * 32 + 255) / 256), 256, 0, st>>>(a);
-    check(cudaGetLastError());
+    check(launch_k(L.pdl, update_kernel, dim3((unsigned)(((size_t)L.C * 32 + 255) / 256)), dim3(256),
+                   0, st, a));
   }
 };
 
@@ -1063,7 +1074,6 @@ int build_graph(LogregBatched* lb, int L, int impl) {
     B.metric_gram();
     B.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
     B.trace_grad();
-    B.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), lb->cap_body));
     B.update(UP_FPN, dummy);
     loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
     B.check(cudaGetLastError());
@@ -1109,7 +1119,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
   }
   lb->g_L = L;
   lb->g_impl = impl;
-  lb->g_chol = lb->chol_fp64 * 16 + lb->chol_cpw;
+  lb->g_chol = lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl;
   return GJ_OK;
 }
 
@@ -1128,7 +1138,7 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
     g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
     return GJ_ENOTSUP;
   }
-  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64 * 16 + lb->chol_cpw) {
+  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl) {
     // the capture streams must not see unfinished work of the caller's stream
     cudaStreamSynchronize(st);
     const int rc = build_graph(lb, sp.L, gemm_impl);

@@ -40,6 +40,9 @@ LogregStats logreg_batched_stats(const LogregBatched* lb);
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);
 // chains per warp in the metric factorisation: 1, 2, 4, 8 or 0 (automatic)
 void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw);
+// 1: the pipeline's kernels are launched as programmatic dependents (their
+// set-up overlaps the preceding kernel's tail); 0 (default): stream order
+void logreg_batched_set_pdl(LogregBatched* lb, int on);
 void logreg_batched_set_profile(LogregBatched* lb, int on);
 
 // D[M, N] = A[M, K]·B[N, K]ᵀ through the split-BF16 GEMM `impl` (test hook;

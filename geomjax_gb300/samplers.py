@@ -66,7 +66,8 @@ class Kernel:
 
     def __init__(self, sampler: int, integrator="implicit_midpoint", divergence_threshold=1000.0,
                  max_iters=100, tol=1e-6, alpha2_fix=False, logreg_path="auto", threads_per_block=None,
-                 loop="graph", cholesky="fp64", chol_chains_per_warp=0, chain_groups=0):
+                 loop="graph", cholesky="fp64", chol_chains_per_warp=0, chain_groups=0,
+                 pdl=False):
         if integrator not in INTEGRATORS:
             raise ValueError(f"integrator must be one of {sorted(INTEGRATORS)}")
         if logreg_path not in LOGREG_PATHS:
@@ -88,6 +89,7 @@ class Kernel:
             self.options[L.GJ_OPT_CHOL_CHAINS_PER_WARP] = int(chol_chains_per_warp)
         if chain_groups:
             self.options[L.GJ_OPT_CHAIN_GROUPS] = int(chain_groups)
+        self.options[L.GJ_OPT_PDL] = 1 if pdl else 0
         if threads_per_block:
             self.options[L.GJ_OPT_THREADS_PER_BLOCK] = int(threads_per_block)
         self._ctx = {}
@@ -214,14 +216,15 @@ class rmhmc:
     @staticmethod
     def build_kernel(integrator="implicit_midpoint", divergence_threshold=1000.0, max_iters=100,
                      tol=1e-6, logreg_path="auto", loop="graph", cholesky="fp64",
-                     chol_chains_per_warp=0, chain_groups=0):
+                     chol_chains_per_warp=0, chain_groups=0, pdl=False):
         """``rmhmc.py:110-176``; kernel(rng_key, state, target, step_size,
         num_integration_steps).  ``logreg_path``, ``loop``, ``cholesky`` and
-        ``chol_chains_per_warp`` and ``chain_groups`` select the implementation
-        of the batched dense-Fisher path."""
+        ``chol_chains_per_warp``, ``chain_groups`` and ``pdl`` select the
+        implementation of the batched dense-Fisher path."""
         return Kernel(L.GJ_SAMPLER_RMHMC, integrator, divergence_threshold, max_iters, tol,
                       logreg_path=logreg_path, loop=loop, cholesky=cholesky,
-                      chol_chains_per_warp=chol_chains_per_warp, chain_groups=chain_groups)
+                      chol_chains_per_warp=chol_chains_per_warp, chain_groups=chain_groups,
+                      pdl=pdl)
 
     def __new__(cls, target: Target, step_size: float, num_integration_steps: int, *,
                 divergence_threshold=1000.0, integrator="implicit_midpoint", max_iters=100,

@@ -168,6 +168,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * FP64 factorisation may overlap another group's GEMMs.  Results are
  * bit-identical for any group count. */
 #define GJ_OPT_CHAIN_GROUPS 6
+/* batched path: 1 = launch the pipeline's kernels with programmatic
+ * dependent launch (each kernel's set-up overlaps its predecessor's last
+ * wave; it waits on the predecessor before touching global memory),
+ * 0 (default) = ordinary stream order.  On GB300 at d = 25, 4096 chains,
+ * PDL measured 2.28M against 2.53M leapfrog steps/s without it. */
+#define GJ_OPT_PDL 7
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */

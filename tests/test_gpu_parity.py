@@ -341,3 +341,32 @@ def test_logreg_batched_chain_groups_bitwise(groups):
     for a, b in zip(out[1], out[groups]):
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x, y)
+
+
+def test_logreg_batched_pdl_bitwise():
+    """Programmatic dependent launch only moves each kernel's set-up ahead of
+    its predecessor's end: transitions are bit-identical with it on or off
+    (a missing wait before a global access would show here)."""
+    import geomjax_gb300 as gj
+    from geomjax_gb300.base import Draws
+
+    kw = dict(N=700, d=25, seed=4)
+    dt = device_target("logreg", "mixed", **kw)
+    C = 1024
+    q0 = start_positions(dt.dim, C, seed=2, scale=0.2).astype(np.float32).astype(np.float64)
+    out = {}
+    for pdl in (False, True):
+        kern = gj.rmhmc.build_kernel(loop="graph", pdl=pdl)
+        st = gj.rmhmc.init(q0, dt)
+        rng = np.random.Generator(np.random.PCG64(9))
+        rec = []
+        for h in (0.05, 0.03, 0.05):
+            z = rng.standard_normal((C, dt.dim)).astype(np.float32).astype(np.float64)
+            u = rng.random(C)
+            st, info = kern(Draws(z, u), st, dt, h, 8)
+            rec.append((_np(st.position), _np(st.logdensity), _np(st.logdensity_grad),
+                        _np(info.energy), _np(info.fixed_point_iters)))
+        out[pdl] = rec
+    for a, b in zip(out[False], out[True]):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
