@@ -409,7 +409,7 @@ int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s
 
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n < 0) return fail(GJ_EINVAL, "bad arguments");
-  int64_t v[5] = {0, 0, 0, 0, 0};
+  int64_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (!ctx->lbs.empty()) {
     for (gj::LogregBatched* lb : ctx->lbs) {
       const gj::LogregStats s = gj::logreg_batched_stats(lb);
@@ -418,11 +418,14 @@ int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
       v[2] += s.other_launches;
       v[3] += (int64_t)s.gemm_flops;
       v[4] += (int64_t)s.gemm_ns;
+      v[5] += s.chol_launches;
+      v[6] += (int64_t)s.chol_flops;
+      v[7] += (int64_t)s.chol_ns;
     }
   } else {
     v[2] = 1;  // the per-chain and warp-per-chain paths launch one kernel per step
   }
-  const int m = n < 5 ? n : 5;
+  const int m = n < 8 ? n : 8;
   for (int i = 0; i < m; ++i) out[i] = v[i];
   return m;
 }

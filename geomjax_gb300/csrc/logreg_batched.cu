@@ -573,6 +573,8 @@ struct LogregBatched {
   int g_L, g_impl, g_chol;
   std::vector<cudaEvent_t> ev;
   size_t ev_used;
+  std::vector<cudaEvent_t> cev;  // the same around the factorisations
+  size_t cev_used;
   LogregStats stats;
 };
 
@@ -603,6 +605,7 @@ void logreg_batched_destroy(LogregBatched* lb) {
     if (o) tc_operand_destroy(o);
   for (void* p : lb->owned) cudaFree(p);
   for (cudaEvent_t e : lb->ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : lb->cev) cudaEventDestroy(e);
   if (lb->gexec) cudaGraphExecDestroy(lb->gexec);
   if (lb->cap_main) cudaStreamDestroy(lb->cap_main);
   if (lb->cap_body) cudaStreamDestroy(lb->cap_body);
@@ -628,6 +631,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->pdl = 0;
   lb->prof = 0;
   lb->ev_used = 0;
+  lb->cev_used = 0;
   lb->gexec = nullptr;
   lb->g_L = lb->g_impl = lb->g_chol = -1;
   lb->cap_main = lb->cap_body = nullptr;
@@ -837,6 +841,23 @@ struct Runner {
     a.active = only_active ? L.active : nullptr;
     a.bad = L.bad;
     a.mom_info = mom_info;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (L.prof) {
+      while (L.cev.size() < L.cev_used + 2) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) break;
+        L.cev.push_back(ev);
+      }
+      if (L.cev.size() >= L.cev_used + 2) {
+        e0 = L.cev[L.cev_used];
+        e1 = L.cev[L.cev_used + 1];
+        L.cev_used += 2;
+        cudaEventRecord(e0, st);
+      }
+    }
+    const double dd = L.d;
+    L.stats.chol_launches++;
+    L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + (mode == CH_ENERGY ? 1.0 : 2.0) * dd * dd);
     const CholCfg cf =
         chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw);
     const int per_cta = cf.warps * cf.cpw;
@@ -844,6 +865,7 @@ struct Runner {
     // the dynamic shared-memory limit was raised at context creation
     check(L.chol_fp64 ? chol_launch<double>(cf, grid, a, L.pdl, st)
                       : chol_launch<float>(cf, grid, a, L.pdl, st));
+    if (e1) cudaEventRecord(e1, st);
   }
 
   // (4)-(6) after the factorisation
@@ -934,6 +956,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   }
   lb->stats = LogregStats{};
   lb->ev_used = 0;
+  lb->cev_used = 0;
   Runner R{lb, gemm_impl, st};
   const int C = lb->C, d = lb->d;
   begin_kernel<<<(C + 127) / 128, 128, 0, st>>>(C, d, pos, lb->q0, lb->qc, lb->qf, lb->Qb,
@@ -989,6 +1012,12 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
       if (cudaEventElapsedTime(&ms, lb->ev[i], lb->ev[i + 1]) == cudaSuccess) ns += 1e6 * ms;
     }
     lb->stats.gemm_ns = ns;
+    double cns = 0.0;
+    for (size_t i = 0; i + 1 < lb->cev_used; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, lb->cev[i], lb->cev[i + 1]) == cudaSuccess) cns += 1e6 * ms;
+    }
+    lb->stats.chol_ns = cns;
   }
   if (R.err != cudaSuccess) {
     g_err = std::string("batched logistic-regression step: ") + cudaGetErrorString(R.err);

@@ -35,6 +35,9 @@ struct LogregStats {
   long long other_launches;  // other kernels launched
   double gemm_flops;         // algorithmic flops of the GEMMs issued
   double gemm_ns;            // GPU time of the GEMM launches (profiling on)
+  long long chol_launches;   // metric factorisations launched
+  double chol_flops;         // their algorithmic FP64 flops (d³/3 + 2d² per chain)
+  double chol_ns;            // their GPU time (profiling on)
 };
 LogregStats logreg_batched_stats(const LogregBatched* lb);
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);

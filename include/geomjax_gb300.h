@@ -189,8 +189,10 @@ int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_state* s
 /* Counters of the last step on this context: out[0] fixed-point map
  * evaluations, out[1] GEMM launches, out[2] other kernel launches,
  * out[3] algorithmic GEMM flops, out[4] GPU time of the GEMM launches in
- * nanoseconds (only while profiling is on).  Returns the number written
- * (<= n).  No counterpart in the reference (measurement only). */
+ * nanoseconds (only while profiling is on), out[5] metric factorisations
+ * launched, out[6] their algorithmic FP64 flops (d³/3 + 2d² per chain, d³/3
+ * + d² for an energy evaluation), out[7] their GPU time in nanoseconds
+ * (profiling on).  Returns the number written (<= n, at most 8).  No counterpart in the reference (measurement only). */
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n);
 /* 1 = bracket every GEMM launch with CUDA events so gj_stats reports their
  * GPU time (the step then synchronises at its end); 0 = off (default).
