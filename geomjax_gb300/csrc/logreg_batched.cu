@@ -218,7 +218,15 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   }
   __syncwarp();
   // right-looking Cholesky; log det G = log Π pivots, accumulated as
-  // mantissa · 2^exponent so that one logarithm is taken per chain
+  // mantissa · 2^exponent so that one logarithm is taken per chain.  Outside
+  // DRAW the right-hand side p is known, so y = L⁻¹p rides along as a
+  // bordered row: at step j, y_j is scaled with the pivot and y_k (k > j)
+  // updated in the same phase as the trailing triangle (no separate serial
+  // forward substitution).
+  const bool border = a.mode != CH_DRAW;
+  if (border) {
+    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
+  }
   bool bad = false;
   double pm = 1.0;
   int pe = 0;
@@ -234,9 +242,14 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     if (sl == 0) {
       L[cj] = djj * inv;
       rdiag[j] = inv;
+      if (border) y[j] *= inv;
     }
     for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
     __syncwarp();
+    if (border) {
+      const F yj = y[j];
+      for (int k = j + 1 + sl; k < d; k += LPC) y[k] -= yj * L[cj + k - j];
+    }
     // trailing triangle: column j is read-only here and disjoint from the
     // entries written, so the iterations' loads may be issued together
     const int cn = cj + (d - j);  // colstart(j + 1)
@@ -277,18 +290,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     }
     zz = group_sum<LPC>(zz);
     if (sl == 0 && live) a.quad[c] = zz;
-  } else {
-    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
-    __syncwarp();
-    int cs = 0;
-    for (int j = 0; j < d; ++j) {
-      const F yj = y[j] * rdiag[j];
-      __syncwarp();
-      if (sl == 0) y[j] = yj;
-      for (int i = j + 1 + sl; i < d; i += LPC) y[i] -= L[cs + i - j] * yj;
-      cs += d - j;
-      __syncwarp();
-    }
+  } else {  // y = L⁻¹p was formed with the factor
     if (a.mode == CH_ENERGY) {
       double q = 0.0;
       for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
