@@ -151,7 +151,8 @@ def run_ours(args, wl):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     C, Lsteps, h = wl["C"], wl["L"], wl["h"]
-    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else 1))
+    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else
+                                       (1 if args.gemm_two_cta else -1)))
     if wl["sampler"] == "rmhmc":
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
@@ -291,7 +292,8 @@ def run_ours(args, wl):
                    "step_size": h, "precision": "fp64" if wl["sampler"] == "rmhmc_funnel" else "mixed",
                    "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
-                   "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n, "gemm_ctas_per_sm": 1 if args.gemm_one_cta else 2,
+                   "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
+                   "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
@@ -320,7 +322,8 @@ def run_batch(args, wl):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     B, C, Lsteps, h = wl["B"], wl["C"], wl["L"], wl["h"]
-    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else 1))
+    L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else
+                                       (1 if args.gemm_two_cta else -1)))
     Ns, ds = uneven_logreg_batch(B, seed=rank)
     t_setup = time.perf_counter()
     data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
@@ -672,10 +675,12 @@ def main():
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="fixed-point loop driver of the batched path (host: profilable by ncu)")
     ap.add_argument("--cholesky", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--gemm-tile-n", type=int, default=128, choices=[64, 128],
-                    help="tcgen05 GEMM output tile width for N > 64")
+    ap.add_argument("--gemm-tile-n", type=int, default=0, choices=[0, 64, 128],
+                    help="tcgen05 GEMM output tile width for N > 64 (0 = automatic)")
     ap.add_argument("--gemm-one-cta", action="store_true",
-                    help="deeper operand ring, one CTA per SM")
+                    help="deep operand ring, one CTA per SM, for every GEMM")
+    ap.add_argument("--gemm-two-cta", action="store_true",
+                    help="operand ring cut back to two CTAs per SM for every GEMM")
     ap.add_argument("--pdl", action="store_true",
                     help="launch the batched pipeline's kernels with programmatic dependent launch")
     ap.add_argument("--groups", type=int, default=0,

@@ -671,8 +671,10 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
 }
 
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm) {
-  if (tile_n_wide != 64 && tile_n_wide != 128) return fail(GJ_EINVAL, "tile width must be 64 or 128");
-  if (two_ctas_per_sm != 0 && two_ctas_per_sm != 1) return fail(GJ_EINVAL, "two_ctas_per_sm must be 0 or 1");
+  if (tile_n_wide != 0 && tile_n_wide != 64 && tile_n_wide != 128)
+    return fail(GJ_EINVAL, "tile width must be 0 (automatic), 64 or 128");
+  if (two_ctas_per_sm < -1 || two_ctas_per_sm > 1)
+    return fail(GJ_EINVAL, "two_ctas_per_sm must be -1 (automatic), 0 or 1");
   gj::gemm_tc_set_tuning(tile_n_wide, two_ctas_per_sm);
   return GJ_OK;
 }

@@ -189,9 +189,10 @@ TcOperand* tc_operand_create(const SplitMat& s, int box_rows, const char** err);
 void tc_operand_destroy(TcOperand* op);
 bool tc_available();
 cudaError_t gemm_tc_prepare();  // raises the kernel's shared-memory limit (call before capture)
-// Process-wide tile policy: bn_wide = 64 or 128 for N > 64; two_ctas = 1
-// limits the operand ring so that two CTAs share an SM.  Takes effect for
-// launches (and graph captures) made after the call.
+// Process-wide tile policy: bn_wide = 64 or 128 for N > 64 (0 = automatic);
+// two_ctas = 1 limits the operand ring so that two CTAs share an SM, 0 keeps
+// a deep ring, -1 = automatic.  Takes effect for launches (and graph
+// captures) made after the call.
 void gemm_tc_set_tuning(int bn_wide, int two_ctas);
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);

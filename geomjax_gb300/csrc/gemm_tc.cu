@@ -461,14 +461,20 @@ cudaError_t gemm_tc_prepare() {
 
 namespace {
 
-// Tile and pipeline choice.  BN: the narrowest of 32 / 64 covering N, else
-// 128 (or 64 when asked).  Stages: as many as the K blocks need (at most
-// MAX_STAGES), cut back towards the shared memory that lets two CTAs share
-// an SM but never below two stages when there are several K blocks (one
-// stage would serialise every TMA load with its MMAs).
+// Tile and pipeline choice (automatic unless forced by gemm_tc_set_tuning):
+// * BN: the narrowest of 32 / 64 covering N; for N > 64, 64 for a two-plane
+//   GEMM with at most 8 K blocks (more CTAs, two per SM), else 128;
+// * stages: with 8 or more K blocks a 3-stage ring (one CTA per SM keeps
+//   the TMA pipeline full); with fewer, as many as the K blocks need, cut
+//   back towards the shared memory that lets two CTAs share an SM but never
+//   below two stages when there are several K blocks.
+// Measured per GEMM at N = 1000, d = 25, 4096 chains (µs, ncu launch list):
+// trace (2 planes, 6 K blocks) 31.9 → 27.7 with BN = 64; Gram (2 planes,
+// 16 K blocks) 18.4 → 16.7 and gradient (3 planes, 16 K blocks) 21.9 → 20.7
+// with the 3-stage ring; Xβ and S (1 K block) best at BN = 128.
 struct TcTuning {
-  int bn_wide = 128;       // tile width for N > 64
-  int two_ctas = 1;        // prefer two CTAs per SM
+  int bn_wide = 0;         // tile width for N > 64: 0 = automatic, 64 or 128
+  int two_ctas = -1;       // -1 = automatic, 1 = prefer two CTAs per SM, 0 = deep ring
 };
 TcTuning g_tune;
 
@@ -480,7 +486,8 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   using C = Cfg<NPL, BN>;
   const int kb = (g.K + BK - 1) / BK;
   int ns = std::max(1, std::min(C::MAX_STAGES, kb));
-  if (g_tune.two_ctas)  // keep two stages when there is more than one K block
+  const bool two = g_tune.two_ctas < 0 ? kb < 8 : g_tune.two_ctas != 0;
+  if (two)  // keep two stages when there is more than one K block
     while (ns > 2 && C::smem(ns) > kTwoCtaSmem) --ns;
   else
     ns = std::min(ns, 3);
@@ -494,15 +501,17 @@ template <int NPL>
 cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
                              cudaStream_t st) {
   if (g.N <= 32) return launch_tc<NPL, 32>(g, a, b, err, st);
-  if (g.N <= 64 || g_tune.bn_wide == 64) return launch_tc<NPL, 64>(g, a, b, err, st);
+  const int kb = (g.K + BK - 1) / BK;
+  const bool narrow = g_tune.bn_wide == 0 ? (NPL == 2 && kb <= 8) : g_tune.bn_wide == 64;
+  if (g.N <= 64 || narrow) return launch_tc<NPL, 64>(g, a, b, err, st);
   return launch_tc<NPL, 128>(g, a, b, err, st);
 }
 
 }  // namespace
 
 void gemm_tc_set_tuning(int bn_wide, int two_ctas) {
-  g_tune.bn_wide = bn_wide == 64 ? 64 : 128;
-  g_tune.two_ctas = two_ctas ? 1 : 0;
+  g_tune.bn_wide = (bn_wide == 64 || bn_wide == 128) ? bn_wide : 0;
+  g_tune.two_ctas = two_ctas < 0 ? -1 : (two_ctas ? 1 : 0);
 }
 
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,

@@ -267,10 +267,11 @@ int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_ch
                             const float* z, const double* u, gj_info* info, void* stream);
 
 /* Process-wide tile policy of the tcgen05 split-BF16 GEMMs: output tile
- * width for N > 64 (64 or 128; narrower N always takes 32 or 64) and whether
- * the operand ring is cut back so that two CTAs share an SM (1, default) or
- * kept up to three stages (0).  Applies to launches and CUDA-graph captures
- * made after the call (a context's captured graph keeps its tiles). */
+ * width for N > 64 (0 = automatic per shape, or 64 / 128; narrower N always
+ * takes 32 or 64) and whether the operand ring is cut back so that two CTAs
+ * share an SM (1), kept up to three stages (0) or chosen per shape (-1,
+ * default).  Applies to launches and CUDA-graph captures made after the
+ * call (a context's captured graph keeps its tiles). */
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm);
 
 /* Derivatives of one RMHMC transition with the generalized leapfrog, for a

@@ -102,6 +102,7 @@ def test_argument_checks_without_gpu():
     assert lib.gj_batch_create(tp, 1, 64, 4, ctypes.byref(bh)) == L.GJ_ENOTSUP
     assert lib.gj_batch_destroy(None) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(128, 2) == L.GJ_EINVAL
+    assert lib.gj_set_gemm_tiling(0, -1) == L.GJ_OK  # back to the automatic policy
     # the differentiated transition checks its arguments on the host
     assert lib.gj_logreg_gl_transition_jvp(None, 1, None, None, 0.1, 0.5, 1, 2, 2, 1, None,
                                            None) == L.GJ_EINVAL
