@@ -1,18 +1,20 @@
 // tcgen05 implementation of the split-BF16 contraction (gemm.cuh) for sm_103a.
 //
-// One CTA computes one 128 x 128 output tile D = A·Bᵀ (both operands K-major):
+// One CTA computes one 128 x BN output tile D = A·Bᵀ (both operands K-major,
+// BN = 32, 64 or 128):
 //   warp 0      TMA producer: per 64-wide K chunk, one 128 x 64 BF16 box per
-//               plane of A and of B (128B-swizzled) into a 3-stage (two
-//               planes) or 2-stage (three planes) ring
-//   warp 1      allocates 128 TMEM columns; one elected thread issues
-//               tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M = N = 128,
+//               plane of A and one BN x 64 box per plane of B (128B-swizzled)
+//               into a ring of 1-4 stages sized at launch
+//   warp 1      allocates max(32, BN) TMEM columns; one elected thread issues
+//               tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M = 128, N = BN,
 //               K = 16): the plane products A_i·B_j with i + j < planes per
 //               K step, and tcgen05.commit frees each stage / signals the
 //               accumulator
 //   warps 2-9   epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes
 //               32·(w%4) .. +31 = output rows; the two warps of a lane
-//               quarter take alternate 32-column chunks), staged through
-//               shared memory so every global access is a whole row
+//               quarter take alternate 32-column chunks), staged once through
+//               shared memory and processed as row segments (8 values of one
+//               row per lane, 16-byte global accesses)
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in *err and skips the rest of its work, releasing TMEM before exit.
 #include <cuda.h>

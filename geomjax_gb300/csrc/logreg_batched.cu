@@ -564,7 +564,6 @@ struct LogregBatched {
   int prof;
   // graph path: device step parameters, staging buffers, captured graph
   StepDev* spd;
-  StepDev* sp_host;  // pinned
   float *pos_s, *grad_s, *z_s, *mom_s;
   double *ld_s, *u_s, *acc_s, *energy_s;
   uint8_t *accepted_s, *divergent_s, *status_s;
@@ -611,7 +610,6 @@ void logreg_batched_destroy(LogregBatched* lb) {
   if (lb->gexec) cudaGraphExecDestroy(lb->gexec);
   if (lb->cap_main) cudaStreamDestroy(lb->cap_main);
   if (lb->cap_body) cudaStreamDestroy(lb->cap_body);
-  if (lb->sp_host) cudaFreeHost(lb->sp_host);
   if (lb->n_active_h) cudaFreeHost(lb->n_active_h);
   delete lb;
 }
@@ -637,7 +635,6 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->gexec = nullptr;
   lb->g_L = lb->g_impl = lb->g_chol = -1;
   lb->cap_main = lb->cap_body = nullptr;
-  lb->sp_host = nullptr;
   lb->stats = LogregStats{};
   bool ok = true;
   const int N = lb->N, d = lb->d, P = lb->P;
@@ -695,7 +692,6 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->status_s = dalloc<uint8_t>(C, lb->owned, &ok);
   lb->fpit_s = dalloc<int>(C, lb->owned, &ok);
   lb->trips = dalloc<int>(1, lb->owned, &ok);
-  if (cudaMallocHost(&lb->sp_host, sizeof(StepDev)) != cudaSuccess) ok = false;
   if (cudaStreamCreateWithFlags(&lb->cap_main, cudaStreamNonBlocking) != cudaSuccess) ok = false;
   if (cudaStreamCreateWithFlags(&lb->cap_body, cudaStreamNonBlocking) != cudaSuccess) ok = false;
   if (cudaMallocHost(&lb->n_active_h, sizeof(int)) != cudaSuccess) ok = false;
