@@ -21,10 +21,12 @@ from .base import (AdaptationAlgorithm, AdaptationResults, Draws, LMCInfo, LMCSt
 from .diagnostics import effective_sample_size, ess, potential_scale_reduction, rhat
 from .samplers import Kernel, lmc, lmcmonge, rmhmc
 from .targets import funnel, hierarchical_gaussian, logistic_regression
+from .adaptation import gradient_step_size_adaptation, step_size_adaptation, window_adaptation
 
 __all__ = [
     "AdaptationAlgorithm", "AdaptationResults", "Draws", "LMCInfo", "LMCState", "RMHMCInfo",
     "RMHMCState", "SamplingAlgorithm", "Kernel", "rmhmc", "lmc", "lmcmonge", "funnel",
     "logistic_regression", "hierarchical_gaussian", "effective_sample_size", "ess",
-    "potential_scale_reduction", "rhat",
+    "potential_scale_reduction", "rhat", "window_adaptation", "step_size_adaptation",
+    "gradient_step_size_adaptation",
 ]

@@ -202,3 +202,82 @@ def step_size_adaptation(algorithm, target, initial_step_size=1.0, target_accept
         return AdaptationResults(state, params), infos
 
     return AdaptationAlgorithm(run)
+
+
+class GradientStepSizeResult(NamedTuple):
+    step_size: float
+    mean_acceptance: float
+    iterations: int
+    history: list  # (step size, mean p_accept, d mean p_accept / dh) per iteration
+
+
+def gradient_step_size_adaptation(target, positions, num_integration_steps,
+                                  initial_step_size=0.05, target_acceptance_rate=0.80,
+                                  metric_regulariser=None, num_iterations=40, tol=1e-4, seed=0,
+                                  kp=6, kq=6):
+    """Step size of generalized-leapfrog RMHMC by a safeguarded Newton method
+    on the mean acceptance probability, with its exact derivative from the
+    differentiated trajectory (``gj_logreg_gl_transition_jvp``).
+
+    The reference consumes trajectory derivatives the same way in its ChEES
+    adaptation, ``jax.jacfwd`` through the integrator
+    (``adaptation/chees_adaptation_lmcmonge.py:497-519``), there for the
+    trajectory length.  Here the criterion is ⟨min(1, e^{−ΔH})⟩(h) = δ over
+    fixed momentum draws (common random numbers), so every iterate solves the
+    same equation.  A chain whose transition is not finite counts as
+    rejected (p_accept 0, zero derivative), as the reference's accept treats
+    a NaN energy.
+
+    Iteration: the step sizes on either side of δ bracket the root; a Newton
+    step (derivative negative) is taken when it lands inside the bracket,
+    otherwise the bracket is bisected geometrically; before a bracket exists
+    h is at most halved or doubled per iteration.  The mean may jump where a
+    chain starts to diverge, so the result is within tol of δ, or at such a
+    jump with the bracket shrunk to a relative width of 1e-6.  float64
+    logistic-regression targets only (d <= 64).
+    """
+    from . import autodiff as AD
+
+    q0 = torch.as_tensor(positions, dtype=torch.float64).to(target.device).contiguous()
+    C, d = q0.shape
+    gen = torch.Generator(device="cpu").manual_seed(int(seed))
+    z = torch.randn(C, d, generator=gen, dtype=torch.float64).to(target.device)
+    lam = 1.0 / target.prior_var if metric_regulariser is None else float(metric_regulariser)
+    delta = float(target_acceptance_rate)
+
+    def evaluate(h):
+        J = AD.transition_jacobian(target, q0, z, h, lam, num_integration_steps, kp, kq)
+        ok = torch.isfinite(J).all(dim=1)
+        pa = torch.where(ok, J[:, 0], torch.zeros_like(J[:, 0]))
+        dpa = torch.where(ok, J[:, 1], torch.zeros_like(J[:, 1]))
+        return float(pa.mean()), float(dpa.mean())
+
+    h = float(initial_step_size)
+    lo = hi = None  # step sizes with acceptance above / below the target
+    history = []
+    it = 0
+    pa = float("nan")
+    for it in range(1, num_iterations + 1):
+        pa, dpa = evaluate(h)
+        history.append((h, pa, dpa))
+        err = pa - delta
+        if abs(err) < tol:
+            break
+        if err > 0:
+            lo = h if lo is None else max(lo, h)
+        else:
+            hi = h if hi is None else min(hi, h)
+        if lo is not None and hi is not None and (hi - lo) < 1e-6 * hi:
+            break
+        cand = h - err / dpa if dpa < 0 else None
+        if lo is not None and hi is not None:
+            if cand is None or not (lo < cand < hi):
+                cand = math.sqrt(lo * hi)
+        else:
+            if cand is None or cand <= 0:
+                cand = 2.0 * h if err > 0 else 0.5 * h
+            cand = min(max(cand, 0.5 * h), 2.0 * h)
+        h = cand
+    else:
+        pa, _ = evaluate(h)
+    return GradientStepSizeResult(h, pa, it, history)

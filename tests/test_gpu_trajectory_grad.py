@@ -136,3 +136,20 @@ def test_full_size_config_tangents_match_central_differences():
     J = AD.transition_jacobian(tg, q0, z, h, lam, L).cpu().numpy()
     fd_l = (dH(h, lam * (1 + e)) - dH(h, lam * (1 - e))) / (2 * e * lam)
     assert _normwise(J[:, 5], fd_l) < 1e-4
+
+
+def test_gradient_step_size_adaptation_hits_target_acceptance():
+    """Newton iterations on ⟨p_accept⟩(h) with the exact derivative reach the
+    target acceptance on the common momentum draws."""
+    from geomjax_gb300.adaptation import gradient_step_size_adaptation
+
+    tg = device_target("logreg", "fp64", N=N, d=D, prior_var=PRIOR_VAR)
+    q0, _ = _inputs(C=64)
+    res = gradient_step_size_adaptation(tg, q0, 10, initial_step_size=0.05,
+                                        target_acceptance_rate=0.8, num_iterations=40, tol=1e-4)
+    # within tol of the target, or at a jump where one of the 64 chains starts
+    # to diverge (at most 1/64 of the mean)
+    assert abs(res.mean_acceptance - 0.8) < 1.0 / 64, res
+    assert res.step_size > 0.05  # 0.05 accepts nearly everything here
+    assert all(np.isfinite(hd) for _, _, hd in res.history)
+    assert res.iterations < 40
