@@ -44,14 +44,48 @@ __device__ __forceinline__ float wget(const WVec<E>& a, int i) {
 }
 
 // warp-level target: log density + gradient and HVP for funnel / hier.
+// The scale constants are precomputed once per transition: on GB300 an FP64
+// division or logarithm inside the step loop costs more than the whole FP32
+// step (the FP64 pipe was 85 % busy with them in the loop).
 struct WarpTarget {
   TargetDev t;
   int lane;
+  float inv_a2, inv_b2;   // funnel: 1/σ² (a); hier: 1/σ_μ² (a), 1/σ_v² (b)
+  double inv_a2d, inv_b2d;  // the same in FP64, for the log density
+  double ld_const;          // the log density's constant terms
 };
 
+__device__ inline WarpTarget make_warp_target(const TargetDev& t, int lane) {
+  WarpTarget W;
+  W.t = t;
+  W.lane = lane;
+  if (t.family == GJ_FUNNEL) {
+    W.inv_a2d = 1.0 / (t.p0 * t.p0);
+    W.inv_b2d = 0.0;
+    W.inv_a2 = float(W.inv_a2d);
+    W.inv_b2 = 0.f;
+    W.ld_const = -log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
+  } else {
+    const int J = t.n;
+    const float* sg = static_cast<const float*>(t.s);
+    double c = 0.0;
+    for (int i = lane; i < J; i += 32) c += -log(double(sg[i])) - 0.5 * kLog2Pi;
+    c = warp_sum(c);
+    W.inv_a2d = 1.0 / (t.p0 * t.p0);
+    W.inv_b2d = 1.0 / (t.p1 * t.p1);
+    W.inv_a2 = float(W.inv_a2d);
+    W.inv_b2 = float(W.inv_b2d);
+    W.ld_const = c - J * 0.5 * kLog2Pi - log(t.p0) - 0.5 * kLog2Pi - log(t.p1) - 0.5 * kLog2Pi;
+  }
+  return W;
+}
+
 // funnel: v = θ[d−1]
+// The FP64 log density is formed only when need_ld (the proposal's, after
+// the last step); the gradient is FP32.
 template <int E>
-__device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<E>& g, float* sx_out) {
+__device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<E>& g, float* sx_out,
+                                    bool need_ld = true) {
   const TargetDev& t = W.t;
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
@@ -65,17 +99,16 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
       sx = fmaf(x, x, sx);
     }
     sx = warp_sum(sx);
-    const double s = t.p0;
-    const float gv = float(-double(v) / (s * s) - 0.5 * (d - 1)) + 0.5f * ev * sx;
+    const float gv = -v * W.inv_a2 - 0.5f * float(d - 1) + 0.5f * ev * sx;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
       g.x[k] = (i < d - 1) ? -q.x[k] * ev : ((i == d - 1) ? gv : 0.f);
     }
     *sx_out = sx;
-    double ld = -0.5 * double(v) * double(v) / (s * s) - log(s) - 0.5 * kLog2Pi;
-    ld += -0.5 * double(ev) * double(sx) - (d - 1) * (0.5 * double(v) + 0.5 * kLog2Pi);
-    return ld;
+    if (!need_ld) return 0.0;
+    return W.ld_const - 0.5 * double(v) * double(v) * W.inv_a2d - 0.5 * double(ev) * double(sx) -
+           (d - 1) * 0.5 * double(v);
   }
   // hierarchical Gaussian: θ = [θ_1..θ_J, μ, v]
   const int J = t.n;
@@ -84,7 +117,6 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
   const float mu = wget<E>(q, J), v = wget<E>(q, J + 1);
   const float ev = expf(-v);
   float sr = 0.f, srr = 0.f;
-  double ldp = 0.0;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
@@ -95,15 +127,12 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
       g.x[k] = e * is2 - r * ev;
       sr += r;
       srr = fmaf(r, r, srr);
-      ldp += -0.5 * double(e) * double(e) * double(is2) - log(double(sg[i])) - 0.5 * kLog2Pi;
     }
   }
   sr = warp_sum(sr);
   srr = warp_sum(srr);
-  ldp = warp_sum(ldp);
-  const double sm = t.p0, sv = t.p1;
-  const float gmu = sr * ev - mu * float(1.0 / (sm * sm));
-  const float gvv = 0.5f * ev * srr - 0.5f * J - v * float(1.0 / (sv * sv));
+  const float gmu = sr * ev - mu * W.inv_a2;
+  const float gvv = 0.5f * ev * srr - 0.5f * J - v * W.inv_b2;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
@@ -112,10 +141,19 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
     if (i > J + 1) g.x[k] = 0.f;
   }
   *sx_out = srr;
-  double ld = ldp - 0.5 * double(ev) * double(srr) - J * (0.5 * double(v) + 0.5 * kLog2Pi);
-  ld += -0.5 * double(mu) * double(mu) / (sm * sm) - log(sm) - 0.5 * kLog2Pi;
-  ld += -0.5 * double(v) * double(v) / (sv * sv) - log(sv) - 0.5 * kLog2Pi;
-  return ld;
+  if (!need_ld) return 0.0;
+  double se = 0.0;  // Σ (y_j − θ_j)² / σ_j², in FP64 as the initial log density
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = W.lane + 32 * k;
+    if (i < J) {
+      const double e = double(y[i]) - double(q.x[k]);
+      se += e * e / (double(sg[i]) * double(sg[i]));
+    }
+  }
+  se = warp_sum(se);
+  return W.ld_const - 0.5 * se - 0.5 * double(ev) * double(srr) - J * 0.5 * double(v) -
+         0.5 * double(mu) * double(mu) * W.inv_a2d - 0.5 * double(v) * double(v) * W.inv_b2d;
 }
 
 // Hessian-vector product; `sx` is the Σx² (funnel) / Σr² (hier) of the
@@ -135,7 +173,7 @@ __device__ void w_hvp(const WarpTarget& W, const WVec<E>& q, const WVec<E>& u, f
       if (i < d - 1) xu = fmaf(q.x[k], u.x[k], xu);
     }
     xu = warp_sum(xu);
-    const float ov = ev * xu + (float(-1.0 / (t.p0 * t.p0)) - 0.5f * ev * sx) * uv;
+    const float ov = ev * xu + (-W.inv_a2 - 0.5f * ev * sx) * uv;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
@@ -163,8 +201,8 @@ __device__ void w_hvp(const WarpTarget& W, const WVec<E>& q, const WVec<E>& u, f
   sr = warp_sum(sr);
   sut = warp_sum(sut);
   sru = warp_sum(sru);
-  const float om = ev * sut + (-float(J) * ev - float(1.0 / (t.p0 * t.p0))) * um - ev * sr * uv;
-  const float ovv = ev * sru - ev * sr * um + (-0.5f * ev * sx - float(1.0 / (t.p1 * t.p1))) * uv;
+  const float om = ev * sut + (-float(J) * ev - W.inv_a2) * um - ev * sr * uv;
+  const float ovv = ev * sru - ev * sr * um + (-0.5f * ev * sx - W.inv_b2) * uv;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
@@ -184,8 +222,12 @@ __device__ void w_half(float a2, WVec<E>& v, double* J, const WVec<E>& gn, const
     dl_ig.x[k] = im.x[k] * gn.x[k];
     igH.x[k] = im.x[k] * Hdl.x[k];
   }
-  const float det1 = 1.f + 0.5f * eps * a2 * wdot<E>(hv, dl_ig);
-  *J -= log(fabs(double(det1)));
+  // log|det1| and log|1 − ½εα²(Hdl·v)| as FP32 log1p of the small terms
+  // (det1 is an FP32 value, so an FP64 logarithm adds nothing); the running
+  // sum J stays FP64
+  const float x1 = 0.5f * eps * a2 * wdot<E>(hv, dl_ig);
+  const float det1 = 1.f + x1;
+  *J -= double(x1 > -1.f ? log1pf(x1) : logf(fabsf(det1)));
   const float sL = sqrtf(L);
   // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
   float pd = 0.f;
@@ -202,7 +244,8 @@ __device__ void w_half(float a2, WVec<E>& v, double* J, const WVec<E>& gn, const
   if (fix) corr *= a2;
 #pragma unroll
   for (int k = 0; k < E; ++k) v.x[k] = vt.x[k] - corr * dl_ig.x[k];
-  *J += log(fabs(1.0 - 0.5 * double(eps) * double(a2) * double(wdot<E>(Hdl, v))));
+  const float x2 = -0.5f * eps * a2 * wdot<E>(Hdl, v);
+  *J += double(x2 > -1.f ? log1pf(x2) : logf(fabsf(1.f + x2)));
 }
 
 // inclusive warp scan (ascending lane order)
@@ -233,7 +276,7 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= C) return;  // whole warp exits together
   const int d = t.d;
-  const WarpTarget W{t, lane};
+  const WarpTarget W = make_warp_target(t, lane);
   const float a2 = float(sp.alpha2);
   const float eps = float(sp.h);
   const float* imv = static_cast<const float*>(sp.inv_mass);
@@ -246,7 +289,7 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
     q.x[k] = in ? pos[(size_t)c * d + i] : 0.f;
     g.x[k] = in ? grad[(size_t)c * d + i] : 0.f;
     im.x[k] = in ? (imv ? imv[i] : 1.f) : 0.f;
-    if (in) slm_part += -log(double(im.x[k]));
+    if (in) slm_part += -double(logf(im.x[k]));  // cancels in H1 − H0
   }
   const double slm = warp_sum(slm_part);  // Σ log M
   const double ld0 = logdens[c];
@@ -262,7 +305,7 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
     // Σx² at the current q for the HVPs (one extra gradient pass is avoided by
     // recomputing only the reduction)
     WVec<E> gtmp;
-    (void)w_logdensity_grad<E>(W, q, gtmp, &sx);
+    (void)w_logdensity_grad<E>(W, q, gtmp, &sx, false);
   }
   WVec<E> dl_ig;
 #pragma unroll
@@ -328,7 +371,7 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
     w_half<E>(a2, v, &J, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
 #pragma unroll
     for (int k = 0; k < E; ++k) q.x[k] = fmaf(eps, v.x[k], q.x[k]);
-    ld = w_logdensity_grad<E>(W, q, g, &sx);
+    ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1);
     float Ls = 0.f;
 #pragma unroll
     for (int k = 0; k < E; ++k) Ls = fmaf(im.x[k] * g.x[k], g.x[k], Ls);
