@@ -131,12 +131,15 @@ __host__ __device__ inline size_t chol_chain_bytes(int d, size_t fsz) {
 // chains (leapfrog steps/s of the whole transition): FP64 1.64M / 1.96M /
 // 2.06M / 1.74M and FP32 2.29M / 2.46M / 2.35M / 2.00M for 1 / 2 / 4 / 8
 // chains per warp, so the automatic choice is 4 for FP64 (whose issue slots
-// bound the factorisation) and 2 for FP32 (where latency does).
-inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0) {
+// bound the factorisation) and 2 for FP32 (where latency does).  With few
+// chains (C < 1024) the GPU is far from full and one warp's serial path sets
+// the kernel's time, so the automatic choice is one chain per warp (all 32
+// lanes on one chain's trailing updates).
+inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) {
   CholCfg c{};
   c.stride = chol_chain_bytes(d, fsz);
   c.tab = chol_table_bytes(d);
-  c.cpw = cpw_req > 0 ? cpw_req : (fsz == sizeof(double) ? 4 : 2);
+  c.cpw = cpw_req > 0 ? cpw_req : (C < 1024 ? 1 : (fsz == sizeof(double) ? 4 : 2));
   while (c.cpw > 1 && (size_t)c.cpw * c.stride > 40 * 1024) c.cpw >>= 1;
   c.lpc = 32 / c.cpw;
   c.warps = c.cpw >= 4 ? 1 : 4 / c.cpw;
@@ -857,7 +860,7 @@ struct Runner {
     L.stats.chol_launches++;
     L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + (mode == CH_ENERGY ? 1.0 : 2.0) * dd * dd);
     const CholCfg cf =
-        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw);
+        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.C);
     const int per_cta = cf.warps * cf.cpw;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
     // the dynamic shared-memory limit was raised at context creation
