@@ -12,7 +12,9 @@
 // uses the O(d) closed-form Cholesky factor of diag(M⁻¹) − α²·w·wᵀ (rank-one
 // modification, Gill, Golub, Murray & Saunders 1974) instead of the
 // reference's dense d x d Cholesky (lmcmonge/metrics.py:162-166).
-// FP64: log det / volume adjustment J and the Hamiltonian difference.
+// FP64: the volume adjustment J across transitions (a transition's
+// increments are summed in FP32), the log density at the proposal and the
+// Hamiltonian difference; nothing in the step loop runs on the FP64 pipe.
 #include "chain_kernels.cuh"
 
 namespace gj {
@@ -212,9 +214,11 @@ __device__ void w_hvp(const WarpTarget& W, const WVec<E>& q, const WVec<E>& u, f
   }
 }
 
-// half_step_omega (lmcmonge/integrators.py:158-194), im = diag(M⁻¹)
+// half_step_omega (lmcmonge/integrators.py:158-194), im = diag(M⁻¹).  dJ
+// accumulates this transition's volume-term increments in FP32 (each is
+// ≈ 1e-3; 4 per step); the caller adds the sum to the FP64 J once.
 template <int E>
-__device__ void w_half(float a2, WVec<E>& v, double* J, const WVec<E>& gn, const WVec<E>& hv, float L,
+__device__ void w_half(float a2, WVec<E>& v, float* dJ, const WVec<E>& gn, const WVec<E>& hv, float L,
                        const WVec<E>& im, const WVec<E>& Hdl, float eps, int fix) {
   WVec<E> dl_ig, igH;
 #pragma unroll
@@ -223,11 +227,10 @@ __device__ void w_half(float a2, WVec<E>& v, double* J, const WVec<E>& gn, const
     igH.x[k] = im.x[k] * Hdl.x[k];
   }
   // log|det1| and log|1 − ½εα²(Hdl·v)| as FP32 log1p of the small terms
-  // (det1 is an FP32 value, so an FP64 logarithm adds nothing); the running
-  // sum J stays FP64
+  // (det1 is an FP32 value, so an FP64 logarithm adds nothing)
   const float x1 = 0.5f * eps * a2 * wdot<E>(hv, dl_ig);
   const float det1 = 1.f + x1;
-  *J -= double(x1 > -1.f ? log1pf(x1) : logf(fabsf(det1)));
+  *dJ -= x1 > -1.f ? log1pf(x1) : logf(fabsf(det1));
   const float sL = sqrtf(L);
   // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
   float pd = 0.f;
@@ -245,7 +248,7 @@ __device__ void w_half(float a2, WVec<E>& v, double* J, const WVec<E>& gn, const
 #pragma unroll
   for (int k = 0; k < E; ++k) v.x[k] = vt.x[k] - corr * dl_ig.x[k];
   const float x2 = -0.5f * eps * a2 * wdot<E>(Hdl, v);
-  *J += double(x2 > -1.f ? log1pf(x2) : logf(fabsf(1.f + x2)));
+  *dJ += x2 > -1.f ? log1pf(x2) : logf(fabsf(1.f + x2));
 }
 
 // inclusive warp scan (ascending lane order)
@@ -366,9 +369,10 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
            0.5 * double(Lc) * double(a2) * double(vg) * double(vg);
   };
   const double H0 = -ld0 + kinetic(L) - J0;
-  double ld = ld0, J = J0;
+  double ld = ld0;
+  float dJ = 0.f;  // this transition's volume-term increments
   for (int s = 0; s < sp.L; ++s) {  // lan_integrator.one_step
-    w_half<E>(a2, v, &J, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
+    w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
 #pragma unroll
     for (int k = 0; k < E; ++k) q.x[k] = fmaf(eps, v.x[k], q.x[k]);
     ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1);
@@ -389,11 +393,12 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
       hv.x[k] /= sL;
       Hdl.x[k] /= sL;
     }
-    w_half<E>(a2, v, &J, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
+    w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
     w_hvp<E>(W, q, v, sx, hv);
 #pragma unroll
     for (int k = 0; k < E; ++k) hv.x[k] /= sL;
   }
+  const double J = J0 + double(dJ);
   const double H1 = -ld + kinetic(L) - J;
   const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
