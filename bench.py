@@ -46,7 +46,7 @@ METRIC = "min-ESS/s and leapfrog steps/s, batched mixed-precision vs plain FP64 
 # workload (4096 chains), averaged over the five GEMMs of one map evaluation,
 # from one ncu capture (profiles/gemm_tc_and_chol_logreg_N1000_d25_C4096_ncu.md).
 # Reported only for that chain count.
-NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 24.0e6}
+NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 23.9e6}
 
 WORKLOADS = {
     "logreg": dict(name="logistic_regression_N1000_d25_rmhmc_fisher_4096chains", N=1000, d=25,
