@@ -58,3 +58,40 @@ def test_welford(diagonal):
     im = A.regularized_inverse_mass(s).numpy()
     exp = (37 / 42) * (np.diag(ref) if diagonal else ref) + 1e-3 * (5 / 42) * (1 if diagonal else np.eye(4))
     np.testing.assert_allclose(im, exp, rtol=1e-10)
+
+
+def test_gradient_step_size_adaptation_brackets_and_converges(monkeypatch):
+    """The safeguarded Newton iteration on a synthetic acceptance curve: a
+    smooth decreasing p(h) with a chain that diverges (contributing NaN)
+    beyond h = 0.6 reaches the target, and non-finite chains count as
+    rejected."""
+    import torch
+
+    from geomjax_gb300 import adaptation as A
+    from geomjax_gb300 import autodiff as AD
+
+    C = 8
+
+    def fake_jacobian(target, q0, z, h, lam, L, kp, kq):
+        p = torch.full((C,), float(np.exp(-(h / 0.3) ** 2)), dtype=torch.float64)
+        dp = torch.full((C,), float(-2 * h / 0.09 * np.exp(-(h / 0.3) ** 2)), dtype=torch.float64)
+        J = torch.zeros(C, 6, dtype=torch.float64)
+        J[:, 0], J[:, 1] = p, dp
+        if h > 0.6:
+            J[0, :] = float("nan")
+        return J
+
+    class FakeTarget:
+        device = "cpu"
+        prior_var = 100.0
+
+    monkeypatch.setattr(AD, "transition_jacobian", fake_jacobian)
+    res = A.gradient_step_size_adaptation(FakeTarget(), np.zeros((C, 3)), 5, initial_step_size=0.01,
+                                          target_acceptance_rate=0.5, tol=1e-8)
+    h_star = 0.3 * np.sqrt(np.log(2.0))
+    assert abs(res.step_size - h_star) < 1e-6 and abs(res.mean_acceptance - 0.5) < 1e-8
+    # from far above the root: the NaN chain counts as rejected, the bracket still closes
+    res = A.gradient_step_size_adaptation(FakeTarget(), np.zeros((C, 3)), 5, initial_step_size=2.0,
+                                          target_acceptance_rate=0.5, tol=1e-8)
+    assert abs(res.step_size - h_star) < 1e-6
+    assert any(np.isfinite(pa) and pa < 1.0 / C + 1e-12 for _, pa, _ in res.history)
