@@ -22,6 +22,19 @@
  *                      jax.value_and_grad (rmhmc/integrators.py:111),
  *                      util.hvp = jvp(grad f) (util.py:120-121),
  *                      metric_fn (rmhmc/metrics.py:42-58)
+ *   gj_metric_vjp      the vector-Jacobian product of metric_fn that JAX
+ *                      autodiff forms inside the kinetic-energy gradient
+ *                      (rmhmc/integrators.py:111-114)
+ *   gj_batch_*         a loop over posteriors around the rmhmc kernel,
+ *                      posteriors of different sizes in one call
+ *   gj_logreg_gl_transition_jvp
+ *                      jax.jacfwd through a trajectory with respect to the
+ *                      step size and a metric parameter
+ *                      (adaptation/chees_adaptation_lmcmonge.py:497-519)
+ *   gj_gemm_split_bf16, gj_gemm_split_bf16_noalloc, gj_stats, gj_profile,
+ *   gj_set_option, gj_set_gemm_tiling
+ *                      no reference counterpart: the split-BF16 contraction
+ *                      as a test hook, measurement and tuning
  *
  * The reference's user-supplied Python callables become a registered device
  * target family (gj_target).  The reference draws its randomness from a JAX
