@@ -131,12 +131,9 @@ def _dist():
 def _barrier_max(x, ws):
     if ws == 1:
         return x
-    import torch
-    import torch.distributed as dist
+    from geomjax_gb300.distributed import max_over_ranks
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return max_over_ranks(x, device="cuda")
 
 
 def run_ours(args, wl):
@@ -232,8 +229,11 @@ def run_ours(args, wl):
     steps_per_s = ws * C * Lsteps * K / dev_s
     min_ess = float("nan")
     if K >= 4:
-        ess = gj.effective_sample_size(trace, chain_axis=1, sample_axis=0)
-        min_ess = float(torch.min(ess).item())
+        # ESS over every rank's chains (one gather of the traces; replicas
+        # exchange nothing while sampling)
+        from geomjax_gb300.distributed import global_min_ess
+
+        min_ess = global_min_ess(trace, chain_axis=1, sample_axis=0)
     # --- e2e through the public API with host buffers
     Zh = torch.empty(C, d, dtype=target.dtype).pin_memory()
     Uh = torch.empty(C, dtype=torch.float64).pin_memory()
@@ -296,7 +296,7 @@ def run_ours(args, wl):
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
-        "min_ess_per_s": (round(ws * min_ess / dev_s, 2) if K >= 4 else None),
+        "min_ess_per_s": (round(min_ess / dev_s, 2) if K >= 4 else None),
         "min_ess": (round(min_ess, 2) if K >= 4 else None),
         "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
         "e2e": {"value": round(e2e, 1), "unit": "leapfrog steps/s", "h2d_bytes_per_step": int(h2d),
