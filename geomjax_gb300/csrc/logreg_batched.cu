@@ -26,6 +26,7 @@
 // evaluated per chain in FP32 with an FP64 sum.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -717,6 +718,8 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
     // only ever grows (a context for a small d must not lower the limit a
     // larger context's captured launches rely on).
     static size_t s_chol_smem = 0;
+    static std::mutex s_mu;  // contexts may be created from several threads
+    std::lock_guard<std::mutex> lock(s_mu);
     size_t smax = 0;
     for (int cpw = 1; cpw <= 8; cpw *= 2) {
       smax = std::max(smax, chol_config(d, sizeof(double), cpw).smem);
