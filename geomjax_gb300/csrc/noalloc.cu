@@ -28,7 +28,7 @@ static __device__ __align__(256) bf16 g_scratch[kHeaderElems + kScratchElems];
 
 constexpr int kMaxDevices = 64;
 bf16* g_base[kMaxDevices];  // device address of g_scratch, per device
-std::string g_err;
+thread_local std::string g_err;
 
 inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
 
