@@ -10,9 +10,10 @@ torch = pytest.importorskip("torch")
 
 pytestmark = pytest.mark.gpu
 
-# the largest d first: a later, smaller context must not lower the
-# process-wide shared-memory limit the larger one's launches need
-SIZES = [(220, 110), (200, 8), (350, 21), (260, 40)]
+# the largest d (the path's maximum, 128) first: a later, smaller context
+# must not lower the process-wide shared-memory limit the larger one's
+# launches need
+SIZES = [(220, 128), (200, 8), (350, 21), (260, 40)]
 C = 64
 
 
