@@ -234,8 +234,16 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   bool bad = false;
   double pm = 1.0;
   int pe = 0;
-  int cj = 0;  // colstart(j)
-  for (int j = 0; j < d; ++j) {
+  // The FP64 factorisation takes one column per step: its DFMA count bounds
+  // it, and rank-2 blocking (one pass over the trailing triangle for two
+  // columns) measured no faster for F = double.  For F = float, where
+  // latency bounds the kernel, columns are taken two at a time: pivot j,
+  // scale column j, update column j + 1 with it, pivot j + 1, scale column
+  // j + 1, then one pass applies both columns to the trailing triangle.
+  // pivot(j): 1/L_jj from the current diagonal, log det product, and the
+  // bordered y_j (all lanes compute the same scalars; lane 0 of the chain
+  // writes them)
+  auto pivot = [&](int j, int cj) -> F {
     const F djj = L[cj];
     if (!(djj > F(0))) bad = true;
     const F inv = rsqrt_nr(djj);  // 1/L_jj
@@ -250,19 +258,53 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     }
     for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
     __syncwarp();
-    if (border) {
-      const F yj = y[j];
-      for (int k = j + 1 + sl; k < d; k += LPC) y[k] -= yj * L[cj + k - j];
+    return inv;
+  };
+  constexpr bool kRank2 = sizeof(F) == sizeof(float);
+  int cj = 0;  // colstart(j)
+  for (int j = 0; j < d; j += kRank2 ? 2 : 1) {
+    pivot(j, cj);
+    const int cj1 = cj + (d - j);  // colstart(j + 1)
+    if (!kRank2 || j + 1 == d) {
+      // rank-1 step: bordered y and the trailing triangle with column j
+      if (border) {
+        const F yj = y[j];
+        for (int k = j + 1 + sl; k < d; k += LPC) y[k] -= yj * L[cj + k - j];
+      }
+      const F* __restrict__ colj = L + cj - j;  // colj[i] = L(i, j)
+      F* __restrict__ tr = L;
+#pragma unroll 4
+      for (int t = cj1 + sl; t < P; t += LPC) {
+        const uint32_t ik = tab[t];
+        tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
+      }
+      cj = cj1;
+      __syncwarp();
+      continue;
     }
-    // trailing triangle: column j is read-only here and disjoint from the
-    // entries written, so the iterations' loads may be issued together
-    const int cn = cj + (d - j);  // colstart(j + 1)
-    const F* __restrict__ colj = L + cj - j;  // colj[i] = L(i, j)
+    // column j + 1 (rows j + 1 ..) and y_{j+1} reduced by column j
+    {
+      const F l10 = L[cj + 1];  // L(j + 1, j)
+      for (int i = j + 1 + sl; i < d; i += LPC) L[cj1 + i - j - 1] -= L[cj + i - j] * l10;
+      if (border && sl == 0) y[j + 1] -= y[j] * l10;
+    }
+    __syncwarp();
+    pivot(j + 1, cj1);
+    // trailing triangle (columns k >= j + 2): both columns are read-only
+    // here and disjoint from the entries written
+    const int cn = cj1 + (d - j - 1);  // colstart(j + 2)
+    const F* __restrict__ c0 = L + cj - j;        // c0[i] = L(i, j)
+    const F* __restrict__ c1 = L + cj1 - j - 1;   // c1[i] = L(i, j + 1)
     F* __restrict__ tr = L;
+    if (border) {
+      const F y0 = y[j], y1 = y[j + 1];
+      for (int k = j + 2 + sl; k < d; k += LPC) y[k] -= y0 * c0[k] + y1 * c1[k];
+    }
 #pragma unroll 4
     for (int t = cn + sl; t < P; t += LPC) {
       const uint32_t ik = tab[t];
-      tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
+      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+      tr[t] -= c0[i] * c0[k] + c1[i] * c1[k];
     }
     cj = cn;
     __syncwarp();
@@ -328,20 +370,35 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     Li[t] = (ik & 0xffffu) == (ik >> 16) ? 1.f : 0.f;
   }
   __syncwarp();
+  // two rows at a time: rows k and k + 1 are made final (row k scaled; row
+  // k + 1 reduced by row k, then scaled), then rows i > k + 1 are reduced
+  // by both in one pass
   int ck = 0;  // colstart(k)
-  for (int k = 0; k < d; ++k) {
+  for (int k = 0; k < d; k += 2) {
     const float ikk = float(rdiag[k]);
     for (int cc = sl; cc <= k; cc += LPC) Li[colstart(cc, d) + k - cc] *= ikk;
     __syncwarp();
-    for (int i = k + 1 + sl; i < d; i += LPC) {
-      const float lik = float(L[ck + i - k]);
+    const int ck1 = ck + (d - k);  // colstart(k + 1)
+    if (k + 1 == d) break;
+    const float l10 = float(L[ck + 1]);  // L(k + 1, k)
+    const float ik1 = float(rdiag[k + 1]);
+    for (int cc = sl; cc <= k + 1; cc += LPC) {
+      const int o = colstart(cc, d);
+      const float v = (cc <= k) ? Li[o + k + 1 - cc] - l10 * Li[o + k - cc] : Li[o];
+      Li[o + k + 1 - cc] = v * ik1;
+    }
+    __syncwarp();
+    for (int i = k + 2 + sl; i < d; i += LPC) {
+      const float li0 = float(L[ck + i - k]);       // L(i, k)
+      const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
       int cc0 = 0;  // colstart(cc)
       for (int cc = 0; cc <= k; ++cc) {
-        Li[cc0 + i - cc] -= lik * Li[cc0 + k - cc];
+        Li[cc0 + i - cc] -= li0 * Li[cc0 + k - cc] + li1 * Li[cc0 + k + 1 - cc];
         cc0 += d - cc;
       }
+      Li[cc0 + i - k - 1] -= li1 * Li[cc0];  // cc = k + 1: Li(k, k + 1) = 0
     }
-    ck += d - k;
+    ck = ck1 + (d - k - 1);
     __syncwarp();
   }
   // G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients (row-major upper triangle, whose
