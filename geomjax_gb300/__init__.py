@@ -22,11 +22,14 @@ from .diagnostics import effective_sample_size, ess, potential_scale_reduction, 
 from .samplers import Kernel, lmc, lmcmonge, rmhmc
 from .targets import funnel, hierarchical_gaussian, logistic_regression
 from .adaptation import gradient_step_size_adaptation, step_size_adaptation, window_adaptation
+from .chees import (adam, chees_adaptation, dynamic_lmc, dynamic_lmcmonge, dynamic_rmhmc,
+                    lmcmonge_chees_adaptation)
 
 __all__ = [
     "AdaptationAlgorithm", "AdaptationResults", "Draws", "LMCInfo", "LMCState", "RMHMCInfo",
     "RMHMCState", "SamplingAlgorithm", "Kernel", "rmhmc", "lmc", "lmcmonge", "funnel",
     "logistic_regression", "hierarchical_gaussian", "effective_sample_size", "ess",
     "potential_scale_reduction", "rhat", "window_adaptation", "step_size_adaptation",
-    "gradient_step_size_adaptation",
+    "gradient_step_size_adaptation", "chees_adaptation", "lmcmonge_chees_adaptation",
+    "dynamic_rmhmc", "dynamic_lmc", "dynamic_lmcmonge", "adam",
 ]

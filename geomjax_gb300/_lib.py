@@ -49,6 +49,11 @@ class GjChainState(ctypes.Structure):
     ]
 
 
+# GjInfo's fields in order, as keys of the samplers' info dicts
+INFO_FIELDS = ("acceptance_rate", "is_accepted", "is_divergent", "energy", "fp_iters", "status",
+               "momentum", "proposal_position", "proposal_velocity")
+
+
 class GjInfo(ctypes.Structure):
     _fields_ = [
         ("acceptance_rate", c_void_p),
@@ -58,6 +63,8 @@ class GjInfo(ctypes.Structure):
         ("fp_iters", c_void_p),
         ("status", c_void_p),
         ("momentum", c_void_p),
+        ("proposal_position", c_void_p),
+        ("proposal_velocity", c_void_p),
     ]
 
 
@@ -110,6 +117,10 @@ SIGNATURES = {
     "gj_logreg_gl_transition_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_void_p, c_void_p,
                                               c_double, c_double, c_int32, c_int32, c_int32,
                                               c_int32, c_void_p, c_void_p]),
+    "gj_chees_workspace_size": (c_int64, [c_int32, c_int32]),
+    "gj_chees_statistics": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p]),
     "gj_metric_vjp": (c_int32, [POINTER(GjTarget), c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                 c_void_p]),
 }

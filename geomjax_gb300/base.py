@@ -40,6 +40,15 @@ class RMHMCState(NamedTuple):
     logdensity_grad: Any
 
 
+class Proposal(NamedTuple):
+    """The end of the trajectory after the momentum / velocity flip
+    (``RMHMCInfo.proposal.state``, ``rmhmc/rmhmc.py:425-437``): ``velocity``
+    is −G⁻¹p for RMHMC and −v for LMC, whether or not it was accepted."""
+
+    position: Any
+    velocity: Any
+
+
 class RMHMCInfo(NamedTuple):
     momentum: Any
     acceptance_rate: Any
@@ -49,6 +58,7 @@ class RMHMCInfo(NamedTuple):
     num_integration_steps: int
     fixed_point_iters: Any
     status: Any
+    proposal: Any = None
 
 
 class LMCState(NamedTuple):
@@ -66,3 +76,4 @@ class LMCInfo(NamedTuple):
     energy: Any
     num_integration_steps: int
     status: Any
+    proposal: Any = None

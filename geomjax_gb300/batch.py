@@ -138,9 +138,7 @@ class PosteriorBatch:
         p.divergence_threshold = self.divergence_threshold
         st = L.GjChainState(L.ptr(state.position), L.ptr(state.logdensity_grad),
                             L.ptr(state.logdensity), None, self.B * self.C)
-        inf = L.GjInfo(*(L.ptr(info.get(k)) for k in ("acceptance_rate", "is_accepted",
-                                                     "is_divergent", "energy", "fp_iters",
-                                                     "status", "momentum")))
+        inf = L.GjInfo(*(L.ptr(info.get(k)) for k in L.INFO_FIELDS))
         L.check(self.lib.gj_batch_rmhmc_step(self.h, ctypes.byref(p), ctypes.byref(st), L.ptr(z),
                                              L.ptr(u), ctypes.byref(inf), _stream()))
 

@@ -33,6 +33,7 @@ UNITS = [
     ("capi.cu", []),
     ("noalloc.cu", []),
     ("traj_jvp.cu", []),
+    ("chees.cu", []),
 ]
 
 

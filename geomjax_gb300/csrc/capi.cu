@@ -137,6 +137,8 @@ gj::InfoDev<T> info_offset(gj::InfoDev<T> i, size_t c0, int d) {
   if (i.fp_iters) i.fp_iters += c0;
   if (i.status) i.status += c0;
   if (i.momentum) i.momentum += c0 * d;
+  if (i.prop_q) i.prop_q += c0 * d;
+  if (i.prop_v) i.prop_v += c0 * d;
   return i;
 }
 
@@ -537,6 +539,42 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const do
 }
 
 // ---------------------------------------------------------------------------
+// ChEES cross-chain statistics
+// ---------------------------------------------------------------------------
+int64_t gj_chees_workspace_size(int32_t num_chains, int32_t dim) {
+  if (num_chains < 1 || dim < 1) return -1;
+  return (int64_t)gj::chees_workspace_bytes(num_chains, dim);
+}
+
+int32_t gj_chees_statistics(int32_t precision, int32_t num_chains, int32_t dim,
+                            const void* proposal_position, const void* proposal_velocity,
+                            const void* initial_position, const void* proposal_alpha2_tangent,
+                            const double* acceptance_rate, const uint8_t* is_divergent,
+                            void* workspace, double* out, void* stream) {
+  if (precision != GJ_FP64 && precision != GJ_MIXED) return fail(GJ_EINVAL, "bad precision");
+  if (num_chains < 1 || dim < 1) return fail(GJ_EINVAL, "num_chains and dim must be >= 1");
+  if (!proposal_position || !proposal_velocity || !initial_position || !acceptance_rate ||
+      !workspace || !out)
+    return fail(GJ_EINVAL, "a required array is NULL");
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  double* w = static_cast<double*>(workspace);
+  cudaError_t e;
+  if (precision == GJ_FP64)
+    e = gj::chees_statistics<double>(num_chains, dim, static_cast<const double*>(proposal_position),
+                                     static_cast<const double*>(proposal_velocity),
+                                     static_cast<const double*>(initial_position),
+                                     static_cast<const double*>(proposal_alpha2_tangent),
+                                     acceptance_rate, is_divergent, w, out, cs);
+  else
+    e = gj::chees_statistics<float>(num_chains, dim, static_cast<const float*>(proposal_position),
+                                    static_cast<const float*>(proposal_velocity),
+                                    static_cast<const float*>(initial_position),
+                                    static_cast<const float*>(proposal_alpha2_tangent),
+                                    acceptance_rate, is_divergent, w, out, cs);
+  return cuda_status(e, "gj_chees_statistics");
+}
+
+// ---------------------------------------------------------------------------
 // batches of independent dense-Fisher logistic-regression posteriors
 // ---------------------------------------------------------------------------
 }  // extern "C"
@@ -657,6 +695,8 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
     const size_t po = b->pos_off[i], co = (size_t)i * b->C;
     gj::InfoDev<float> ig = info_offset(inf, co, 0);
     if (inf.momentum) ig.momentum = inf.momentum + po;
+    if (inf.prop_q) ig.prop_q = inf.prop_q + po;
+    if (inf.prop_v) ig.prop_v = inf.prop_v + po;
     const int rc = gj::logreg_batched_rmhmc_step_graph(
         b->lbs[i], sp, (float*)s->position + po, (float*)s->logdensity_grad + po,
         s->logdensity + co, z + po, u + co, ig, 2, b->streams[i % b->S]);

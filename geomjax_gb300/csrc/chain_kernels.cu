@@ -264,6 +264,14 @@ __global__ void __launch_bounds__(128) rmhmc_chain_kernel(TargetDev t, StepDev s
   // flip_momentum (rmhmc.py:443-462) does not change K; H1 at the proposal
   eval_metric<T, DMAX>(t, q, M, false, &bad);
   const double H1 = -ld + kinetic_rm<T, DMAX>(M, d, p);
+  if (info.prop_q || info.prop_v) {  // RMHMCInfo.proposal.state: q_L and −G⁻¹(q_L)p_L
+    double vel[DMAX];
+    metric_solve<T, DMAX>(M, d, p, vel);
+    for (int i = 0; i < d; ++i) {
+      if (info.prop_q) info.prop_q[(size_t)c * d + i] = q[i];
+      if (info.prop_v) info.prop_v[(size_t)c * d + i] = T(-vel[i]);
+    }
+  }
   const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
     for (int i = 0; i < d; ++i) {
@@ -449,6 +457,10 @@ __global__ void __launch_bounds__(128) lmc_chain_kernel(TargetDev t, StepDev sp,
   }
   logdet = lmc_metric<T, DMAX>(t, q, W, diag, &bad);
   const double H1 = -ld + lmc_kinetic<DMAX>(W, d, logdet, v, diag) - J;
+  for (int i = 0; i < d; ++i) {  // LMCInfo.proposal.state: q_L and −v_L (flip_velocity)
+    if (info.prop_q) info.prop_q[(size_t)c * d + i] = q[i];
+    if (info.prop_v) info.prop_v[(size_t)c * d + i] = T(-v[i]);
+  }
   const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
     for (int i = 0; i < d; ++i) {
@@ -588,6 +600,10 @@ __global__ void __launch_bounds__(128) monge_chain_kernel(TargetDev t, StepDev s
     for (int i = 0; i < d; ++i) hv[i] = T(double(hv[i]) / sL);
   }
   const double H1 = -ld + kinetic(L) - J;  // flip_velocity leaves K unchanged
+  for (int i = 0; i < d; ++i) {  // LMCInfo.proposal.state: q_L and −v_L
+    if (info.prop_q) info.prop_q[(size_t)c * d + i] = q[i];
+    if (info.prop_v) info.prop_v[(size_t)c * d + i] = T(-double(v[i]));
+  }
   const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
     for (int i = 0; i < d; ++i) {

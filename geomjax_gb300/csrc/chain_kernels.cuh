@@ -42,4 +42,13 @@ cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos,
                               const InfoDev<float>& info, int C, cudaStream_t st);
 bool monge_warp_supported(const TargetDev& t);
 
+// ChEES cross-chain statistics (chees.cu): out[0] harmonic mean of the
+// acceptance probabilities, out[1] the trajectory-length gradient, out[2]
+// the α² gradient (0 without D); work holds chees_workspace_bytes(C, d)
+size_t chees_workspace_bytes(int C, int d);
+template <typename T>
+cudaError_t chees_statistics(int C, int d, const T* P, const T* V, const T* I, const T* D,
+                             const double* acc, const uint8_t* div, double* work, double* out,
+                             cudaStream_t st);
+
 }  // namespace gj

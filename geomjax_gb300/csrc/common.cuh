@@ -74,6 +74,8 @@ struct InfoDev {
   int32_t* fp_iters;
   uint8_t* status;
   T* momentum;
+  T* prop_q;  // proposal position [C, d]
+  T* prop_v;  // proposal velocity (flipped) [C, d]
 };
 
 template <typename T>
@@ -87,6 +89,8 @@ inline InfoDev<T> to_dev(const gj_info* i) {
     r.fp_iters = i->fp_iters;
     r.status = i->status;
     r.momentum = static_cast<T*>(i->momentum);
+    r.prop_q = static_cast<T*>(i->proposal_position);
+    r.prop_v = static_cast<T*>(i->proposal_velocity);
   }
   return r;
 }

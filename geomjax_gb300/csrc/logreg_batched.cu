@@ -89,6 +89,7 @@ struct CholArgs {
   const uint8_t* active;  // EVAL: skip inactive chains (may be NULL)
   uint8_t* bad;        // [C] non-SPD flag (sticky)
   float* mom_info;     // DRAW: info.momentum (may be NULL)
+  float* vel_info;     // ENERGY: the proposal velocity −G⁻¹p (may be NULL)
 };
 
 // Chain packing.  The FP64 pipe issues one warp instruction for all 32 lanes
@@ -342,7 +343,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
       q = group_sum<LPC>(q);
       if (sl == 0 && live) a.quad[c] = q;
-      return;
+      if (!a.vel_info) return;  // uniform: the proposal velocity was not asked for
     }
   }
   __syncwarp();
@@ -356,6 +357,11 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     if (sl == 0) xv[j] = xj;
     for (int i = sl; i < j; i += LPC) xv[i] -= L[colstart(i, d) + j - i] * xj;
     __syncwarp();
+  }
+  if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
+    if (live)
+      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = float(-xv[i]);
+    return;
   }
   if (live) {
     for (int i = sl; i < d; i += LPC) {
@@ -555,6 +561,8 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
   const double H0 = -ld0[c] + 0.5 * H0q[c] + 0.5 * logdet0[c] + cst;
   const double H1 = -ld1 + 0.5 * quad1[c] + 0.5 * logdet1[c] + cst;
   const AcceptOut a = metropolis(H0, H1, uacc[c], spd ? spd->div_threshold : div_thr);
+  if (info.prop_q)  // RMHMCInfo.proposal.state.position
+    for (int i = 0; i < d; ++i) info.prop_q[(size_t)c * d + i] = float(qc[(size_t)c * d + i]);
   if (a.accept) {
     for (int i = 0; i < d; ++i) {
       const double q = qc[(size_t)c * d + i];
@@ -625,14 +633,23 @@ struct LogregBatched {
   int prof;
   // graph path: device step parameters, staging buffers, captured graph
   StepDev* spd;
-  float *pos_s, *grad_s, *z_s, *mom_s;
+  float *pos_s, *grad_s, *z_s, *mom_s, *propq_s, *propv_s;
   double *ld_s, *u_s, *acc_s, *energy_s;
   uint8_t *accepted_s, *divergent_s, *status_s;
   int* fpit_s;
   int* trips;
   cudaStream_t cap_main, cap_body;
-  cudaGraphExec_t gexec;
-  int g_L, g_impl, g_chol;
+  // Captured transitions, one per (number of steps, GEMM implementation,
+  // factorisation set-up, proposal velocity wanted), least recently used
+  // evicted beyond kMaxGraphs: a jittered trajectory length
+  // (rmhmc/rmhmc.py:179-244) draws the number of steps per transition.
+  struct Graph {
+    int L, impl, cfg, prop;
+    cudaGraphExec_t exec;
+    unsigned long long used;
+  };
+  std::vector<Graph> graphs;
+  unsigned long long graph_tick;
   std::vector<cudaEvent_t> ev;
   size_t ev_used;
   std::vector<cudaEvent_t> cev;  // the same around the factorisations
@@ -668,7 +685,7 @@ void logreg_batched_destroy(LogregBatched* lb) {
   for (void* p : lb->owned) cudaFree(p);
   for (cudaEvent_t e : lb->ev) cudaEventDestroy(e);
   for (cudaEvent_t e : lb->cev) cudaEventDestroy(e);
-  if (lb->gexec) cudaGraphExecDestroy(lb->gexec);
+  for (auto& g : lb->graphs) cudaGraphExecDestroy(g.exec);
   if (lb->cap_main) cudaStreamDestroy(lb->cap_main);
   if (lb->cap_body) cudaStreamDestroy(lb->cap_body);
   if (lb->n_active_h) cudaFreeHost(lb->n_active_h);
@@ -693,8 +710,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->prof = 0;
   lb->ev_used = 0;
   lb->cev_used = 0;
-  lb->gexec = nullptr;
-  lb->g_L = lb->g_impl = lb->g_chol = -1;
+  lb->graph_tick = 0;
   lb->cap_main = lb->cap_body = nullptr;
   lb->stats = LogregStats{};
   bool ok = true;
@@ -744,6 +760,8 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->grad_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
   lb->z_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
   lb->mom_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->propq_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
+  lb->propv_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
   lb->ld_s = dalloc<double>(C, lb->owned, &ok);
   lb->u_s = dalloc<double>(C, lb->owned, &ok);
   lb->acc_s = dalloc<double>(C, lb->owned, &ok);
@@ -881,7 +899,7 @@ struct Runner {
   }
 
   void chol(int mode, const float* z, double* logdet, double* quad, float* mom_info,
-            bool only_active = false) {
+            bool only_active = false, float* vel_info = nullptr) {
     LogregBatched& L = *lb;
     CholArgs a{};
     a.mode = mode;
@@ -902,6 +920,7 @@ struct Runner {
     a.active = only_active ? L.active : nullptr;
     a.bad = L.bad;
     a.mom_info = mom_info;
+    a.vel_info = vel_info;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (L.prof) {
       while (L.cev.size() < L.cev_used + 2) {
@@ -918,7 +937,8 @@ struct Runner {
     }
     const double dd = L.d;
     L.stats.chol_launches++;
-    L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + (mode == CH_ENERGY ? 1.0 : 2.0) * dd * dd);
+    const double solves = (mode == CH_ENERGY && !vel_info) ? 1.0 : 2.0;
+    L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + solves * dd * dd);
     const CholCfg cf =
         chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.C);
     const int per_cta = cf.warps * cf.cpw;
@@ -953,12 +973,13 @@ struct Runner {
     gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
   }
 
-  // energy at the proposal: ℓ row sums, Gram, log det and ||L⁻¹p||², ∇ℓ
-  void energy() {
+  // energy at the proposal: ℓ row sums, Gram, log det and ||L⁻¹p||², ∇ℓ;
+  // with vel_out, also the flipped proposal velocity −G⁻¹p
+  void energy(float* vel_out) {
     LogregBatched& L = *lb;
     check(cudaMemsetAsync(L.ldnew, 0, sizeof(double) * L.C, st));
     metric_gram(L.ldnew);
-    chol(CH_ENERGY, nullptr, L.logdet1, L.quad1, nullptr);
+    chol(CH_ENERGY, nullptr, L.logdet1, L.quad1, nullptr, false, vel_out);
     Epi o{};
     o.mode = EPI_STORE;
     o.D = L.Gout;
@@ -1063,7 +1084,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
     R.chol(CH_DRAW, z, lb->logdet0, lb->quad0, info.momentum);
   }
   // energy at the proposal (3-plane Xβ row sums, Gram, log det, ∇ℓ) and accept
-  R.energy();
+  R.energy(info.prop_v);
   R.accept(logdens, u, sp.div_threshold, pos, grad, logdens, info);
   if (R.err == cudaSuccess && lb->prof && lb->ev_used) {
     R.check(cudaStreamSynchronize(st));
@@ -1106,14 +1127,16 @@ int graph_fail(const char* what, cudaError_t e) {
   return GJ_ECUDA;
 }
 
+constexpr size_t kMaxGraphs = 64;
+
+int graph_cfg(const LogregBatched* lb) { return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl; }
+
 // Capture one whole transition (all L steps, each fixed-point solve a
-// conditional WHILE node) into lb->gexec.  The graph reads and writes the
-// context's staging buffers; step parameters come from lb->spd.
-int build_graph(LogregBatched* lb, int L, int impl) {
-  if (lb->gexec) {
-    cudaGraphExecDestroy(lb->gexec);
-    lb->gexec = nullptr;
-  }
+// conditional WHILE node) into *out.  The graph reads and writes the
+// context's staging buffers; step parameters come from lb->spd.  With prop,
+// the energy factorisation also writes the proposal velocity.
+int build_graph(LogregBatched* lb, int L, int impl, bool prop, cudaGraphExec_t* out) {
+  *out = nullptr;
   const int C = lb->C, d = lb->d;
   cudaStream_t s = lb->cap_main;
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -1180,7 +1203,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
     R.metric_gram();
     R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
   }
-  R.energy();
+  R.energy(prop ? lb->propv_s : nullptr);
   InfoDev<float> inf{};
   inf.acc_rate = lb->acc_s;
   inf.accepted = lb->accepted_s;
@@ -1189,6 +1212,7 @@ int build_graph(LogregBatched* lb, int L, int impl) {
   inf.fp_iters = lb->fpit_s;
   inf.status = lb->status_s;
   inf.momentum = nullptr;
+  inf.prop_q = lb->propq_s;
   R.accept(lb->ld_s, lb->u_s, 0.0, lb->pos_s, lb->grad_s, lb->ld_s, inf);
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(s, &g);
@@ -1201,15 +1225,39 @@ int build_graph(LogregBatched* lb, int L, int impl) {
     cudaGraphDestroy(g);
     return graph_fail("kernels", R.err);
   }
-  e = cudaGraphInstantiate(&lb->gexec, g, 0);
+  e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
-    lb->gexec = nullptr;
+    *out = nullptr;
     return graph_fail("instantiate", e);
   }
-  lb->g_L = L;
-  lb->g_impl = impl;
-  lb->g_chol = lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl;
+  return GJ_OK;
+}
+
+// The captured transition for these settings, captured now if absent.
+int find_graph(LogregBatched* lb, int L, int impl, bool prop, cudaStream_t st,
+               cudaGraphExec_t* out) {
+  const int cfg = graph_cfg(lb);
+  for (auto& g : lb->graphs)
+    if (g.L == L && g.impl == impl && g.cfg == cfg && g.prop == (int)prop) {
+      g.used = ++lb->graph_tick;
+      *out = g.exec;
+      return GJ_OK;
+    }
+  // the capture streams must not see unfinished work of the caller's stream
+  cudaStreamSynchronize(st);
+  if (lb->graphs.size() >= kMaxGraphs) {
+    size_t lru = 0;
+    for (size_t i = 1; i < lb->graphs.size(); ++i)
+      if (lb->graphs[i].used < lb->graphs[lru].used) lru = i;
+    cudaGraphExecDestroy(lb->graphs[lru].exec);
+    lb->graphs.erase(lb->graphs.begin() + lru);
+  }
+  cudaGraphExec_t ex = nullptr;
+  const int rc = build_graph(lb, L, impl, prop, &ex);
+  if (rc) return rc;
+  lb->graphs.push_back({L, impl, cfg, (int)prop, ex, ++lb->graph_tick});
+  *out = ex;
   return GJ_OK;
 }
 
@@ -1228,12 +1276,9 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
     g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
     return GJ_ENOTSUP;
   }
-  if (!lb->gexec || lb->g_L != sp.L || lb->g_impl != gemm_impl || lb->g_chol != lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl) {
-    // the capture streams must not see unfinished work of the caller's stream
-    cudaStreamSynchronize(st);
-    const int rc = build_graph(lb, sp.L, gemm_impl);
-    if (rc) return rc;
-  }
+  cudaGraphExec_t gexec = nullptr;
+  const int rc = find_graph(lb, sp.L, gemm_impl, info.prop_v != nullptr, st, &gexec);
+  if (rc) return rc;
   const int C = lb->C, d = lb->d;
   lb->stats = LogregStats{};
   set_step_kernel<<<1, 1, 0, st>>>(lb->spd, sp);
@@ -1243,7 +1288,7 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
   copy_out(lb->ld_s, logdens, (size_t)C, st, &e);
   copy_out(lb->z_s, z, (size_t)C * d, st, &e);
   copy_out(lb->u_s, u, (size_t)C, st, &e);
-  if (e == cudaSuccess) e = cudaGraphLaunch(lb->gexec, st);
+  if (e == cudaSuccess) e = cudaGraphLaunch(gexec, st);
   copy_out(pos, lb->pos_s, (size_t)C * d, st, &e);
   copy_out(grad, lb->grad_s, (size_t)C * d, st, &e);
   copy_out(logdens, lb->ld_s, (size_t)C, st, &e);
@@ -1254,6 +1299,8 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
   copy_out(info.fp_iters, lb->fpit_s, (size_t)C, st, &e);
   copy_out(info.status, lb->status_s, (size_t)C, st, &e);
   copy_out(info.momentum, lb->mom_s, (size_t)C * d, st, &e);
+  copy_out(info.prop_q, lb->propq_s, (size_t)C * d, st, &e);
+  copy_out(info.prop_v, lb->propv_s, (size_t)C * d, st, &e);
   if (e != cudaSuccess) {
     g_err = std::string("graph step: ") + cudaGetErrorString(e);
     return GJ_ECUDA;

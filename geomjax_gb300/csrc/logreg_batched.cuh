@@ -20,10 +20,12 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
 
 // Same transition as one CUDA-graph launch: every fixed-point solve is a
 // conditional WHILE node driven by the device-side count of active chains
-// (no host synchronisation inside the step).  The graph is captured on the
-// first call and again when the number of steps, the GEMM implementation or
-// the factorisation precision changes; step size, tolerance, iteration cap
-// and divergence threshold are read from device memory at run time.
+// (no host synchronisation inside the step).  One graph is captured per
+// number of steps, GEMM implementation, factorisation set-up and whether the
+// proposal velocity is asked for (up to 64, least recently used evicted), so
+// a jittered number of steps per transition reuses its graphs; step size,
+// tolerance, iteration cap and divergence threshold are read from device
+// memory at run time.
 int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
                                     double* logdens, const float* z, const double* u,
                                     const InfoDev<float>& info, int gemm_impl, cudaStream_t st);

@@ -400,6 +400,16 @@ __global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp
   }
   const double J = J0 + double(dJ);
   const double H1 = -ld + kinetic(L) - J;
+  if (info.prop_q || info.prop_v) {  // LMCInfo.proposal.state: q_L and −v_L
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = lane + 32 * k;
+      if (i < d) {
+        if (info.prop_q) info.prop_q[(size_t)c * d + i] = q.x[k];
+        if (info.prop_v) info.prop_v[(size_t)c * d + i] = -v.x[k];
+      }
+    }
+  }
   const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
 #pragma unroll

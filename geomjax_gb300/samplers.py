@@ -27,7 +27,7 @@ import ctypes
 import torch
 
 from . import _lib as L
-from .base import (Draws, LMCInfo, LMCState, RMHMCInfo, RMHMCState, SamplingAlgorithm)
+from .base import (Draws, LMCInfo, LMCState, Proposal, RMHMCInfo, RMHMCState, SamplingAlgorithm)
 from .targets import PRECISIONS, Target
 
 INTEGRATORS = {"implicit_midpoint": L.GJ_IMPLICIT_MIDPOINT,
@@ -144,9 +144,7 @@ class Kernel:
         st = L.GjChainState(L.ptr(state.position), L.ptr(state.logdensity_grad),
                             L.ptr(state.logdensity),
                             L.ptr(getattr(state, "volume_adjustment", None)), C)
-        inf = L.GjInfo(*(L.ptr(info.get(k)) for k in ("acceptance_rate", "is_accepted",
-                                                     "is_divergent", "energy", "fp_iters",
-                                                     "status", "momentum")))
+        inf = L.GjInfo(*(L.ptr(info.get(k)) for k in L.INFO_FIELDS))
         p = self.params(target, step_size, num_integration_steps, alpha2, inverse_mass)
         fn = {L.GJ_SAMPLER_RMHMC: ctx.lib.gj_rmhmc_step, L.GJ_SAMPLER_LMC: ctx.lib.gj_lmc_step,
               L.GJ_SAMPLER_LMCMONGE: ctx.lib.gj_lmcmonge_step}[self.sampler]
@@ -154,8 +152,10 @@ class Kernel:
                    _stream()))
 
     @staticmethod
-    def new_info(C, d, target, device):
-        return {
+    def new_info(C, d, target, device, proposal=False):
+        """Output buffers of one transition; with ``proposal`` also the
+        flipped end state (``proposal_position``, ``proposal_velocity``)."""
+        info = {
             "acceptance_rate": torch.empty(C, dtype=torch.float64, device=device),
             "is_accepted": torch.empty(C, dtype=torch.uint8, device=device),
             "is_divergent": torch.empty(C, dtype=torch.uint8, device=device),
@@ -164,13 +164,17 @@ class Kernel:
             "status": torch.empty(C, dtype=torch.uint8, device=device),
             "momentum": torch.empty(C, d, dtype=target.dtype, device=device),
         }
+        if proposal:
+            info["proposal_position"] = torch.empty(C, d, dtype=target.dtype, device=device)
+            info["proposal_velocity"] = torch.empty(C, d, dtype=target.dtype, device=device)
+        return info
 
     def __call__(self, rng_key, state, target, step_size, num_integration_steps, *, alpha2=0.0,
                  inverse_mass_matrix=None):
         C, d = state.position.shape
         z, u = self.draws(rng_key, C, d, target)
         new = type(state)(*(t.clone() for t in state))
-        info = self.new_info(C, d, target, target.device)
+        info = self.new_info(C, d, target, target.device, proposal=True)
         im = None
         if inverse_mass_matrix is not None:
             im = torch.as_tensor(inverse_mass_matrix).to(device=target.device, dtype=target.dtype)
@@ -179,12 +183,13 @@ class Kernel:
                           inverse_mass=im)
         acc = info["is_accepted"].bool()
         div = info["is_divergent"].bool()
+        prop = Proposal(info["proposal_position"], info["proposal_velocity"])
         if self.sampler == L.GJ_SAMPLER_RMHMC:
             return new, RMHMCInfo(info["momentum"], info["acceptance_rate"], acc, div,
                                   info["energy"], num_integration_steps, info["fp_iters"],
-                                  info["status"])
+                                  info["status"], prop)
         return new, LMCInfo(info["momentum"], info["acceptance_rate"], acc, div, info["energy"],
-                            num_integration_steps, info["status"])
+                            num_integration_steps, info["status"], prop)
 
 
 def _init(target: Target, position, lmc_state: bool):

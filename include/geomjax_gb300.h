@@ -31,6 +31,10 @@
  *                      jax.jacfwd through a trajectory with respect to the
  *                      step size and a metric parameter
  *                      (adaptation/chees_adaptation_lmcmonge.py:497-519)
+ *   gj_chees_statistics, gj_chees_workspace_size
+ *                      the cross-chain reductions of ChEES adaptation
+ *                      (adaptation/chees_adaptation_riemanian.py:145-190,
+ *                      chees_adaptation_lmcmonge.py:151-236)
  *   gj_gemm_split_bf16, gj_gemm_split_bf16_noalloc, gj_stats, gj_profile,
  *   gj_set_option, gj_set_gemm_tiling
  *                      no reference counterpart: the split-BF16 contraction
@@ -126,6 +130,13 @@ typedef struct {
   int32_t* fp_iters;       /* [C] fixed-point iterations summed over the trajectory */
   uint8_t* status;         /* [C] GJ_CHAIN_* bits */
   void* momentum;          /* [C, d] the drawn momentum (RMHMC) or velocity (LMC) */
+  /* The proposal, written whether or not it is accepted: the end of the
+   * trajectory after the flip (rmhmc/rmhmc.py:425-426,443-462,
+   * lmcmonge/lmc.py:506-507, lmcmc/lmc.py:441-442), i.e. RMHMCInfo.proposal.state
+   * / LMCInfo.proposal.state.  ChEES adaptation reads these
+   * (adaptation/chees_adaptation_riemanian.py:161-190). */
+  void* proposal_position; /* [C, d] q_L */
+  void* proposal_velocity; /* [C, d] RMHMC: -G(q_L)^-1 p_L; LMC / LMC-Monge: -v_L */
 } gj_info;
 
 typedef struct {
@@ -305,6 +316,28 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t num_chains,
                                     const double* z, double step_size, double metric_reg,
                                     int32_t num_integration_steps, int32_t kp, int32_t kq,
                                     int32_t tangents, double* out, void* stream);
+
+/* ChEES cross-chain statistics of one transition
+ * (adaptation/chees_adaptation_riemanian.py:145-190 and
+ * chees_adaptation_lmcmonge.py:151-236), from the proposal the step wrote
+ * into gj_info (proposal_position P, proposal_velocity V) and the positions
+ * I the transition started from, all [C, d] in the precision's vector dtype:
+ *   out[0] = 1 / mean(1 / acceptance_rate) over non-divergent chains
+ *   out[1] = Σ a_c g_c / Σ a_c over non-divergent chains, with
+ *            g_c = (|P̃_c|² − |Ĩ_c|²)(P̃_c · V_c), P̃ = P − nanmean over chains,
+ *            Ĩ = I − nanmean over chains
+ *   out[2] = the same weighted mean with V replaced by the tangent
+ *            D = ∂P/∂α² (0 when proposal_alpha2_tangent is NULL)
+ * The reference multiplies out[1] and out[2] by jitter × trajectory length.
+ * is_divergent may be NULL (no chain divergent).  out: 3 doubles of DEVICE
+ * memory; workspace: gj_chees_workspace_size(C, d) bytes of device memory.
+ * Deterministic (fixed reduction order). */
+int64_t gj_chees_workspace_size(int32_t num_chains, int32_t dim);
+int32_t gj_chees_statistics(int32_t precision, int32_t num_chains, int32_t dim,
+                            const void* proposal_position, const void* proposal_velocity,
+                            const void* initial_position, const void* proposal_alpha2_tangent,
+                            const double* acceptance_rate, const uint8_t* is_divergent,
+                            void* workspace, double* out, void* stream);
 
 #ifdef __cplusplus
 }

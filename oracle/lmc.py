@@ -38,6 +38,7 @@ class LMCInfo:
     is_divergent: np.ndarray
     energy: np.ndarray
     num_integration_steps: int
+    proposal: object = None  # the flipped end state (position, velocity, ...)
 
 
 @dataclass
@@ -178,4 +179,4 @@ def kernel(target, state: LMCState, z, u, step_size, num_integration_steps, *,
         np.where(a, s.logdensity_grad, state.logdensity_grad),
         np.where(acc, s.volume_adjustment, state.volume_adjustment),
     )
-    return new, LMCInfo(v, p_acc, acc, div, H1, num_integration_steps)
+    return new, LMCInfo(v, p_acc, acc, div, H1, num_integration_steps, s)

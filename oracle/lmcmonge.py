@@ -59,6 +59,7 @@ class LMCInfo:
     is_divergent: np.ndarray
     energy: np.ndarray
     num_integration_steps: int
+    proposal: object = None  # the flipped end state (position, velocity, ...)
 
 
 def init(target, position):
@@ -200,4 +201,4 @@ def kernel(target, state: LMCState, z, u, step_size, inverse_mass_matrix, num_in
         np.where(a, grad_prop, state.logdensity_grad),
         np.where(acc, s.volume_adjustment, state.volume_adjustment),
     )
-    return new, LMCInfo(v, p_acc, acc, div, H1, num_integration_steps)
+    return new, LMCInfo(v, p_acc, acc, div, H1, num_integration_steps, s)

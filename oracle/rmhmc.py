@@ -212,6 +212,7 @@ class RMHMCInfo:
     num_integration_steps: int
     fixed_point_iters: np.ndarray
     fixed_point_success: np.ndarray
+    proposal: "IntegratorState" = None  # the flipped end state (rmhmc.py:425-437)
 
 
 def init(target, position):
@@ -257,5 +258,5 @@ def kernel(target, state, z, u, step_size, num_integration_steps, *,
         np.where(acc, s.logdensity, state.logdensity),
         np.where(a, s.logdensity_grad, state.logdensity_grad),
     )
-    info = RMHMCInfo(p, p_acc, acc, div, H1, num_integration_steps, fp_iters, fp_ok)
+    info = RMHMCInfo(p, p_acc, acc, div, H1, num_integration_steps, fp_iters, fp_ok, s)
     return new, info

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _header_symbols():
     text = open(os.path.join(ROOT, "include", "geomjax_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int32_t|const char\*)\s+(gj_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int32_t|int64_t|const char\*)\s+(gj_\w+)\s*\(", text, re.M)))
 
 
 def test_library_exports_every_header_symbol():
@@ -40,7 +40,7 @@ def test_struct_layouts_match_c(tmp_path):
             ctypes.sizeof(L.GjStepParams), ctypes.sizeof(L.GjChainState), ctypes.sizeof(L.GjInfo))
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
-        assert ours == (56, 24, 48, 64, 40, 56)
+        assert ours == (56, 24, 48, 64, 40, 72)
         return
     src = tmp_path / "off.c"
     src.write_text(
@@ -118,6 +118,16 @@ def test_argument_checks_without_gpu():
                                            None) == L.GJ_EINVAL
     assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 0, 2, 1, 1,
                                            None) == L.GJ_EINVAL
+    # ChEES statistics: workspace size and host checks
+    assert lib.gj_chees_workspace_size(4096, 25) == 8 * (2 * 25 + 5 * 4096)
+    assert lib.gj_chees_workspace_size(0, 25) == -1
+    assert lib.gj_chees_statistics(7, 4, 2, 1, 1, 1, None, 1, None, 1, 1, None) == L.GJ_EINVAL
+    assert lib.gj_chees_statistics(L.GJ_FP64, 0, 2, 1, 1, 1, None, 1, None, 1, 1,
+                                   None) == L.GJ_EINVAL
+    assert lib.gj_chees_statistics(L.GJ_FP64, 4, 2, None, 1, 1, None, 1, None, 1, 1,
+                                   None) == L.GJ_EINVAL
+    assert lib.gj_chees_statistics(L.GJ_FP64, 4, 2, 1, 1, 1, None, 1, None, None, 1,
+                                   None) == L.GJ_EINVAL
     assert lib.gj_gemm_split_bf16(3, 2, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
     assert lib.gj_gemm_split_bf16(1, 4, 1, 1, 1, None, None, None, None) == L.GJ_EINVAL
     assert lib.gj_destroy(h) == L.GJ_OK
