@@ -117,6 +117,9 @@ SIGNATURES = {
     "gj_logreg_gl_transition_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_void_p, c_void_p,
                                               c_double, c_double, c_int32, c_int32, c_int32,
                                               c_int32, c_void_p, c_void_p]),
+    "gj_lmcmonge_alpha2_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_int32,
+                                         POINTER(GjStepParams), c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p]),
     "gj_chees_workspace_size": (c_int64, [c_int32, c_int32]),
     "gj_chees_statistics": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

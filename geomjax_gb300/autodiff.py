@@ -156,3 +156,40 @@ def transition_jacobian(target, q0, z, step_size, metric_reg, num_integration_st
                                             int(num_integration_steps), int(kp), int(kq), 1,
                                             L.ptr(out), _stream()))
     return out
+
+
+def lmcmonge_alpha2_tangent(target: Target, positions, z, step_size: float,
+                            num_integration_steps: int, alpha2: float, inverse_mass_matrix=None,
+                            alpha2_fix: bool = False):
+    """Proposal position q_L of one LMC-Monge transition from ``positions``
+    with normals ``z``, and ∂q_L/∂α² (``gj_lmcmonge_alpha2_jvp``, forward
+    mode in float64 through the velocity draw and every half step).  The
+    reference takes it with ``jax.jacfwd`` of the proposal position
+    (``adaptation/chees_adaptation_lmcmonge.py:469-519``).  Returns two
+    [C, d] tensors in the target's dtype."""
+    q = _q(target, torch.as_tensor(positions))
+    zz = torch.as_tensor(z).to(device=target.device, dtype=target.dtype).contiguous()
+    if zz.shape != q.shape:
+        raise ValueError("z must have the positions' shape")
+    im = None
+    if inverse_mass_matrix is not None:
+        im = torch.as_tensor(inverse_mass_matrix).to(device=target.device,
+                                                     dtype=target.dtype).contiguous()
+    p = L.GjStepParams()
+    p.step_size = float(step_size)
+    p.num_integration_steps = int(num_integration_steps)
+    p.integrator = 0
+    p.max_iters = 0
+    p.tol = 0.0
+    p.divergence_threshold = 1000.0
+    p.alpha2 = float(alpha2)
+    p.inverse_mass = L.ptr(im)
+    p.alpha2_fix = int(bool(alpha2_fix))
+    p.reserved = 0
+    qL = torch.empty_like(q)
+    dq = torch.empty_like(q)
+    desc = target.descriptor()
+    L.check(L.lib().gj_lmcmonge_alpha2_jvp(ctypes.byref(desc), PRECISIONS[target.precision],
+                                           q.shape[0], ctypes.byref(p), L.ptr(q), L.ptr(zz),
+                                           L.ptr(qL), L.ptr(dq), _stream()))
+    return qL, dq

@@ -34,6 +34,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("traj_jvp.cu", []),
     ("chees.cu", []),
+    ("monge_jvp.cu", []),
 ]
 
 

@@ -25,10 +25,12 @@ sequence of ``:468-471`` is used.
 The reference's LMC-Monge variant cannot run as written: its dynamic kernel
 builds ``LMCState`` with an extra ``alpha2`` field and calls the base kernel
 without ``alpha2`` (``lmcmonge/lmc.py:281-287``).  ``lmcmonge_chees_adaptation``
-implements the evident intent (α² held in the adaptation state and passed to
-every transition) for the step size and trajectory length; the α² update
-(``update_alpha=True``, ``chees_adaptation_lmcmonge.py:219-256``) needs
-∂q_L/∂α² (``jax.jacfwd`` at ``:507``) and is rejected.
+implements the evident intent: the adaptation state's α² (the given
+``alpha2`` at first) is passed to every transition.  With ``update_alpha``
+the α² gradient of ``chees_adaptation_lmcmonge.py:219-256`` uses
+∂q_L/∂α² from ``gj_lmcmonge_alpha2_jvp`` (forward mode on the device, where
+the reference takes ``jax.jacfwd`` at ``:507``), and α² follows its own
+optimiser step and moving average.
 """
 from __future__ import annotations
 
@@ -41,7 +43,8 @@ import torch
 from . import _lib as L
 from .adaptation import DualAveragingState, dual_averaging_init, dual_averaging_update
 from .base import AdaptationAlgorithm, AdaptationResults, Draws, LMCState, RMHMCState
-from .samplers import lmc, lmcmonge, rmhmc
+from .autodiff import lmcmonge_alpha2_tangent
+from .samplers import Kernel, lmc, lmcmonge, rmhmc
 from .targets import PRECISIONS
 
 # optimal tuning for HMC (chees_adaptation_riemanian.py:21)
@@ -119,6 +122,7 @@ class ChEESAdaptationState(NamedTuple):
     step: int
     alpha2: float = 1.0
     log_alpha2_moving_average: float = 0.0
+    optim_state_alpha2: Any = None
 
 
 class ChEESStatistics(NamedTuple):
@@ -131,16 +135,18 @@ def chees_init(random_generator_arg: int, step_size: float, optim: GradientTrans
                alpha2: float = 1.0) -> ChEESAdaptationState:
     """``chees_adaptation_riemanian.py:221-231``: T starts at the step size."""
     return ChEESAdaptationState(step_size, 0.0, step_size, 0.0, dual_averaging_init(step_size),
-                                optim.init(step_size), random_generator_arg, 1, alpha2, 0.0)
+                                optim.init(step_size), random_generator_arg, 1, alpha2, 0.0,
+                                optim.init(1.0))
 
 
 def chees_update(s: ChEESAdaptationState, stats: ChEESStatistics, jitter: float,
                  optim: GradientTransformation, next_random_arg_fn: Callable,
                  target_acceptance_rate: float = OPTIMAL_TARGET_ACCEPTANCE_RATE,
-                 decay_rate: float = 0.5) -> ChEESAdaptationState:
-    """``compute_parameters`` (``chees_adaptation_riemanian.py:104-219``)
-    given the device statistics; ``jitter`` is the jitter of this step's
-    ``random_generator_arg``."""
+                 decay_rate: float = 0.5, update_alpha: bool = False) -> ChEESAdaptationState:
+    """``compute_parameters`` (``chees_adaptation_riemanian.py:104-219``,
+    with ``update_alpha`` the α² step of ``chees_adaptation_lmcmonge.py:
+    219-256``) given the device statistics; ``jitter`` is the jitter of this
+    step's ``random_generator_arg``."""
     da_ = dual_averaging_update(s.da_state, target_acceptance_rate - stats.harmonic_mean_acceptance)
     step_size_ = _exp(da_.log_step_size)
     if math.isfinite(step_size_):
@@ -159,10 +165,24 @@ def chees_update(s: ChEESAdaptationState, stats: ChEESStatistics, jitter: float,
     else:
         new_log_T, new_opt = log_T, s.optim_state
     new_log_T_ma = (1.0 - w) * s.log_trajectory_length_moving_average + w * new_log_T
+
+    alpha2, log_a2_ma, opt_a = s.alpha2, s.log_alpha2_moving_average, s.optim_state_alpha2
+    if update_alpha:
+        grad_a = jitter * s.trajectory_length * stats.alpha2_gradient
+        log_a2 = math.log(s.alpha2)
+        upd_a, opt_a_ = optim.update(grad_a, s.optim_state_alpha2, log_a2)
+        log_a2_ = log_a2 + upd_a
+        if math.isfinite(log_a2_):
+            new_log_a2 = log_a2_
+            opt_a = opt_a_
+        else:
+            new_log_a2 = log_a2
+        log_a2_ma = (1.0 - w) * s.log_alpha2_moving_average + w * new_log_a2
+        alpha2 = _exp(log_a2_ma)
     return ChEESAdaptationState(new_step_size, new_log_step_ma, _exp(new_log_T_ma),
                                 new_log_T_ma, new_da, new_opt,
                                 next_random_arg_fn(s.random_generator_arg), s.step + 1,
-                                s.alpha2, s.log_alpha2_moving_average)
+                                alpha2, log_a2_ma, opt_a)
 
 
 def chees_statistics(proposal_position: torch.Tensor, proposal_velocity: torch.Tensor,
@@ -302,7 +322,7 @@ class ChEESWarmupInfo(NamedTuple):
 # ---------------------------------------------------------------------------
 def _chees(target, num_chains, dynamics, *, jitter_generator, jitter_amount,
            target_acceptance_rate, decay_rate, inverse_mass_matrix=None, alpha2=1.0,
-           kernel_options=None):
+           update_alpha=False, kernel_options=None):
     dyn = _DYNAMIC[dynamics]
     kernel_options = dict(kernel_options or {})
 
@@ -337,24 +357,33 @@ def _chees(target, num_chains, dynamics, *, jitter_generator, jitter_amount,
         im = None
         if inverse_mass_matrix is not None:
             im = torch.as_tensor(inverse_mass_matrix).to(device=target.device, dtype=target.dtype)
-        extra = {"alpha2": s.alpha2, "inverse_mass_matrix": im} if dynamics == "lmcmonge" else {}
+        alpha2_fix = bool(kernel_options.get("alpha2_fix", False))
+        C, d = states.position.shape
         work = None
         history = []
         for i in range(num_steps):
             key = gen if draws is None else draws[i]
+            z, u = Kernel.draws(key, C, d, target)
             T_adj = s.trajectory_length / s.step_size
             n = integration_steps_fn(states.random_generator_arg, T_adj)
-            new_states, info = kernel(key, states, target, s.step_size,
+            extra = {}
+            if dynamics == "lmcmonge":
+                extra = {"alpha2": s.alpha2, "inverse_mass_matrix": im}
+            new_states, info = kernel(Draws(z, u), states, target, s.step_size,
                                       trajectory_length_adjusted=T_adj, **extra)
             if work is None:
-                nbytes = int(L.lib().gj_chees_workspace_size(*q.shape))
+                nbytes = int(L.lib().gj_chees_workspace_size(C, d))
                 work = torch.empty((nbytes + 7) // 8, dtype=torch.float64, device=target.device)
+            tangent = None
+            if update_alpha:  # ∂q_L/∂α² of the same transition (:469-519)
+                _, tangent = lmcmonge_alpha2_tangent(target, states.position, z, s.step_size, n,
+                                                     s.alpha2, im, alpha2_fix)
             stats = chees_statistics(info.proposal.position, info.proposal.velocity,
                                      states.position, info.acceptance_rate, info.is_divergent,
-                                     workspace=work)
+                                     alpha2_tangent=tangent, workspace=work)
             jit = jitter_gn(s.random_generator_arg)
             s = chees_update(s, stats, jit, optim, next_random_arg_fn, target_acceptance_rate,
-                             decay_rate)
+                             decay_rate, update_alpha)
             history.append(ChEESWarmupInfo(s, n, stats))
             states = new_states
         T_adj = _exp(s.log_trajectory_length_moving_average - s.log_step_size_moving_average)
@@ -395,12 +424,12 @@ def lmcmonge_chees_adaptation(target, inverse_mass_matrix, num_chains: int, *,
                               target_acceptance_rate: float = OPTIMAL_TARGET_ACCEPTANCE_RATE,
                               decay_rate: float = 0.5, update_alpha: bool = False,
                               alpha2: float = 0.001, **kernel_options) -> AdaptationAlgorithm:
-    """``chees_adaptation_lmcmonge.py:322-568`` with α² fixed at ``alpha2``
-    (see the module docstring for the reference's own α² handling)."""
-    if update_alpha:
-        raise NotImplementedError("the α² update needs ∂q_L/∂α² through the Monge trajectory "
-                                  "(chees_adaptation_lmcmonge.py:497-519), which is not built")
+    """``chees_adaptation_lmcmonge.py:322-568``: step size and trajectory
+    length, and with ``update_alpha`` α² as well, starting from ``alpha2``
+    (see the module docstring for the reference's own α² handling).  The
+    returned ``parameters["alpha2"]`` is the adaptation state's α²."""
     return _chees(target, num_chains, "lmcmonge", jitter_generator=jitter_generator,
                   jitter_amount=jitter_amount, target_acceptance_rate=target_acceptance_rate,
                   decay_rate=decay_rate, inverse_mass_matrix=inverse_mass_matrix,
-                  alpha2=float(alpha2), kernel_options=kernel_options)
+                  alpha2=float(alpha2), update_alpha=bool(update_alpha),
+                  kernel_options=kernel_options)

@@ -539,8 +539,38 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const do
 }
 
 // ---------------------------------------------------------------------------
-// ChEES cross-chain statistics
+// ChEES: the LMC-Monge proposal's derivative in α², cross-chain statistics
 // ---------------------------------------------------------------------------
+int32_t gj_lmcmonge_alpha2_jvp(const gj_target* target, int32_t precision, int32_t num_chains,
+                               const gj_step_params* p, const void* position, const void* z,
+                               void* proposal_position, void* proposal_alpha2_tangent,
+                               void* stream) {
+  int st = check_target(target, precision);
+  if (!st) st = check_params(p);
+  if (st) return st;
+  const gj::TargetDev t = gj::to_dev(*target);
+  if (!gj::monge_alpha2_jvp_supported(t))
+    return fail(GJ_ENOTSUP, "the α² derivative supports the funnel and the hierarchical Gaussian, d <= 256");
+  if (num_chains < 1 || !position || !z || !proposal_alpha2_tangent)
+    return fail(GJ_EINVAL, "bad arguments");
+  const gj::StepDev sp = gj::to_dev(*p);
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (precision == GJ_FP64)
+    e = gj::launch_monge_alpha2_jvp<double>(t, sp, static_cast<const double*>(position),
+                                            static_cast<const double*>(z),
+                                            static_cast<double*>(proposal_position),
+                                            static_cast<double*>(proposal_alpha2_tangent),
+                                            num_chains, cs);
+  else
+    e = gj::launch_monge_alpha2_jvp<float>(t, sp, static_cast<const float*>(position),
+                                           static_cast<const float*>(z),
+                                           static_cast<float*>(proposal_position),
+                                           static_cast<float*>(proposal_alpha2_tangent),
+                                           num_chains, cs);
+  return cuda_status(e, "gj_lmcmonge_alpha2_jvp");
+}
+
 int64_t gj_chees_workspace_size(int32_t num_chains, int32_t dim) {
   if (num_chains < 1 || dim < 1) return -1;
   return (int64_t)gj::chees_workspace_bytes(num_chains, dim);

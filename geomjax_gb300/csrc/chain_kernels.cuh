@@ -42,6 +42,13 @@ cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos,
                               const InfoDev<float>& info, int C, cudaStream_t st);
 bool monge_warp_supported(const TargetDev& t);
 
+// q_L and ∂q_L/∂α² of one LMC-Monge transition, forward mode in float64
+// (monge_jvp.cu); qL may be NULL
+bool monge_alpha2_jvp_supported(const TargetDev& t);
+template <typename T>
+cudaError_t launch_monge_alpha2_jvp(const TargetDev& t, const StepDev& sp, const T* pos,
+                                    const T* z, T* qL, T* dq, int C, cudaStream_t st);
+
 // ChEES cross-chain statistics (chees.cu): out[0] harmonic mean of the
 // acceptance probabilities, out[1] the trajectory-length gradient, out[2]
 // the α² gradient (0 without D); work holds chees_workspace_bytes(C, d)

@@ -31,6 +31,10 @@
  *                      jax.jacfwd through a trajectory with respect to the
  *                      step size and a metric parameter
  *                      (adaptation/chees_adaptation_lmcmonge.py:497-519)
+ *   gj_lmcmonge_alpha2_jvp
+ *                      jax.jacfwd of the LMC-Monge proposal position with
+ *                      respect to alpha2
+ *                      (adaptation/chees_adaptation_lmcmonge.py:469-519)
  *   gj_chees_statistics, gj_chees_workspace_size
  *                      the cross-chain reductions of ChEES adaptation
  *                      (adaptation/chees_adaptation_riemanian.py:145-190,
@@ -316,6 +320,22 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t num_chains,
                                     const double* z, double step_size, double metric_reg,
                                     int32_t num_integration_steps, int32_t kp, int32_t kq,
                                     int32_t tangents, double* out, void* stream);
+
+/* Proposal position q_L of one LMC-Monge transition and its derivative
+ * ∂q_L/∂α², by forward-mode propagation of d/dα² through the velocity draw,
+ * the normalising constant and every half_step_omega (float64 throughout,
+ * whatever the precision of the arrays).  Replaces
+ * jax.jacfwd(trajectory_proposal_position, argnums=0) of
+ * adaptation/chees_adaptation_lmcmonge.py:469-519.  params gives the step
+ * size, the number of steps, alpha2, the inverse mass (NULL = ones) and
+ * alpha2_fix as for gj_lmcmonge_step; position and z are the transition's
+ * start and normals, [C, d] in the precision's vector dtype, as are the
+ * outputs (proposal_position may be NULL).  Targets: GJ_FUNNEL and
+ * GJ_HIERGAUSS, d <= 256 (GJ_ENOTSUP otherwise). */
+int32_t gj_lmcmonge_alpha2_jvp(const gj_target* target, int32_t precision, int32_t num_chains,
+                               const gj_step_params* params, const void* position, const void* z,
+                               void* proposal_position, void* proposal_alpha2_tangent,
+                               void* stream);
 
 /* ChEES cross-chain statistics of one transition
  * (adaptation/chees_adaptation_riemanian.py:145-190 and

@@ -114,18 +114,25 @@ class ChEESState:
     optim_state: AdamState
     random_generator_arg: int
     step: int
+    alpha2: float = 1.0
+    log_alpha2_moving_average: float = 0.0
+    optim_state_alpha2: AdamState = None
 
 
-def init(random_generator_arg, step_size):
-    """chees_adaptation_riemanian.py:221-231."""
+def init(random_generator_arg, step_size, alpha2=1.0):
+    """chees_adaptation_riemanian.py:221-231 (+ chees_adaptation_lmcmonge.py:
+    272-284, whose optimiser state for α² starts from 1.0)."""
     return ChEESState(step_size, 0.0, step_size, 0.0, da_init(step_size), adam_init(step_size),
-                      random_generator_arg, 1)
+                      random_generator_arg, 1, alpha2, 0.0, adam_init(1.0))
 
 
 def compute_parameters(s, harmonic, grad_raw, jitter, learning_rate,
-                       target_acceptance_rate=OPTIMAL_TARGET_ACCEPTANCE_RATE, decay_rate=0.5):
+                       target_acceptance_rate=OPTIMAL_TARGET_ACCEPTANCE_RATE, decay_rate=0.5,
+                       grad_alpha_raw=None):
     """chees_adaptation_riemanian.py:104-219 given the statistics of
-    ``statistics``; ``jitter`` = jitter_generator(random_generator_arg)."""
+    ``statistics``; ``jitter`` = jitter_generator(random_generator_arg).
+    With ``grad_alpha_raw`` also the α² step of chees_adaptation_lmcmonge.py:
+    219-256 (its gradient before the jitter × trajectory-length factor)."""
     da_ = da_update(s.da_state, target_acceptance_rate - harmonic)
     step_size_ = math.exp(da_.log_x)
     if math.isfinite(step_size_):
@@ -143,8 +150,20 @@ def compute_parameters(s, harmonic, grad_raw, jitter, learning_rate,
     else:
         new_log_T, new_opt = log_T, s.optim_state
     new_log_T_ma = (1.0 - w) * s.log_trajectory_length_moving_average + w * new_log_T
+    alpha2, log_a2_ma, opt_a = s.alpha2, s.log_alpha2_moving_average, s.optim_state_alpha2
+    if grad_alpha_raw is not None:
+        log_a2 = math.log(s.alpha2)
+        upd_a, opt_a_ = adam_update(jitter * s.trajectory_length * grad_alpha_raw,
+                                    s.optim_state_alpha2, learning_rate)
+        if math.isfinite(log_a2 + upd_a):
+            new_log_a2, opt_a = log_a2 + upd_a, opt_a_
+        else:
+            new_log_a2 = log_a2
+        log_a2_ma = (1.0 - w) * s.log_alpha2_moving_average + w * new_log_a2
+        alpha2 = math.exp(log_a2_ma)
     return ChEESState(new_step_size, new_log_step_ma, math.exp(new_log_T_ma), new_log_T_ma,
-                      new_da, new_opt, s.random_generator_arg + 1, s.step + 1)
+                      new_da, new_opt, s.random_generator_arg + 1, s.step + 1, alpha2, log_a2_ma,
+                      opt_a)
 
 
 def run(transition, positions, step_size, learning_rate, num_steps, *, max_sampling_steps=1000,

@@ -118,6 +118,16 @@ def test_argument_checks_without_gpu():
                                            None) == L.GJ_EINVAL
     assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 0, 2, 1, 1,
                                            None) == L.GJ_EINVAL
+    # the α² derivative of the LMC-Monge proposal: host checks
+    pp = L.GjStepParams(0.02, 8, 0, 0, 0.0, 1000.0, 1.0, None, 0, 0)
+    assert lib.gj_lmcmonge_alpha2_jvp(None, 0, 4, ctypes.byref(pp), 1, 1, None, 1,
+                                      None) == L.GJ_EINVAL
+    tf = L.GjTarget(L.GJ_FUNNEL, L.GJ_METRIC_DIAG_FISHER, 3, 0, None, None, None, 3.0, 0.0)
+    assert lib.gj_lmcmonge_alpha2_jvp(ctypes.byref(tf), 0, 4, ctypes.byref(pp), None, 1, None, 1,
+                                      None) == L.GJ_EINVAL
+    tg = L.GjTarget(L.GJ_LOGREG, L.GJ_METRIC_DENSE_FISHER, 5, 10, 1, 1, None, 100.0, 0.0)
+    assert lib.gj_lmcmonge_alpha2_jvp(ctypes.byref(tg), 0, 4, ctypes.byref(pp), 1, 1, None, 1,
+                                      None) == L.GJ_ENOTSUP
     # ChEES statistics: workspace size and host checks
     assert lib.gj_chees_workspace_size(4096, 25) == 8 * (2 * 25 + 5 * 4096)
     assert lib.gj_chees_workspace_size(0, 25) == -1

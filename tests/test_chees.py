@@ -104,10 +104,32 @@ def test_oracle_statistics_by_hand():
     assert math.isnan(h) and math.isnan(g)
 
 
-def test_lmcmonge_update_alpha_is_rejected():
+def test_alpha2_update_sequence_matches_oracle():
+    """With update_alpha, α² follows its own Adam step on log α² and moving
+    average (chees_adaptation_lmcmonge.py:219-256), as the oracle's."""
+    from geomjax_gb300.chees import ChEESStatistics, adam, chees_init, chees_update
+
+    rng = np.random.default_rng(2)
+    opt = adam(0.05)
+    s = chees_init(0, 0.02, opt, alpha2=0.3)
+    o = OC.init(0, 0.02, alpha2=0.3)
+    for i in range(40):
+        h, g, ga = float(rng.uniform(0.3, 1.0)), float(rng.normal()), float(rng.normal() * 3)
+        jit = float(rng.uniform(0.1, 1.0))
+        s = chees_update(s, ChEESStatistics(h, g, ga), jit, opt, lambda a: a + 1,
+                         update_alpha=True)
+        o = OC.compute_parameters(o, h, g, jit, 0.05, grad_alpha_raw=ga)
+        assert s.alpha2 == pytest.approx(o.alpha2, rel=1e-12), i
+        assert s.step_size == pytest.approx(o.step_size, rel=1e-12)
+        assert s.trajectory_length == pytest.approx(o.trajectory_length, rel=1e-12)
+    # without update_alpha α² stays where it started
+    s = chees_update(chees_init(0, 0.02, opt, alpha2=0.3), ChEESStatistics(0.5, 1.0, 9.0), 0.5,
+                     opt, lambda a: a + 1)
+    assert s.alpha2 == 0.3
+
+
+def test_bad_dynamics_rejected():
     import geomjax_gb300 as gj
 
-    with pytest.raises(NotImplementedError):
-        gj.lmcmonge_chees_adaptation(None, None, 4, update_alpha=True)
     with pytest.raises(ValueError):
         gj.chees_adaptation(None, 4, dynamics="nuts")

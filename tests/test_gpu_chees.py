@@ -280,3 +280,58 @@ def test_lmcmonge_chees_run():
     assert math.isfinite(params["step_size"]) and params["step_size"] > 0
     assert all(x.num_integration_steps >= 1 for x in hist)
     assert np.isfinite(_np(state.position)).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind,kw,alpha2,fix", [
+    ("funnel", dict(D=7, metric="diag"), 0.5, False),
+    ("funnel", dict(D=100, metric="diag"), 1.0, False),
+    ("hier", dict(J=6), 0.3, True),
+], ids=str)
+def test_alpha2_tangent_matches_oracle_differences(kind, kw, alpha2, fix, precision):
+    """gj_lmcmonge_alpha2_jvp: q_L equals the oracle's proposal position and
+    ∂q_L/∂α² equals central differences of it in α² (relative step 1e-5),
+    normwise max|J − FD| / max|FD| < 1e-6 in FP64.  In the mixed precision
+    the arrays (and the hierarchical data) are float32: q_L to 1e-5 and the
+    tangent to 1e-4."""
+    from geomjax_gb300 import autodiff as AD
+
+    ot = oracle_target(kind, **kw)
+    dt = device_target(kind, precision, **kw)
+    C, h, L = 5, 0.02, 8
+    q0 = start_positions(ot.dim, C, seed=3, scale=0.5)
+    z, _ = normals(C, ot.dim, 4, np.float32 if precision == "mixed" else np.float64)
+    im = np.linspace(0.8, 1.2, ot.dim)
+    if precision == "mixed":
+        q0 = q0.astype(np.float32).astype(np.float64)
+        im = im.astype(np.float32).astype(np.float64)
+    qL, dq = AD.lmcmonge_alpha2_tangent(dt, q0, z, h, L, alpha2, im, fix)
+
+    def prop(a2):
+        _, oi = O_monge.kernel(ot, O_monge.init(ot, q0), z, -np.ones(C), h, im, L, alpha2=a2,
+                               alpha2_fix=fix)
+        return oi.proposal.position
+
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    assert rel_err(_np(qL), prop(alpha2)) < tol
+    e = 1e-5 * alpha2
+    fd = (prop(alpha2 + e) - prop(alpha2 - e)) / (2 * e)
+    err = np.max(np.abs(_np(dq) - fd)) / np.max(np.abs(fd))
+    assert err < (1e-6 if precision == "fp64" else 1e-4), err
+
+
+def test_lmcmonge_chees_run_updates_alpha2():
+    """update_alpha: α² moves from its start by its own optimiser steps on
+    the device tangent's statistic, and stays finite and positive."""
+    import geomjax_gb300 as gj
+
+    dt = device_target("funnel", "mixed", D=100, metric="diag")
+    C = 512
+    q0 = np.ones((C, 100))
+    warm = gj.lmcmonge_chees_adaptation(dt, np.ones(100), C, alpha2=0.5, update_alpha=True)
+    (state, params), hist = warm.run(0, q0, 0.02, gj.adam(0.05), 40)
+    a2 = [x.adaptation_state.alpha2 for x in hist]
+    assert all(math.isfinite(a) and a > 0 for a in a2)
+    assert abs(a2[-1] - 0.5) > 1e-3
+    assert params["alpha2"] == a2[-1]
+    assert all(math.isfinite(x.statistics.alpha2_gradient) for x in hist)
