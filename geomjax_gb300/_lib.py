@@ -83,6 +83,28 @@ class GjStepParams(ctypes.Structure):
     ]
 
 
+class GjNutsParams(ctypes.Structure):
+    _fields_ = [
+        ("step_size", c_double),
+        ("max_num_doublings", c_int32),
+        ("integrator", c_int32),
+        ("criterion", c_int32),
+        ("max_iters", c_int32),
+        ("tol", c_double),
+        ("divergence_threshold", c_double),
+    ]
+
+
+# GjNutsInfo's fields in order, as keys of the NUTS info dicts
+NUTS_INFO_FIELDS = ("acceptance_rate", "is_divergent", "is_turning", "energy",
+                    "num_trajectory_expansions", "num_integration_steps", "fp_iters", "status",
+                    "momentum", "leftmost_position", "rightmost_position")
+
+
+class GjNutsInfo(ctypes.Structure):
+    _fields_ = [(k, c_void_p) for k in NUTS_INFO_FIELDS]
+
+
 # every symbol the header declares, with its ctypes signature
 SIGNATURES = {
     "gj_version": (c_int32, []),
@@ -97,6 +119,8 @@ SIGNATURES = {
                                    c_void_p, c_void_p, POINTER(GjInfo), c_void_p]),
     "gj_lmc_step": (c_int32, [c_void_p, POINTER(GjStepParams), POINTER(GjChainState), c_void_p,
                               c_void_p, POINTER(GjInfo), c_void_p]),
+    "gj_rmhmc_nuts_step": (c_int32, [c_void_p, POINTER(GjNutsParams), POINTER(GjChainState),
+                                     c_void_p, c_void_p, c_int32, POINTER(GjNutsInfo), c_void_p]),
     "gj_stats": (c_int32, [c_void_p, POINTER(c_int64), c_int32]),
     "gj_profile": (c_int32, [c_void_p, c_int32]),
     "gj_gemm_split_bf16": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p,

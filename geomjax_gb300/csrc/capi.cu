@@ -354,6 +354,49 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
   return cuda_status(e, "gj_rmhmc_step");
 }
 
+int32_t gj_rmhmc_nuts_step(gj_ctx* ctx, const gj_nuts_params* p, gj_chain_state* s,
+                           const void* z, const double* uniforms, int32_t uniforms_per_chain,
+                           gj_nuts_info* info, void* stream) {
+  if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
+  if (ctx->sampler != GJ_SAMPLER_RMHMC) return fail(GJ_EINVAL, "context is not an RMHMC context");
+  if (!p) return fail(GJ_EINVAL, "params is NULL");
+  if (p->max_num_doublings < 1 || p->max_num_doublings > 16)
+    return fail(GJ_EINVAL, "max_num_doublings must be 1..16");
+  if (p->criterion < 0 || p->criterion > 2) return fail(GJ_EINVAL, "criterion must be 0, 1 or 2");
+  if (p->integrator != GJ_IMPLICIT_MIDPOINT && p->integrator != GJ_GENERALIZED_LEAPFROG)
+    return fail(GJ_EINVAL, "bad integrator");
+  if (!(p->step_size == p->step_size) || p->max_iters < 0)
+    return fail(GJ_EINVAL, "bad step size or iteration cap");
+  const int M = p->max_num_doublings;
+  if (uniforms_per_chain < 2 * M + (1 << M) - 1)
+    return fail(GJ_EINVAL, "uniforms_per_chain must be >= 2M + 2^M - 1");
+  int st = check_state(s, ctx->C, false);
+  if (st) return st;
+  if (!z || !uniforms) return fail(GJ_EINVAL, "z and uniforms must be device arrays");
+  const gj::TargetDev t = gj::to_dev(ctx->target);
+  if (t.d > 32) return fail(GJ_ENOTSUP, "NUTS supports d <= 32");
+  gj::StepDev sp{};
+  sp.h = p->step_size;
+  sp.L = 0;
+  sp.integrator = p->integrator;
+  sp.max_iters = p->max_iters;
+  sp.tol = p->tol;
+  sp.div_threshold = p->divergence_threshold;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (ctx->precision == GJ_FP64)
+    e = gj::launch_rmhmc_nuts<double>(t, sp, M, p->criterion, (double*)s->position,
+                                      (double*)s->logdensity_grad, s->logdensity, (const double*)z,
+                                      uniforms, uniforms_per_chain, gj::to_dev<double>(info),
+                                      ctx->C, ctx->tpb, cs);
+  else
+    e = gj::launch_rmhmc_nuts<float>(t, sp, M, p->criterion, (float*)s->position,
+                                     (float*)s->logdensity_grad, s->logdensity, (const float*)z,
+                                     uniforms, uniforms_per_chain, gj::to_dev<float>(info), ctx->C,
+                                     ctx->tpb, cs);
+  return cuda_status(e, "gj_rmhmc_nuts_step");
+}
+
 int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, const void* z,
                     const double* u, gj_info* info, void* stream) {
   if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");

@@ -290,6 +290,231 @@ __global__ void __launch_bounds__(128) rmhmc_chain_kernel(TargetDev t, StepDev s
                      (isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
 }
 
+
+// ---------------------------------------------------------------------------
+// iterative NUTS with the Riemannian metric (rmhmc/nuts.py), thread per chain
+// ---------------------------------------------------------------------------
+// One chain's trajectory: the extreme states are integrated in place (the
+// subtrajectory of expansion k starts at the extreme on its side and that
+// extreme becomes its last state, which is where the merged trajectory of
+// mcmc/trajectory.py:635-640 ends), the momentum / velocity sums, the
+// sampled proposal and the numpyro-style U-turn checkpoints
+// (mcmc/termination.py:30-119).  Uniforms: u[k] the direction of expansion k,
+// u[M + k] its biased merge, u[2M + 2^k − 1 + j] step j of expansion k.
+constexpr int kNutsMaxDoublings = 16;
+
+__device__ __forceinline__ double logaddexp(double a, double b) {
+  if (a == -INFINITY) return b;
+  if (b == -INFINITY) return a;
+  const double m = fmax(a, b);
+  return m + log1p(exp(-fabs(a - b)));
+}
+__device__ __forceinline__ double expit(double x) {
+  if (x >= 0.0) return 1.0 / (1.0 + exp(-x));
+  const double e = exp(x);
+  return e / (1.0 + e);  // NaN stays NaN
+}
+
+// the generalized U-turn of rmhmc/metrics.py:76-118 (criterion 0 "euc",
+// 1 "bet", 2 "riem")
+template <int DMAX>
+__device__ bool nuts_turning(int d, int crit, const double* m_l, const double* m_r,
+                             const double* m_sum, const double* v_l, const double* v_r,
+                             const double* v_sum) {
+  const double* rho = crit == 1 ? m_sum : v_sum;
+  const double* a = crit == 2 ? m_l : v_l;
+  const double* b = crit == 2 ? m_r : v_r;
+  double sa = 0.0, sb = 0.0;
+  for (int i = 0; i < d; ++i) {
+    sa += a[i] * rho[i];
+    sb += b[i] * rho[i];
+  }
+  return sa <= 0.0 || sb <= 0.0;
+}
+
+template <typename T, int DMAX>
+struct NutsEnd {  // an extreme state: q, p, ∇ℓ, ℓ and v = G⁻¹p in float64
+  T q[DMAX], p[DMAX], g[DMAX];
+  double pd[DMAX], v[DMAX];
+  double ld;
+};
+
+template <typename T, int DMAX>
+__global__ void __launch_bounds__(128) rmhmc_nuts_kernel(TargetDev t, StepDev sp, int M, int crit,
+                                                         T* pos, T* grad, double* logdens,
+                                                         const T* z, const double* uni, int U,
+                                                         NutsInfoDev<T> info, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const int d = t.d;
+  const double* u = uni + (size_t)c * U;
+  bool bad = false, all_conv = true;
+  int iters = 0;
+  MetricEval<DMAX> Mv;
+  NutsEnd<T, DMAX> Lf, Rt;
+  for (int i = 0; i < d; ++i) {
+    Lf.q[i] = pos[(size_t)c * d + i];
+    Lf.g[i] = grad[(size_t)c * d + i];
+  }
+  Lf.ld = logdens[c];
+  // momentum p = chol(G)·z and v = G⁻¹p (rmhmc/nuts.py:144-146)
+  eval_metric<T, DMAX>(t, Lf.q, Mv, false, &bad);
+  for (int i = 0; i < d; ++i) {
+    if (Mv.diag) {
+      Lf.p[i] = T(sqrt(Mv.L[i]) * double(z[(size_t)c * d + i]));
+    } else {
+      double s = 0.0;
+      for (int k = 0; k <= i; ++k) s += Mv.L[i * d + k] * double(z[(size_t)c * d + k]);
+      Lf.p[i] = T(s);
+    }
+    Lf.pd[i] = double(Lf.p[i]);
+    if (info.momentum) info.momentum[(size_t)c * d + i] = Lf.p[i];
+  }
+  metric_solve<T, DMAX>(Mv, d, Lf.p, Lf.v);
+  const double H0 = -Lf.ld + kinetic_rm<T, DMAX>(Mv, d, Lf.p);
+  Rt = Lf;
+  // the sampled proposal (mcmc/proposal.py:23-38)
+  T prop_q[DMAX], prop_g[DMAX];
+  double prop_ld = Lf.ld, prop_E = H0, prop_w = 0.0, prop_sl = -INFINITY;
+  for (int i = 0; i < d; ++i) {
+    prop_q[i] = Lf.q[i];
+    prop_g[i] = Lf.g[i];
+  }
+  double psum[DMAX], vsum[DMAX];
+  for (int i = 0; i < d; ++i) {
+    psum[i] = Lf.pd[i];
+    vsum[i] = Lf.v[i];
+  }
+  int n_states = 0;
+  double ck_r[kNutsMaxDoublings][DMAX], ck_rs[kNutsMaxDoublings][DMAX];
+  double ck_v[kNutsMaxDoublings][DMAX], ck_vs[kNutsMaxDoublings][DMAX];
+  for (int k = 0; k < M; ++k)
+    for (int i = 0; i < d; ++i) ck_r[k][i] = ck_rs[k][i] = ck_v[k][i] = ck_vs[k][i] = 0.0;
+  int idx_min = 0, idx_max = 0;
+  int step = 0;
+  bool div = false, turning = false;
+  while (step < M && !div && !turning) {  // dynamic_multiplicative_expansion
+    const int dir = u[step] < 0.5 ? 1 : -1;
+    NutsEnd<T, DMAX>& E = dir > 0 ? Rt : Lf;
+    StepDev sd = sp;
+    sd.h = dir * sp.h;
+    const int base = 2 * M + (1 << step) - 1;
+    double spsum[DMAX], svsum[DMAX];
+    T sq[DMAX], sg[DMAX];
+    double s_ld = 0.0, s_E = 0.0, s_w = 0.0, s_sl = 0.0;
+    int s_n = 0;
+    bool sdiv = false, sterm = false;
+    for (int j = 0; j < (1 << step) && !sterm && !sdiv; ++j) {  // dynamic_progressive_integration
+      bool conv = true;
+      if (sp.integrator == GJ_GENERALIZED_LEAPFROG)
+        iters += gl_step<T, DMAX>(t, sd, E.q, E.p, E.g, &E.ld, Mv, &conv, &bad);
+      else
+        iters += im_step<T, DMAX>(t, sd, E.q, E.p, E.g, &E.ld, Mv, &conv, &bad);
+      all_conv &= conv;
+      eval_metric<T, DMAX>(t, E.q, Mv, false, &bad);
+      const double H1 = -E.ld + kinetic_rm<T, DMAX>(Mv, d, E.p);
+      metric_solve<T, DMAX>(Mv, d, E.p, E.v);
+      for (int i = 0; i < d; ++i) E.pd[i] = double(E.p[i]);
+      double w = H0 - H1;  // proposal_from_energy_diff (mcmc/proposal.py:87-121)
+      if (isnan(w)) w = -INFINITY;
+      const double sl = fmin(w, 0.0);
+      sdiv = -w > sp.div_threshold;
+      bool take;
+      if (j == 0) {
+        for (int i = 0; i < d; ++i) {
+          spsum[i] = E.pd[i];
+          svsum[i] = E.v[i];
+        }
+        s_n = 1;
+        take = true;
+        s_w = w;
+        s_sl = sl;
+      } else {  // progressive_uniform_sampling (mcmc/proposal.py:186-212)
+        for (int i = 0; i < d; ++i) {
+          spsum[i] += E.pd[i];
+          svsum[i] += E.v[i];
+        }
+        ++s_n;
+        take = u[base + j] < expit(w - s_w);
+        s_w = logaddexp(s_w, w);
+        s_sl = logaddexp(s_sl, sl);
+      }
+      if (take) {
+        for (int i = 0; i < d; ++i) {
+          sq[i] = E.q[i];
+          sg[i] = E.g[i];
+        }
+        s_ld = E.ld;
+        s_E = H1;
+      }
+      // iterative U-turn: checkpoint update and check (termination.py:48-119)
+      int hi = __popc((unsigned)j >> 1);
+      const int lo = hi - (__ffs(~(unsigned)j) - 1) + 1;
+      if (j % 2 == 0)
+        for (int i = 0; i < d; ++i) {
+          ck_r[hi][i] = E.pd[i];
+          ck_rs[hi][i] = spsum[i];
+          ck_v[hi][i] = E.v[i];
+          ck_vs[hi][i] = svsum[i];
+        }
+      idx_min = lo;
+      idx_max = hi;
+      for (int k = idx_max; k >= idx_min && !sterm; --k) {
+        double srs[DMAX], svs[DMAX];
+        for (int i = 0; i < d; ++i) {
+          srs[i] = spsum[i] - ck_rs[k][i] + ck_r[k][i];
+          svs[i] = svsum[i] - ck_vs[k][i] + ck_v[k][i];
+        }
+        sterm = nuts_turning<DMAX>(d, crit, ck_r[k], E.pd, srs, ck_v[k], E.v, svs);
+      }
+    }
+    // the expansion's proposal (mcmc/trajectory.py:609-632)
+    if (sdiv || sterm) {
+      prop_sl = logaddexp(prop_sl, s_sl);
+    } else {  // progressive_biased_sampling (mcmc/proposal.py:215-245)
+      const double pa = fmin(exp(s_w - prop_w), 1.0);
+      const bool take = u[M + step] < pa;
+      prop_w = logaddexp(prop_w, s_w);
+      prop_sl = logaddexp(prop_sl, s_sl);
+      if (take) {
+        for (int i = 0; i < d; ++i) {
+          prop_q[i] = sq[i];
+          prop_g[i] = sg[i];
+        }
+        prop_ld = s_ld;
+        prop_E = s_E;
+      }
+    }
+    // merge and the whole trajectory's U-turn (trajectory.py:634-650)
+    for (int i = 0; i < d; ++i) {
+      psum[i] += spsum[i];
+      vsum[i] += svsum[i];
+    }
+    n_states += s_n;
+    const bool whole = nuts_turning<DMAX>(d, crit, Lf.pd, Rt.pd, psum, Lf.v, Rt.v, vsum);
+    div = sdiv;
+    turning = sterm || whole;
+    ++step;
+  }
+  for (int i = 0; i < d; ++i) {
+    pos[(size_t)c * d + i] = prop_q[i];
+    grad[(size_t)c * d + i] = prop_g[i];
+    if (info.left_q) info.left_q[(size_t)c * d + i] = Lf.q[i];
+    if (info.right_q) info.right_q[(size_t)c * d + i] = Rt.q[i];
+  }
+  logdens[c] = prop_ld;
+  if (info.acc_rate) info.acc_rate[c] = exp(prop_sl) / n_states;
+  if (info.divergent) info.divergent[c] = div;
+  if (info.turning) info.turning[c] = turning;
+  if (info.energy) info.energy[c] = prop_E;
+  if (info.doublings) info.doublings[c] = step;
+  if (info.steps) info.steps[c] = n_states;
+  if (info.fp_iters) info.fp_iters[c] = iters;
+  if (info.status)
+    info.status[c] = (all_conv ? 0u : GJ_CHAIN_FP_NOT_CONVERGED) |
+                     (isfinite(prop_E) ? 0u : GJ_CHAIN_NONFINITE) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
+}
+
 // ---------------------------------------------------------------------------
 // dense-metric LMC (lmcmc/*)
 // ---------------------------------------------------------------------------
@@ -715,6 +940,16 @@ cudaError_t launch_rmhmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T*
 }
 
 template <typename T>
+cudaError_t launch_rmhmc_nuts(const TargetDev& t, const StepDev& sp, int max_doublings, int criterion,
+                              T* pos, T* grad, double* ld, const T* z, const double* u, int U,
+                              const NutsInfoDev<T>& info, int C, int tpb, cudaStream_t st) {
+  if (max_doublings < 0 || max_doublings > kNutsMaxDoublings) return cudaErrorInvalidValue;
+  GJ_DISPATCH_DMAX(t.d, 32, rmhmc_nuts_kernel<T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+                                t, sp, max_doublings, criterion, pos, grad, ld, z, u, U, info, C));
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_lmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
                              double* vol, const T* z, const double* u, const InfoDev<T>& info,
                              int C, int tpb, cudaStream_t st) {
@@ -763,6 +998,9 @@ cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out
   template cudaError_t launch_rmhmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,  \
                                              const T*, const double*, const InfoDev<T>&, int,   \
                                              int, cudaStream_t);                                 \
+  template cudaError_t launch_rmhmc_nuts<T>(const TargetDev&, const StepDev&, int, int, T*, T*,  \
+                                            double*, const T*, const double*, int,              \
+                                            const NutsInfoDev<T>&, int, int, cudaStream_t);     \
   template cudaError_t launch_lmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,    \
                                            double*, const T*, const double*, const InfoDev<T>&, \
                                            int, int, cudaStream_t);                              \

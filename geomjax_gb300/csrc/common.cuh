@@ -78,6 +78,41 @@ struct InfoDev {
   T* prop_v;  // proposal velocity (flipped) [C, d]
 };
 
+// Output pointers of one NUTS transition
+template <typename T>
+struct NutsInfoDev {
+  double* acc_rate;
+  uint8_t* divergent;
+  uint8_t* turning;
+  double* energy;
+  int32_t* doublings;
+  int32_t* steps;
+  int32_t* fp_iters;
+  uint8_t* status;
+  T* momentum;
+  T* left_q;
+  T* right_q;
+};
+
+template <typename T>
+inline NutsInfoDev<T> to_dev(const gj_nuts_info* i) {
+  NutsInfoDev<T> r{};
+  if (i) {
+    r.acc_rate = i->acceptance_rate;
+    r.divergent = i->is_divergent;
+    r.turning = i->is_turning;
+    r.energy = i->energy;
+    r.doublings = i->num_trajectory_expansions;
+    r.steps = i->num_integration_steps;
+    r.fp_iters = i->fp_iters;
+    r.status = i->status;
+    r.momentum = static_cast<T*>(i->momentum);
+    r.left_q = static_cast<T*>(i->leftmost_position);
+    r.right_q = static_cast<T*>(i->rightmost_position);
+  }
+  return r;
+}
+
 template <typename T>
 inline InfoDev<T> to_dev(const gj_info* i) {
   InfoDev<T> r{};
