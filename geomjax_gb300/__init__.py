@@ -22,7 +22,7 @@ from .diagnostics import effective_sample_size, ess, potential_scale_reduction, 
 from .samplers import Kernel, lmc, lmcmonge, rmhmc
 from .targets import funnel, hierarchical_gaussian, logistic_regression
 from .adaptation import gradient_step_size_adaptation, step_size_adaptation, window_adaptation
-from .nuts import NUTSDraws, nutsrmhmc
+from .nuts import NUTSDraws, nutslmc, nutslmcmonge, nutsrmhmc
 from .chees import (adam, chees_adaptation, dynamic_lmc, dynamic_lmcmonge, dynamic_rmhmc,
                     lmcmonge_chees_adaptation)
 
@@ -32,5 +32,6 @@ __all__ = [
     "logistic_regression", "hierarchical_gaussian", "effective_sample_size", "ess",
     "potential_scale_reduction", "rhat", "window_adaptation", "step_size_adaptation",
     "gradient_step_size_adaptation", "chees_adaptation", "lmcmonge_chees_adaptation",
-    "dynamic_rmhmc", "dynamic_lmc", "dynamic_lmcmonge", "adam", "nutsrmhmc", "NUTSDraws",
+    "dynamic_rmhmc", "dynamic_lmc", "dynamic_lmcmonge", "adam", "nutsrmhmc", "nutslmc", "nutslmcmonge",
+    "NUTSDraws",
 ]

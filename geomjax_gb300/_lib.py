@@ -92,6 +92,10 @@ class GjNutsParams(ctypes.Structure):
         ("max_iters", c_int32),
         ("tol", c_double),
         ("divergence_threshold", c_double),
+        ("alpha2", c_double),
+        ("inverse_mass", c_void_p),
+        ("alpha2_fix", c_int32),
+        ("reserved", c_int32),
     ]
 
 
@@ -119,7 +123,7 @@ SIGNATURES = {
                                    c_void_p, c_void_p, POINTER(GjInfo), c_void_p]),
     "gj_lmc_step": (c_int32, [c_void_p, POINTER(GjStepParams), POINTER(GjChainState), c_void_p,
                               c_void_p, POINTER(GjInfo), c_void_p]),
-    "gj_rmhmc_nuts_step": (c_int32, [c_void_p, POINTER(GjNutsParams), POINTER(GjChainState),
+    "gj_nuts_step": (c_int32, [c_void_p, POINTER(GjNutsParams), POINTER(GjChainState),
                                      c_void_p, c_void_p, c_int32, POINTER(GjNutsInfo), c_void_p]),
     "gj_stats": (c_int32, [c_void_p, POINTER(c_int64), c_int32]),
     "gj_profile": (c_int32, [c_void_p, c_int32]),

@@ -354,11 +354,10 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
   return cuda_status(e, "gj_rmhmc_step");
 }
 
-int32_t gj_rmhmc_nuts_step(gj_ctx* ctx, const gj_nuts_params* p, gj_chain_state* s,
-                           const void* z, const double* uniforms, int32_t uniforms_per_chain,
-                           gj_nuts_info* info, void* stream) {
+int32_t gj_nuts_step(gj_ctx* ctx, const gj_nuts_params* p, gj_chain_state* s, const void* z,
+                     const double* uniforms, int32_t uniforms_per_chain, gj_nuts_info* info,
+                     void* stream) {
   if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
-  if (ctx->sampler != GJ_SAMPLER_RMHMC) return fail(GJ_EINVAL, "context is not an RMHMC context");
   if (!p) return fail(GJ_EINVAL, "params is NULL");
   if (p->max_num_doublings < 1 || p->max_num_doublings > 16)
     return fail(GJ_EINVAL, "max_num_doublings must be 1..16");
@@ -370,7 +369,8 @@ int32_t gj_rmhmc_nuts_step(gj_ctx* ctx, const gj_nuts_params* p, gj_chain_state*
   const int M = p->max_num_doublings;
   if (uniforms_per_chain < 2 * M + (1 << M) - 1)
     return fail(GJ_EINVAL, "uniforms_per_chain must be >= 2M + 2^M - 1");
-  int st = check_state(s, ctx->C, false);
+  const bool lmc_like = ctx->sampler != GJ_SAMPLER_RMHMC;
+  int st = check_state(s, ctx->C, lmc_like);
   if (st) return st;
   if (!z || !uniforms) return fail(GJ_EINVAL, "z and uniforms must be device arrays");
   const gj::TargetDev t = gj::to_dev(ctx->target);
@@ -382,19 +382,22 @@ int32_t gj_rmhmc_nuts_step(gj_ctx* ctx, const gj_nuts_params* p, gj_chain_state*
   sp.max_iters = p->max_iters;
   sp.tol = p->tol;
   sp.div_threshold = p->divergence_threshold;
+  sp.alpha2 = p->alpha2;
+  sp.inv_mass = p->inverse_mass;
+  sp.alpha2_fix = p->alpha2_fix;
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   cudaError_t e;
   if (ctx->precision == GJ_FP64)
-    e = gj::launch_rmhmc_nuts<double>(t, sp, M, p->criterion, (double*)s->position,
-                                      (double*)s->logdensity_grad, s->logdensity, (const double*)z,
-                                      uniforms, uniforms_per_chain, gj::to_dev<double>(info),
-                                      ctx->C, ctx->tpb, cs);
+    e = gj::launch_nuts<double>(ctx->sampler, t, sp, M, p->criterion, (double*)s->position,
+                                (double*)s->logdensity_grad, s->logdensity, s->volume_adjustment,
+                                (const double*)z, uniforms, uniforms_per_chain,
+                                gj::to_dev<double>(info), ctx->C, ctx->tpb, cs);
   else
-    e = gj::launch_rmhmc_nuts<float>(t, sp, M, p->criterion, (float*)s->position,
-                                     (float*)s->logdensity_grad, s->logdensity, (const float*)z,
-                                     uniforms, uniforms_per_chain, gj::to_dev<float>(info), ctx->C,
-                                     ctx->tpb, cs);
-  return cuda_status(e, "gj_rmhmc_nuts_step");
+    e = gj::launch_nuts<float>(ctx->sampler, t, sp, M, p->criterion, (float*)s->position,
+                               (float*)s->logdensity_grad, s->logdensity, s->volume_adjustment,
+                               (const float*)z, uniforms, uniforms_per_chain,
+                               gj::to_dev<float>(info), ctx->C, ctx->tpb, cs);
+  return cuda_status(e, "gj_nuts_step");
 }
 
 int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, const void* z,

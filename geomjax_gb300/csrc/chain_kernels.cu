@@ -332,189 +332,6 @@ __device__ bool nuts_turning(int d, int crit, const double* m_l, const double* m
   return sa <= 0.0 || sb <= 0.0;
 }
 
-template <typename T, int DMAX>
-struct NutsEnd {  // an extreme state: q, p, ∇ℓ, ℓ and v = G⁻¹p in float64
-  T q[DMAX], p[DMAX], g[DMAX];
-  double pd[DMAX], v[DMAX];
-  double ld;
-};
-
-template <typename T, int DMAX>
-__global__ void __launch_bounds__(128) rmhmc_nuts_kernel(TargetDev t, StepDev sp, int M, int crit,
-                                                         T* pos, T* grad, double* logdens,
-                                                         const T* z, const double* uni, int U,
-                                                         NutsInfoDev<T> info, int C) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= C) return;
-  const int d = t.d;
-  const double* u = uni + (size_t)c * U;
-  bool bad = false, all_conv = true;
-  int iters = 0;
-  MetricEval<DMAX> Mv;
-  NutsEnd<T, DMAX> Lf, Rt;
-  for (int i = 0; i < d; ++i) {
-    Lf.q[i] = pos[(size_t)c * d + i];
-    Lf.g[i] = grad[(size_t)c * d + i];
-  }
-  Lf.ld = logdens[c];
-  // momentum p = chol(G)·z and v = G⁻¹p (rmhmc/nuts.py:144-146)
-  eval_metric<T, DMAX>(t, Lf.q, Mv, false, &bad);
-  for (int i = 0; i < d; ++i) {
-    if (Mv.diag) {
-      Lf.p[i] = T(sqrt(Mv.L[i]) * double(z[(size_t)c * d + i]));
-    } else {
-      double s = 0.0;
-      for (int k = 0; k <= i; ++k) s += Mv.L[i * d + k] * double(z[(size_t)c * d + k]);
-      Lf.p[i] = T(s);
-    }
-    Lf.pd[i] = double(Lf.p[i]);
-    if (info.momentum) info.momentum[(size_t)c * d + i] = Lf.p[i];
-  }
-  metric_solve<T, DMAX>(Mv, d, Lf.p, Lf.v);
-  const double H0 = -Lf.ld + kinetic_rm<T, DMAX>(Mv, d, Lf.p);
-  Rt = Lf;
-  // the sampled proposal (mcmc/proposal.py:23-38)
-  T prop_q[DMAX], prop_g[DMAX];
-  double prop_ld = Lf.ld, prop_E = H0, prop_w = 0.0, prop_sl = -INFINITY;
-  for (int i = 0; i < d; ++i) {
-    prop_q[i] = Lf.q[i];
-    prop_g[i] = Lf.g[i];
-  }
-  double psum[DMAX], vsum[DMAX];
-  for (int i = 0; i < d; ++i) {
-    psum[i] = Lf.pd[i];
-    vsum[i] = Lf.v[i];
-  }
-  int n_states = 0;
-  double ck_r[kNutsMaxDoublings][DMAX], ck_rs[kNutsMaxDoublings][DMAX];
-  double ck_v[kNutsMaxDoublings][DMAX], ck_vs[kNutsMaxDoublings][DMAX];
-  for (int k = 0; k < M; ++k)
-    for (int i = 0; i < d; ++i) ck_r[k][i] = ck_rs[k][i] = ck_v[k][i] = ck_vs[k][i] = 0.0;
-  int idx_min = 0, idx_max = 0;
-  int step = 0;
-  bool div = false, turning = false;
-  while (step < M && !div && !turning) {  // dynamic_multiplicative_expansion
-    const int dir = u[step] < 0.5 ? 1 : -1;
-    NutsEnd<T, DMAX>& E = dir > 0 ? Rt : Lf;
-    StepDev sd = sp;
-    sd.h = dir * sp.h;
-    const int base = 2 * M + (1 << step) - 1;
-    double spsum[DMAX], svsum[DMAX];
-    T sq[DMAX], sg[DMAX];
-    double s_ld = 0.0, s_E = 0.0, s_w = 0.0, s_sl = 0.0;
-    int s_n = 0;
-    bool sdiv = false, sterm = false;
-    for (int j = 0; j < (1 << step) && !sterm && !sdiv; ++j) {  // dynamic_progressive_integration
-      bool conv = true;
-      if (sp.integrator == GJ_GENERALIZED_LEAPFROG)
-        iters += gl_step<T, DMAX>(t, sd, E.q, E.p, E.g, &E.ld, Mv, &conv, &bad);
-      else
-        iters += im_step<T, DMAX>(t, sd, E.q, E.p, E.g, &E.ld, Mv, &conv, &bad);
-      all_conv &= conv;
-      eval_metric<T, DMAX>(t, E.q, Mv, false, &bad);
-      const double H1 = -E.ld + kinetic_rm<T, DMAX>(Mv, d, E.p);
-      metric_solve<T, DMAX>(Mv, d, E.p, E.v);
-      for (int i = 0; i < d; ++i) E.pd[i] = double(E.p[i]);
-      double w = H0 - H1;  // proposal_from_energy_diff (mcmc/proposal.py:87-121)
-      if (isnan(w)) w = -INFINITY;
-      const double sl = fmin(w, 0.0);
-      sdiv = -w > sp.div_threshold;
-      bool take;
-      if (j == 0) {
-        for (int i = 0; i < d; ++i) {
-          spsum[i] = E.pd[i];
-          svsum[i] = E.v[i];
-        }
-        s_n = 1;
-        take = true;
-        s_w = w;
-        s_sl = sl;
-      } else {  // progressive_uniform_sampling (mcmc/proposal.py:186-212)
-        for (int i = 0; i < d; ++i) {
-          spsum[i] += E.pd[i];
-          svsum[i] += E.v[i];
-        }
-        ++s_n;
-        take = u[base + j] < expit(w - s_w);
-        s_w = logaddexp(s_w, w);
-        s_sl = logaddexp(s_sl, sl);
-      }
-      if (take) {
-        for (int i = 0; i < d; ++i) {
-          sq[i] = E.q[i];
-          sg[i] = E.g[i];
-        }
-        s_ld = E.ld;
-        s_E = H1;
-      }
-      // iterative U-turn: checkpoint update and check (termination.py:48-119)
-      int hi = __popc((unsigned)j >> 1);
-      const int lo = hi - (__ffs(~(unsigned)j) - 1) + 1;
-      if (j % 2 == 0)
-        for (int i = 0; i < d; ++i) {
-          ck_r[hi][i] = E.pd[i];
-          ck_rs[hi][i] = spsum[i];
-          ck_v[hi][i] = E.v[i];
-          ck_vs[hi][i] = svsum[i];
-        }
-      idx_min = lo;
-      idx_max = hi;
-      for (int k = idx_max; k >= idx_min && !sterm; --k) {
-        double srs[DMAX], svs[DMAX];
-        for (int i = 0; i < d; ++i) {
-          srs[i] = spsum[i] - ck_rs[k][i] + ck_r[k][i];
-          svs[i] = svsum[i] - ck_vs[k][i] + ck_v[k][i];
-        }
-        sterm = nuts_turning<DMAX>(d, crit, ck_r[k], E.pd, srs, ck_v[k], E.v, svs);
-      }
-    }
-    // the expansion's proposal (mcmc/trajectory.py:609-632)
-    if (sdiv || sterm) {
-      prop_sl = logaddexp(prop_sl, s_sl);
-    } else {  // progressive_biased_sampling (mcmc/proposal.py:215-245)
-      const double pa = fmin(exp(s_w - prop_w), 1.0);
-      const bool take = u[M + step] < pa;
-      prop_w = logaddexp(prop_w, s_w);
-      prop_sl = logaddexp(prop_sl, s_sl);
-      if (take) {
-        for (int i = 0; i < d; ++i) {
-          prop_q[i] = sq[i];
-          prop_g[i] = sg[i];
-        }
-        prop_ld = s_ld;
-        prop_E = s_E;
-      }
-    }
-    // merge and the whole trajectory's U-turn (trajectory.py:634-650)
-    for (int i = 0; i < d; ++i) {
-      psum[i] += spsum[i];
-      vsum[i] += svsum[i];
-    }
-    n_states += s_n;
-    const bool whole = nuts_turning<DMAX>(d, crit, Lf.pd, Rt.pd, psum, Lf.v, Rt.v, vsum);
-    div = sdiv;
-    turning = sterm || whole;
-    ++step;
-  }
-  for (int i = 0; i < d; ++i) {
-    pos[(size_t)c * d + i] = prop_q[i];
-    grad[(size_t)c * d + i] = prop_g[i];
-    if (info.left_q) info.left_q[(size_t)c * d + i] = Lf.q[i];
-    if (info.right_q) info.right_q[(size_t)c * d + i] = Rt.q[i];
-  }
-  logdens[c] = prop_ld;
-  if (info.acc_rate) info.acc_rate[c] = exp(prop_sl) / n_states;
-  if (info.divergent) info.divergent[c] = div;
-  if (info.turning) info.turning[c] = turning;
-  if (info.energy) info.energy[c] = prop_E;
-  if (info.doublings) info.doublings[c] = step;
-  if (info.steps) info.steps[c] = n_states;
-  if (info.fp_iters) info.fp_iters[c] = iters;
-  if (info.status)
-    info.status[c] = (all_conv ? 0u : GJ_CHAIN_FP_NOT_CONVERGED) |
-                     (isfinite(prop_E) ? 0u : GJ_CHAIN_NONFINITE) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
-}
-
 // ---------------------------------------------------------------------------
 // dense-metric LMC (lmcmc/*)
 // ---------------------------------------------------------------------------
@@ -847,6 +664,411 @@ __global__ void __launch_bounds__(128) monge_chain_kernel(TargetDev t, StepDev s
 }
 
 // ---------------------------------------------------------------------------
+// NUTS dynamics: one integrator step of a chain's extreme state, in place.
+// Each policy holds its per-chain work space and exposes, per state, the
+// momentum m and velocity u in float64 for the U-turn criterion.
+// ---------------------------------------------------------------------------
+// RMHMC (rmhmc/nuts.py): IntegratorState (q, p, v = G⁻¹p, ℓ, ∇ℓ), energy
+// −ℓ + K (mcmc/metrics.py:160-166)
+template <typename T, int DMAX>
+struct RmDyn {
+  struct State {
+    T q[DMAX], p[DMAX], g[DMAX];
+    double m[DMAX], u[DMAX];
+    double ld;
+  };
+  TargetDev t;
+  StepDev sp;
+  MetricEval<DMAX> Mv;
+  bool bad = false, conv_all = true;
+  int iters = 0;
+
+  __device__ double start(State& s, const T* q, const T* g, double ld, double, const T* z,
+                          T* draw_out) {
+    const int d = t.d;
+    for (int i = 0; i < d; ++i) {
+      s.q[i] = q[i];
+      s.g[i] = g[i];
+    }
+    s.ld = ld;
+    // p = chol(G)·z, v = G⁻¹p (rmhmc/nuts.py:144-146)
+    eval_metric<T, DMAX>(t, s.q, Mv, false, &bad);
+    for (int i = 0; i < d; ++i) {
+      if (Mv.diag) {
+        s.p[i] = T(sqrt(Mv.L[i]) * double(z[i]));
+      } else {
+        double acc = 0.0;
+        for (int k = 0; k <= i; ++k) acc += Mv.L[i * d + k] * double(z[k]);
+        s.p[i] = T(acc);
+      }
+      s.m[i] = double(s.p[i]);
+      if (draw_out) draw_out[i] = s.p[i];
+    }
+    metric_solve<T, DMAX>(Mv, d, s.p, s.u);
+    return -s.ld + kinetic_rm<T, DMAX>(Mv, d, s.p);
+  }
+  __device__ double step(State& s, double h) {
+    const int d = t.d;
+    StepDev sd = sp;
+    sd.h = h;
+    bool conv = true;
+    if (sp.integrator == GJ_GENERALIZED_LEAPFROG)
+      iters += gl_step<T, DMAX>(t, sd, s.q, s.p, s.g, &s.ld, Mv, &conv, &bad);
+    else
+      iters += im_step<T, DMAX>(t, sd, s.q, s.p, s.g, &s.ld, Mv, &conv, &bad);
+    conv_all &= conv;
+    eval_metric<T, DMAX>(t, s.q, Mv, false, &bad);
+    metric_solve<T, DMAX>(Mv, d, s.p, s.u);
+    for (int i = 0; i < d; ++i) s.m[i] = double(s.p[i]);
+    return -s.ld + kinetic_rm<T, DMAX>(Mv, d, s.p);
+  }
+  __device__ void store(const State& s, T* q, T* g, double* ld, double*) const {
+    for (int i = 0; i < t.d; ++i) {
+      q[i] = s.q[i];
+      g[i] = s.g[i];
+    }
+    *ld = s.ld;
+  }
+  __device__ uint8_t status() const {
+    return (conv_all ? 0u : GJ_CHAIN_FP_NOT_CONVERGED) | (bad ? GJ_CHAIN_NOT_SPD : 0u);
+  }
+};
+
+// dense LMC (lmcmc/nuts.py): IntegratorState (q, Gv, v, ℓ, ∇ℓ, J), energy
+// −ℓ + K − J (lmcmc/metrics.py:209-219), the lan integrator
+// (lmcmc/integrators.py:93-144)
+template <typename T, int DMAX>
+struct LmcDyn {
+  struct State {
+    T q[DMAX], g[DMAX];
+    double m[DMAX], u[DMAX];
+    double ld, J;
+  };
+  TargetDev t;
+  StepDev sp;
+  LmcWork<DMAX> W;
+  bool bad = false, conv_all = true;
+  int iters = 0;
+
+  __device__ double finish(State& s) {  // Gv and the energy at s.q (W holds G after lmc_metric)
+    const int d = t.d;
+    const bool diag = metric_is_diag(t.metric);
+    const double logdet = lmc_metric<T, DMAX>(t, s.q, W, diag, &bad);
+    for (int i = 0; i < d; ++i) {
+      if (diag) {
+        s.m[i] = W.G[i] * s.u[i];
+      } else {
+        double acc = 0.0;
+        for (int k = 0; k < d; ++k) acc += W.G[i * d + k] * s.u[k];
+        s.m[i] = acc;
+      }
+    }
+    return -s.ld + lmc_kinetic<DMAX>(W, d, logdet, s.u, diag) - s.J;
+  }
+  __device__ double start(State& s, const T* q, const T* g, double ld, double J, const T* z,
+                          T* draw_out) {
+    const int d = t.d;
+    const bool diag = metric_is_diag(t.metric);
+    for (int i = 0; i < d; ++i) {
+      s.q[i] = q[i];
+      s.g[i] = g[i];
+    }
+    s.ld = ld;
+    s.J = J;
+    // v = L⁻ᵀz (lmcmc/metrics.py:75-91)
+    lmc_metric<T, DMAX>(t, s.q, W, diag, &bad);
+    if (diag) {
+      for (int i = 0; i < d; ++i) s.u[i] = double(z[i]) / sqrt(W.G[i]);
+    } else {
+      double zz[DMAX];
+      for (int i = 0; i < d; ++i) zz[i] = double(z[i]);
+      chol_bwd(W.Om, d, zz, s.u);
+    }
+    for (int i = 0; i < d; ++i)
+      if (draw_out) draw_out[i] = T(s.u[i]);
+    return finish(s);
+  }
+  __device__ double step(State& s, double h) {
+    const int d = t.d;
+    const bool diag = metric_is_diag(t.metric);
+    lmc_half_step<T, DMAX>(t, s.q, s.u, &s.J, s.g, h, W, diag, &bad);
+    for (int i = 0; i < d; ++i) s.q[i] = T(double(s.q[i]) + h * s.u[i]);
+    s.ld = logdensity_grad<T>(t, s.q, s.g);
+    lmc_half_step<T, DMAX>(t, s.q, s.u, &s.J, s.g, h, W, diag, &bad);
+    return finish(s);
+  }
+  __device__ void store(const State& s, T* q, T* g, double* ld, double* vol) const {
+    for (int i = 0; i < t.d; ++i) {
+      q[i] = s.q[i];
+      g[i] = s.g[i];
+    }
+    *ld = s.ld;
+    *vol = s.J;
+  }
+  __device__ uint8_t status() const { return bad ? GJ_CHAIN_NOT_SPD : 0u; }
+};
+
+// LMC-Monge (lmcmonge/nuts.py): RiemannianIntegratorState (lmcmonge/
+// integrators.py:26-40), energy −ℓ + K − J (lmcmonge/metrics.py:267-284),
+// momentum = the metric-vector product with the raw gradient
+// (lmcmonge/metrics.py:243-255, as lmc.py:202-204 calls it)
+template <typename T, int DMAX>
+struct MongeDyn {
+  struct State {
+    T q[DMAX], v[DMAX], gn[DMAX], dl_ig[DMAX], Hdl[DMAX], igH[DMAX], hv[DMAX];
+    double m[DMAX], u[DMAX];
+    double ld, L, J;
+  };
+  TargetDev t;
+  StepDev sp;
+  T im[DMAX];
+  double slm = 0.0;  // Σ log M
+  bool bad = false, conv_all = true;
+  int iters = 0;
+
+  __device__ void init_mass() {
+    const T* imv = static_cast<const T*>(sp.inv_mass);
+    for (int i = 0; i < t.d; ++i) {
+      im[i] = imv ? imv[i] : T(1);
+      slm += -log(double(im[i]));
+    }
+  }
+  __device__ double finish(State& s) {  // momentum, u = v and the energy
+    const int d = t.d;
+    const double a2 = sp.alpha2, sL = sqrt(s.L);
+    double vg = 0.0, vgn = 0.0, vmv = 0.0;
+    for (int i = 0; i < d; ++i) {
+      vg += double(s.v[i]) * double(s.gn[i]) * sL;
+      vgn += double(s.v[i]) * double(s.gn[i]);
+      vmv += double(s.v[i]) * double(s.v[i]) / double(im[i]);
+    }
+    for (int i = 0; i < d; ++i) {
+      s.u[i] = double(s.v[i]);
+      s.m[i] = double(s.v[i]) / double(im[i]) + a2 * s.L * vg * double(s.gn[i]) * sL;
+    }
+    const double K = -0.5 * (log(s.L) + slm) + 0.5 * vmv + 0.5 * s.L * a2 * vgn * vgn;
+    return -s.ld + K - s.J;
+  }
+  __device__ void at_q(State& s, const T* g) {  // L, normalised and weighted gradients, HVP
+    const int d = t.d;
+    const double a2 = sp.alpha2;
+    double L = 0.0;
+    for (int i = 0; i < d; ++i) L += double(im[i]) * double(g[i]) * double(g[i]);
+    s.L = 1.0 + a2 * L;
+    const double sL = sqrt(s.L);
+    for (int i = 0; i < d; ++i) {
+      s.gn[i] = T(double(g[i]) / sL);
+      s.dl_ig[i] = im[i] * s.gn[i];
+    }
+    hvp<T>(t, s.q, s.dl_ig, s.Hdl);
+    for (int i = 0; i < d; ++i) {
+      s.Hdl[i] = T(double(s.Hdl[i]) / sL);
+      s.igH[i] = im[i] * s.Hdl[i];
+    }
+  }
+  __device__ void hv_at(State& s) {
+    const double sL = sqrt(s.L);
+    hvp<T>(t, s.q, s.v, s.hv);
+    for (int i = 0; i < t.d; ++i) s.hv[i] = T(double(s.hv[i]) / sL);
+  }
+  __device__ double start(State& s, const T* q, const T* g, double ld, double J, const T* z,
+                          T* draw_out) {
+    const int d = t.d;
+    const double a2 = sp.alpha2;
+    init_mass();
+    for (int i = 0; i < d; ++i) s.q[i] = q[i];
+    s.ld = ld;
+    s.J = J;
+    at_q(s, g);
+    // velocity: the closed-form factor of diag(M⁻¹) − α²·w·wᵀ
+    // (lmcmonge/metrics.py:155-166)
+    double suf = 0.0, tau_next[DMAX];
+    for (int i = d - 1; i >= 0; --i) {
+      const double ui = double(s.dl_ig[i]) / sqrt(double(im[i]));
+      suf += ui * ui;
+      tau_next[i] = 1.0 / s.L + a2 * suf - a2 * ui * ui;
+    }
+    double pre = 0.0;
+    for (int i = 0; i < d; ++i) {
+      const double ui = double(s.dl_ig[i]) / sqrt(double(im[i]));
+      const double tn = tau_next[i], ta = tn + a2 * ui * ui;
+      const double zi = double(z[i]);
+      const double y = sqrt(tn / ta) * zi - a2 * ui * pre;
+      pre += ui * zi / sqrt(ta * tn);
+      s.v[i] = T(sqrt(double(im[i])) * y);
+      if (draw_out) draw_out[i] = s.v[i];
+    }
+    hv_at(s);
+    return finish(s);
+  }
+  __device__ double step(State& s, double h) {  // lan_integrator.one_step
+    const int d = t.d;
+    const double a2 = sp.alpha2;
+    monge_half<T, DMAX>(a2, s.v, &s.J, s.gn, s.hv, s.L, s.dl_ig, s.Hdl, s.igH, h, sp.alpha2_fix, d);
+    for (int i = 0; i < d; ++i) s.q[i] = T(double(s.q[i]) + h * double(s.v[i]));
+    T g[DMAX];
+    s.ld = logdensity_grad<T>(t, s.q, g);
+    at_q(s, g);
+    hv_at(s);
+    monge_half<T, DMAX>(a2, s.v, &s.J, s.gn, s.hv, s.L, s.dl_ig, s.Hdl, s.igH, h, sp.alpha2_fix, d);
+    hv_at(s);
+    return finish(s);
+  }
+  __device__ void store(const State& s, T* q, T* g, double* ld, double* vol) const {
+    const double sL = sqrt(s.L);
+    for (int i = 0; i < t.d; ++i) {
+      q[i] = s.q[i];
+      g[i] = T(double(s.gn[i]) * sL);  // lmcmonge/nuts.py:197-203
+    }
+    *ld = s.ld;
+    *vol = s.J;
+  }
+  __device__ uint8_t status() const { return 0u; }
+};
+
+// ---------------------------------------------------------------------------
+// iterative NUTS (rmhmc/nuts.py, lmcmc/nuts.py, lmcmonge/nuts.py), one
+// thread per chain
+// ---------------------------------------------------------------------------
+// A chain's trajectory: the two extreme states, integrated in place (the
+// subtrajectory of expansion k starts at the extreme on its side and that
+// extreme becomes its last state, which is where the merged trajectory of
+// mcmc/trajectory.py:634-640 ends), the momentum and velocity sums, the
+// sampled proposal and the numpyro-style U-turn checkpoints
+// (mcmc/termination.py:30-119).  Uniforms: u[k] the direction of expansion
+// k, u[M + k] its biased merge, u[2M + 2^k − 1 + j] step j of expansion k.
+template <class Dyn, typename T, int DMAX>
+__global__ void __launch_bounds__(128) nuts_kernel(TargetDev t, StepDev sp, int M, int crit, T* pos,
+                                                   T* grad, double* logdens, double* vol,
+                                                   const T* z, const double* uni, int U,
+                                                   NutsInfoDev<T> info, int C) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  Dyn dyn;
+  dyn.t = t;
+  dyn.sp = sp;
+  const int d = dyn.t.d;
+  const double* u = uni + (size_t)c * U;
+  using S = typename Dyn::State;
+  S Lf;
+  const double H0 = dyn.start(Lf, pos + (size_t)c * d, grad + (size_t)c * d, logdens[c],
+                              vol ? vol[c] : 0.0, z + (size_t)c * d,
+                              info.momentum ? info.momentum + (size_t)c * d : nullptr);
+  S Rt = Lf;
+  S prop = Lf;  // the sampled proposal (mcmc/proposal.py:23-38)
+  double prop_E = H0, prop_w = 0.0, prop_sl = -INFINITY;
+  double psum[DMAX], vsum[DMAX];
+  for (int i = 0; i < d; ++i) {
+    psum[i] = Lf.m[i];
+    vsum[i] = Lf.u[i];
+  }
+  int n_states = 0;
+  double ck_r[kNutsMaxDoublings][DMAX], ck_rs[kNutsMaxDoublings][DMAX];
+  double ck_v[kNutsMaxDoublings][DMAX], ck_vs[kNutsMaxDoublings][DMAX];
+  for (int k = 0; k < M; ++k)
+    for (int i = 0; i < d; ++i) ck_r[k][i] = ck_rs[k][i] = ck_v[k][i] = ck_vs[k][i] = 0.0;
+  int step = 0;
+  bool div = false, turning = false;
+  while (step < M && !div && !turning) {  // dynamic_multiplicative_expansion
+    const int dir = u[step] < 0.5 ? 1 : -1;
+    S& E = dir > 0 ? Rt : Lf;
+    const int base = 2 * M + (1 << step) - 1;
+    double spsum[DMAX], svsum[DMAX];
+    S sub;
+    double s_E = 0.0, s_w = 0.0, s_sl = 0.0;
+    int s_n = 0;
+    bool sdiv = false, sterm = false;
+    for (int j = 0; j < (1 << step) && !sterm && !sdiv; ++j) {  // dynamic_progressive_integration
+      const double H1 = dyn.step(E, dir * dyn.sp.h);
+      double w = H0 - H1;  // proposal_from_energy_diff (mcmc/proposal.py:87-121)
+      if (isnan(w)) w = -INFINITY;
+      const double sl = fmin(w, 0.0);
+      sdiv = -w > dyn.sp.div_threshold;
+      bool take;
+      if (j == 0) {
+        for (int i = 0; i < d; ++i) {
+          spsum[i] = E.m[i];
+          svsum[i] = E.u[i];
+        }
+        s_n = 1;
+        take = true;
+        s_w = w;
+        s_sl = sl;
+      } else {  // progressive_uniform_sampling (mcmc/proposal.py:186-212)
+        for (int i = 0; i < d; ++i) {
+          spsum[i] += E.m[i];
+          svsum[i] += E.u[i];
+        }
+        ++s_n;
+        take = u[base + j] < expit(w - s_w);
+        s_w = logaddexp(s_w, w);
+        s_sl = logaddexp(s_sl, sl);
+      }
+      if (take) {
+        sub = E;
+        s_E = H1;
+      }
+      // iterative U-turn: checkpoint update and check (termination.py:48-119)
+      const int hi = __popc((unsigned)j >> 1);
+      const int lo = hi - (__ffs(~(unsigned)j) - 1) + 1;
+      if (j % 2 == 0)
+        for (int i = 0; i < d; ++i) {
+          ck_r[hi][i] = E.m[i];
+          ck_rs[hi][i] = spsum[i];
+          ck_v[hi][i] = E.u[i];
+          ck_vs[hi][i] = svsum[i];
+        }
+      for (int k = hi; k >= lo && !sterm; --k) {
+        double srs[DMAX], svs[DMAX];
+        for (int i = 0; i < d; ++i) {
+          srs[i] = spsum[i] - ck_rs[k][i] + ck_r[k][i];
+          svs[i] = svsum[i] - ck_vs[k][i] + ck_v[k][i];
+        }
+        sterm = nuts_turning<DMAX>(d, crit, ck_r[k], E.m, srs, ck_v[k], E.u, svs);
+      }
+    }
+    // the expansion's proposal (mcmc/trajectory.py:609-632)
+    if (sdiv || sterm) {
+      prop_sl = logaddexp(prop_sl, s_sl);
+    } else {  // progressive_biased_sampling (mcmc/proposal.py:215-245)
+      const double pa = fmin(exp(s_w - prop_w), 1.0);
+      const bool take = u[M + step] < pa;
+      prop_w = logaddexp(prop_w, s_w);
+      prop_sl = logaddexp(prop_sl, s_sl);
+      if (take) {
+        prop = sub;
+        prop_E = s_E;
+      }
+    }
+    // merge and the whole trajectory's U-turn (trajectory.py:634-650)
+    for (int i = 0; i < d; ++i) {
+      psum[i] += spsum[i];
+      vsum[i] += svsum[i];
+    }
+    n_states += s_n;
+    const bool whole = nuts_turning<DMAX>(d, crit, Lf.m, Rt.m, psum, Lf.u, Rt.u, vsum);
+    div = sdiv;
+    turning = sterm || whole;
+    ++step;
+  }
+  double J_out = 0.0;
+  dyn.store(prop, pos + (size_t)c * d, grad + (size_t)c * d, &logdens[c], &J_out);
+  if (vol) vol[c] = J_out;
+  if (info.left_q)
+    for (int i = 0; i < d; ++i) info.left_q[(size_t)c * d + i] = Lf.q[i];
+  if (info.right_q)
+    for (int i = 0; i < d; ++i) info.right_q[(size_t)c * d + i] = Rt.q[i];
+  if (info.acc_rate) info.acc_rate[c] = exp(prop_sl) / n_states;
+  if (info.divergent) info.divergent[c] = div;
+  if (info.turning) info.turning[c] = turning;
+  if (info.energy) info.energy[c] = prop_E;
+  if (info.doublings) info.doublings[c] = step;
+  if (info.steps) info.steps[c] = n_states;
+  if (info.fp_iters) info.fp_iters[c] = dyn.iters;
+  if (info.status) info.status[c] = dyn.status() | (isfinite(prop_E) ? 0u : GJ_CHAIN_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
 // operator kernels
 // ---------------------------------------------------------------------------
 template <typename T, int DMAX>
@@ -940,12 +1162,27 @@ cudaError_t launch_rmhmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T*
 }
 
 template <typename T>
-cudaError_t launch_rmhmc_nuts(const TargetDev& t, const StepDev& sp, int max_doublings, int criterion,
-                              T* pos, T* grad, double* ld, const T* z, const double* u, int U,
-                              const NutsInfoDev<T>& info, int C, int tpb, cudaStream_t st) {
+cudaError_t launch_nuts(int sampler, const TargetDev& t, const StepDev& sp, int max_doublings,
+                        int criterion, T* pos, T* grad, double* ld, double* vol, const T* z,
+                        const double* u, int U, const NutsInfoDev<T>& info, int C, int tpb,
+                        cudaStream_t st) {
   if (max_doublings < 0 || max_doublings > kNutsMaxDoublings) return cudaErrorInvalidValue;
-  GJ_DISPATCH_DMAX(t.d, 32, rmhmc_nuts_kernel<T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
-                                t, sp, max_doublings, criterion, pos, grad, ld, z, u, U, info, C));
+  if (sampler == GJ_SAMPLER_RMHMC) {
+    GJ_DISPATCH_DMAX(t.d, 32, {
+      nuts_kernel<RmDyn<T, DM>, T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+          t, sp, max_doublings, criterion, pos, grad, ld, nullptr, z, u, U, info, C);
+    });
+  } else if (sampler == GJ_SAMPLER_LMC) {
+    GJ_DISPATCH_DMAX(t.d, 32, {
+      nuts_kernel<LmcDyn<T, DM>, T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+          t, sp, max_doublings, criterion, pos, grad, ld, vol, z, u, U, info, C);
+    });
+  } else {
+    GJ_DISPATCH_DMAX(t.d, 32, {
+      nuts_kernel<MongeDyn<T, DM>, T, DM><<<grid_for(C, tpb), tpb, 0, st>>>(
+          t, sp, max_doublings, criterion, pos, grad, ld, vol, z, u, U, info, C);
+    });
+  }
   return cudaGetLastError();
 }
 
@@ -998,9 +1235,9 @@ cudaError_t launch_metric_vjp(const TargetDev& t, const T* q, const T* W, T* out
   template cudaError_t launch_rmhmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,  \
                                              const T*, const double*, const InfoDev<T>&, int,   \
                                              int, cudaStream_t);                                 \
-  template cudaError_t launch_rmhmc_nuts<T>(const TargetDev&, const StepDev&, int, int, T*, T*,  \
-                                            double*, const T*, const double*, int,              \
-                                            const NutsInfoDev<T>&, int, int, cudaStream_t);     \
+  template cudaError_t launch_nuts<T>(int, const TargetDev&, const StepDev&, int, int, T*, T*,   \
+                                      double*, double*, const T*, const double*, int,           \
+                                      const NutsInfoDev<T>&, int, int, cudaStream_t);           \
   template cudaError_t launch_lmc_chain<T>(const TargetDev&, const StepDev&, T*, T*, double*,    \
                                            double*, const T*, const double*, const InfoDev<T>&, \
                                            int, int, cudaStream_t);                              \

@@ -9,11 +9,13 @@ template <typename T>
 cudaError_t launch_rmhmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
                                const T* z, const double* u, const InfoDev<T>& info, int C, int tpb,
                                cudaStream_t st);
-// iterative Riemannian NUTS, thread per chain; u: [C, U] uniforms
+// iterative NUTS with the dynamics of `sampler` (GJ_SAMPLER_*), thread per
+// chain; u: [C, U] uniforms; vol: the volume adjustment (LMC samplers)
 template <typename T>
-cudaError_t launch_rmhmc_nuts(const TargetDev& t, const StepDev& sp, int max_doublings, int criterion,
-                              T* pos, T* grad, double* ld, const T* z, const double* u, int U,
-                              const NutsInfoDev<T>& info, int C, int tpb, cudaStream_t st);
+cudaError_t launch_nuts(int sampler, const TargetDev& t, const StepDev& sp, int max_doublings,
+                        int criterion, T* pos, T* grad, double* ld, double* vol, const T* z,
+                        const double* u, int U, const NutsInfoDev<T>& info, int C, int tpb,
+                        cudaStream_t st);
 template <typename T>
 cudaError_t launch_lmc_chain(const TargetDev& t, const StepDev& sp, T* pos, T* grad, double* ld,
                              double* vol, const T* z, const double* u, const InfoDev<T>& info,

@@ -16,7 +16,8 @@
  *   gj_init           replaces init(position, logdensity_fn)
  *                      geomjax/rmhmc/rmhmc.py:96-98, lmcmonge/lmc.py:101-109,
  *                      lmcmc/lmc.py:98-101 (value_and_grad at the position)
- *   gj_rmhmc_nuts_step replaces the iterative NUTS kernel of rmhmc/nuts.py:78-161
+ *   gj_nuts_step       replaces the iterative NUTS kernels of rmhmc/nuts.py:78-161,
+ *                      lmcmc/nuts.py and lmcmonge/nuts.py
  *   gj_logdensity_grad / gj_hvp / gj_metric
  *                      the operators the reference obtains by autodiff of the
  *                      user's logdensity_fn / metric_fn:
@@ -158,17 +159,22 @@ typedef struct {
   int32_t reserved;
 } gj_step_params;
 
-/* Iterative NUTS (rmhmc/nuts.py:78-161): the trajectory doubles in a random
- * direction until the generalized U-turn criterion holds, a divergence
- * occurs or max_num_doublings expansions were made. */
+/* Iterative NUTS (rmhmc/nuts.py:78-161, lmcmc/nuts.py, lmcmonge/nuts.py):
+ * the trajectory doubles in a random direction until the generalized
+ * U-turn criterion holds, a divergence occurs or max_num_doublings
+ * expansions were made. */
 typedef struct {
   double step_size;
   int32_t max_num_doublings;   /* reference default 10; at most 16 */
-  int32_t integrator;          /* gj_integrator */
+  int32_t integrator;          /* gj_integrator (RMHMC) */
   int32_t criterion;           /* stopping_criterion: 0 "euc" (default), 1 "bet", 2 "riem" */
-  int32_t max_iters;           /* fixed-point iteration cap */
-  double tol;                  /* fixed-point tolerance */
+  int32_t max_iters;           /* fixed-point iteration cap (RMHMC) */
+  double tol;                  /* fixed-point tolerance (RMHMC) */
   double divergence_threshold; /* reference default 1000 */
+  double alpha2;               /* LMC-Monge alpha^2 */
+  const void* inverse_mass;    /* LMC-Monge diagonal inverse mass [d] (NULL = ones) */
+  int32_t alpha2_fix;          /* LMC-Monge, as gj_step_params.alpha2_fix */
+  int32_t reserved;
 } gj_nuts_params;
 
 /* NUTSInfo (rmhmc/nuts.py:37-75), device pointers, each may be NULL. */
@@ -181,7 +187,7 @@ typedef struct {
   int32_t* num_integration_steps;     /* [C] states in the trajectory */
   int32_t* fp_iters;                  /* [C] fixed-point iterations over the trajectory */
   uint8_t* status;                    /* [C] GJ_CHAIN_* bits */
-  void* momentum;                     /* [C, d] the drawn momentum */
+  void* momentum;                     /* [C, d] the drawn momentum (RMHMC) or velocity (LMC) */
   void* leftmost_position;            /* [C, d] trajectory_leftmost_state.position */
   void* rightmost_position;           /* [C, d] trajectory_rightmost_state.position */
 } gj_nuts_info;
@@ -243,18 +249,20 @@ int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_sta
 int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* params, gj_chain_state* state,
                     const void* z, const double* u, gj_info* info, void* stream);
 
-/* One iterative-NUTS transition of every chain of an RMHMC context
- * (rmhmc/nuts.py:112-159, iterative_nuts_proposal :253-348), one thread per
- * chain, d <= 32.  The state moves to the sampled proposal.  z: [C, d]
- * momentum normals; uniforms: [C, uniforms_per_chain] float64 with
+/* One iterative-NUTS transition of every chain of a context, with the
+ * context's dynamics: RMHMC (rmhmc/nuts.py:112-159, iterative_nuts_proposal
+ * :253-348), dense LMC (lmcmc/nuts.py) or LMC-Monge (lmcmonge/nuts.py, the
+ * kernel named nutslmc there); one thread per chain, d <= 32.  The state
+ * (with the volume adjustment for the LMC samplers) moves to the sampled
+ * proposal.  z: [C, d] momentum / velocity normals; uniforms: [C, uniforms_per_chain] float64 with
  * uniforms_per_chain >= 2M + 2^M - 1 (M = max_num_doublings), laid out per
  * chain as u[k] the direction of expansion k (+1 iff u < 1/2), u[M + k] the
  * biased merge of expansion k, u[2M + 2^k - 1 + j] the progressive sample
  * of step j (>= 1) of expansion k -- the draws the reference takes from its
  * split keys. */
-int32_t gj_rmhmc_nuts_step(gj_ctx* ctx, const gj_nuts_params* params, gj_chain_state* state,
-                           const void* z, const double* uniforms, int32_t uniforms_per_chain,
-                           gj_nuts_info* info, void* stream);
+int32_t gj_nuts_step(gj_ctx* ctx, const gj_nuts_params* params, gj_chain_state* state,
+                     const void* z, const double* uniforms, int32_t uniforms_per_chain,
+                     gj_nuts_info* info, void* stream);
 
 /* Counters of the last step on this context: out[0] fixed-point map
  * evaluations, out[1] GEMM launches, out[2] other kernel launches,

@@ -1,9 +1,12 @@
-"""Iterative NUTS with the Riemannian metric (float64, one chain at a time).
+"""Iterative NUTS (float64, one chain at a time) with the RMHMC, dense LMC or
+LMC-Monge dynamics.
 
 TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).
 
 Restates ``rmhmc/nuts.py`` (``build_kernel`` :78-161, ``iterative_nuts_proposal``
-:253-348) over ``mcmc/trajectory.py`` (``Trajectory`` :54-118,
+:253-348), ``lmcmc/nuts.py`` and ``lmcmonge/nuts.py`` (the same tree over
+the lan integrators and the LMC energies; LMC-Monge returns the gradient
+de-normalised, ``lmcmonge/nuts.py:196-203``) over ``mcmc/trajectory.py`` (``Trajectory`` :54-118,
 ``dynamic_progressive_integration`` :149-317, ``dynamic_multiplicative_expansion``
 :517-668), ``mcmc/termination.py`` (``iterative_uturn_numpyro`` :30-119),
 ``mcmc/proposal.py`` (``proposal_from_energy_diff`` :87-121,
@@ -43,12 +46,12 @@ def _expit(x):
 
 
 @dataclass
-class State:  # IntegratorState of one chain (rmhmc/integrators.py)
+class State:  # one chain's integrator state and its U-turn vectors
+    inner: object       # the dynamics' own (batched, C = 1) state
+    m: np.ndarray       # momentum
+    u: np.ndarray       # velocity
     q: np.ndarray
-    p: np.ndarray
-    v: np.ndarray
     ld: float
-    g: np.ndarray
 
 
 @dataclass
@@ -121,26 +124,132 @@ class Termination:
         return False
 
 
-def _step(target, s: State, h, integrator, tol, max_iters):
+def _nan_like(s: State):
+    nan = np.full_like(s.q, np.nan)
+    return State(None, nan, nan.copy(), nan.copy(), float("nan"))
+
+
+class RmDynamics:
+    """RMHMC: IntegratorState (q, p, G⁻¹p, ℓ, ∇ℓ), energy −ℓ + K."""
+
+    def __init__(self, target, integrator="implicit_midpoint", tol=1e-6, max_iters=100, **_):
+        self.t, self.integ, self.tol, self.max_iters = target, integrator, tol, max_iters
+
+    def _wrap(self, st):
+        return State(st, st.momentum[0], st.velocity[0], st.position[0], float(st.logdensity[0]))
+
+    def start(self, q, ld, g, J, z):
+        p = R.momentum_from_normals(self.t, q[None], z[None])
+        v = R.inverse_metric_vector_product(self.t, q[None], p)
+        return self._wrap(R.IntegratorState(q[None], p, v, np.array([ld]), g[None]))
+
+    def step(self, s, h):
+        new, _ = R.INTEGRATORS[self.integ](self.t, s.inner, h, tol=self.tol,
+                                           max_iters=self.max_iters)
+        return self._wrap(new)
+
+    def energy(self, s):  # hmc_energy (mcmc/metrics.py:160-166)
+        return -s.ld + float(R.kinetic_energy(self.t, s.inner.position, s.inner.momentum)[0])
+
+    def out(self, s):
+        return s.q, s.ld, s.inner.logdensity_grad[0], 0.0
+
+
+class LmcDynamics:
+    """dense LMC: IntegratorState (q, Gv, v, ℓ, ∇ℓ, J), energy −ℓ + K − J."""
+
+    def __init__(self, target, **_):
+        self.t = target
+
+    def _wrap(self, st):
+        return State(st, st.momentum[0], st.velocity[0], st.position[0], float(st.logdensity[0]))
+
+    def start(self, q, ld, g, J, z):
+        from . import lmc as Lm
+
+        v = Lm.velocity(self.t, q[None], z[None])
+        mom = Lm.metric_vector_product(self.t, q[None], v)
+        return self._wrap(Lm.IntegratorState(q[None], mom, v, np.array([ld]), g[None],
+                                             np.array([J])))
+
+    def step(self, s, h):
+        from . import lmc as Lm
+
+        return self._wrap(Lm.lan_step(self.t, s.inner, h))
+
+    def energy(self, s):
+        from . import lmc as Lm
+
+        return float(Lm.energy(self.t, s.inner)[0])
+
+    def out(self, s):
+        return s.q, s.ld, s.inner.logdensity_grad[0], float(s.inner.volume_adjustment[0])
+
+
+class MongeDynamics:
+    """LMC-Monge: RiemannianIntegratorState, energy −ℓ + K − J."""
+
+    def __init__(self, target, alpha2=0.001, inverse_mass_matrix=None, alpha2_fix=False, **_):
+        self.t, self.a2, self.fix = target, alpha2, alpha2_fix
+        self.im = (np.ones(target.dim) if inverse_mass_matrix is None
+                   else np.asarray(inverse_mass_matrix, dtype=np.float64))
+        self.mass = 1.0 / self.im
+
+    def _wrap(self, st):
+        return State(st, st.momentum[0], st.velocity[0], st.position[0], float(st.logdensity[0]))
+
+    def start(self, q, ld, g, J, z):
+        from . import lmcmonge as Mo
+
+        a2, im = self.a2, self.im
+        q1, g1 = q[None], g[None]
+        L = Mo.normalizing_constant(a2, im, g1)
+        sL = np.sqrt(L)[:, None]
+        g_n = g1 / sL
+        dl_ig = im * g_n
+        Hdl_ig = self.t.hvp(q1, dl_ig) / sL
+        v = Mo.velocity_dense(a2, im, dl_ig, z[None])
+        mom = Mo.metric_vector_product(v, a2, g1, L, self.mass)
+        hv_n = self.t.hvp(q1, v) / sL
+        return self._wrap(Mo.MongeState(a2, q1, mom, v, np.array([ld]), g_n, dl_ig, Hdl_ig,
+                                        im * Hdl_ig, hv_n, L, np.array([J])))
+
+    def step(self, s, h):
+        from . import lmcmonge as Mo
+
+        return self._wrap(Mo.lan_step(self.t, s.inner, h, self.im, self.mass, self.fix))
+
+    def energy(self, s):
+        from . import lmcmonge as Mo
+
+        return float(Mo.energy(s.inner, self.mass)[0])
+
+    def out(self, s):
+        st = s.inner
+        g = st.logdensity_grad_norm[0] * np.sqrt(st.determinant_metric[0])
+        return s.q, s.ld, g, float(st.volume_adjustment[0])
+
+
+DYNAMICS = {"rmhmc": RmDynamics, "lmc": LmcDynamics, "lmcmonge": MongeDynamics}
+
+
+def _safe_step(dyn, s, h):
     """One integrator step; a metric that stops being positive definite
     gives a NaN state (JAX's solve and Cholesky return NaN where NumPy
     raises), which the energy difference turns into a divergence."""
-    st = R.IntegratorState(s.q[None], s.p[None], s.v[None], np.array([s.ld]), s.g[None])
     try:
         with np.errstate(all="ignore"):
-            new, _ = R.INTEGRATORS[integrator](target, st, h, tol=tol, max_iters=max_iters)
+            return dyn.step(s, h)
     except np.linalg.LinAlgError:
-        nan = np.full_like(s.q, np.nan)
-        return State(nan, nan.copy(), nan.copy(), float("nan"), nan.copy())
-    return State(new.position[0], new.momentum[0], new.velocity[0], float(new.logdensity[0]),
-                 new.logdensity_grad[0])
+        return _nan_like(s)
 
 
-def _energy(target, s: State):
-    """hmc_energy: −ℓ + K (mcmc/metrics.py:160-166)."""
+def _safe_energy(dyn, s):
+    if s.inner is None:
+        return float("nan")
     try:
         with np.errstate(all="ignore"):
-            return -s.ld + float(R.kinetic_energy(target, s.q[None], s.p[None])[0])
+            return dyn.energy(s)
     except np.linalg.LinAlgError:
         return float("nan")
 
@@ -166,17 +275,18 @@ class NUTSInfo:
     acceptance_rate: float
 
 
-def transition_one(target, q, ld, g, z, u, step_size, max_num_doublings=10, *,
-                   integrator="implicit_midpoint", criterion="euc", tol=1e-6, max_iters=100,
-                   divergence_threshold=1000.0):
-    """One NUTS transition of one chain (rmhmc/nuts.py:112-159)."""
+def transition_one(target, q, ld, g, z, u, step_size, max_num_doublings=10, *, dynamics="rmhmc",
+                   criterion="euc", divergence_threshold=1000.0, volume_adjustment=0.0, **dyn_kw):
+    """One NUTS transition of one chain (rmhmc/nuts.py:112-159 and its LMC
+    twins); ``dyn_kw`` configures the dynamics (integrator, tol, max_iters
+    for RMHMC; alpha2, inverse_mass_matrix, alpha2_fix for LMC-Monge).
+    Returns ((q, ℓ, ∇ℓ, J) of the sampled proposal, NUTSInfo)."""
+    dyn = DYNAMICS[dynamics](target, **dyn_kw)
     M = max_num_doublings
-    p = R.momentum_from_normals(target, q[None], z[None])[0]
-    v = R.inverse_metric_vector_product(target, q[None], p[None])[0]
-    s0 = State(q, p, v, float(ld), g)
-    H0 = _energy(target, s0)
+    s0 = dyn.start(q, float(ld), g, float(volume_adjustment), z)
+    H0 = dyn.energy(s0)
     proposal = Proposal(s0, H0, 0.0, -np.inf)
-    traj = Traj(s0, s0, p.copy(), v.copy(), 0)
+    traj = Traj(s0, s0, s0.m.copy(), s0.u.copy(), 0)
     term = Termination(M, q.shape[0])
     step = 0
     div = turning = False
@@ -187,26 +297,26 @@ def transition_one(target, q, ld, g, z, u, step_size, max_num_doublings=10, *,
         base = 2 * M + 2 ** step - 1
         cur = start
         sub_prop = None
-        sub = Traj(start, start, start.p, start.v, 0)
+        sub = None
         j = 0
         sub_div = sub_term = False
         while j < 2 ** step and not sub_term and not sub_div:
-            new = _step(target, cur, direction * step_size, integrator, tol, max_iters)
-            new_prop = _from_energy_diff(H0, _energy(target, new), new)
+            new = _safe_step(dyn, cur, direction * step_size)
+            new_prop = _from_energy_diff(H0, _safe_energy(dyn, new), new)
             sub_div = -new_prop.weight > divergence_threshold
             if j == 0:
-                sub = Traj(new, new, new.p.copy(), new.v.copy(), 1)
+                sub = Traj(new, new, new.m.copy(), new.u.copy(), 1)
                 sub_prop = new_prop
             else:
-                sub = Traj(sub.left, new, sub.p_sum + new.p, sub.v_sum + new.v, sub.n + 1)
+                sub = Traj(sub.left, new, sub.p_sum + new.m, sub.v_sum + new.u, sub.n + 1)
                 # progressive_uniform_sampling (proposal.py:186-212)
                 acc = u[base + j] < _expit(new_prop.weight - sub_prop.weight)
                 w = _logaddexp(sub_prop.weight, new_prop.weight)
                 sl = _logaddexp(sub_prop.sum_log_p_accept, new_prop.sum_log_p_accept)
                 sub_prop = Proposal(new if acc else sub_prop.state,
                                     new_prop.energy if acc else sub_prop.energy, w, sl)
-            term.update(sub.p_sum, new.p, sub.v_sum, new.v, j)
-            sub_term = term.turning(sub.p_sum, new.p, sub.v_sum, new.v, criterion)
+            term.update(sub.p_sum, new.m, sub.v_sum, new.u, j)
+            sub_term = term.turning(sub.p_sum, new.m, sub.v_sum, new.u, criterion)
             cur = new
             j += 1
         if direction < 0:
@@ -226,27 +336,34 @@ def transition_one(target, q, ld, g, z, u, step_size, max_num_doublings=10, *,
         left_t, right_t = (traj, sub) if direction > 0 else (sub, traj)
         traj = Traj(left_t.left, right_t.right, left_t.p_sum + right_t.p_sum,
                     left_t.v_sum + right_t.v_sum, left_t.n + right_t.n)
-        whole = is_turning(traj.left.p, traj.right.p, traj.p_sum, traj.left.v, traj.right.v,
+        whole = is_turning(traj.left.m, traj.right.m, traj.p_sum, traj.left.u, traj.right.u,
                            traj.v_sum, criterion)
         div = sub_div
         turning = sub_term or whole
         step += 1
     acc_rate = float(np.exp(proposal.sum_log_p_accept) / traj.n)
-    info = NUTSInfo(p, div, turning, proposal.energy, traj.left, traj.right, step, traj.n,
+    info = NUTSInfo(s0.m, div, turning, proposal.energy, traj.left, traj.right, step, traj.n,
                     acc_rate)
-    return proposal.state, info
+    return dyn.out(proposal.state), info
 
 
-def kernel(target, state, z, u, step_size, max_num_doublings=10, **kw):
-    """All chains of an ``rmhmc.RMHMCState``; ``u``: [C, num_uniforms(M)]."""
+def kernel(target, state, z, u, step_size, max_num_doublings=10, *, dynamics="rmhmc", **kw):
+    """All chains of an ``rmhmc.RMHMCState`` (or an LMC state with a volume
+    adjustment); ``u``: [C, num_uniforms(M)].  Returns the new state (the
+    same type) and the per-chain infos."""
     C = state.position.shape[0]
-    qs, lds, gs, infos = [], [], [], []
+    vol = getattr(state, "volume_adjustment", None)
+    outs, infos = [], []
     for c in range(C):
-        s, info = transition_one(target, state.position[c], state.logdensity[c],
+        o, info = transition_one(target, state.position[c], state.logdensity[c],
                                  state.logdensity_grad[c], z[c], u[c], step_size,
-                                 max_num_doublings, **kw)
-        qs.append(s.q)
-        lds.append(s.ld)
-        gs.append(s.g)
+                                 max_num_doublings, dynamics=dynamics,
+                                 volume_adjustment=0.0 if vol is None else vol[c], **kw)
+        outs.append(o)
         infos.append(info)
-    return R.RMHMCState(np.array(qs), np.array(lds), np.array(gs)), infos
+    q = np.array([o[0] for o in outs])
+    ld = np.array([o[1] for o in outs])
+    g = np.array([o[2] for o in outs])
+    if vol is None:
+        return R.RMHMCState(q, ld, g), infos
+    return type(state)(q, ld, g, np.array([o[3] for o in outs])), infos

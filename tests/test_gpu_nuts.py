@@ -1,5 +1,6 @@
-"""Iterative Riemannian NUTS on the device (``gj_rmhmc_nuts_step``) against
-the float64 oracle's per-chain restatement of rmhmc/nuts.py.
+"""Iterative NUTS on the device (``gj_nuts_step``) with the RMHMC, dense-LMC
+and LMC-Monge dynamics, against the float64 oracle's per-chain restatement
+of rmhmc/nuts.py, lmcmc/nuts.py and lmcmonge/nuts.py.
 
 FP64: positions, log densities, energies and acceptance rates to 1e-9
 (e = max |gpu − oracle| / (1 + |oracle|)); the discrete outcomes (number of
@@ -68,6 +69,57 @@ def test_nuts_matches_oracle(kind, kw, h, integrator, criterion):
                        np.array([i.left.q for i in oinfo])[ok]) < 1e-9
         assert rel_err(_np(info.trajectory_rightmost_position)[ok],
                        np.array([i.right.q for i in oinfo])[ok]) < 1e-9
+
+
+@pytest.mark.parametrize("criterion", ["euc", "bet", "riem"])
+@pytest.mark.parametrize("dynamics,kind,kw,h", [
+    ("lmc", "funnel", dict(D=3, metric="pullback"), 0.1),
+    ("lmc", "hier", dict(J=3), 0.1),
+    ("lmcmonge", "funnel", dict(D=5, metric="diag"), 0.05),
+    ("lmcmonge", "hier", dict(J=4), 0.05),
+], ids=str)
+def test_lmc_nuts_matches_oracle(dynamics, kind, kw, h, criterion):
+    import geomjax_gb300 as gj
+    from oracle import lmc as O_lmc
+    from oracle import lmcmonge as O_mo
+
+    ot = oracle_target(kind, **kw)
+    dt = device_target(kind, "fp64", **kw)
+    C, M, d = 8, 6, ot.dim
+    q0 = start_positions(d, C, seed=2, scale=0.5)
+    im = np.linspace(0.9, 1.1, d)
+    a2 = 0.5
+    if dynamics == "lmc":
+        kern = gj.nutslmc.build_kernel()
+        st = gj.nutslmc.init(q0, dt)
+        so = O_lmc.init(ot, q0)
+        okw = {}
+    else:
+        kern0 = gj.nutslmcmonge.build_kernel(max_num_doublings=M)
+        imt = torch.as_tensor(im, device="cuda")
+
+        def kern(key, s, t, hh, MM, stopping_criterion):
+            return kern0(key, s, t, hh, imt, a2, stopping_criterion)
+        st = gj.nutslmcmonge.init(q0, dt)
+        so = O_mo.init(ot, q0)
+        okw = dict(alpha2=a2, inverse_mass_matrix=im)
+    rng = np.random.Generator(np.random.PCG64(13))
+    for t in range(3):
+        z = rng.standard_normal((C, d))
+        u = rng.random((C, ON.num_uniforms(M)))
+        so, oinfo = ON.kernel(ot, so, z, u, h, M, dynamics=dynamics, criterion=criterion, **okw)
+        st, info = kern(gj.NUTSDraws(z, u), st, dt, h, M, stopping_criterion=criterion)
+        np.testing.assert_array_equal(_np(info.num_integration_steps),
+                                      [i.num_integration_steps for i in oinfo])
+        np.testing.assert_array_equal(_np(info.num_trajectory_expansions),
+                                      [i.num_trajectory_expansions for i in oinfo])
+        np.testing.assert_array_equal(_np(info.is_turning).astype(bool),
+                                      [i.is_turning for i in oinfo])
+        assert rel_err(_np(st.position), so.position) < 1e-9, t
+        assert rel_err(_np(st.volume_adjustment), so.volume_adjustment) < 1e-9
+        assert rel_err(_np(st.logdensity_grad), so.logdensity_grad) < 1e-9
+        assert rel_err(_np(info.acceptance_rate), [i.acceptance_rate for i in oinfo]) < 1e-9
+        assert rel_err(_np(info.energy), [i.energy for i in oinfo]) < 1e-9
 
 
 def test_nuts_keeps_the_funnel_stationary():

@@ -45,3 +45,38 @@ def test_one_expansion_is_one_rmhmc_step(kind, kw, direction):
     np.testing.assert_allclose([i.acceptance_rate for i in infos], info_r.acceptance_rate,
                                rtol=1e-13)
     assert all(i.num_integration_steps == 1 and i.num_trajectory_expansions == 1 for i in infos)
+
+
+@pytest.mark.parametrize("dynamics", ["lmc", "lmcmonge"])
+def test_one_expansion_is_one_lmc_step(dynamics):
+    """The same pin for the LMC samplers: one expansion is one lan step with
+    the static Metropolis accept (lmcmc/lmc.py:411-476, lmcmonge/lmc.py:
+    472-536), the volume adjustment included."""
+    from oracle import lmc as O_lmc
+    from oracle import lmcmonge as O_mo
+
+    kind, kw = ("funnel", dict(D=3, metric="pullback")) if dynamics == "lmc" else \
+        ("funnel", dict(D=5, metric="diag"))
+    ot = oracle_target(kind, **kw)
+    C = 5
+    q0 = start_positions(ot.dim, C, seed=4, scale=0.4)
+    rng = np.random.default_rng(7)
+    z = rng.standard_normal((C, ot.dim))
+    ua = rng.random(C)
+    u = np.stack([np.full(C, 0.25), ua, np.zeros(C)], axis=1)
+    im = np.linspace(0.9, 1.1, ot.dim)
+    if dynamics == "lmc":
+        st = O_lmc.init(ot, q0)
+        st.volume_adjustment = rng.standard_normal(C) * 0.1
+        new_n, infos = ON.kernel(ot, st, z, u, 0.05, 1, dynamics="lmc")
+        new_r, info_r = O_lmc.kernel(ot, st, z, ua, 0.05, 1)
+    else:
+        st = O_mo.init(ot, q0)
+        new_n, infos = ON.kernel(ot, st, z, u, 0.05, 1, dynamics="lmcmonge", alpha2=0.5,
+                                 inverse_mass_matrix=im)
+        new_r, info_r = O_mo.kernel(ot, st, z, ua, 0.05, im, 1, alpha2=0.5)
+    np.testing.assert_allclose(new_n.position, new_r.position, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(new_n.volume_adjustment, new_r.volume_adjustment, atol=1e-13)
+    np.testing.assert_allclose(new_n.logdensity_grad, new_r.logdensity_grad, atol=1e-12)
+    np.testing.assert_allclose([i.acceptance_rate for i in infos], info_r.acceptance_rate,
+                               rtol=1e-12)
