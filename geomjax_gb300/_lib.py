@@ -148,6 +148,7 @@ SIGNATURES = {
     "gj_lmcmonge_alpha2_jvp": (c_int32, [POINTER(GjTarget), c_int32, c_int32,
                                          POINTER(GjStepParams), c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_void_p]),
+    "gj_fma_peak": (c_int32, [c_int32, POINTER(c_double), c_void_p]),
     "gj_chees_workspace_size": (c_int64, [c_int32, c_int32]),
     "gj_chees_statistics": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

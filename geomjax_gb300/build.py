@@ -35,6 +35,7 @@ UNITS = [
     ("traj_jvp.cu", []),
     ("chees.cu", []),
     ("monge_jvp.cu", []),
+    ("peaks.cu", []),
 ]
 
 

@@ -584,6 +584,13 @@ int32_t gj_logreg_gl_transition_jvp(const gj_target* target, int32_t C, const do
   return cuda_status(e, "gj_logreg_gl_transition_jvp");
 }
 
+int32_t gj_fma_peak(int32_t precision, double* tflops, void* stream) {
+  if (precision != GJ_FP64 && precision != GJ_MIXED) return fail(GJ_EINVAL, "bad precision");
+  if (!tflops) return fail(GJ_EINVAL, "tflops is NULL");
+  return cuda_status(gj::fma_peak(precision == GJ_FP64, tflops, static_cast<cudaStream_t>(stream)),
+                     "gj_fma_peak");
+}
+
 // ---------------------------------------------------------------------------
 // ChEES: the LMC-Monge proposal's derivative in α², cross-chain statistics
 // ---------------------------------------------------------------------------

@@ -56,6 +56,9 @@ template <typename T>
 cudaError_t launch_monge_alpha2_jvp(const TargetDev& t, const StepDev& sp, const T* pos,
                                     const T* z, T* qL, T* dq, int C, cudaStream_t st);
 
+// FMA throughput of the CUDA cores in TFLOP/s (peaks.cu; synchronises)
+cudaError_t fma_peak(int fp64, double* tflops, cudaStream_t st);
+
 // ChEES cross-chain statistics (chees.cu): out[0] harmonic mean of the
 // acceptance probabilities, out[1] the trajectory-length gradient, out[2]
 // the α² gradient (0 without D); work holds chees_workspace_bytes(C, d)

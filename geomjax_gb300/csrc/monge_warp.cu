@@ -270,8 +270,12 @@ __device__ __forceinline__ float warp_incl_rscan(float x, int lane) {
   return x;
 }
 
+// three 256-thread CTAs per SM (at most 85 registers a thread): the kernel
+// is bound by the latency of its warp reductions, and 24 warps per SM hide
+// it better than 16 (D = 100 ran 0.28 ms per transition at 80 registers,
+// 0.36 ms at the 120 the compiler picks unbounded)
 template <int E>
-__global__ void __launch_bounds__(256) monge_warp_kernel(TargetDev t, StepDev sp, float* pos,
+__global__ void __launch_bounds__(256, 3) monge_warp_kernel(TargetDev t, StepDev sp, float* pos,
                                                          float* grad, double* logdens, double* vol,
                                                          const float* z, const double* uacc,
                                                          InfoDev<float> info, int C) {

@@ -272,6 +272,14 @@ int32_t gj_nuts_step(gj_ctx* ctx, const gj_nuts_params* params, gj_chain_state* 
  * + d² for an energy evaluation), out[7] their GPU time in nanoseconds
  * (profiling on).  Returns the number written (<= n, at most 8).  No counterpart in the reference (measurement only). */
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n);
+/* FMA throughput of this device's CUDA cores, in TFLOP/s (2 flops per FMA):
+ * float64 for GJ_FP64, float32 for GJ_MIXED.  Eight independent FMA chains
+ * per thread, 2048 threads per SM, timed with CUDA events on `stream`
+ * (allocates a scratch buffer and synchronises).  The roofline denominator
+ * of the FP64 metric factorisation and of the FP32 Monge kernel; no
+ * counterpart in the reference (measurement only). */
+int32_t gj_fma_peak(int32_t precision, double* tflops, void* stream);
+
 /* 1 = bracket every GEMM launch with CUDA events so gj_stats reports their
  * GPU time (the step then synchronises at its end); 0 = off (default).
  * No counterpart in the reference (measurement only). */

@@ -75,3 +75,18 @@ def test_gemm_tcgen05(M, N, K, planes):
     exact = A.double() @ B.double().T
     # three planes: FP32-exact operands, the error is the FP32 accumulation
     assert torch.max((D - exact).abs() / scale).item() < (1e-4 if planes == 2 else 4e-6)
+
+
+def test_fma_peak_plausible():
+    """gj_fma_peak: FP32 FMA throughput tens of TFLOP/s, FP64 about 1/64 of
+    it on GB300 (nominal 1.25 TFLOP/s)."""
+    import ctypes
+
+    from geomjax_gb300 import _lib as L
+
+    v32, v64 = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    assert L.lib().gj_fma_peak(L.GJ_MIXED, ctypes.byref(v32), None) == L.GJ_OK
+    assert L.lib().gj_fma_peak(L.GJ_FP64, ctypes.byref(v64), None) == L.GJ_OK
+    assert 20.0 < v32.value < 200.0, v32.value
+    assert 0.2 < v64.value < 5.0, v64.value
+    assert v64.value < v32.value / 8
