@@ -9,6 +9,10 @@ Restates the reference's Stan-style warm-up:
 * ``window_adaptation`` (``window_adaptation.py:245-357``) and
   ``step_size_adaptation`` (``adaptation/step_size_adaptation.py:100-203``).
 
+The adaptation loops drive the static-length samplers (``rmhmc``, ``lmc``,
+``lmcmonge``) and the NUTS samplers (``nutsrmhmc``, ``nutslmc``,
+``nutslmcmonge``), each through its own kernel signature.
+
 Batching: the reference adapts one chain (users vmap it).  Here all chains
 of a context share one step size (the kernels take a scalar step size): the
 dual-averaging statistic is the mean acceptance probability over chains and
@@ -127,21 +131,52 @@ def build_schedule(num_steps: int, initial_buffer_size=75, final_buffer_size=50,
     return schedule
 
 
-def _kernel_and_init(algorithm):
+def _stepper(algorithm, extra):
+    """(step(gen, state, target, step_size, inverse_mass), init, adapts the
+    mass) for a static-length sampler (extra: num_integration_steps, alpha2
+    for lmcmonge) or a NUTS sampler (extra: max_num_doublings, alpha2 for
+    nutslmcmonge), each called with its own kernel signature."""
+    from .nuts import nutslmc, nutslmcmonge, nutsrmhmc
+
     if algorithm is rmhmc or algorithm is lmc or algorithm is lmcmonge:
-        return algorithm.build_kernel(), algorithm.init
-    raise ValueError("algorithm must be geomjax_gb300.rmhmc, lmc or lmcmonge")
+        kernel = algorithm.build_kernel()
+        L = int(extra["num_integration_steps"])
+        monge = algorithm is lmcmonge
+
+        def step(gen, state, target, h, inv_mass):
+            kw = dict(alpha2=extra.get("alpha2", 0.001), inverse_mass_matrix=inv_mass) if monge \
+                else {}
+            return kernel(gen, state, target, h, L, **kw)
+
+        return step, algorithm.init, monge
+    if algorithm is nutsrmhmc or algorithm is nutslmc:
+        kernel = algorithm.build_kernel()
+        M = int(extra.get("max_num_doublings", 10))
+
+        def step(gen, state, target, h, inv_mass):
+            return kernel(gen, state, target, h, M)
+
+        return step, algorithm.init, False
+    if algorithm is nutslmcmonge:
+        kernel = algorithm.build_kernel(max_num_doublings=int(extra.get("max_num_doublings", 10)))
+
+        def step(gen, state, target, h, inv_mass):
+            return kernel(gen, state, target, h, inv_mass, extra.get("alpha2", 0.001))
+
+        return step, algorithm.init, True
+    raise ValueError("algorithm must be one of geomjax_gb300's rmhmc, lmc, lmcmonge, nutsrmhmc, "
+                     "nutslmc, nutslmcmonge")
 
 
 def window_adaptation(algorithm, target, is_mass_matrix_diagonal=True, initial_step_size=1.0,
                       target_acceptance_rate=0.80, progress_bar=False, **extra_parameters):
-    """window_adaptation.py:245-357.  ``extra_parameters``: at least
-    ``num_integration_steps``; ``alpha2`` for lmcmonge."""
-    kernel, init = _kernel_and_init(algorithm)
-    adapt_mass = algorithm is lmcmonge
+    """window_adaptation.py:245-357.  ``extra_parameters``: for the static
+    samplers ``num_integration_steps``, for NUTS ``max_num_doublings``
+    (default 10); ``alpha2`` for the Monge samplers, whose diagonal inverse
+    mass matrix is adapted too."""
+    kstep, init, adapt_mass = _stepper(algorithm, extra_parameters)
     if adapt_mass and not is_mass_matrix_diagonal:
         raise ValueError("the Monge metric takes a diagonal inverse mass matrix")
-    L = int(extra_parameters.pop("num_integration_steps"))
 
     def run(rng_key, position, num_steps: int = 1000):
         gen = rng_key if isinstance(rng_key, torch.Generator) else \
@@ -154,9 +189,7 @@ def window_adaptation(algorithm, target, is_mass_matrix_diagonal=True, initial_s
         inv_mass = torch.ones(d, dtype=target.dtype, device=target.device)
         infos = []
         for stage, is_end in build_schedule(num_steps):
-            kw = dict(alpha2=extra_parameters.get("alpha2", 0.001),
-                      inverse_mass_matrix=inv_mass) if adapt_mass else {}
-            state, info = kernel(gen, state, target, step_size, L, **kw)
+            state, info = kstep(gen, state, target, step_size, inv_mass)
             acc = float(info.acceptance_rate.mean().item())
             infos.append(acc)
             if stage == 1 and adapt_mass:
@@ -169,8 +202,7 @@ def window_adaptation(algorithm, target, is_mass_matrix_diagonal=True, initial_s
                     wf = welford_init(d, True, target.device)
                 da = dual_averaging_init(math.exp(da.log_step_size_avg))
                 step_size = math.exp(da.log_step_size)
-        params = {"step_size": math.exp(da.log_step_size_avg), "num_integration_steps": L,
-                  **extra_parameters}
+        params = {"step_size": math.exp(da.log_step_size_avg), **extra_parameters}
         if adapt_mass:
             params["inverse_mass_matrix"] = inv_mass
         return AdaptationResults(state, params), infos
@@ -180,9 +212,11 @@ def window_adaptation(algorithm, target, is_mass_matrix_diagonal=True, initial_s
 
 def step_size_adaptation(algorithm, target, initial_step_size=1.0, target_acceptance_rate=0.80,
                          progress_bar=False, lower_bound=1e-3, **extra_parameters):
-    """adaptation/step_size_adaptation.py:100-203."""
-    kernel, init = _kernel_and_init(algorithm)
-    L = int(extra_parameters.pop("num_integration_steps"))
+    """adaptation/step_size_adaptation.py:100-203 (``extra_parameters`` as
+    for ``window_adaptation``; the Monge samplers use the given
+    ``inverse_mass_matrix``, ones by default)."""
+    kstep, init, _ = _stepper(algorithm, extra_parameters)
+    im0 = extra_parameters.get("inverse_mass_matrix")
 
     def run(rng_key, position, num_steps: int = 1000):
         gen = rng_key if isinstance(rng_key, torch.Generator) else \
@@ -191,14 +225,16 @@ def step_size_adaptation(algorithm, target, initial_step_size=1.0, target_accept
         da = dual_averaging_init(initial_step_size)
         step_size = initial_step_size
         infos = []
+        inv_mass = (torch.ones(target.dim, dtype=target.dtype, device=target.device) if im0 is None
+                    else torch.as_tensor(im0).to(device=target.device, dtype=target.dtype))
         for _ in range(num_steps):
-            state, info = kernel(gen, state, target, step_size, L, **extra_parameters)
+            state, info = kstep(gen, state, target, step_size, inv_mass)
             acc = float(info.acceptance_rate.mean().item())
             infos.append(acc)
             da = dual_averaging_update(da, target_acceptance_rate - acc)
             step_size = math.exp(da.log_step_size)
         params = {"step_size": max(math.exp(da.log_step_size_avg), lower_bound),
-                  "num_integration_steps": L, **extra_parameters}
+                  **extra_parameters}
         return AdaptationResults(state, params), infos
 
     return AdaptationAlgorithm(run)

@@ -110,3 +110,27 @@ def test_step_size_adaptation_rmhmc_logreg():
     (state, params), infos = ssa.run(5, torch.zeros(256, 6), num_steps=60)
     assert 0.02 < params["step_size"] < 2.0
     assert abs(np.mean(infos[-20:]) - 0.8) < 0.15
+
+
+@pytest.mark.parametrize("alg", ["nutsrmhmc", "nutslmcmonge"])
+def test_window_adaptation_nuts(alg):
+    """window_adaptation drives the NUTS samplers (the Monge one adapts its
+    inverse mass too); the adapted step size keeps NUTS's mean acceptance
+    statistic near the target."""
+    import geomjax_gb300 as gj
+    from geomjax_gb300.adaptation import window_adaptation
+
+    algorithm = getattr(gj, alg)
+    if alg == "nutsrmhmc":
+        tg = gj.funnel(D=2, precision="fp64")
+        extra = dict(max_num_doublings=6)
+    else:
+        tg = gj.funnel(D=10, precision="mixed")
+        extra = dict(max_num_doublings=6, alpha2=1.0)
+    wa = window_adaptation(algorithm, tg, initial_step_size=0.1, target_acceptance_rate=0.8,
+                           **extra)
+    (state, params), infos = wa.run(4, torch.zeros(256, tg.dim), num_steps=150)
+    assert params["step_size"] > 0 and params["max_num_doublings"] == 6
+    if alg == "nutslmcmonge":
+        assert torch.all(params["inverse_mass_matrix"] > 0)
+    assert 0.55 < np.mean(infos[-40:]) < 0.97, np.mean(infos[-40:])
