@@ -118,6 +118,23 @@ def test_argument_checks_without_gpu():
                                            None) == L.GJ_EINVAL
     assert lib.gj_logreg_gl_transition_jvp(ctypes.byref(tl), 1, 1, 1, 0.1, 0.5, 1, 0, 2, 1, 1,
                                            None) == L.GJ_EINVAL
+    # NUTS: host checks on a context (no GPU touched before the launch)
+    np_ = L.GjNutsParams(0.1, 17, 0, 0, 100, 1e-6, 1000.0, 0.0, None, 0, 0)
+    st4 = L.GjChainState(1, 1, 1, None, 4)
+    assert lib.gj_nuts_step(None, ctypes.byref(np_), ctypes.byref(st4), 1, 1, 10**6, None,
+                            None) == L.GJ_EINVAL
+    assert lib.gj_nuts_step(h, ctypes.byref(np_), ctypes.byref(st4), 1, 1, 10**6, None,
+                            None) == L.GJ_EINVAL  # 17 doublings
+    np_.max_num_doublings = 4
+    np_.criterion = 3
+    assert lib.gj_nuts_step(h, ctypes.byref(np_), ctypes.byref(st4), 1, 1, 100, None,
+                            None) == L.GJ_EINVAL
+    np_.criterion = 0
+    assert lib.gj_nuts_step(h, ctypes.byref(np_), ctypes.byref(st4), 1, 1, 2 * 4 + 15 - 1, None,
+                            None) == L.GJ_EINVAL  # one uniform short
+    assert lib.gj_nuts_step(h, ctypes.byref(np_), ctypes.byref(st4), None, 1, 100, None,
+                            None) == L.GJ_EINVAL
+    assert lib.gj_fma_peak(5, ctypes.byref(ctypes.c_double()), None) == L.GJ_EINVAL
     # the α² derivative of the LMC-Monge proposal: host checks
     pp = L.GjStepParams(0.02, 8, 0, 0, 0.0, 1000.0, 1.0, None, 0, 0)
     assert lib.gj_lmcmonge_alpha2_jvp(None, 0, 4, ctypes.byref(pp), 1, 1, None, 1,

@@ -170,3 +170,19 @@ def test_nuts_argument_checks():
         kern(gj.NUTSDraws(np.zeros((4, 2)), np.zeros((4, 5))), st, dt, 0.1, 3)
     with pytest.raises(ValueError):
         kern(0, st, dt, 0.1, 3, stopping_criterion="x")
+
+
+def test_nuts_lmcmonge_mixed_precision_runs():
+    """The float32 Monge dynamics (D = 20 funnel, α² = 1) through NUTS."""
+    import geomjax_gb300 as gj
+
+    dt = device_target("funnel", "mixed", D=20, metric="diag")
+    alg = gj.nutslmcmonge(dt, 0.05, torch.ones(20, device="cuda"), alpha2=1.0,
+                          max_num_doublings=6)
+    st = alg.init(np.ones((512, 20)))
+    for s in range(3):
+        st, info = alg.step(s, st)
+    assert np.isfinite(_np(st.position)).all()
+    assert np.isfinite(_np(st.volume_adjustment)).all()
+    assert (_np(info.num_integration_steps) >= 1).all()
+    assert 0.0 < _np(info.acceptance_rate).mean() <= 1.0
