@@ -486,6 +486,22 @@ def run_jvp(args, wl):
     t0 = time.perf_counter()
     Jh = AD.transition_jacobian(tg, q0, z, wl["h"], wl["lam"], wl["L"]).cpu()
     e2e_s = time.perf_counter() - t0
+    # roofline: the dual-number Gram assemblies G = XᵀΛX (and its two
+    # tangents), 1 + K_q = 7 per step, each N·d(d+1)/2 terms of one product
+    # and three FMAs (7 FP64 flops): a lower bound on the kernel's
+    # algorithmic FP64 work, against the FP64 FMA throughput measured here
+    N, P = wl["N"], d * (d + 1) // 2
+    grams = wl["L"] * (1 + 6)
+    flops = grams * N * P * 7.0 * C
+    achieved = flops / (dev_s / K) / 1e12
+    p64 = _fma_peak(True)
+    roof = {"bound": "fp64", "kernel": "gl_trajectory_kernel (CTA per chain, Dual<2> float64)",
+            "achieved": round(achieved, 4), "peak": round(p64, 4) if p64 else 1.25,
+            "unit": "TFLOP/s", "frac": round(achieved / (p64 or 1.25), 4),
+            "peak_source": ("measured FP64 FMA throughput (gj_fma_peak)" if p64
+                            else "nominal GB300 FP64 (measurement failed)"),
+            "flops_counted": "Gram assemblies only: L*(1+K_q) * N * d(d+1)/2 * 7 per chain",
+            "traffic": None}
     return {
         "metric": "differentiated leapfrog steps/s (d/dh and d/dlambda, float64 forward mode), 1 GB300",
         "value": round(ws * C * wl["L"] * K / dev_s, 1), "unit": "leapfrog steps/s", "n_gpus": ws,
@@ -499,7 +515,7 @@ def run_jvp(args, wl):
         "mean_p_accept": float(Jh[:, 0].mean()),
         "e2e": {"value": round(ws * C * wl["L"] / e2e_s, 1), "unit": "leapfrog steps/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(Jh.numel() * 8)},
-        "gpu_launches": K, "clocks": clk,
+        "gpu_launches": K, "roofline": roof, "clocks": clk,
     }
 
 
