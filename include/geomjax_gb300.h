@@ -42,7 +42,7 @@
  *                      (adaptation/chees_adaptation_riemanian.py:145-190,
  *                      chees_adaptation_lmcmonge.py:151-236)
  *   gj_gemm_split_bf16, gj_gemm_split_bf16_noalloc, gj_stats, gj_profile,
- *   gj_set_option, gj_set_gemm_tiling
+ *   gj_fma_peak, gj_set_option, gj_set_gemm_tiling
  *                      no reference counterpart: the split-BF16 contraction
  *                      as a test hook, measurement and tuning
  *
