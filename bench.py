@@ -207,6 +207,11 @@ def run_ours(args, wl):
     U = torch.rand(K + W, C, generator=gen, device=dev, dtype=torch.float64)
     info = kern.new_info(C, d, target, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tuned = None
+    if args.autotune and wl["sampler"] == "rmhmc":  # before the warm-up, on a copy of the state
+        res = gj.autotune(kern, target, state, h, Lsteps, transitions=3)
+        tuned = {"best": res.best, "ms_per_transition": round(res.ms_per_transition, 3),
+                 "candidates": len(res.table)}
     # warm-up
     for i in range(W):
         kern.step_inplace(target, state, Z[i], U[i], info, h, Lsteps, **extra)
@@ -340,7 +345,7 @@ def run_ours(args, wl):
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "autotune": tuned},
         "min_ess_per_s": (round(min_ess / dev_s, 2) if K >= 4 else None),
         "min_ess": (round(min_ess, 2) if K >= 4 else None),
         "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
@@ -384,6 +389,12 @@ def run_batch(args, wl):
     U = torch.rand(K + W, B * C, generator=gen, device=dev, dtype=torch.float64)
     info = pb.new_info()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tuned = None
+    if args.autotune:  # a short candidate list: one transition of the batch takes seconds
+        res = gj.autotune_batch(pb, state, h, Lsteps, transitions=1,
+                                tilings=((0, -1), (0, 1), (64, -1)), chol_chains_per_warp=(0, 2))
+        tuned = {"best": res.best, "ms_per_transition": round(res.ms_per_transition, 3),
+                 "candidates": len(res.table)}
     for i in range(W):
         pb.step_inplace(state, Z[i], U[i], info, h, Lsteps)
     torch.cuda.synchronize()
@@ -437,7 +448,7 @@ def run_batch(args, wl):
                    "integration_steps": Lsteps, "step_size": h, "streams": args.streams,
                    "mean_N": float(np.mean(Ns)), "mean_d": float(np.mean(ds)),
                    "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "autotune": tuned},
         "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
         "e2e": {"value": round(ws * B * C * Lsteps * e2e_steps / e2e_s, 1), "unit": "leapfrog steps/s",
                 "h2d_bytes_per_step": int(Zh.numel() * 4 + Uh.numel() * 8),
@@ -731,6 +742,9 @@ def main():
     ap.add_argument("--workload", default="logreg", choices=sorted(WORKLOADS))
     ap.add_argument("--logreg-path", default="tcgen05", choices=["auto", "simt", "tcgen05", "per_chain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the GEMM tile policy and the factorisation's chains per warp by "
+                         "timing the candidates before the warm-up (batched paths)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 per-chain arm")
     ap.add_argument("--chains", type=int, default=None, help="override the chain count (small cases)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],

@@ -22,6 +22,7 @@ from .diagnostics import effective_sample_size, ess, potential_scale_reduction, 
 from .samplers import Kernel, lmc, lmcmonge, rmhmc
 from .targets import funnel, hierarchical_gaussian, logistic_regression
 from .adaptation import gradient_step_size_adaptation, step_size_adaptation, window_adaptation
+from .autotune import autotune, autotune_batch
 from .nuts import NUTSDraws, nutslmc, nutslmcmonge, nutsrmhmc
 from .chees import (adam, chees_adaptation, dynamic_lmc, dynamic_lmcmonge, dynamic_rmhmc,
                     lmcmonge_chees_adaptation)
@@ -33,5 +34,5 @@ __all__ = [
     "potential_scale_reduction", "rhat", "window_adaptation", "step_size_adaptation",
     "gradient_step_size_adaptation", "chees_adaptation", "lmcmonge_chees_adaptation",
     "dynamic_rmhmc", "dynamic_lmc", "dynamic_lmcmonge", "adam", "nutsrmhmc", "nutslmc", "nutslmcmonge",
-    "NUTSDraws",
+    "NUTSDraws", "autotune", "autotune_batch",
 ]

@@ -262,7 +262,9 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     return GJ_OK;
   }
   if (key == GJ_OPT_THREADS_PER_BLOCK) {
-    if (value < 32 || value > 1024 || (value % 32)) return fail(GJ_EINVAL, "bad threads per block");
+    // the per-chain kernels are compiled for at most 128 threads per block
+    if (value < 32 || value > 128 || (value % 32))
+      return fail(GJ_EINVAL, "threads per block must be 32, 64, 96 or 128");
     ctx->tpb = (int)value;
     return GJ_OK;
   }

@@ -194,6 +194,9 @@ cudaError_t gemm_tc_prepare();  // raises the kernel's shared-memory limit (call
 // a deep ring, -1 = automatic.  Takes effect for launches (and graph
 // captures) made after the call.
 void gemm_tc_set_tuning(int bn_wide, int two_ctas);
+// a small integer identifying the current tile policy (part of the key of
+// captured graphs, whose launches keep the tiles they were captured with)
+int gemm_tc_tuning_code();
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
 

@@ -511,6 +511,8 @@ cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOper
 
 }  // namespace
 
+int gemm_tc_tuning_code() { return (g_tune.bn_wide / 64) * 3 + (g_tune.two_ctas + 1); }
+
 void gemm_tc_set_tuning(int bn_wide, int two_ctas) {
   g_tune.bn_wide = (bn_wide == 64 || bn_wide == 128) ? bn_wide : 0;
   g_tune.two_ctas = two_ctas < 0 ? -1 : (two_ctas ? 1 : 0);

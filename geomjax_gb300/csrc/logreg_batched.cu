@@ -1129,7 +1129,9 @@ int graph_fail(const char* what, cudaError_t e) {
 
 constexpr size_t kMaxGraphs = 64;
 
-int graph_cfg(const LogregBatched* lb) { return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl; }
+int graph_cfg(const LogregBatched* lb) {
+  return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl + 512 * gemm_tc_tuning_code();
+}
 
 // Capture one whole transition (all L steps, each fixed-point solve a
 // conditional WHILE node) into *out.  The graph reads and writes the

@@ -212,6 +212,7 @@ int32_t gj_destroy(gj_ctx* ctx);
  * tcgen05 BF16 hi/lo GEMM, 3 = per-chain kernel. */
 int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
 #define GJ_OPT_LOGREG_PATH 1
+/* threads per block of the per-chain kernels: 32, 64, 96 or 128 (default) */
 #define GJ_OPT_THREADS_PER_BLOCK 2
 /* batched path loop driver: 0 = one CUDA-graph launch per transition with
  * conditional WHILE nodes for the fixed-point solves (default), 1 = host
@@ -356,8 +357,9 @@ int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_ch
  * width for N > 64 (0 = automatic per shape, or 64 / 128; narrower N always
  * takes 32 or 64) and whether the operand ring is cut back so that two CTAs
  * share an SM (1), kept up to three stages (0) or chosen per shape (-1,
- * default).  Applies to launches and CUDA-graph captures made after the
- * call (a context's captured graph keeps its tiles). */
+ * default).  Applies to the launches made after the call; a context keeps
+ * one captured graph per policy, so changing it (as the autotuner of
+ * geomjax_gb300.autotune does) captures anew. */
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm);
 
 /* Derivatives of one RMHMC transition with the generalized leapfrog, for a

@@ -82,6 +82,8 @@ def test_argument_checks_without_gpu():
     for v in (0, 1, 2, 4, 8):
         assert lib.gj_set_option(h, L.GJ_OPT_CHOL_CHAINS_PER_WARP, v) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 9) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_THREADS_PER_BLOCK, 256) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_THREADS_PER_BLOCK, 64) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_PDL, 2) == L.GJ_EINVAL
     assert lib.gj_set_option(h, L.GJ_OPT_PDL, 0) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 2) == L.GJ_OK
