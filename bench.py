@@ -2,11 +2,14 @@
 
 Workload (default, ``--workload logreg``): Bayesian logistic regression,
 X ∈ R^{1000×25} iid N(0,1) float32, β* ~ N(0, I), y ~ Bernoulli(σ(Xβ*)),
-prior N(0, 100·I), RMHMC (implicit midpoint, fixed-point tol 1e-6, at most
-100 iterations) with the Fisher metric XᵀΛX + I/100, 4096 chains, 8 steps of
-0.05 per transition, mixed precision (FP32 state, split-BF16 tcgen05
-contractions, FP64 Cholesky / log det / accept).  Synthetic seeded data;
-the reference publishes no dataset for this path.
+prior N(0, 100·I), RMHMC with the generalized leapfrog (implicit momentum
+and position fixed-point half-steps, explicit final momentum step;
+fixed-point tol 1e-6, at most 100 iterations; ``--integrator
+implicit_midpoint`` runs the reference's own integrator instead, on every
+arm) with the Fisher metric XᵀΛX + I/100, 4096 chains, 8 steps of 0.05 per
+transition, mixed precision (FP32 state, split-BF16 tcgen05 contractions,
+FP64 Cholesky / log det / accept).  Synthetic seeded data; the reference
+publishes no dataset for this path.
 
 A "step" is one transition of every chain.  ``value`` = leapfrog steps/s =
 chains × integration steps × timed transitions / device seconds, with the
@@ -182,7 +185,7 @@ def run_ours(args, wl):
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
         kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path, loop=args.loop,
-                                     cholesky=args.cholesky,
+                                     integrator=args.integrator, cholesky=args.cholesky,
                                      chol_chains_per_warp=args.chol_cpw,
                                      chain_groups=args.groups, pdl=args.pdl)
         d = wl["d"]
@@ -340,6 +343,8 @@ def run_ours(args, wl):
         "data": "synthetic (seeded)",
         "config": {"workload": wl["name"], "chains_per_gpu": C, "integration_steps": Lsteps,
                    "step_size": h, "precision": "fp64" if wl["sampler"] == "rmhmc_funnel" else "mixed",
+                   "integrator": (args.integrator if wl["sampler"] == "rmhmc" else
+                                  ("generalized_leapfrog" if wl["sampler"] == "rmhmc_funnel" else None)),
                    "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
@@ -377,7 +382,7 @@ def run_batch(args, wl):
     Ns, ds = uneven_logreg_batch(B, seed=rank)
     t_setup = time.perf_counter()
     data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
-    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev)
+    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev, integrator=args.integrator)
     del data
     g0 = torch.Generator().manual_seed(rank)
     state = pb.init([0.01 * torch.randn(C, int(d), generator=g0) for d in ds])
@@ -546,7 +551,7 @@ def run_plain_fp64(args, wl):
         C = min(wl["C"], 256)
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="fp64", device=dev)
-        kern = gj.rmhmc.build_kernel()
+        kern = gj.rmhmc.build_kernel(integrator=wl["integrator"])
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(0),
@@ -609,7 +614,8 @@ def cpu_baseline(wl, budget_s=12.0):
             q = rng.standard_normal((C, d)) * 0.01
             s = O_rm.init(ot, q)
             t = time.perf_counter()
-            O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
+            O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"],
+                        integrator=wl["integrator"])
             return time.perf_counter() - t
     elif wl["sampler"] == "rmhmc_funnel":
         ot = OT.Funnel(D=wl["D"], metric="diag")
@@ -675,7 +681,8 @@ def run_reference(args, wl):
         s = O_rm.init(ot, rng.standard_normal((C, d)) * 0.01)
 
         def step(s):
-            s2, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"])
+            s2, _ = O_rm.kernel(ot, s, rng.standard_normal((C, d)), rng.random(C), wl["h"], wl["L"],
+                                integrator=wl["integrator"])
             return s2
     elif wl["sampler"] == "batch":
         # a bounded sample of the uneven batch: 8 chains of each of the first
@@ -695,7 +702,7 @@ def run_reference(args, wl):
             out = []
             for ot_i, d_i, s_i in s:
                 s2, _ = O_rm.kernel(ot_i, s_i, rng.standard_normal((8, d_i)), rng.random(8),
-                                    wl["h"], wl["L"])
+                                    wl["h"], wl["L"], integrator=wl["integrator"])
                 out.append((ot_i, d_i, s2))
             return out
 
@@ -723,7 +730,10 @@ def run_reference(args, wl):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)", "impl": "reference",
         "config": {"workload": wl["name"], "chains_sampled": C, "integration_steps": wl["L"],
-                   "step_size": wl["h"]},
+                   "step_size": wl["h"],
+                   "integrator": (wl["integrator"] if wl["sampler"] in ("rmhmc", "batch") else
+                                  ("generalized_leapfrog" if wl["sampler"] == "rmhmc_funnel"
+                                   else None))},
         "cpu_baseline": {"value": round(v, 2), "unit": "leapfrog steps/s", "cores": cores,
                          "kind": "port",
                          "sample": f"{C} chains per step (JAX reference not installable; float64 "
@@ -742,6 +752,9 @@ def main():
     ap.add_argument("--workload", default="logreg", choices=sorted(WORKLOADS))
     ap.add_argument("--logreg-path", default="tcgen05", choices=["auto", "simt", "tcgen05", "per_chain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--integrator", default="generalized_leapfrog",
+                    choices=["implicit_midpoint", "generalized_leapfrog"],
+                    help="RMHMC integrator of the logistic-regression workloads")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the GEMM tile policy and the factorisation's chains per warp by "
                          "timing the candidates before the warm-up (batched paths)")
@@ -766,6 +779,7 @@ def main():
                     help="chains per warp in the metric factorisation (0 = automatic)")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
+    wl["integrator"] = args.integrator  # the logistic-regression workloads' RMHMC integrator
     if args.chains:
         wl["C"] = args.chains
         wl["name"] = wl["name"].rsplit("_", 1)[0] + f"_{args.chains}chains"

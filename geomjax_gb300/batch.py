@@ -48,11 +48,13 @@ class BatchInfo(NamedTuple):
 
 class PosteriorBatch:
     """B logistic-regression posteriors ``datasets = [(X_b, y_b), ...]``,
-    ``chains`` RMHMC chains each (implicit midpoint, mixed precision)."""
+    ``chains`` RMHMC chains each (mixed precision; ``integrator``
+    "implicit_midpoint", the reference's, or "generalized_leapfrog")."""
 
     def __init__(self, datasets: Sequence, chains: int, prior_var: float = 100.0,
                  num_streams: int = 16, max_iters: int = 100, tol: float = 1e-6,
-                 divergence_threshold: float = 1000.0, device="cuda"):
+                 divergence_threshold: float = 1000.0, device="cuda",
+                 integrator: str = "implicit_midpoint"):
         self.lib = L.lib()
         self.device = torch.device(device)
         self.targets = [logistic_regression(X, y, prior_var=prior_var, precision="mixed",
@@ -62,6 +64,8 @@ class PosteriorBatch:
         self.dims = [t.dim for t in self.targets]
         self.offsets = np.concatenate([[0], np.cumsum([self.C * d for d in self.dims])])
         self.max_iters, self.tol = int(max_iters), float(tol)
+        self.integrator = {"implicit_midpoint": L.GJ_IMPLICIT_MIDPOINT,
+                           "generalized_leapfrog": L.GJ_GENERALIZED_LEAPFROG}[integrator]
         self.divergence_threshold = float(divergence_threshold)
         descs = (L.GjTarget * self.B)(*(t.descriptor() for t in self.targets))
         self._descs = descs
@@ -132,7 +136,7 @@ class PosteriorBatch:
         p = L.GjStepParams()
         p.step_size = float(step_size)
         p.num_integration_steps = int(num_integration_steps)
-        p.integrator = L.GJ_IMPLICIT_MIDPOINT
+        p.integrator = self.integrator
         p.max_iters = self.max_iters
         p.tol = self.tol
         p.divergence_threshold = self.divergence_threshold

@@ -305,8 +305,6 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
   // dense-Fisher logistic regression in mixed precision: batched pipeline
   if (ctx->precision == GJ_MIXED && t.family == GJ_LOGREG && t.metric == GJ_METRIC_DENSE_FISHER &&
       ctx->logreg_path != 3) {
-    if (p->integrator != GJ_IMPLICIT_MIDPOINT)
-      return fail(GJ_ENOTSUP, "the batched logistic-regression path implements the implicit midpoint");
     int rc = ensure_groups(ctx, t);
     if (rc) return rc;
     const int gemm = (ctx->logreg_path == 1) ? 1 : 2;
@@ -767,8 +765,8 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
   if (!st) st = check_state(s, b->B * b->C, false);
   if (st) return st;
   if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
-  if (p->integrator != GJ_IMPLICIT_MIDPOINT)
-    return fail(GJ_ENOTSUP, "the batched logistic-regression path implements the implicit midpoint");
+  if (p->integrator != GJ_IMPLICIT_MIDPOINT && p->integrator != GJ_GENERALIZED_LEAPFROG)
+    return fail(GJ_EINVAL, "bad integrator");
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const gj::InfoDev<float> inf = gj::to_dev<float>(info);

@@ -15,7 +15,7 @@ namespace gj {
 
 using bf16 = __nv_bfloat16;
 
-enum EpiMode : int { EPI_STORE = 0, EPI_SIGMOID = 1, EPI_TRACE = 2 };
+enum EpiMode : int { EPI_STORE = 0, EPI_SIGMOID = 1, EPI_TRACE = 2, EPI_R2W = 3 };
 
 // A split BF16 matrix, `rows` x `kdim`, as `planes` BF16 planes whose sum is
 // the value: x0 = bf16(x), x1 = bf16(x − x0) and, with three planes,
@@ -62,6 +62,12 @@ struct Epi {
   int r_off;
   // EPI_SIGMOID, when set: ld_acc[m] += Σ_n [y_n a − log(1 + e^a)] (FP64 sum)
   double* ld_acc;
+  // EPI_TRACE, when set: w is also stored into w_out[m, n] (stride s_ld)
+  float* w_out;
+  // EPI_R2W: a = s = x_nᵀu_m  ->  r2 = Λ'(w − s²) into r (rows r_off + m),
+  // w read from W[m, n] (stride s_ld): the momentum-only re-evaluation of
+  // the generalized leapfrog, where w = x_nᵀG⁻¹x_n is fixed
+  const float* W;
 };
 
 __device__ __forceinline__ float softplus(float a) {
@@ -78,9 +84,14 @@ __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
     split_store(e.lam, m, n, lam);
     e.lp[(size_t)m * e.lp_ld + n] = lam * (1.f - 2.f * sg);
     split_store(e.r, m, n, e.y[n] - sg);
-  } else {
+  } else if (e.mode == EPI_TRACE) {
     const float s = e.S[(size_t)m * e.s_ld + n];
     const float r2 = e.lp[(size_t)m * e.lp_ld + n] * (v - s * s);
+    split_store(e.r, e.r_off + m, n, r2);
+    if (e.w_out) e.w_out[(size_t)m * e.s_ld + n] = v;
+  } else {  // EPI_R2W
+    const float w = e.W[(size_t)m * e.s_ld + n];
+    const float r2 = e.lp[(size_t)m * e.lp_ld + n] * (w - v * v);
     split_store(e.r, e.r_off + m, n, r2);
   }
 }
@@ -106,64 +117,6 @@ __device__ __forceinline__ void split_store8(const SplitMat& s, int r, int k, co
   if (s.planes == 3)
     *reinterpret_cast<uint4*>(s.p + (size_t)(2 * s.rpad + r) * s.ld + k) =
         make_uint4(w2[0], w2[1], w2[2], w2[3]);
-}
-
-// Columns n0 .. n0+31 of row m (one tcgen05.ld chunk): vector loads/stores
-// when the chunk is complete and the row strides allow 16-byte access,
-// element-wise otherwise.
-__device__ __forceinline__ void epi_row32(const Epi& e, int m, int n0, int N, const float* v) {
-  const bool full = n0 + 32 <= N;
-  if (e.mode == EPI_SIGMOID && e.ld_acc) {
-    double acc = 0.0;
-    for (int j = 0; j < 32; ++j)
-      if (n0 + j < N) acc += double(e.y[n0 + j] * v[j] - softplus(v[j]));
-    atomicAdd(&e.ld_acc[m], acc);
-    Epi e2 = e;
-    e2.ld_acc = nullptr;
-    epi_row32(e2, m, n0, N, v);
-    return;
-  }
-  if (!full || (e.mode == EPI_STORE && (e.ldd & 3)) ||
-      (e.mode != EPI_STORE && ((e.lp_ld & 3) || (e.mode == EPI_TRACE && (e.s_ld & 3))))) {
-    for (int j = 0; j < 32; ++j)
-      if (n0 + j < N) epi_apply(e, m, n0 + j, v[j]);
-    return;
-  }
-  if (e.mode == EPI_STORE) {
-    float4* dst = reinterpret_cast<float4*>(e.D + (size_t)m * e.ldd + n0);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-  } else if (e.mode == EPI_SIGMOID) {
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-      float lam[8], lp[8], r1[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float sg = 1.f / (1.f + __expf(-v[8 * g + j]));
-        lam[j] = sg * (1.f - sg);
-        lp[j] = lam[j] * (1.f - 2.f * sg);
-        r1[j] = e.y[n0 + 8 * g + j] - sg;
-      }
-      split_store8(e.lam, m, n0 + 8 * g, lam);
-      split_store8(e.r, m, n0 + 8 * g, r1);
-      float4* lpd = reinterpret_cast<float4*>(e.lp + (size_t)m * e.lp_ld + n0 + 8 * g);
-      lpd[0] = make_float4(lp[0], lp[1], lp[2], lp[3]);
-      lpd[1] = make_float4(lp[4], lp[5], lp[6], lp[7]);
-    }
-  } else {
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-      const float4* sp = reinterpret_cast<const float4*>(e.S + (size_t)m * e.s_ld + n0 + 8 * g);
-      const float4* lpp = reinterpret_cast<const float4*>(e.lp + (size_t)m * e.lp_ld + n0 + 8 * g);
-      const float4 s0 = sp[0], s1 = sp[1], l0 = lpp[0], l1 = lpp[1];
-      const float sv[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
-      const float lv[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
-      float r2[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) r2[j] = lv[j] * (v[8 * g + j] - sv[j] * sv[j]);
-      split_store8(e.r, e.r_off + m, n0 + 8 * g, r2);
-    }
-  }
 }
 
 struct GemmArgs {

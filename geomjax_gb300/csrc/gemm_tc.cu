@@ -234,8 +234,18 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
         ld += __shfl_xor_sync(0xffffffffu, ld, 2);
         if ((lane & 3) == 0 && m < M) atomicAdd(&e.ld_acc[m], ld);
       }
+    } else if (e.mode == EPI_R2W) {  // a = s: r2 = Λ'(w − s²) with w stored
+      if (m < M) {
+        float wv[8], lv[8], r2[8];
+        load8(e.W + (size_t)m * e.s_ld + n, n, N, full && aligned16(e.W, e.s_ld), wv);
+        load8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r2[k] = lv[k] * (wv[k] - a[k] * a[k]);
+        split8(e.r, e.r_off + m, n, N, full, r2);
+      }
     } else {  // EPI_TRACE: r2 = Λ'(w − s²)
       if (m < M) {
+        if (e.w_out) store8(e.w_out + (size_t)m * e.s_ld + n, n, N, full && aligned16(e.w_out, e.s_ld), a);
         float sv[8], lv[8], r2[8];
         load8(e.S + (size_t)m * e.s_ld + n, n, N, full && aligned16(e.S, e.s_ld), sv);
         load8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lv);

@@ -42,7 +42,14 @@ thread_local std::string g_err;
 inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
 
 enum CholMode : int { CH_DRAW = 0, CH_EVAL = 1, CH_ENERGY = 2 };
-enum UpdMode : int { UP_FP0 = 0, UP_FPN = 1, UP_EXPLICIT = 2 };
+// implicit midpoint: the eager and the iterated map evaluation, the explicit
+// half step; generalized leapfrog: the momentum solve (eager, iterated), the
+// position solve (eager, iterated), the explicit final momentum
+enum UpdMode : int {
+  UP_FP0 = 0, UP_FPN = 1, UP_EXPLICIT = 2,
+  UP_GLP0 = 3, UP_GLPN = 4, UP_GLQ0 = 5, UP_GLQN = 6, UP_GLPX = 7
+};
+__host__ __device__ inline bool upd_iterated(int m) { return m == UP_FPN || m == UP_GLPN || m == UP_GLQN; }
 
 // ---------------------------------------------------------------------------
 // constants: X and Z = vech(x xᵀ) as split-BF16 planes
@@ -90,6 +97,8 @@ struct CholArgs {
   uint8_t* bad;        // [C] non-SPD flag (sticky)
   float* mom_info;     // DRAW: info.momentum (may be NULL)
   float* vel_info;     // ENERGY: the proposal velocity −G⁻¹p (may be NULL)
+  double* Lout;        // DRAW / EVAL: the packed factor, kept for later solves (may be NULL)
+  int no_inverse;      // EVAL: stop after u = G⁻¹p (no L⁻¹, no packed G⁻¹)
 };
 
 // Chain packing.  The FP64 pipe issues one warp instruction for all 32 lanes
@@ -315,6 +324,14 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
   }
+  if (a.Lout && live) {  // the factor at this position serves the momentum solves,
+    // with 1/L_jj in place of the diagonal (the solves multiply by it)
+    for (int t = sl; t < P; t += LPC) {
+      const uint32_t ik = tab[t];
+      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+      a.Lout[(size_t)c * P + t] = i == k ? double(rdiag[i]) : double(L[t]);
+    }
+  }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
   // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
@@ -369,6 +386,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       split_store(a.Ub, c, i, float(xv[i]));
     }
   }
+  if (a.no_inverse) return;  // uniform: the position solve needs u only
   // L⁻¹ in FP32 by forward substitution of the identity, all columns at
   // once: row k is final once scaled, then rows i > k are reduced by it
   for (int t = sl; t < P; t += LPC) {
@@ -460,6 +478,7 @@ struct UpdArgs {
   const float* Gout;  // [2C, ldo]
   int ldo;
   const double* u;
+  const double* u0;           // generalized leapfrog: G(q0)⁻¹p½
   double *q0, *p0, *qc, *pc;  // FP64 fixed-point iterates
   float* qf;                  // FP32 copy of the position after each step
   double* norm;
@@ -479,6 +498,64 @@ __global__ void update_kernel(UpdArgs a) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   bool act = false;
+  if (a.mode >= UP_GLP0) {  // generalized leapfrog (grid-uniform)
+    if (c < a.C && !(upd_iterated(a.mode) && !a.active[c])) {  // warp-uniform
+      const int d = a.d;
+      const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
+      const double tol = a.spd ? a.spd->tol : a.tol;
+      const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
+      double nrm = 0.0;
+      bool nan = false;
+      for (int i = lane; i < d; i += 32) {
+        const size_t o = (size_t)c * d + i;
+        const double q = a.qc[o];
+        if (a.mode == UP_GLQ0 || a.mode == UP_GLQN) {
+          // q' = q0 + h/2 [G⁻¹(q0) + G⁻¹(q_k)] p½; the eager map uses q_k = q0
+          const double uk = a.mode == UP_GLQ0 ? a.u0[o] : a.u[o];
+          const double qn = a.q0[o] + hh * (a.u0[o] + uk);
+          const double e = qn - q;
+          nan |= isnan(e);
+          nrm = fmax(nrm, fabs(e));
+          a.qc[o] = qn;
+          split_store(a.Qb, c, i, float(qn));
+        } else {
+          // ∂_qH = ∂_qK − ∇ℓ at the current position
+          const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
+          const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
+          if (a.mode == UP_GLPX) {  // p' = p½ − h/2 ∂_qH(q', p½)
+            const double pn = a.pc[o] - hh * (dK - g);
+            a.pc[o] = pn;
+            a.p0[o] = pn;
+            a.q0[o] = q;
+            a.qf[o] = float(q);
+          } else {  // p½ = p0 − h/2 ∂_qH(q0, p_k)
+            const double pn = a.p0[o] - hh * (dK - g);
+            const double e = pn - a.pc[o];
+            nan |= isnan(e);
+            nrm = fmax(nrm, fabs(e));
+            a.pc[o] = pn;
+          }
+        }
+      }
+      if (a.mode != UP_GLPX) {
+        nrm = warp_max(nrm);
+        nan = __any_sync(0xffffffffu, nan);
+        if (nan) nrm = NAN;
+        const int it = upd_iterated(a.mode) ? a.iters[c] + 1 : 0;
+        act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
+        if (lane == 0) {
+          a.iters[c] = it;
+          a.norm[c] = nrm;
+          a.active[c] = act;
+          if (upd_iterated(a.mode)) a.iters_total[c] += 1;
+          if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
+        }
+      }
+    }
+    if (a.mode == UP_GLPX) return;
+    if (__syncthreads_or(act) && threadIdx.x == 0) *a.n_active = 1;
+    return;
+  }
   if (c < a.C && !(a.mode == UP_FPN && !a.active[c])) {  // warp-uniform
     const int d = a.d;
     const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
@@ -524,6 +601,71 @@ __global__ void update_kernel(UpdArgs a) {
   }
   if (a.mode == UP_EXPLICIT) return;  // uniform over the grid
   if (__syncthreads_or(act) && threadIdx.x == 0) *a.n_active = 1;
+}
+
+// u = G⁻¹·rhs with a stored factor (packed column-major lower, L(i, k) at
+// colstart(k) + i − k, the diagonal holding 1/L_jj): forward then backward
+// substitution, both column-oriented (no reductions: each step broadcasts
+// one solved component and the lanes update their rows), one warp per chain
+// with lanes over rows (E slots: d <= 32·E).  FP64 divisions and FP64 warp
+// reductions cost tens of FP64 instructions each on this part, so neither
+// appears here.  Inactive chains (active set, flag 0) are skipped.
+template <int E>
+__global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const double* __restrict__ Lf,
+                                                    const double* __restrict__ rhs, double* u,
+                                                    SplitMat Ub, int split, const uint8_t* active) {
+  pdl_wait();
+  const int lane = threadIdx.x & 31;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= C || (active && !active[c])) return;  // warp-uniform
+  const double* Lc = Lf + (size_t)c * P;
+  auto get = [&](const double(&v)[E], int j) {
+    double x = 0.0;
+#pragma unroll
+    for (int k = 0; k < E; ++k)
+      if (k == (j >> 5)) x = v[k];
+    return __shfl_sync(0xffffffffu, x, j & 31);
+  };
+  double y[E], x[E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = lane + 32 * k;
+    y[k] = i < d ? rhs[(size_t)c * d + i] : 0.0;
+    x[k] = 0.0;
+  }
+  int cj = 0;  // colstart(j)
+  for (int j = 0; j < d; ++j) {  // L y = rhs, column j eliminated from the rows below
+    const double yj = get(y, j) * Lc[cj];
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = lane + 32 * k;
+      if (i == j) y[k] = yj;
+      else if (i > j && i < d) y[k] -= Lc[cj + i - j] * yj;
+    }
+    cj += d - j;
+  }
+  // Lᵀ x = y: x_j final once rows below are done; then row j of L (L(j, i),
+  // i < j, at colstart(i) + j − i) updates the components above
+#pragma unroll
+  for (int k = 0; k < E; ++k) x[k] = y[k];
+  for (int j = d - 1; j >= 0; --j) {
+    cj -= d - j;
+    const double xj = get(x, j) * Lc[cj];
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = lane + 32 * k;
+      if (i == j) x[k] = xj;
+      else if (i < j) x[k] -= Lc[i * d - i * (i - 1) / 2 + j - i] * xj;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = lane + 32 * k;
+    if (i < d) {
+      u[(size_t)c * d + i] = x[k];
+      if (split) split_store(Ub, c, i, float(x[k]));
+    }
+  }
 }
 
 __global__ void begin_kernel(int C, int d, const float* pos, double* q0, double* qc, float* qf,
@@ -621,6 +763,10 @@ struct LogregBatched {
   double *q0, *p0, *qc, *pc;
   float *qf, *gnew;
   double *u, *norm, *logdet0, *quad0, *logdet1, *quad1, *ldnew;
+  // generalized leapfrog (allocated on first use): the factor and
+  // w = x_nᵀG⁻¹x_n at the step's start position, and G(q0)⁻¹p½
+  double *Lf, *u0;
+  float* W;
   int *iters, *iters_total, *n_active_d;
   int* n_active_h;  // pinned
   uint8_t *active, *notconv, *bad;
@@ -899,7 +1045,8 @@ struct Runner {
   }
 
   void chol(int mode, const float* z, double* logdet, double* quad, float* mom_info,
-            bool only_active = false, float* vel_info = nullptr) {
+            bool only_active = false, float* vel_info = nullptr, double* Lout = nullptr,
+            bool no_inverse = false) {
     LogregBatched& L = *lb;
     CholArgs a{};
     a.mode = mode;
@@ -921,6 +1068,8 @@ struct Runner {
     a.bad = L.bad;
     a.mom_info = mom_info;
     a.vel_info = vel_info;
+    a.Lout = Lout;
+    a.no_inverse = no_inverse ? 1 : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (L.prof) {
       while (L.cev.size() < L.cev_used + 2) {
@@ -950,7 +1099,7 @@ struct Runner {
   }
 
   // (4)-(6) after the factorisation
-  void trace_grad() {
+  void trace_grad(float* w_out = nullptr) {
     LogregBatched& L = *lb;
     Epi s{};
     s.mode = EPI_STORE;
@@ -959,6 +1108,7 @@ struct Runner {
     gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
     Epi w{};
     w.mode = EPI_TRACE;
+    w.w_out = w_out;
     w.S = L.S;
     w.s_ld = L.Npad;
     w.lp = L.Lp;
@@ -971,6 +1121,67 @@ struct Runner {
     o.D = L.Gout;
     o.ldd = L.dpad;
     gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
+  }
+
+  // ---- generalized leapfrog (Girolami and Calderhead 2011, eqs. 16-18)
+  // out = G⁻¹·rhs with the factor stored at the step's start position
+  void solve(const double* rhs, double* out, bool split, bool only_active) {
+    LogregBatched& L = *lb;
+    const dim3 grid((unsigned)(((size_t)L.C * 32 + 255) / 256)), th(256);
+    const uint8_t* act = only_active ? L.active : nullptr;
+    if (L.d <= 32)
+      check(launch_k(L.pdl, solve_kernel<1>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
+                     rhs, out, L.Ub, split ? 1 : 0, act));
+    else if (L.d <= 64)
+      check(launch_k(L.pdl, solve_kernel<2>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
+                     rhs, out, L.Ub, split ? 1 : 0, act));
+    else
+      check(launch_k(L.pdl, solve_kernel<4>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
+                     rhs, out, L.Ub, split ? 1 : 0, act));
+    L.stats.other_launches++;
+  }
+  // ∂_qH at the step's start position q0 for the current momentum: the
+  // metric, its factor, Λ' and w = x_nᵀG⁻¹x_n are those of q0 (kept from
+  // the evaluation that ended the previous step), so only u = G⁻¹p,
+  // s = x_nᵀu and the two contractions are recomputed
+  void p_eval(bool only_active) {
+    LogregBatched& L = *lb;
+    solve(L.pc, L.u, true, only_active);
+    Epi s{};
+    s.mode = EPI_R2W;
+    s.W = L.W;
+    s.s_ld = L.Npad;
+    s.lp = L.Lp;
+    s.lp_ld = L.Npad;
+    s.r = L.Rb;
+    s.r_off = L.C;
+    gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
+    Epi o{};
+    o.mode = EPI_STORE;
+    o.D = L.Gout;
+    o.ldd = L.dpad;
+    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
+    L.stats.evals++;
+  }
+  // u = G(q_k)⁻¹ p½ at the position iterate (the factorisation without the
+  // inverse)
+  void q_eval(bool only_active) {
+    LogregBatched& L = *lb;
+    metric_gram();
+    chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, only_active, nullptr, nullptr, true);
+    L.stats.evals++;
+  }
+  // everything at (qc, pc), keeping the factor and w for the next momentum
+  // solve
+  void full_eval(int mode, const float* z, float* mom_info) {
+    LogregBatched& L = *lb;
+    metric_gram();
+    if (mode == CH_DRAW)
+      chol(CH_DRAW, z, L.logdet0, L.quad0, mom_info, false, nullptr, L.Lf);
+    else
+      chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, false, nullptr, L.Lf);
+    trace_grad(L.W);
+    L.stats.evals++;
   }
 
   // energy at the proposal: ℓ row sums, Gram, log det and ||L⁻¹p||², ∇ℓ;
@@ -1009,6 +1220,7 @@ struct Runner {
     a.Gout = L.Gout;
     a.ldo = L.dpad;
     a.u = L.u;
+    a.u0 = L.u0;
     a.q0 = L.q0;
     a.p0 = L.p0;
     a.qc = L.qc;
@@ -1029,12 +1241,32 @@ struct Runner {
 
 }  // namespace
 
+// the generalized leapfrog's buffers, allocated on its first use (never
+// while a graph is being captured)
+static int ensure_gl(LogregBatched* lb) {
+  if (lb->Lf) return GJ_OK;
+  bool ok = true;
+  lb->Lf = dalloc<double>((size_t)lb->C * lb->P, lb->owned, &ok);
+  lb->u0 = dalloc<double>((size_t)lb->C * lb->d, lb->owned, &ok);
+  lb->W = dalloc<float>((size_t)lb->C * lb->Npad, lb->owned, &ok);
+  if (!ok) {
+    g_err = "device allocation failed for the generalized leapfrog's buffers";
+    return GJ_ENOMEM;
+  }
+  return GJ_OK;
+}
+
 int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, float* grad,
                               double* logdens, const float* z, const double* u,
                               const InfoDev<float>& info, int gemm_impl, cudaStream_t st) {
   if (gemm_impl == 2 && !lb->tc_ok) {
     g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
     return GJ_ENOTSUP;
+  }
+  const bool gl = sp.integrator == GJ_GENERALIZED_LEAPFROG;
+  if (gl) {
+    const int rc = ensure_gl(lb);
+    if (rc) return rc;
   }
   lb->stats = LogregStats{};
   lb->ev_used = 0;
@@ -1044,7 +1276,38 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   begin_kernel<<<(C + 127) / 128, 128, 0, st>>>(C, d, pos, lb->q0, lb->qc, lb->qf, lb->Qb,
                                                  lb->iters_total, lb->notconv, lb->bad);
   R.check(cudaGetLastError());
-  for (int s = 0; s < sp.L; ++s) {
+  // a fixed-point solve driven from the host: the eager update, then body +
+  // update while some chain is active (at most max_iters + 1 bodies)
+  auto host_solve = [&](int eager, auto body, int iterated) {
+    R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
+    R.update(eager, sp);
+    for (int guard = 0;; ++guard) {
+      R.check(cudaMemcpyAsync(lb->n_active_h, lb->n_active_d, sizeof(int),
+                              cudaMemcpyDeviceToHost, st));
+      R.check(cudaStreamSynchronize(st));
+      if (R.err != cudaSuccess || *lb->n_active_h == 0 || guard > sp.max_iters) break;
+      body();
+      R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
+      R.update(iterated, sp);
+    }
+  };
+  for (int s = 0; gl && s < sp.L; ++s) {
+    // (1) p½ = p − h/2 ∂_qH(q, p½) at the fixed position q: the first map
+    // evaluation at (q, p) draws the momentum at s == 0
+    if (s == 0)
+      R.full_eval(CH_DRAW, z, info.momentum);
+    else
+      R.p_eval(false);
+    host_solve(UP_GLP0, [&] { R.p_eval(true); }, UP_GLPN);
+    // (2) q' = q + h/2 [G⁻¹(q) + G⁻¹(q')] p½
+    R.solve(lb->pc, lb->u0, false, false);
+    host_solve(UP_GLQ0, [&] { R.q_eval(true); }, UP_GLQN);
+    // (3) p' = p½ − h/2 ∂_qH(q', p½), keeping the factor and w at q' for the
+    // next step's momentum solve
+    R.full_eval(CH_EVAL, nullptr, nullptr);
+    R.update(UP_GLPX, sp);
+  }
+  for (int s = 0; !gl && s < sp.L; ++s) {
     // fixed-point evaluation #0 (rmhmc/integrators.py:84); at s == 0 it also
     // draws p = chol(G(q0))·z (rmhmc/metrics.py:45-58)
     R.metric_gram();
@@ -1137,7 +1400,7 @@ int graph_cfg(const LogregBatched* lb) {
 // conditional WHILE node) into *out.  The graph reads and writes the
 // context's staging buffers; step parameters come from lb->spd.  With prop,
 // the energy factorisation also writes the proposal velocity.
-int build_graph(LogregBatched* lb, int L, int impl, bool prop, cudaGraphExec_t* out) {
+int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGraphExec_t* out) {
   *out = nullptr;
   const int C = lb->C, d = lb->d;
   cudaStream_t s = lb->cap_main;
@@ -1148,53 +1411,79 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, cudaGraphExec_t* 
   begin_kernel<<<(C + 127) / 128, 128, 0, s>>>(C, d, lb->pos_s, lb->q0, lb->qc, lb->qf, lb->Qb,
                                                 lb->iters_total, lb->notconv, lb->bad);
   StepDev dummy{};
-  for (int st = 0; st < L && R.err == cudaSuccess; ++st) {
-    R.metric_gram();
-    if (st == 0)
-      R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
-    else
-      R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
-    R.trace_grad();
+  // one fixed-point solve: the eager update, then a conditional WHILE node
+  // whose body is `body` + the iterated update, repeated while some chain is
+  // active (at most max_iters + 1 times)
+  auto add_solve = [&](int eager, auto body, int iterated) -> cudaError_t {
     R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), s));
-    R.update(UP_FP0, dummy);
+    R.update(eager, dummy);
     R.check(cudaMemsetAsync(lb->trips, 0, sizeof(int), s));
     cudaStreamCaptureStatus cs;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
-    e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    if (e != cudaSuccess) break;
+    cudaError_t r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (r != cudaSuccess) return r;
     cudaGraphConditionalHandle h;
-    e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
-    if (e != cudaSuccess) break;
+    r = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+    if (r != cudaSuccess) return r;
     loop_cond_kernel<<<1, 1, 0, s>>>(h, lb->n_active_d, lb->trips, lb->spd);
-    e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    if (e != cudaSuccess) break;
+    r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (r != cudaSuccess) return r;
     cudaGraphNodeParams np{};
     np.type = cudaGraphNodeTypeConditional;
     np.conditional.handle = h;
     np.conditional.type = cudaGraphCondTypeWhile;
     np.conditional.size = 1;
     cudaGraphNode_t node;
-    e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
-    if (e != cudaSuccess) break;
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-    if (e != cudaSuccess) break;
-    e = cudaStreamBeginCaptureToGraph(lb->cap_body, body, nullptr, nullptr, 0,
+    r = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+    if (r != cudaSuccess) return r;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    r = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (r != cudaSuccess) return r;
+    r = cudaStreamBeginCaptureToGraph(lb->cap_body, bodyg, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) break;
+    if (r != cudaSuccess) return r;
     Runner B{lb, impl, lb->cap_body};
     B.spd = lb->spd;
-    B.metric_gram();
-    B.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
-    B.trace_grad();
-    B.update(UP_FPN, dummy);
+    body(B);
+    B.update(iterated, dummy);
     loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
     B.check(cudaGetLastError());
     cudaGraph_t bout = nullptr;
-    e = cudaStreamEndCapture(lb->cap_body, &bout);
-    if (e == cudaSuccess && B.err != cudaSuccess) e = B.err;
+    r = cudaStreamEndCapture(lb->cap_body, &bout);
+    if (r == cudaSuccess && B.err != cudaSuccess) r = B.err;
+    return r;
+  };
+  for (int st = 0; st < L && R.err == cudaSuccess && e == cudaSuccess; ++st) {
+    if (gl) {
+      // generalized leapfrog: momentum solve at the fixed position, position
+      // solve, explicit final momentum (the factor and w at q' are kept for
+      // the next step's momentum solve)
+      if (st == 0)
+        R.full_eval(CH_DRAW, lb->z_s, lb->mom_s);
+      else
+        R.p_eval(false);
+      e = add_solve(UP_GLP0, [](Runner& B) { B.p_eval(true); }, UP_GLPN);
+      if (e != cudaSuccess) break;
+      R.solve(lb->pc, lb->u0, false, false);
+      e = add_solve(UP_GLQ0, [](Runner& B) { B.q_eval(true); }, UP_GLQN);
+      if (e != cudaSuccess) break;
+      R.full_eval(CH_EVAL, nullptr, nullptr);
+      R.update(UP_GLPX, dummy);
+      continue;
+    }
+    R.metric_gram();
+    if (st == 0)
+      R.chol(CH_DRAW, lb->z_s, lb->logdet0, lb->quad0, lb->mom_s);
+    else
+      R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
+    R.trace_grad();
+    e = add_solve(UP_FP0, [lb](Runner& B) {
+      B.metric_gram();
+      B.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
+      B.trace_grad();
+    }, UP_FPN);
     if (e != cudaSuccess) break;
     R.metric_gram();
     R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr);
@@ -1237,9 +1526,9 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, cudaGraphExec_t* 
 }
 
 // The captured transition for these settings, captured now if absent.
-int find_graph(LogregBatched* lb, int L, int impl, bool prop, cudaStream_t st,
+int find_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaStream_t st,
                cudaGraphExec_t* out) {
-  const int cfg = graph_cfg(lb);
+  const int cfg = graph_cfg(lb) + (gl ? (1 << 20) : 0);
   for (auto& g : lb->graphs)
     if (g.L == L && g.impl == impl && g.cfg == cfg && g.prop == (int)prop) {
       g.used = ++lb->graph_tick;
@@ -1256,7 +1545,7 @@ int find_graph(LogregBatched* lb, int L, int impl, bool prop, cudaStream_t st,
     lb->graphs.erase(lb->graphs.begin() + lru);
   }
   cudaGraphExec_t ex = nullptr;
-  const int rc = build_graph(lb, L, impl, prop, &ex);
+  const int rc = build_graph(lb, L, impl, prop, gl, &ex);
   if (rc) return rc;
   lb->graphs.push_back({L, impl, cfg, (int)prop, ex, ++lb->graph_tick});
   *out = ex;
@@ -1278,8 +1567,13 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
     g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
     return GJ_ENOTSUP;
   }
+  const bool gl = sp.integrator == GJ_GENERALIZED_LEAPFROG;
+  if (gl) {
+    const int rg = ensure_gl(lb);
+    if (rg) return rg;
+  }
   cudaGraphExec_t gexec = nullptr;
-  const int rc = find_graph(lb, sp.L, gemm_impl, info.prop_v != nullptr, st, &gexec);
+  const int rc = find_graph(lb, sp.L, gemm_impl, info.prop_v != nullptr, gl, st, &gexec);
   if (rc) return rc;
   const int C = lb->C, d = lb->d;
   lb->stats = LogregStats{};

@@ -332,7 +332,7 @@ int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_ch
 /* ---- batches of independent posteriors ----------------------------------
  * A batch holds B dense-Fisher logistic-regression posteriors of any sizes
  * (n_data and dim may differ; dim <= 128), each sampled by C RMHMC chains
- * through the batched mixed-precision pipeline (implicit midpoint).  Every
+ * through the batched mixed-precision pipeline (either integrator).  Every
  * posterior's transition is one CUDA graph; the graphs are spread
  * round-robin over num_streams streams forked from and joined to the
  * caller's stream, so many small posteriors fill the GPU together.

@@ -41,14 +41,15 @@ def _np(t):
     return t.detach().cpu().numpy()
 
 
-def test_batch_matches_oracle_per_posterior():
+@pytest.mark.parametrize("integrator", ["implicit_midpoint", "generalized_leapfrog"])
+def test_batch_matches_oracle_per_posterior(integrator):
     from geomjax_gb300.base import Draws
     from geomjax_gb300.batch import PosteriorBatch
     from oracle import rmhmc as O_rm
     from oracle import targets as OT
 
     data = _data()
-    pb = PosteriorBatch(data, C, num_streams=3)
+    pb = PosteriorBatch(data, C, num_streams=3, integrator=integrator)
     q0 = _starts()
     zs, _ = _draws(7)
     us = [-np.ones(C) for _ in SIZES]  # accept every proposal: compare trajectories
@@ -60,7 +61,8 @@ def test_batch_matches_oracle_per_posterior():
         for b, (X, y) in enumerate(data):
             ot = OT.LogisticRegression(X, y, prior_var=100.0)
             traj = []
-            _, oi = O_rm.kernel(ot, O_rm.init(ot, q0[b]), zs[b], us[b], h, L, trajectory=traj)
+            _, oi = O_rm.kernel(ot, O_rm.init(ot, q0[b]), zs[b], us[b], h, L, trajectory=traj,
+                                integrator=integrator)
             e = rel_err(_np(pb.positions(st, b)), traj[-1].position)
             assert e < 1e-5, (b, L, e)
             eb = _np(info.energy)[b * C:(b + 1) * C]

@@ -244,17 +244,26 @@ def test_accept_agreement_monge_funnel100():
     assert agree / total >= 0.999
 
 
-@pytest.mark.parametrize("path,loop,chol,d,C", [
-    ("simt", "host", "fp64", 9, 160), ("tcgen05", "host", "fp64", 9, 160),
-    ("tcgen05", "graph", "fp64", 9, 160), ("simt", "graph", "fp64", 9, 160),
-    ("tcgen05", "graph", "fp32", 9, 160),
+IM, GL = "implicit_midpoint", "generalized_leapfrog"
+
+
+@pytest.mark.parametrize("path,loop,chol,d,C,integrator", [
+    ("simt", "host", "fp64", 9, 160, IM), ("tcgen05", "host", "fp64", 9, 160, IM),
+    ("tcgen05", "graph", "fp64", 9, 160, IM), ("simt", "graph", "fp64", 9, 160, IM),
+    ("tcgen05", "graph", "fp32", 9, 160, IM),
     # 8 chains share a warp in the factorisation at d = 9; at d = 40 two do,
     # and 37 chains leave a ragged last warp
-    ("tcgen05", "graph", "fp64", 40, 37), ("tcgen05", "host", "fp32", 40, 37)])
-def test_logreg_batched_per_step(path, loop, chol, d, C):
+    ("tcgen05", "graph", "fp64", 40, 37, IM), ("tcgen05", "host", "fp32", 40, 37, IM),
+    # the generalized leapfrog: momentum solves on the stored factor and w,
+    # position solves, the explicit final momentum
+    ("tcgen05", "graph", "fp64", 9, 160, GL), ("tcgen05", "host", "fp64", 9, 160, GL),
+    ("simt", "host", "fp64", 9, 160, GL), ("tcgen05", "graph", "fp64", 40, 37, GL),
+    ("tcgen05", "graph", "fp32", 9, 160, GL)])
+def test_logreg_batched_per_step(path, loop, chol, d, C, integrator):
     """The batched dense-Fisher path (split-BF16 contractions, FP64 fixed-point
     iterates, FP64 or FP32 factorisation, host-driven loop or one CUDA-graph
-    launch) against the oracle: per-step positions over 10 steps within 1e-5."""
+    launch, either integrator) against the oracle: per-step positions over
+    10 steps within 1e-5."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
@@ -266,8 +275,10 @@ def test_logreg_batched_per_step(path, loop, chol, d, C):
     z, _ = normals(C, ot.dim, 2, np.float32)
     u = -np.ones(C)
     traj = []
-    _, oinfo = O_rm.kernel(ot, O_rm.init(ot, q0), z, u, h, L, trajectory=traj)
-    kern = gj.rmhmc.build_kernel(logreg_path=path, loop=loop, cholesky=chol)
+    _, oinfo = O_rm.kernel(ot, O_rm.init(ot, q0), z, u, h, L, trajectory=traj,
+                           integrator=integrator)
+    kern = gj.rmhmc.build_kernel(logreg_path=path, loop=loop, cholesky=chol,
+                                 integrator=integrator)
     st0 = gj.rmhmc.init(q0, dt)
     for step in (1, 2, 5, 10):
         st, info = kern(Draws(z, u), st0, dt, h, step)
