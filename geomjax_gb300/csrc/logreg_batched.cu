@@ -98,6 +98,7 @@ struct CholArgs {
   float* mom_info;     // DRAW: info.momentum (may be NULL)
   float* vel_info;     // ENERGY: the proposal velocity −G⁻¹p (may be NULL)
   double* Lout;        // DRAW / EVAL: the packed factor, kept for later solves (may be NULL)
+  float* Lout32;       // DRAW / EVAL: the same in FP32 (may be NULL)
   int no_inverse;      // EVAL: stop after u = G⁻¹p (no L⁻¹, no packed G⁻¹)
 };
 
@@ -324,12 +325,14 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
   }
-  if (a.Lout && live) {  // the factor at this position serves the momentum solves,
-    // with 1/L_jj in place of the diagonal (the solves multiply by it)
+  if ((a.Lout || a.Lout32) && live) {  // the factor at this position serves the
+    // momentum solves, with 1/L_jj in place of the diagonal (the solves multiply)
     for (int t = sl; t < P; t += LPC) {
       const uint32_t ik = tab[t];
       const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
-      a.Lout[(size_t)c * P + t] = i == k ? double(rdiag[i]) : double(L[t]);
+      const double v = i == k ? double(rdiag[i]) : double(L[t]);
+      if (a.Lout) a.Lout[(size_t)c * P + t] = v;
+      if (a.Lout32) a.Lout32[(size_t)c * P + t] = float(v);
     }
   }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
@@ -610,32 +613,32 @@ __global__ void update_kernel(UpdArgs a) {
 // with lanes over rows (E slots: d <= 32·E).  FP64 divisions and FP64 warp
 // reductions cost tens of FP64 instructions each on this part, so neither
 // appears here.  Inactive chains (active set, flag 0) are skipped.
-template <int E>
-__global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const double* __restrict__ Lf,
+template <typename T, int E>
+__global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const T* __restrict__ Lf,
                                                     const double* __restrict__ rhs, double* u,
                                                     SplitMat Ub, int split, const uint8_t* active) {
   pdl_wait();
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= C || (active && !active[c])) return;  // warp-uniform
-  const double* Lc = Lf + (size_t)c * P;
-  auto get = [&](const double(&v)[E], int j) {
-    double x = 0.0;
+  const T* Lc = Lf + (size_t)c * P;
+  auto get = [&](const T(&v)[E], int j) {
+    T x = T(0);
 #pragma unroll
     for (int k = 0; k < E; ++k)
       if (k == (j >> 5)) x = v[k];
     return __shfl_sync(0xffffffffu, x, j & 31);
   };
-  double y[E], x[E];
+  T y[E], x[E];
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
-    y[k] = i < d ? rhs[(size_t)c * d + i] : 0.0;
-    x[k] = 0.0;
+    y[k] = i < d ? T(rhs[(size_t)c * d + i]) : T(0);
+    x[k] = T(0);
   }
   int cj = 0;  // colstart(j)
   for (int j = 0; j < d; ++j) {  // L y = rhs, column j eliminated from the rows below
-    const double yj = get(y, j) * Lc[cj];
+    const T yj = get(y, j) * Lc[cj];
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
@@ -650,7 +653,7 @@ __global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const d
   for (int k = 0; k < E; ++k) x[k] = y[k];
   for (int j = d - 1; j >= 0; --j) {
     cj -= d - j;
-    const double xj = get(x, j) * Lc[cj];
+    const T xj = get(x, j) * Lc[cj];
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
@@ -662,7 +665,7 @@ __global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const d
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
     if (i < d) {
-      u[(size_t)c * d + i] = x[k];
+      if (u) u[(size_t)c * d + i] = double(x[k]);
       if (split) split_store(Ub, c, i, float(x[k]));
     }
   }
@@ -766,7 +769,7 @@ struct LogregBatched {
   // generalized leapfrog (allocated on first use): the factor and
   // w = x_nᵀG⁻¹x_n at the step's start position, and G(q0)⁻¹p½
   double *Lf, *u0;
-  float* W;
+  float *W, *Lf32;
   int *iters, *iters_total, *n_active_d;
   int* n_active_h;  // pinned
   uint8_t *active, *notconv, *bad;
@@ -1046,7 +1049,7 @@ struct Runner {
 
   void chol(int mode, const float* z, double* logdet, double* quad, float* mom_info,
             bool only_active = false, float* vel_info = nullptr, double* Lout = nullptr,
-            bool no_inverse = false) {
+            bool no_inverse = false, float* Lout32 = nullptr) {
     LogregBatched& L = *lb;
     CholArgs a{};
     a.mode = mode;
@@ -1069,6 +1072,7 @@ struct Runner {
     a.mom_info = mom_info;
     a.vel_info = vel_info;
     a.Lout = Lout;
+    a.Lout32 = Lout32;
     a.no_inverse = no_inverse ? 1 : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (L.prof) {
@@ -1125,20 +1129,32 @@ struct Runner {
 
   // ---- generalized leapfrog (Girolami and Calderhead 2011, eqs. 16-18)
   // out = G⁻¹·rhs with the factor stored at the step's start position
-  void solve(const double* rhs, double* out, bool split, bool only_active) {
+  // fp32: with the FP32 copy of the factor, for the momentum evaluations,
+  // whose u reaches ∂_qK only through the split-BF16 product s = x_nᵀu
+  // (FP32-level either way); the FP64 factor serves G(q0)⁻¹p½, which enters
+  // the position iterates
+  template <typename T>
+  void solve_t(const T* Lf, const double* rhs, double* out, bool split, const uint8_t* act) {
     LogregBatched& L = *lb;
     const dim3 grid((unsigned)(((size_t)L.C * 32 + 255) / 256)), th(256);
-    const uint8_t* act = only_active ? L.active : nullptr;
     if (L.d <= 32)
-      check(launch_k(L.pdl, solve_kernel<1>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
-                     rhs, out, L.Ub, split ? 1 : 0, act));
+      check(launch_k(L.pdl, solve_kernel<T, 1>, grid, th, 0, st, L.C, L.d, L.P, Lf, rhs, out,
+                     L.Ub, split ? 1 : 0, act));
     else if (L.d <= 64)
-      check(launch_k(L.pdl, solve_kernel<2>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
-                     rhs, out, L.Ub, split ? 1 : 0, act));
+      check(launch_k(L.pdl, solve_kernel<T, 2>, grid, th, 0, st, L.C, L.d, L.P, Lf, rhs, out,
+                     L.Ub, split ? 1 : 0, act));
     else
-      check(launch_k(L.pdl, solve_kernel<4>, grid, th, 0, st, L.C, L.d, L.P, (const double*)L.Lf,
-                     rhs, out, L.Ub, split ? 1 : 0, act));
+      check(launch_k(L.pdl, solve_kernel<T, 4>, grid, th, 0, st, L.C, L.d, L.P, Lf, rhs, out,
+                     L.Ub, split ? 1 : 0, act));
     L.stats.other_launches++;
+  }
+  void solve(const double* rhs, double* out, bool split, bool only_active, bool fp32 = false) {
+    LogregBatched& L = *lb;
+    const uint8_t* act = only_active ? L.active : nullptr;
+    if (fp32)
+      solve_t<float>(L.Lf32, rhs, out, split, act);
+    else
+      solve_t<double>(L.Lf, rhs, out, split, act);
   }
   // ∂_qH at the step's start position q0 for the current momentum: the
   // metric, its factor, Λ' and w = x_nᵀG⁻¹x_n are those of q0 (kept from
@@ -1146,7 +1162,7 @@ struct Runner {
   // s = x_nᵀu and the two contractions are recomputed
   void p_eval(bool only_active) {
     LogregBatched& L = *lb;
-    solve(L.pc, L.u, true, only_active);
+    solve(L.pc, nullptr, true, only_active, true);
     Epi s{};
     s.mode = EPI_R2W;
     s.W = L.W;
@@ -1177,9 +1193,9 @@ struct Runner {
     LogregBatched& L = *lb;
     metric_gram();
     if (mode == CH_DRAW)
-      chol(CH_DRAW, z, L.logdet0, L.quad0, mom_info, false, nullptr, L.Lf);
+      chol(CH_DRAW, z, L.logdet0, L.quad0, mom_info, false, nullptr, L.Lf, false, L.Lf32);
     else
-      chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, false, nullptr, L.Lf);
+      chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, false, nullptr, L.Lf, false, L.Lf32);
     trace_grad(L.W);
     L.stats.evals++;
   }
@@ -1249,6 +1265,7 @@ static int ensure_gl(LogregBatched* lb) {
   lb->Lf = dalloc<double>((size_t)lb->C * lb->P, lb->owned, &ok);
   lb->u0 = dalloc<double>((size_t)lb->C * lb->d, lb->owned, &ok);
   lb->W = dalloc<float>((size_t)lb->C * lb->Npad, lb->owned, &ok);
+  lb->Lf32 = dalloc<float>((size_t)lb->C * lb->P, lb->owned, &ok);
   if (!ok) {
     g_err = "device allocation failed for the generalized leapfrog's buffers";
     return GJ_ENOMEM;
