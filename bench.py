@@ -187,7 +187,8 @@ def run_ours(args, wl):
         kern = gj.rmhmc.build_kernel(logreg_path=args.logreg_path, loop=args.loop,
                                      integrator=args.integrator, cholesky=args.cholesky,
                                      chol_chains_per_warp=args.chol_cpw,
-                                     chain_groups=args.groups, pdl=args.pdl)
+                                     chain_groups=args.groups, pdl=args.pdl,
+                                     gemm_ksplit=args.gemm_ksplit)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -348,6 +349,7 @@ def run_ours(args, wl):
                    "loop": args.loop,
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
+                   "gemm_ksplit": args.gemm_ksplit or "auto",
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}", "autotune": tuned},
@@ -769,6 +771,8 @@ def main():
                     help="deep operand ring, one CTA per SM, for every GEMM")
     ap.add_argument("--gemm-two-cta", action="store_true",
                     help="operand ring cut back to two CTAs per SM for every GEMM")
+    ap.add_argument("--gemm-ksplit", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="K slices of the gradient contraction (0 = automatic)")
     ap.add_argument("--pdl", action="store_true",
                     help="launch the batched pipeline's kernels with programmatic dependent launch")
     ap.add_argument("--groups", type=int, default=0,

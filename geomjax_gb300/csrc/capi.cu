@@ -93,6 +93,7 @@ struct gj_ctx {
   int chol_cpw;   // GJ_OPT_CHOL_CHAINS_PER_WARP
   int groups;     // GJ_OPT_CHAIN_GROUPS (0 = automatic)
   int pdl;        // GJ_OPT_PDL
+  int ksplit;     // GJ_OPT_GEMM_KSPLIT (0 = automatic)
   // batched dense-Fisher path: one context per chain group; in graph mode
   // the groups' transitions run on their own streams, forked from and joined
   // to the caller's stream by events, so one group's factorisation can share
@@ -159,6 +160,10 @@ int ensure_groups(gj_ctx* ctx, const gj::TargetDev& t) {
     gj::logreg_batched_set_chol_fp64(lb, ctx->chol_fp64);
     gj::logreg_batched_set_chol_cpw(lb, ctx->chol_cpw);
     gj::logreg_batched_set_pdl(lb, ctx->pdl);
+    gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
+    // every group makes the automatic choices of the whole context, so that
+    // results do not depend on the group count
+    gj::logreg_batched_set_auto_chains(lb, ctx->C);
     ctx->lbs.push_back(lb);
   }
   if (G > 1) {
@@ -213,6 +218,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->chol_cpw = 0;
   c->groups = 0;
   c->pdl = 0;
+  c->ksplit = 0;
   *out = c;
   return GJ_OK;
 }
@@ -253,6 +259,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     if (value < 0 || value > 1) return fail(GJ_EINVAL, "PDL flag must be 0 or 1");
     ctx->pdl = (int)value;
     for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_pdl(lb, ctx->pdl);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_GEMM_KSPLIT) {
+    if (value < 0 || value > 4) return fail(GJ_EINVAL, "K slices must be 0 (automatic) .. 4");
+    ctx->ksplit = (int)value;
+    for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
     return GJ_OK;
   }
   if (key == GJ_OPT_CHAIN_GROUPS) {

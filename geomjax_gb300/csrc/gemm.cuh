@@ -48,6 +48,10 @@ struct Epi {
   // EPI_STORE
   float* D;
   int ldd;
+  // EPI_STORE with the K range split over gridDim.z CTAs (GemmArgs::ksplit):
+  // slice z stores its partial product at D + z·d_slice (elements); the
+  // consumer adds the slices in order
+  size_t d_slice;
   // EPI_SIGMOID: a = x_nᵀβ_m  ->  Λ = σ(1−σ) into lam, Λ' = Λ(1−2σ) into lp,
   // r1 = y_n − σ into r (rows [0, C))
   const float* y;
@@ -125,7 +129,23 @@ struct GemmArgs {
   int M, N, K;
   Epi epi;
   bool pdl = false;  // tcgen05 path: launch as a programmatic dependent
+  // tcgen05 path, EPI_STORE only: the K blocks split into this many
+  // contiguous slices, one CTA per output tile and slice, so that a GEMM
+  // with few output tiles and a long K fills the SMs.  Every slice must get
+  // at least one K block (gemm_ksplit_valid).
+  int ksplit = 1;
+  // tcgen05 path: the A rows start at this row of each plane (output row m
+  // is A row a_row0 + m); a_row0 + M must not exceed the planes' row pitch
+  int a_row0 = 0;
 };
+
+// whether `ksplit` slices of ⌈K/64⌉ K blocks are all non-empty
+inline bool gemm_ksplit_valid(int K, int ksplit) {
+  const int kb = (K + 63) / 64;
+  if (ksplit < 1 || ksplit > kb) return false;
+  const int per = (kb + ksplit - 1) / ksplit;
+  return (ksplit - 1) * per < kb;
+}
 
 cudaError_t gemm_simt(const GemmArgs& g, cudaStream_t st);
 

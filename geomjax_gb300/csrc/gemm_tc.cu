@@ -211,7 +211,8 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
 #pragma unroll
     for (int k = 0; k < 8; ++k) a[k] = stg[rr * 33 + cc + k];
     if (e.mode == EPI_STORE) {
-      if (m < M) store8(e.D + (size_t)m * e.ldd + n, n, N, full && aligned16(e.D, e.ldd), a);
+      float* D = e.D + (size_t)blockIdx.z * e.d_slice;  // K slice (0 unless split)
+      if (m < M) store8(D + (size_t)m * e.ldd + n, n, N, full && aligned16(D, e.ldd), a);
     } else if (e.mode == EPI_SIGMOID) {
       float yv[8], lam[8], lp[8], r1[8];
       load8(e.y + n, n, N, full && aligned16(e.y, 0), yv);
@@ -263,7 +264,8 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
 template <int NPL, int BN>
 __global__ void __launch_bounds__(320, 2)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err, int STAGES) {
+                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err, int STAGES,
+                   int a_row0) {
   using C = Cfg<NPL, BN>;
   constexpr int STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
@@ -278,7 +280,11 @@ __global__ void __launch_bounds__(320, 2)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int KB = (K + BK - 1) / BK;
+  // this CTA's contiguous range of K blocks (the whole K unless split)
+  const int KB_all = (K + BK - 1) / BK;
+  const int kper = (KB_all + (int)gridDim.z - 1) / (int)gridDim.z;
+  const int kb_first = (int)blockIdx.z * kper;
+  const int KB = max(0, min(KB_all, kb_first + kper) - kb_first);
 
   if (warp == 0 && lane == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -314,10 +320,10 @@ __global__ void __launch_bounds__(320, 2)
         }
         unsigned char* st = base + s * STAGE_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
-        const int x = kb * BK;
+        const int x = (kb_first + kb) * BK;
 #pragma unroll
         for (int q = 0; q < NPL; ++q) {
-          tma_load_2d(st + q * A_TILE_BYTES, &mapA, &full[s], x, q * rpadA + m0);
+          tma_load_2d(st + q * A_TILE_BYTES, &mapA, &full[s], x, q * rpadA + a_row0 + m0);
           tma_load_2d(st + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES, &mapB, &full[s], x,
                       q * rpadB + n0);
         }
@@ -504,9 +510,9 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   else
     ns = std::min(ns, 3);
   const CUtensorMap& mb = BN == 128 ? b->map : (BN == 64 ? b->map64 : b->map32);
-  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
+  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.ksplit);
   return launch_k(g.pdl, gemm_tc_kernel<NPL, BN>, grid, dim3(320), (size_t)C::smem(ns), st, a->map,
-                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns);
+                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0);
 }
 
 template <int NPL>
@@ -532,8 +538,11 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
                     cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return cudaSuccess;
   // every box must lie inside the padded planes
-  if (g.M > a->s.rpad || g.N > b->s.rpad || g.K > a->s.ld || g.K > b->s.ld ||
-      a->s.planes != b->s.planes)
+  if (g.a_row0 < 0 || g.a_row0 + g.M > a->s.rpad || g.N > b->s.rpad || g.K > a->s.ld ||
+      g.K > b->s.ld || a->s.planes != b->s.planes)
+    return cudaErrorInvalidValue;
+  if (g.ksplit != 1 && (g.epi.mode != EPI_STORE || !gemm_ksplit_valid(g.K, g.ksplit) ||
+                        (g.epi.d_slice & 3)))
     return cudaErrorInvalidValue;
   return a->s.planes == 3 ? launch_tc_planes<3>(g, a, b, err, st)
                           : launch_tc_planes<2>(g, a, b, err, st);

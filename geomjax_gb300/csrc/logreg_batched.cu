@@ -161,26 +161,83 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) 
   return c;
 }
 
-// 1/sqrt(a) without a division: the FP32 estimate (relative error < 2^-22)
-// refined by one Newton step x ← x·(3 − a·x²)/2, whose quadratic
-// convergence leaves a relative error below 2^-43.  The sign / range checks
-// run on the FP32 copy to keep the FP64 pipe for arithmetic.  Non-positive
-// or non-finite a gives NaN.
-__device__ __forceinline__ double rsqrt_nr(double a) {
-  const float af = float(a);
-  const float xf = rsqrtf(af);
-  if (!(af > 0.f) || !(xf > 0.f) || isinf(xf) || isinf(af)) {
-    if (!(a > 0.0) || !isfinite(a)) return NAN;
-    return 1.0 / sqrt(a);  // outside the FP32 range
-  }
-  const double x = double(xf);
-  const double ax = a * x;
-  return x * fma(-0.5 * ax, x, 1.5);
+// Format conversions by integer operations on the IEEE-754 bit patterns.
+// GB300 issues FP64 work at 1/64 of the FP32 rate, and the factorisation's
+// FP64 pipe was half busy with conversions, compares and single-lane
+// scalar work on top of its multiply-adds; these keep that work on the
+// integer pipes.
+//
+// binary32 -> binary64: exact for normal values, zeros, infinities and NaNs;
+// subnormal inputs (below 1.2e-38) become a signed zero.
+__device__ __forceinline__ double widen_f32(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t ex = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned long long man = (unsigned long long)(u & 0x7fffffu) << 29;
+  unsigned long long b = sign;
+  if (ex == 0xffu)
+    b |= (0x7ffull << 52) | man;
+  else if (ex != 0u)
+    b |= ((unsigned long long)(ex + 896u) << 52) | man;
+  return __longlong_as_double((long long)b);
 }
-__device__ __forceinline__ float rsqrt_nr(float a) {
-  if (!(a > 0.f) || !isfinite(a)) return NAN;
+// binary64 -> binary32 rounded to nearest even: integer operations for
+// results in the normal binary32 range (a mantissa carry rounds into the
+// exponent, up to infinity), the conversion instruction for the rest
+// (zeros, subnormal results, overflow, infinities and NaNs)
+__device__ __forceinline__ float narrow_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffu) - 896;  // biased binary32 exponent
+  if (e < 1 || e > 254) return float(x);
+  const uint32_t m = (uint32_t)(b >> 29) & 0x7fffffu;
+  const uint32_t rem = (uint32_t)b & 0x1fffffffu;  // the 29 dropped bits
+  const uint32_t up = (uint32_t)(rem > 0x10000000u) | ((uint32_t)(rem == 0x10000000u) & m);
+  const uint32_t r = (((uint32_t)e << 23) | m) + up;
+  return __uint_as_float(r | ((uint32_t)(b >> 32) & 0x80000000u));
+}
+__device__ __forceinline__ double to_fp(double, float x) { return widen_f32(x); }
+__device__ __forceinline__ float to_fp(float, float x) { return x; }
+__device__ __forceinline__ float to_f32(double x) { return narrow_rn(x); }
+__device__ __forceinline__ float to_f32(float x) { return x; }
+
+// Reciprocal square root of a pivot, without a division, and the pivot's
+// validity.  A usable FP64 pivot is positive, finite and at least 2^-1021
+// (a Schur complement of Gram + I/s² is at least 1/s²); any other marks the
+// chain as not positive definite and gives NaN.  The FP32 estimate of the
+// truncated value (relative error below 2^-22 + 2^-24) is refined by one
+// Newton step x·(3 − a·x²)/2 = x·fma(−a·x, x/2, 3/2), whose quadratic
+// convergence leaves a relative error below 2^-42: three FP64 operations.
+// Pivots outside the binary32 exponent range take 1/sqrt.
+__device__ __forceinline__ double pivot_rsqrt(double a, bool& bad) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const uint32_t hi = (uint32_t)(b >> 52);  // sign and biased exponent
+  if (hi - 2u >= 0x7fdu) {  // negative, zero, below 2^-1021, infinite or NaN
+    bad = true;
+    return NAN;
+  }
+  const int e = (int)hi - 1023;
+  if (e < -126 || e > 127) return 1.0 / sqrt(a);
+  const float af = __uint_as_float(((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu));
+  const float xf = rsqrtf(af);
+  const double x = widen_f32(xf), hx = widen_f32(0.5f * xf);
+  return x * fma(-(a * x), hx, 1.5);
+}
+__device__ __forceinline__ float pivot_rsqrt(float a, bool& bad) {
+  if (!(a > 0.f) || !isfinite(a)) {
+    bad = true;
+    return NAN;
+  }
   float x = rsqrtf(a);
   return x * (1.5f - 0.5f * a * x * x);
+}
+
+// log det accumulation: the running product of the pivots as mantissa
+// m ∈ [0.5, 1) times 2^e, renormalised by integer operations on the bits
+// (m · pivot is normal for every usable pivot)
+__device__ __forceinline__ void ld_accumulate(double& m, int& e, double piv) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(m * piv);
+  e += (int)((b >> 52) & 0x7ffu) - 1022;
+  m = __longlong_as_double((long long)((b & 0x800fffffffffffffull) | 0x3fe0000000000000ull));
 }
 
 __device__ __forceinline__ int colstart(int k, int d) { return k * d - (k * (k - 1)) / 2; }
@@ -224,7 +281,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     const bool diag = (ik & 0xffffu) == (ik >> 16);
     F g;
     if (live) {
-      g = F(a.Gv[(size_t)c * a.gv_ld + t]);
+      g = to_fp(F(0), a.Gv[(size_t)c * a.gv_ld + t]);
       if (diag) g += F(a.prior_inv);
     } else {
       g = diag ? F(1) : F(0);
@@ -243,6 +300,9 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
   }
   bool bad = false;
+  // log det G is needed for the energies (DRAW at the start, ENERGY at the
+  // proposal); the map evaluations (EVAL) skip it
+  const bool want_ld = a.mode != CH_EVAL;
   double pm = 1.0;
   int pe = 0;
   // The FP64 factorisation takes one column per step: its DFMA count bounds
@@ -256,14 +316,11 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   // writes them)
   auto pivot = [&](int j, int cj) -> F {
     const F djj = L[cj];
-    if (!(djj > F(0))) bad = true;
-    const F inv = rsqrt_nr(djj);  // 1/L_jj
-    int e;
-    pm = frexp(pm * double(djj), &e);
-    pe += e;
+    const F inv = pivot_rsqrt(djj, bad);  // 1/L_jj
+    if (want_ld) ld_accumulate(pm, pe, double(djj));
     __syncwarp();
     if (sl == 0) {
-      L[cj] = djj * inv;
+      if (a.mode == CH_DRAW) L[cj] = djj * inv;  // L_jj, read only by p = L z
       rdiag[j] = inv;
       if (border) y[j] *= inv;
     }
@@ -322,7 +379,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   }
   pdl_trigger();  // the factorisation is done; the successor may be scheduled
   if (sl == 0 && live) {
-    a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
+    if (want_ld) a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
     if (bad) a.bad[c] = 1;
   }
   if ((a.Lout || a.Lout32) && live) {  // the factor at this position serves the
@@ -332,13 +389,13 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
       const double v = i == k ? double(rdiag[i]) : double(L[t]);
       if (a.Lout) a.Lout[(size_t)c * P + t] = v;
-      if (a.Lout32) a.Lout32[(size_t)c * P + t] = float(v);
+      if (a.Lout32) a.Lout32[(size_t)c * P + t] = narrow_rn(v);
     }
   }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
   // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
-    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
+    for (int i = sl; i < d; i += LPC) y[i] = live ? to_fp(F(0), a.z[(size_t)c * d + i]) : F(0);
     __syncwarp();
     double zz = 0.0;
     for (int i = sl; i < d; i += LPC) {
@@ -351,7 +408,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       if (live) {
         a.p0[(size_t)c * d + i] = double(sacc);
         a.pc[(size_t)c * d + i] = double(sacc);
-        if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
+        if (a.mom_info) a.mom_info[(size_t)c * d + i] = to_f32(sacc);
       }
       zz += double(y[i]) * double(y[i]);
     }
@@ -380,13 +437,15 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   }
   if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
     if (live)
-      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = float(-xv[i]);
+      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = to_f32(-xv[i]);
     return;
   }
   if (live) {
     for (int i = sl; i < d; i += LPC) {
       a.u[(size_t)c * d + i] = double(xv[i]);
-      split_store(a.Ub, c, i, float(xv[i]));
+      // the position iterates (no inverse) use u alone; the split copy
+      // feeds the S contraction of full evaluations
+      if (!a.no_inverse) split_store(a.Ub, c, i, to_f32(xv[i]));
     }
   }
   if (a.no_inverse) return;  // uniform: the position solve needs u only
@@ -402,13 +461,13 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   // by both in one pass
   int ck = 0;  // colstart(k)
   for (int k = 0; k < d; k += 2) {
-    const float ikk = float(rdiag[k]);
+    const float ikk = to_f32(rdiag[k]);
     for (int cc = sl; cc <= k; cc += LPC) Li[colstart(cc, d) + k - cc] *= ikk;
     __syncwarp();
     const int ck1 = ck + (d - k);  // colstart(k + 1)
     if (k + 1 == d) break;
-    const float l10 = float(L[ck + 1]);  // L(k + 1, k)
-    const float ik1 = float(rdiag[k + 1]);
+    const float l10 = to_f32(L[ck + 1]);  // L(k + 1, k)
+    const float ik1 = to_f32(rdiag[k + 1]);
     for (int cc = sl; cc <= k + 1; cc += LPC) {
       const int o = colstart(cc, d);
       const float v = (cc <= k) ? Li[o + k + 1 - cc] - l10 * Li[o + k - cc] : Li[o];
@@ -416,8 +475,8 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     }
     __syncwarp();
     for (int i = k + 2 + sl; i < d; i += LPC) {
-      const float li0 = float(L[ck + i - k]);       // L(i, k)
-      const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
+      const float li0 = to_f32(L[ck + i - k]);       // L(i, k)
+      const float li1 = to_f32(L[ck1 + i - k - 1]);  // L(i, k + 1)
       int cc0 = 0;  // colstart(cc)
       for (int cc = 0; cc <= k; ++cc) {
         Li[cc0 + i - cc] -= li0 * Li[cc0 + k - cc] + li1 * Li[cc0 + k + 1 - cc];
@@ -478,8 +537,10 @@ struct UpdArgs {
   double hh, prior_inv, tol;
   int max_iters;
   const StepDev* spd;  // when set (graph path), h / tol / max_iters are read from it
-  const float* Gout;  // [2C, ldo]
+  const float* Gout;  // [2C, ldo] per K slice
   int ldo;
+  int gs;          // K slices of the gradient contraction (summed here)
+  size_t gstride;  // elements between slices
   const double* u;
   const double* u0;           // generalized leapfrog: G(q0)⁻¹p½
   double *q0, *p0, *qc, *pc;  // FP64 fixed-point iterates
@@ -492,6 +553,14 @@ struct UpdArgs {
   SplitMat Qb;
   int* n_active;
 };
+
+// the gradient contraction's K slices added in slice order (FP32, as one
+// unsplit accumulation would hold them)
+__device__ __forceinline__ float slice_sum(const float* p, size_t off, int ns, size_t stride) {
+  float v = p[off];
+  for (int s = 1; s < ns; ++s) v += p[off + (size_t)s * stride];
+  return v;
+}
 
 // one warp per chain, lanes over coordinates.  *n_active is only a flag
 // (> 0 while some chain iterates): one plain store per block that has an
@@ -523,8 +592,10 @@ __global__ void update_kernel(UpdArgs a) {
           split_store(a.Qb, c, i, float(qn));
         } else {
           // ∂_qH = ∂_qK − ∇ℓ at the current position
-          const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
-          const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
+          const double g =
+              double(slice_sum(a.Gout, (size_t)c * a.ldo + i, a.gs, a.gstride)) - q * a.prior_inv;
+          const double dK =
+              0.5 * double(slice_sum(a.Gout, (size_t)(a.C + c) * a.ldo + i, a.gs, a.gstride));
           if (a.mode == UP_GLPX) {  // p' = p½ − h/2 ∂_qH(q', p½)
             const double pn = a.pc[o] - hh * (dK - g);
             a.pc[o] = pn;
@@ -571,8 +642,10 @@ __global__ void update_kernel(UpdArgs a) {
     for (int i = lane; i < d; i += 32) {
       const size_t o = (size_t)c * d + i;
       const double q = a.qc[o];
-      const double g = double(a.Gout[(size_t)c * a.ldo + i]) - q * a.prior_inv;
-      const double dK = 0.5 * double(a.Gout[(size_t)(a.C + c) * a.ldo + i]);
+      const double g =
+          double(slice_sum(a.Gout, (size_t)c * a.ldo + i, a.gs, a.gstride)) - q * a.prior_inv;
+      const double dK =
+          0.5 * double(slice_sum(a.Gout, (size_t)(a.C + c) * a.ldo + i, a.gs, a.gstride));
       const double qn = qs[o] + hh * a.u[o];
       const double pn = ps[o] - hh * (dK - g);
       const double e1 = qn - q, e2 = pn - a.pc[o];
@@ -612,16 +685,10 @@ __global__ void update_kernel(UpdArgs a) {
 // one solved component and the lanes update their rows), one warp per chain
 // with lanes over rows (E slots: d <= 32·E).  FP64 divisions and FP64 warp
 // reductions cost tens of FP64 instructions each on this part, so neither
-// appears here.  Inactive chains (active set, flag 0) are skipped.
+// appears here.  y holds the right-hand side on entry (rows lane + 32k) and
+// the solution on exit.
 template <typename T, int E>
-__global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const T* __restrict__ Lf,
-                                                    const double* __restrict__ rhs, double* u,
-                                                    SplitMat Ub, int split, const uint8_t* active) {
-  pdl_wait();
-  const int lane = threadIdx.x & 31;
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (c >= C || (active && !active[c])) return;  // warp-uniform
-  const T* Lc = Lf + (size_t)c * P;
+__device__ __forceinline__ void factor_solve(const T* __restrict__ Lc, int d, int lane, T (&y)[E]) {
   auto get = [&](const T(&v)[E], int j) {
     T x = T(0);
 #pragma unroll
@@ -629,13 +696,6 @@ __global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const T
       if (k == (j >> 5)) x = v[k];
     return __shfl_sync(0xffffffffu, x, j & 31);
   };
-  T y[E], x[E];
-#pragma unroll
-  for (int k = 0; k < E; ++k) {
-    const int i = lane + 32 * k;
-    y[k] = i < d ? T(rhs[(size_t)c * d + i]) : T(0);
-    x[k] = T(0);
-  }
   int cj = 0;  // colstart(j)
   for (int j = 0; j < d; ++j) {  // L y = rhs, column j eliminated from the rows below
     const T yj = get(y, j) * Lc[cj];
@@ -649,26 +709,136 @@ __global__ void __launch_bounds__(256) solve_kernel(int C, int d, int P, const T
   }
   // Lᵀ x = y: x_j final once rows below are done; then row j of L (L(j, i),
   // i < j, at colstart(i) + j − i) updates the components above
-#pragma unroll
-  for (int k = 0; k < E; ++k) x[k] = y[k];
   for (int j = d - 1; j >= 0; --j) {
     cj -= d - j;
-    const T xj = get(x, j) * Lc[cj];
+    const T xj = get(y, j) * Lc[cj];
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
-      if (i == j) x[k] = xj;
-      else if (i < j) x[k] -= Lc[i * d - i * (i - 1) / 2 + j - i] * xj;
+      if (i == j) y[k] = xj;
+      else if (i < j) y[k] -= Lc[i * d - i * (i - 1) / 2 + j - i] * xj;
     }
   }
+}
+
+// For d <= 32 (E = 1) a warp first copies its chain's factor (at most 528
+// entries) into shared memory with coalesced loads: the backward pass reads
+// rows of L, whose entries lie in different columns, and those gathers cost
+// a wavefront per cache line from L1 but about one from shared memory.
+template <typename T, int E>
+struct FactorStage {
+  __device__ __forceinline__ const T* operator()(const T* g, int, int) const { return g; }
+};
+template <typename T>
+struct FactorStage<T, 1> {
+  T* buf;  // this warp's 528 entries
+  __device__ __forceinline__ const T* operator()(const T* g, int P, int lane) const {
+    for (int t = lane; t < P; t += 32) buf[t] = g[t];
+    __syncwarp();
+    return buf;
+  }
+};
+constexpr int kSolveWarps = 8;     // warps per block of the solve kernels
+constexpr int kStageEntries = 528; // packed entries of a factor with d = 32
+
+// Inactive chains (active set, flag 0) are skipped.
+template <typename T, int E>
+__global__ void __launch_bounds__(32 * kSolveWarps) solve_kernel(int C, int d, int P,
+                                                    const T* __restrict__ Lf,
+                                                    const double* __restrict__ rhs, double* u,
+                                                    SplitMat Ub, int split, const uint8_t* active) {
+  __shared__ T stage[E == 1 ? kSolveWarps * kStageEntries : 1];
+  pdl_wait();
+  const int lane = threadIdx.x & 31;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= C || (active && !active[c])) return;  // warp-uniform
+  FactorStage<T, E> sg;
+  if constexpr (E == 1) sg.buf = stage + (threadIdx.x >> 5) * kStageEntries;
+  const T* Lc = sg(Lf + (size_t)c * P, P, lane);
+  T y[E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = lane + 32 * k;
+    y[k] = i < d ? T(rhs[(size_t)c * d + i]) : T(0);
+  }
+  factor_solve<T, E>(Lc, d, lane, y);
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
     if (i < d) {
-      if (u) u[(size_t)c * d + i] = double(x[k]);
-      if (split) split_store(Ub, c, i, float(x[k]));
+      if (u) u[(size_t)c * d + i] = double(y[k]);
+      if (split) split_store(Ub, c, i, to_f32(y[k]));
     }
   }
+}
+
+// The generalized leapfrog's momentum update (UP_GLP0 / UP_GLPN of
+// update_kernel) fused with the next momentum evaluation's solve: a chain
+// still iterating solves u = G(q0)⁻¹p½ with its new iterate on the FP32
+// factor kept at q0 and stores the split copy of u for the S contraction.
+// Converged chains solve nothing, so the loop body that follows needs no
+// solve of its own.
+template <int E>
+__global__ void __launch_bounds__(32 * kSolveWarps) glp_update_solve_kernel(UpdArgs a,
+                                                                            const float* __restrict__ Lf,
+                                                                            int P, SplitMat Ub) {
+  __shared__ float stage[E == 1 ? kSolveWarps * kStageEntries : 1];
+  pdl_wait();
+  const int lane = threadIdx.x & 31;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  bool act = false;
+  if (c < a.C && !(a.mode == UP_GLPN && !a.active[c])) {  // warp-uniform
+    const int d = a.d;
+    const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
+    const double tol = a.spd ? a.spd->tol : a.tol;
+    const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
+    double nrm = 0.0;
+    bool nan = false;
+    float y[E];
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = lane + 32 * k;
+      y[k] = 0.f;
+      if (i < d) {
+        // p½ = p0 − h/2 ∂_qH(q0, p_k), ∂_qH = ∂_qK − ∇ℓ(q0)
+        const size_t o = (size_t)c * d + i;
+        const double g = double(slice_sum(a.Gout, (size_t)c * a.ldo + i, a.gs, a.gstride)) -
+                         a.qc[o] * a.prior_inv;
+        const double dK =
+            0.5 * double(slice_sum(a.Gout, (size_t)(a.C + c) * a.ldo + i, a.gs, a.gstride));
+        const double pn = a.p0[o] - hh * (dK - g);
+        const double e = pn - a.pc[o];
+        nan |= isnan(e);
+        nrm = fmax(nrm, fabs(e));
+        a.pc[o] = pn;
+        y[k] = narrow_rn(pn);
+      }
+    }
+    nrm = warp_max(nrm);
+    nan = __any_sync(0xffffffffu, nan);
+    if (nan) nrm = NAN;
+    const int it = a.mode == UP_GLPN ? a.iters[c] + 1 : 0;
+    act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
+    if (lane == 0) {
+      a.iters[c] = it;
+      a.norm[c] = nrm;
+      a.active[c] = act;
+      if (a.mode == UP_GLPN) a.iters_total[c] += 1;
+      if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
+    }
+    if (act) {  // warp-uniform
+      FactorStage<float, E> sg;
+      if constexpr (E == 1) sg.buf = stage + (threadIdx.x >> 5) * kStageEntries;
+      const float* Lc = sg(Lf + (size_t)c * P, P, lane);
+      factor_solve<float, E>(Lc, d, lane, y);
+#pragma unroll
+      for (int k = 0; k < E; ++k) {
+        const int i = lane + 32 * k;
+        if (i < d) split_store(Ub, c, i, y[k]);
+      }
+    }
+  }
+  if (__syncthreads_or(act) && threadIdx.x == 0) *a.n_active = 1;
 }
 
 __global__ void begin_kernel(int C, int d, const float* pos, double* q0, double* qc, float* qf,
@@ -693,7 +863,8 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
                               const double* logdet0, const double* ldsum, const double* quad1,
                               const double* logdet1, const double* uacc, double div_thr,
                               const StepDev* spd, double prior_var, const double* qc,
-                              const float* Gout, int ldo, float* pos, float* grad,
+                              const float* Gout, int ldo, int gs, size_t gstride, float* pos,
+                              float* grad,
                               double* logdens, InfoDev<float> info, const int* iters_total,
                               const uint8_t* notconv, const uint8_t* bad) {
   pdl_wait();
@@ -712,7 +883,8 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
     for (int i = 0; i < d; ++i) {
       const double q = qc[(size_t)c * d + i];
       pos[(size_t)c * d + i] = float(q);
-      grad[(size_t)c * d + i] = float(double(Gout[(size_t)c * ldo + i]) - q / prior_var);
+      grad[(size_t)c * d + i] =
+          float(double(slice_sum(Gout, (size_t)c * ldo + i, gs, gstride)) - q / prior_var);
     }
     logdens[c] = ld1;
   }
@@ -752,6 +924,10 @@ Tp* dalloc(size_t n, std::vector<void*>& owned, bool* ok) {
   return static_cast<Tp*>(p);
 }
 
+// K slices of the gradient contraction [r₁; r₂]·X at most (its output
+// buffer holds this many partial products)
+constexpr int kMaxGoutSlices = 4;
+
 }  // namespace
 
 struct LogregBatched {
@@ -779,6 +955,10 @@ struct LogregBatched {
   int chol_fp64;
   int chol_cpw;  // chains per warp in the factorisation (0 = automatic)
   int pdl;       // launch the pipeline's kernels as programmatic dependents
+  int gsplit_req;  // K slices of the gradient contraction (0 = automatic)
+  int auto_C;      // chains the automatic rules (K slices, chains per warp)
+                   // size their grids for
+  int sms;         // multiprocessors of the device
   int prof;
   // graph path: device step parameters, staging buffers, captured graph
   StepDev* spd;
@@ -812,6 +992,30 @@ LogregStats logreg_batched_stats(const LogregBatched* lb) { return lb->stats; }
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on) { lb->chol_fp64 = on; }
 void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw) { lb->chol_cpw = cpw; }
 void logreg_batched_set_pdl(LogregBatched* lb, int on) { lb->pdl = on; }
+void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k) { lb->gsplit_req = k; }
+void logreg_batched_set_auto_chains(LogregBatched* lb, int C) { lb->auto_C = C > 0 ? C : lb->C; }
+
+// K slices of the gradient contractions [r₁; r₂]·X (M = 2C) and r₂·X
+// (M = C, the momentum evaluations of the generalized leapfrog), N = d,
+// K = N observations: few output tiles (32 for M = C at 4096 chains and
+// d <= 32) and a long K, so K is split until the M = C grid fills the SMs
+// once, keeping at least 4 K blocks per slice.  The SIMT path does not
+// split.
+static int gout_split(const LogregBatched* lb, int impl) {
+  if (impl != 2) return 1;
+  const int kb = (lb->N + 63) / 64;
+  int s;
+  if (lb->gsplit_req > 0) {
+    s = std::min(lb->gsplit_req, kMaxGoutSlices);
+  } else {
+    const int bn = lb->d <= 32 ? 32 : (lb->d <= 64 ? 64 : 128);
+    const int tiles = ((lb->d + bn - 1) / bn) * ((lb->auto_C + 127) / 128);
+    s = std::max(1, std::min(kMaxGoutSlices, lb->sms / std::max(tiles, 1)));
+    while (s > 1 && kb / s < 4) --s;
+  }
+  while (s > 1 && !gemm_ksplit_valid(lb->N, s)) --s;
+  return s;
+}
 void logreg_batched_set_profile(LogregBatched* lb, int on) { lb->prof = on; }
 
 static SplitMat make_split(LogregBatched* lb, int rows, int kdim, int planes, bool* ok) {
@@ -856,6 +1060,14 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->chol_fp64 = 1;
   lb->chol_cpw = 0;
   lb->pdl = 0;
+  lb->gsplit_req = 0;
+  lb->auto_C = C;
+  lb->sms = 0;
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&lb->sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   lb->prof = 0;
   lb->ev_used = 0;
   lb->cev_used = 0;
@@ -883,7 +1095,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->Lp = dalloc<float>((size_t)C * lb->Npad, lb->owned, &ok);
   lb->S = dalloc<float>((size_t)C * lb->Npad, lb->owned, &ok);
   lb->Gv = dalloc<float>((size_t)C * lb->Pp, lb->owned, &ok);
-  lb->Gout = dalloc<float>((size_t)2 * C * lb->dpad, lb->owned, &ok);
+  lb->Gout = dalloc<float>((size_t)kMaxGoutSlices * 2 * C * lb->dpad, lb->owned, &ok);
   lb->q0 = dalloc<double>((size_t)C * d, lb->owned, &ok);
   lb->p0 = dalloc<double>((size_t)C * d, lb->owned, &ok);
   lb->qc = dalloc<double>((size_t)C * d, lb->owned, &ok);
@@ -990,7 +1202,7 @@ struct Runner {
   const StepDev* spd = nullptr;  // graph path: step parameters in device memory
 
   void gemm(const SplitMat& A, const TcOperand* ta, const SplitMat& B, const TcOperand* tb, int M,
-            int N, int K, const Epi& e) {
+            int N, int K, const Epi& e, int ksplit = 1, int a_row0 = 0) {
     if (err != cudaSuccess) return;
     GemmArgs g;
     g.A = A;
@@ -1000,6 +1212,8 @@ struct Runner {
     g.K = K;
     g.epi = e;
     g.pdl = lb->pdl != 0;
+    g.ksplit = ksplit;
+    g.a_row0 = a_row0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (lb->prof) {
       while (lb->ev.size() < lb->ev_used + 2) {
@@ -1025,6 +1239,26 @@ struct Runner {
   void check(cudaError_t e) {
     if (err == cudaSuccess) err = e;
     lb->stats.other_launches++;
+  }
+  // rows [row0, row0 + M) of the gradient contraction [r₁; r₂]·X into the
+  // same rows of Gout, in gsplit() K slices gstride() elements apart: all
+  // 2C rows at a full evaluation, r₁·X (rows [0, C)) for the energy, r₂·X
+  // (rows [C, 2C)) for the momentum evaluations of the generalized leapfrog,
+  // whose r₁·X at the fixed position stays from the evaluation there
+  int gsplit() const { return gout_split(lb, impl); }
+  size_t gstride() const { return (size_t)2 * lb->C * lb->dpad; }
+  void grad_gemm(int row0, int M) {
+    LogregBatched& L = *lb;
+    if (impl != 2 && row0 > 0) {  // the SIMT GEMM takes no row offset: all rows
+      M += row0;
+      row0 = 0;
+    }
+    Epi o{};
+    o.mode = EPI_STORE;
+    o.D = L.Gout + (size_t)row0 * L.dpad;
+    o.ldd = L.dpad;
+    o.d_slice = gstride();
+    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, M, L.d, L.N, o, gsplit(), row0);
   }
 
   // metric at the current iterate: (1) and (2); with ld_acc the Xβ epilogue
@@ -1093,7 +1327,7 @@ struct Runner {
     const double solves = (mode == CH_ENERGY && !vel_info) ? 1.0 : 2.0;
     L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + solves * dd * dd);
     const CholCfg cf =
-        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.C);
+        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
     const int per_cta = cf.warps * cf.cpw;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
     // the dynamic shared-memory limit was raised at context creation
@@ -1120,11 +1354,7 @@ struct Runner {
     w.r = L.Rb;
     w.r_off = L.C;
     gemm(L.Giv, L.tGiv, L.Zb, L.tZb, L.C, L.N, L.P, w);
-    Epi o{};
-    o.mode = EPI_STORE;
-    o.D = L.Gout;
-    o.ldd = L.dpad;
-    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
+    grad_gemm(0, 2 * L.C);
   }
 
   // ---- generalized leapfrog (Girolami and Calderhead 2011, eqs. 16-18)
@@ -1136,7 +1366,8 @@ struct Runner {
   template <typename T>
   void solve_t(const T* Lf, const double* rhs, double* out, bool split, const uint8_t* act) {
     LogregBatched& L = *lb;
-    const dim3 grid((unsigned)(((size_t)L.C * 32 + 255) / 256)), th(256);
+    // one warp per chain, kSolveWarps warps per block (the staging buffers)
+    const dim3 th(32 * kSolveWarps), grid((unsigned)(((size_t)L.C + kSolveWarps - 1) / kSolveWarps));
     if (L.d <= 32)
       check(launch_k(L.pdl, solve_kernel<T, 1>, grid, th, 0, st, L.C, L.d, L.P, Lf, rhs, out,
                      L.Ub, split ? 1 : 0, act));
@@ -1159,10 +1390,16 @@ struct Runner {
   // ∂_qH at the step's start position q0 for the current momentum: the
   // metric, its factor, Λ' and w = x_nᵀG⁻¹x_n are those of q0 (kept from
   // the evaluation that ended the previous step), so only u = G⁻¹p,
-  // s = x_nᵀu and the two contractions are recomputed
-  void p_eval(bool only_active) {
+  // s = x_nᵀu and the two contractions are recomputed.  Inside the
+  // fixed-point loop the solve is done by the momentum update before it
+  // (glp_update_solve_kernel), so the loop body is p_contract() alone.
+  void p_eval() {
+    solve(lb->pc, nullptr, true, false, true);
+    p_contract();
+  }
+  // s = x_nᵀu and r₂ = Λ'(w − s²) from the split u, then r₂·X
+  void p_contract() {
     LogregBatched& L = *lb;
-    solve(L.pc, nullptr, true, only_active, true);
     Epi s{};
     s.mode = EPI_R2W;
     s.W = L.W;
@@ -1172,11 +1409,7 @@ struct Runner {
     s.r = L.Rb;
     s.r_off = L.C;
     gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
-    Epi o{};
-    o.mode = EPI_STORE;
-    o.D = L.Gout;
-    o.ldd = L.dpad;
-    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, 2 * L.C, L.d, L.N, o);
+    grad_gemm(L.C, L.C);
     L.stats.evals++;
   }
   // u = G(q_k)⁻¹ p½ at the position iterate (the factorisation without the
@@ -1207,11 +1440,7 @@ struct Runner {
     check(cudaMemsetAsync(L.ldnew, 0, sizeof(double) * L.C, st));
     metric_gram(L.ldnew);
     chol(CH_ENERGY, nullptr, L.logdet1, L.quad1, nullptr, false, vel_out);
-    Epi o{};
-    o.mode = EPI_STORE;
-    o.D = L.Gout;
-    o.ldd = L.dpad;
-    gemm(L.Rb, L.tRb, L.XTb, L.tXTb, L.C, L.d, L.N, o);
+    grad_gemm(0, L.C);
   }
 
   void accept(const double* ld0, const double* u, double div_thr, float* pos, float* grad,
@@ -1219,7 +1448,8 @@ struct Runner {
     LogregBatched& L = *lb;
     accept_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(
         L.C, L.d, ld0, L.quad0, L.logdet0, L.ldnew, L.quad1, L.logdet1, u, div_thr, spd,
-        L.t.p0, L.qc, L.Gout, L.dpad, pos, grad, logdens, info, L.iters_total, L.notconv, L.bad);
+        L.t.p0, L.qc, L.Gout, L.dpad, gsplit(), gstride(), pos, grad, logdens, info,
+        L.iters_total, L.notconv, L.bad);
     check(cudaGetLastError());
   }
 
@@ -1235,6 +1465,8 @@ struct Runner {
     a.max_iters = sp.max_iters;
     a.Gout = L.Gout;
     a.ldo = L.dpad;
+    a.gs = gsplit();
+    a.gstride = gstride();
     a.u = L.u;
     a.u0 = L.u0;
     a.q0 = L.q0;
@@ -1250,8 +1482,18 @@ struct Runner {
     a.Qb = L.Qb;
     a.n_active = L.n_active_d;
     a.spd = spd;
-    check(launch_k(L.pdl, update_kernel, dim3((unsigned)(((size_t)L.C * 32 + 255) / 256)), dim3(256),
-                   0, st, a));
+    static_assert(32 * kSolveWarps == 256, "the fused update stages one factor per warp");
+    const dim3 grid((unsigned)(((size_t)L.C * 32 + 255) / 256)), th(256);
+    if (mode == UP_GLP0 || mode == UP_GLPN) {  // with the next evaluation's solve
+      if (L.d <= 32)
+        check(launch_k(L.pdl, glp_update_solve_kernel<1>, grid, th, 0, st, a, L.Lf32, L.P, L.Ub));
+      else if (L.d <= 64)
+        check(launch_k(L.pdl, glp_update_solve_kernel<2>, grid, th, 0, st, a, L.Lf32, L.P, L.Ub));
+      else
+        check(launch_k(L.pdl, glp_update_solve_kernel<4>, grid, th, 0, st, a, L.Lf32, L.P, L.Ub));
+      return;
+    }
+    check(launch_k(L.pdl, update_kernel, grid, th, 0, st, a));
   }
 };
 
@@ -1314,8 +1556,8 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
     if (s == 0)
       R.full_eval(CH_DRAW, z, info.momentum);
     else
-      R.p_eval(false);
-    host_solve(UP_GLP0, [&] { R.p_eval(true); }, UP_GLPN);
+      R.p_eval();
+    host_solve(UP_GLP0, [&] { R.p_contract(); }, UP_GLPN);
     // (2) q' = q + h/2 [G⁻¹(q) + G⁻¹(q')] p½
     R.solve(lb->pc, lb->u0, false, false);
     host_solve(UP_GLQ0, [&] { R.q_eval(true); }, UP_GLQN);
@@ -1410,7 +1652,8 @@ int graph_fail(const char* what, cudaError_t e) {
 constexpr size_t kMaxGraphs = 64;
 
 int graph_cfg(const LogregBatched* lb) {
-  return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl + 512 * gemm_tc_tuning_code();
+  return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl + 512 * gemm_tc_tuning_code() +
+         8192 * lb->gsplit_req;
 }
 
 // Capture one whole transition (all L steps, each fixed-point solve a
@@ -1480,8 +1723,8 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGrap
       if (st == 0)
         R.full_eval(CH_DRAW, lb->z_s, lb->mom_s);
       else
-        R.p_eval(false);
-      e = add_solve(UP_GLP0, [](Runner& B) { B.p_eval(true); }, UP_GLPN);
+        R.p_eval();
+      e = add_solve(UP_GLP0, [](Runner& B) { B.p_contract(); }, UP_GLPN);
       if (e != cudaSuccess) break;
       R.solve(lb->pc, lb->u0, false, false);
       e = add_solve(UP_GLQ0, [](Runner& B) { B.q_eval(true); }, UP_GLQN);

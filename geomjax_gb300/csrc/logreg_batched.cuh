@@ -48,6 +48,14 @@ void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw);
 // 1: the pipeline's kernels are launched as programmatic dependents (their
 // set-up overlaps the preceding kernel's tail); 0 (default): stream order
 void logreg_batched_set_pdl(LogregBatched* lb, int on);
+// K slices of the gradient contraction [r₁; r₂]·X on the tcgen05 path:
+// 1 .. 4, or 0 (automatic: enough slices to fill the SMs once)
+void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k);
+// the chain count the automatic rules (K slices of the gradient contraction,
+// chains per warp of the factorisation) size their grids for (default: the
+// context's own; the chain groups of one sampler pass the sampler's total,
+// so that results do not depend on the group count)
+void logreg_batched_set_auto_chains(LogregBatched* lb, int C);
 void logreg_batched_set_profile(LogregBatched* lb, int on);
 
 // D[M, N] = A[M, K]·B[N, K]ᵀ through the split-BF16 GEMM `impl` (test hook;

@@ -67,7 +67,7 @@ class Kernel:
     def __init__(self, sampler: int, integrator="implicit_midpoint", divergence_threshold=1000.0,
                  max_iters=100, tol=1e-6, alpha2_fix=False, logreg_path="auto", threads_per_block=None,
                  loop="graph", cholesky="fp64", chol_chains_per_warp=0, chain_groups=0,
-                 pdl=False):
+                 pdl=False, gemm_ksplit=0):
         if integrator not in INTEGRATORS:
             raise ValueError(f"integrator must be one of {sorted(INTEGRATORS)}")
         if logreg_path not in LOGREG_PATHS:
@@ -90,6 +90,8 @@ class Kernel:
         if chain_groups:
             self.options[L.GJ_OPT_CHAIN_GROUPS] = int(chain_groups)
         self.options[L.GJ_OPT_PDL] = 1 if pdl else 0
+        if gemm_ksplit:
+            self.options[L.GJ_OPT_GEMM_KSPLIT] = int(gemm_ksplit)
         if threads_per_block:
             self.options[L.GJ_OPT_THREADS_PER_BLOCK] = int(threads_per_block)
         self._ctx = {}
@@ -221,15 +223,16 @@ class rmhmc:
     @staticmethod
     def build_kernel(integrator="implicit_midpoint", divergence_threshold=1000.0, max_iters=100,
                      tol=1e-6, logreg_path="auto", loop="graph", cholesky="fp64",
-                     chol_chains_per_warp=0, chain_groups=0, pdl=False):
+                     chol_chains_per_warp=0, chain_groups=0, pdl=False, gemm_ksplit=0):
         """``rmhmc.py:110-176``; kernel(rng_key, state, target, step_size,
-        num_integration_steps).  ``logreg_path``, ``loop``, ``cholesky`` and
-        ``chol_chains_per_warp``, ``chain_groups`` and ``pdl`` select the
+        num_integration_steps).  ``logreg_path``, ``loop``, ``cholesky``,
+        ``chol_chains_per_warp``, ``chain_groups``, ``pdl`` and ``gemm_ksplit``
+        (K slices of the gradient contraction, 0 = automatic) select the
         implementation of the batched dense-Fisher path."""
         return Kernel(L.GJ_SAMPLER_RMHMC, integrator, divergence_threshold, max_iters, tol,
                       logreg_path=logreg_path, loop=loop, cholesky=cholesky,
                       chol_chains_per_warp=chol_chains_per_warp, chain_groups=chain_groups,
-                      pdl=pdl)
+                      pdl=pdl, gemm_ksplit=gemm_ksplit)
 
     def __new__(cls, target: Target, step_size: float, num_integration_steps: int, *,
                 divergence_threshold=1000.0, integrator="implicit_midpoint", max_iters=100,

@@ -238,6 +238,13 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * 0 (default) = ordinary stream order.  On GB300 at d = 25, 4096 chains,
  * PDL measured 2.28M against 2.53M leapfrog steps/s without it. */
 #define GJ_OPT_PDL 7
+/* batched path, tcgen05 GEMMs: K slices of the gradient contraction
+ * [r1; r2]·X (M = 2 x chains, N = d, K = observations), 1 .. 4, or 0
+ * (automatic, default: as many as fill the SMs once with at least 4 K
+ * blocks per slice).  Slice z writes its partial product to its own buffer
+ * and the consumers add the slices in order, so results do not depend on
+ * scheduling. */
+#define GJ_OPT_GEMM_KSPLIT 8
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */

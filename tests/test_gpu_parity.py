@@ -292,6 +292,34 @@ def test_logreg_batched_per_step(path, loop, chol, d, C, integrator):
     assert diff.max() <= 10 and diff.mean() < (2.5 if d < 32 else 5.0), (diff.max(), diff.mean())
 
 
+@pytest.mark.parametrize("ksplit", [1, 2, 3])
+def test_logreg_batched_gradient_ksplit(ksplit):
+    """The gradient contraction [r1; r2]·X with its K blocks split over 1, 2
+    or 3 CTAs per output tile (partial products added in slice order by the
+    consumers): per-step positions of the generalized leapfrog against the
+    oracle within 1e-5, as unsplit."""
+    import geomjax_gb300 as gj
+    from geomjax_gb300.base import Draws
+
+    kw = dict(N=300, d=9, seed=3)  # 5 K blocks of 64 observations
+    ot = oracle_target("logreg", **kw)
+    dt = device_target("logreg", "mixed", **kw)
+    C, h, L = 160, 0.05, 10
+    q0 = start_positions(ot.dim, C, seed=1, scale=0.2).astype(np.float32).astype(np.float64)
+    z, _ = normals(C, ot.dim, 2, np.float32)
+    u = -np.ones(C)
+    traj = []
+    O_rm.kernel(ot, O_rm.init(ot, q0), z, u, h, L, trajectory=traj, integrator=GL)
+    kern = gj.rmhmc.build_kernel(logreg_path="tcgen05", loop="graph", integrator=GL,
+                                 gemm_ksplit=ksplit)
+    st0 = gj.rmhmc.init(q0, dt)
+    for step in (1, 5, 10):
+        st, _ = kern(Draws(z, u), st0, dt, h, step)
+        e = rel_err(_np(st.position), traj[step - 1].position)
+        assert e < 1e-5, f"step {step}: {e}"
+        assert rel_err(_np(st.logdensity_grad), traj[step - 1].logdensity_grad) < 1e-4
+
+
 def test_logreg_batched_accept_and_graph_reuse():
     """Several transitions through one graph (the captured graph is reused and
     the step size changes between calls) agree with the oracle transition by
@@ -323,17 +351,19 @@ def test_logreg_batched_accept_and_graph_reuse():
     assert agree / total >= 0.99
 
 
-@pytest.mark.parametrize("groups", [2, 3])
-def test_logreg_batched_chain_groups_bitwise(groups):
+@pytest.mark.parametrize("groups,N,d,C", [(2, 300, 9, 301), (3, 300, 9, 301),
+                                         (2, 700, 25, 1024)])
+def test_logreg_batched_chain_groups_bitwise(groups, N, d, C):
     """Chains are independent: splitting them into groups whose graphs run on
     concurrent streams gives bit-identical transitions (positions, log
-    densities, accept decisions, energies, fixed-point counts)."""
+    densities, accept decisions, energies, fixed-point counts).  At N = 700,
+    d = 25 and 1024 chains the gradient contraction is split in K, the same
+    way for every group count."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
-    kw = dict(N=300, d=9, seed=3)
+    kw = dict(N=N, d=d, seed=3)
     dt = device_target("logreg", "mixed", **kw)
-    C = 301
     q0 = start_positions(dt.dim, C, seed=1, scale=0.2).astype(np.float32).astype(np.float64)
     rng = np.random.Generator(np.random.PCG64(5))
     out = {}
