@@ -66,6 +66,9 @@ struct Epi {
   int r_off;
   // EPI_SIGMOID, when set: ld_acc[m] += Σ_n [y_n a − log(1 + e^a)] (FP64 sum)
   double* ld_acc;
+  // EPI_SIGMOID, when set: Λ alone (the metric at a position iterate of the
+  // generalized leapfrog needs neither Λ' nor r₁)
+  int lam_only;
   // EPI_TRACE, when set: w is also stored into w_out[m, n] (stride s_ld)
   float* w_out;
   // EPI_R2W: a = s = x_nᵀu_m  ->  r2 = Λ'(w − s²) into r (rows r_off + m),
@@ -86,6 +89,7 @@ __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
     const float sg = 1.f / (1.f + __expf(-v));
     const float lam = sg * (1.f - sg);
     split_store(e.lam, m, n, lam);
+    if (e.lam_only) return;
     e.lp[(size_t)m * e.lp_ld + n] = lam * (1.f - 2.f * sg);
     split_store(e.r, m, n, e.y[n] - sg);
   } else if (e.mode == EPI_TRACE) {

@@ -227,8 +227,10 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
       }
       if (m < M) {
         split8(e.lam, m, n, N, full, lam);
-        store8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lp);
-        split8(e.r, m, n, N, full, r1);
+        if (!e.lam_only) {
+          store8(e.lp + (size_t)m * e.lp_ld + n, n, N, full && aligned16(e.lp, e.lp_ld), lp);
+          split8(e.r, m, n, N, full, r1);
+        }
       }
       if (e.ld_acc) {  // the 4 lanes of a row, then one atomic per row and chunk
         ld += __shfl_xor_sync(0xffffffffu, ld, 1);

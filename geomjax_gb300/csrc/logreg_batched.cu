@@ -100,6 +100,23 @@ struct CholArgs {
   double* Lout;        // DRAW / EVAL: the packed factor, kept for later solves (may be NULL)
   float* Lout32;       // DRAW / EVAL: the same in FP32 (may be NULL)
   int no_inverse;      // EVAL: stop after u = G⁻¹p (no L⁻¹, no packed G⁻¹)
+  // EVAL with no_inverse: the generalized leapfrog's position update
+  // q' = q0 + h/2 [G⁻¹(q0) + G⁻¹(q_k)] p½ (UP_GLQN of update_kernel) done
+  // here with u = G⁻¹(q_k)p½, with its convergence test
+  int q_update;
+  const StepDev* spd;  // graph path: h / tol / max_iters (else hh, tol, max_iters)
+  double hh, tol;
+  int max_iters;
+  const double* u0;    // G(q0)⁻¹p½
+  const double* q0;
+  double* qc;          // the position iterate
+  SplitMat Qb;         // its split copy for the Xβ contraction
+  double* norm;
+  int* iters;
+  int* iters_total;
+  uint8_t* active_w;   // the active set (the array `active` reads)
+  uint8_t* notconv;
+  int* n_active;       // set while some chain iterates
 };
 
 // Chain packing.  The FP64 pipe issues one warp instruction for all 32 lanes
@@ -248,6 +265,19 @@ __device__ __forceinline__ double group_sum(double v) {
 #pragma unroll
   for (int o = LPC >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+template <int LPC>
+__device__ __forceinline__ double group_max(double v) {
+#pragma unroll
+  for (int o = LPC >> 1; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <int LPC>
+__device__ __forceinline__ bool group_any(bool b) {
+  int v = b ? 1 : 0;
+#pragma unroll
+  for (int o = LPC >> 1; o > 0; o >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, o);
+  return v != 0;
 }
 
 template <typename F, int LPC>  // factorisation type (double / float), lanes per chain
@@ -448,7 +478,42 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       if (!a.no_inverse) split_store(a.Ub, c, i, to_f32(xv[i]));
     }
   }
-  if (a.no_inverse) return;  // uniform: the position solve needs u only
+  if (a.no_inverse) {  // uniform: the position solve needs u only
+    if (a.q_update) {
+      const double hh = a.spd ? 0.5 * a.spd->h : a.hh;
+      const double tol = a.spd ? a.spd->tol : a.tol;
+      const int max_iters = a.spd ? a.spd->max_iters : a.max_iters;
+      double nrm = 0.0;
+      bool nan = false;
+      if (live) {
+        for (int i = sl; i < d; i += LPC) {
+          const size_t o = (size_t)c * d + i;
+          const double qn = a.q0[o] + hh * (a.u0[o] + double(xv[i]));
+          const double e = qn - a.qc[o];
+          nan |= isnan(e);
+          nrm = fmax(nrm, fabs(e));
+          a.qc[o] = qn;
+          split_store(a.Qb, c, i, narrow_rn(qn));
+        }
+      }
+      nrm = group_max<LPC>(nrm);
+      if (group_any<LPC>(nan)) nrm = NAN;
+      bool act = false;
+      if (live) {
+        const int it = a.iters[c] + 1;
+        act = (it < max_iters) && isfinite(nrm) && (nrm < 1e10) && (nrm > tol);
+        if (sl == 0) {
+          a.iters[c] = it;
+          a.norm[c] = nrm;
+          a.active_w[c] = act;
+          a.iters_total[c] += 1;
+          if (!act && !(isfinite(nrm) && nrm <= tol)) a.notconv[c] = 1;
+        }
+      }
+      if (__any_sync(0xffffffffu, act) && lane == 0) *a.n_active = 1;
+    }
+    return;
+  }
   // L⁻¹ in FP32 by forward substitution of the identity, all columns at
   // once: row k is final once scaled, then rows i > k are reduced by it
   for (int t = sl; t < P; t += LPC) {
@@ -1200,6 +1265,7 @@ struct Runner {
   cudaStream_t st;
   cudaError_t err = cudaSuccess;
   const StepDev* spd = nullptr;  // graph path: step parameters in device memory
+  StepDev hsp{};                 // host path: the step parameters
 
   void gemm(const SplitMat& A, const TcOperand* ta, const SplitMat& B, const TcOperand* tb, int M,
             int N, int K, const Epi& e, int ksplit = 1, int a_row0 = 0) {
@@ -1263,11 +1329,12 @@ struct Runner {
 
   // metric at the current iterate: (1) and (2); with ld_acc the Xβ epilogue
   // also sums the data log likelihood per chain
-  void metric_gram(double* ld_acc = nullptr) {
+  void metric_gram(double* ld_acc = nullptr, bool lam_only = false) {
     LogregBatched& L = *lb;
     Epi e{};
     e.mode = EPI_SIGMOID;
     e.ld_acc = ld_acc;
+    e.lam_only = lam_only ? 1 : 0;
     e.y = static_cast<const float*>(L.t.y);
     e.lam = L.Lam;
     e.lp = L.Lp;
@@ -1283,9 +1350,26 @@ struct Runner {
 
   void chol(int mode, const float* z, double* logdet, double* quad, float* mom_info,
             bool only_active = false, float* vel_info = nullptr, double* Lout = nullptr,
-            bool no_inverse = false, float* Lout32 = nullptr) {
+            bool no_inverse = false, float* Lout32 = nullptr, bool q_update = false) {
     LogregBatched& L = *lb;
     CholArgs a{};
+    if (q_update) {
+      a.q_update = 1;
+      a.spd = spd;
+      a.hh = 0.5 * hsp.h;
+      a.tol = hsp.tol;
+      a.max_iters = hsp.max_iters;
+      a.u0 = L.u0;
+      a.q0 = L.q0;
+      a.qc = L.qc;
+      a.Qb = L.Qb;
+      a.norm = L.norm;
+      a.iters = L.iters;
+      a.iters_total = L.iters_total;
+      a.active_w = L.active;
+      a.notconv = L.notconv;
+      a.n_active = L.n_active_d;
+    }
     a.mode = mode;
     a.C = L.C;
     a.d = L.d;
@@ -1413,11 +1497,13 @@ struct Runner {
     L.stats.evals++;
   }
   // u = G(q_k)⁻¹ p½ at the position iterate (the factorisation without the
-  // inverse)
+  // inverse), and with it the position update and its convergence test
+  // (the loop body has no separate update)
   void q_eval(bool only_active) {
     LogregBatched& L = *lb;
-    metric_gram();
-    chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, only_active, nullptr, nullptr, true);
+    metric_gram(nullptr, true);
+    chol(CH_EVAL, nullptr, L.logdet1, L.quad1, nullptr, only_active, nullptr, nullptr, true,
+         nullptr, true);
     L.stats.evals++;
   }
   // everything at (qc, pc), keeping the factor and w for the next momentum
@@ -1531,12 +1617,14 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   lb->ev_used = 0;
   lb->cev_used = 0;
   Runner R{lb, gemm_impl, st};
+  R.hsp = sp;
   const int C = lb->C, d = lb->d;
   begin_kernel<<<(C + 127) / 128, 128, 0, st>>>(C, d, pos, lb->q0, lb->qc, lb->qf, lb->Qb,
                                                  lb->iters_total, lb->notconv, lb->bad);
   R.check(cudaGetLastError());
   // a fixed-point solve driven from the host: the eager update, then body +
-  // update while some chain is active (at most max_iters + 1 bodies)
+  // update while some chain is active (at most max_iters + 1 bodies); with
+  // iterated < 0 the body updates the iterate itself
   auto host_solve = [&](int eager, auto body, int iterated) {
     R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
     R.update(eager, sp);
@@ -1545,9 +1633,9 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
                               cudaMemcpyDeviceToHost, st));
       R.check(cudaStreamSynchronize(st));
       if (R.err != cudaSuccess || *lb->n_active_h == 0 || guard > sp.max_iters) break;
-      body();
       R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
-      R.update(iterated, sp);
+      body();
+      if (iterated >= 0) R.update(iterated, sp);
     }
   };
   for (int s = 0; gl && s < sp.L; ++s) {
@@ -1560,7 +1648,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
     host_solve(UP_GLP0, [&] { R.p_contract(); }, UP_GLPN);
     // (2) q' = q + h/2 [G⁻¹(q) + G⁻¹(q')] p½
     R.solve(lb->pc, lb->u0, false, false);
-    host_solve(UP_GLQ0, [&] { R.q_eval(true); }, UP_GLQN);
+    host_solve(UP_GLQ0, [&] { R.q_eval(true); }, -1);
     // (3) p' = p½ − h/2 ∂_qH(q', p½), keeping the factor and w at q' for the
     // next step's momentum solve
     R.full_eval(CH_EVAL, nullptr, nullptr);
@@ -1672,8 +1760,9 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGrap
                                                 lb->iters_total, lb->notconv, lb->bad);
   StepDev dummy{};
   // one fixed-point solve: the eager update, then a conditional WHILE node
-  // whose body is `body` + the iterated update, repeated while some chain is
-  // active (at most max_iters + 1 times)
+  // whose body is `body` + the iterated update (none when iterated < 0: the
+  // body updates the iterate itself), repeated while some chain is active
+  // (at most max_iters + 1 times)
   auto add_solve = [&](int eager, auto body, int iterated) -> cudaError_t {
     R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), s));
     R.update(eager, dummy);
@@ -1707,7 +1796,7 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGrap
     Runner B{lb, impl, lb->cap_body};
     B.spd = lb->spd;
     body(B);
-    B.update(iterated, dummy);
+    if (iterated >= 0) B.update(iterated, dummy);
     loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
     B.check(cudaGetLastError());
     cudaGraph_t bout = nullptr;
@@ -1727,7 +1816,7 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGrap
       e = add_solve(UP_GLP0, [](Runner& B) { B.p_contract(); }, UP_GLPN);
       if (e != cudaSuccess) break;
       R.solve(lb->pc, lb->u0, false, false);
-      e = add_solve(UP_GLQ0, [](Runner& B) { B.q_eval(true); }, UP_GLQN);
+      e = add_solve(UP_GLQ0, [](Runner& B) { B.q_eval(true); }, -1);
       if (e != cudaSuccess) break;
       R.full_eval(CH_EVAL, nullptr, nullptr);
       R.update(UP_GLPX, dummy);
