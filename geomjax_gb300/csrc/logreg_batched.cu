@@ -178,45 +178,6 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) 
   return c;
 }
 
-// Format conversions by integer operations on the IEEE-754 bit patterns.
-// GB300 issues FP64 work at 1/64 of the FP32 rate, and the factorisation's
-// FP64 pipe was half busy with conversions, compares and single-lane
-// scalar work on top of its multiply-adds; these keep that work on the
-// integer pipes.
-//
-// binary32 -> binary64: exact for normal values, zeros, infinities and NaNs;
-// subnormal inputs (below 1.2e-38) become a signed zero.
-__device__ __forceinline__ double widen_f32(float x) {
-  const uint32_t u = __float_as_uint(x);
-  const uint32_t ex = (u >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  const unsigned long long man = (unsigned long long)(u & 0x7fffffu) << 29;
-  unsigned long long b = sign;
-  if (ex == 0xffu)
-    b |= (0x7ffull << 52) | man;
-  else if (ex != 0u)
-    b |= ((unsigned long long)(ex + 896u) << 52) | man;
-  return __longlong_as_double((long long)b);
-}
-// binary64 -> binary32 rounded to nearest even: integer operations for
-// results in the normal binary32 range (a mantissa carry rounds into the
-// exponent, up to infinity), the conversion instruction for the rest
-// (zeros, subnormal results, overflow, infinities and NaNs)
-__device__ __forceinline__ float narrow_rn(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ffu) - 896;  // biased binary32 exponent
-  if (e < 1 || e > 254) return float(x);
-  const uint32_t m = (uint32_t)(b >> 29) & 0x7fffffu;
-  const uint32_t rem = (uint32_t)b & 0x1fffffffu;  // the 29 dropped bits
-  const uint32_t up = (uint32_t)(rem > 0x10000000u) | ((uint32_t)(rem == 0x10000000u) & m);
-  const uint32_t r = (((uint32_t)e << 23) | m) + up;
-  return __uint_as_float(r | ((uint32_t)(b >> 32) & 0x80000000u));
-}
-__device__ __forceinline__ double to_fp(double, float x) { return widen_f32(x); }
-__device__ __forceinline__ float to_fp(float, float x) { return x; }
-__device__ __forceinline__ float to_f32(double x) { return narrow_rn(x); }
-__device__ __forceinline__ float to_f32(float x) { return x; }
-
 // Reciprocal square root of a pivot, without a division, and the pivot's
 // validity.  A usable FP64 pivot is positive, finite and at least 2^-1021
 // (a Schur complement of Gram + I/s² is at least 1/s²); any other marks the
@@ -236,7 +197,7 @@ __device__ __forceinline__ double pivot_rsqrt(double a, bool& bad) {
   if (e < -126 || e > 127) return 1.0 / sqrt(a);
   const float af = __uint_as_float(((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu));
   const float xf = rsqrtf(af);
-  const double x = widen_f32(xf), hx = widen_f32(0.5f * xf);
+  const double x = double(xf), hx = double(0.5f * xf);
   return x * fma(-(a * x), hx, 1.5);
 }
 __device__ __forceinline__ float pivot_rsqrt(float a, bool& bad) {
@@ -311,7 +272,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     const bool diag = (ik & 0xffffu) == (ik >> 16);
     F g;
     if (live) {
-      g = to_fp(F(0), a.Gv[(size_t)c * a.gv_ld + t]);
+      g = F(a.Gv[(size_t)c * a.gv_ld + t]);
       if (diag) g += F(a.prior_inv);
     } else {
       g = diag ? F(1) : F(0);
@@ -419,13 +380,13 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
       const double v = i == k ? double(rdiag[i]) : double(L[t]);
       if (a.Lout) a.Lout[(size_t)c * P + t] = v;
-      if (a.Lout32) a.Lout32[(size_t)c * P + t] = narrow_rn(v);
+      if (a.Lout32) a.Lout32[(size_t)c * P + t] = float(v);
     }
   }
   // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
   // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
-    for (int i = sl; i < d; i += LPC) y[i] = live ? to_fp(F(0), a.z[(size_t)c * d + i]) : F(0);
+    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
     __syncwarp();
     double zz = 0.0;
     for (int i = sl; i < d; i += LPC) {
@@ -438,7 +399,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       if (live) {
         a.p0[(size_t)c * d + i] = double(sacc);
         a.pc[(size_t)c * d + i] = double(sacc);
-        if (a.mom_info) a.mom_info[(size_t)c * d + i] = to_f32(sacc);
+        if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
       }
       zz += double(y[i]) * double(y[i]);
     }
@@ -467,7 +428,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   }
   if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
     if (live)
-      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = to_f32(-xv[i]);
+      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = float(-xv[i]);
     return;
   }
   if (live) {
@@ -475,7 +436,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       a.u[(size_t)c * d + i] = double(xv[i]);
       // the position iterates (no inverse) use u alone; the split copy
       // feeds the S contraction of full evaluations
-      if (!a.no_inverse) split_store(a.Ub, c, i, to_f32(xv[i]));
+      if (!a.no_inverse) split_store(a.Ub, c, i, float(xv[i]));
     }
   }
   if (a.no_inverse) {  // uniform: the position solve needs u only
@@ -493,7 +454,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
           nan |= isnan(e);
           nrm = fmax(nrm, fabs(e));
           a.qc[o] = qn;
-          split_store(a.Qb, c, i, narrow_rn(qn));
+          split_store(a.Qb, c, i, float(qn));
         }
       }
       nrm = group_max<LPC>(nrm);
@@ -526,13 +487,13 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   // by both in one pass
   int ck = 0;  // colstart(k)
   for (int k = 0; k < d; k += 2) {
-    const float ikk = to_f32(rdiag[k]);
+    const float ikk = float(rdiag[k]);
     for (int cc = sl; cc <= k; cc += LPC) Li[colstart(cc, d) + k - cc] *= ikk;
     __syncwarp();
     const int ck1 = ck + (d - k);  // colstart(k + 1)
     if (k + 1 == d) break;
-    const float l10 = to_f32(L[ck + 1]);  // L(k + 1, k)
-    const float ik1 = to_f32(rdiag[k + 1]);
+    const float l10 = float(L[ck + 1]);  // L(k + 1, k)
+    const float ik1 = float(rdiag[k + 1]);
     for (int cc = sl; cc <= k + 1; cc += LPC) {
       const int o = colstart(cc, d);
       const float v = (cc <= k) ? Li[o + k + 1 - cc] - l10 * Li[o + k - cc] : Li[o];
@@ -540,8 +501,8 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     }
     __syncwarp();
     for (int i = k + 2 + sl; i < d; i += LPC) {
-      const float li0 = to_f32(L[ck + i - k]);       // L(i, k)
-      const float li1 = to_f32(L[ck1 + i - k - 1]);  // L(i, k + 1)
+      const float li0 = float(L[ck + i - k]);       // L(i, k)
+      const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
       int cc0 = 0;  // colstart(cc)
       for (int cc = 0; cc <= k; ++cc) {
         Li[cc0 + i - cc] -= li0 * Li[cc0 + k - cc] + li1 * Li[cc0 + k + 1 - cc];
@@ -832,7 +793,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps) solve_kernel(int C, int d, i
     const int i = lane + 32 * k;
     if (i < d) {
       if (u) u[(size_t)c * d + i] = double(y[k]);
-      if (split) split_store(Ub, c, i, to_f32(y[k]));
+      if (split) split_store(Ub, c, i, float(y[k]));
     }
   }
 }
@@ -876,7 +837,7 @@ __global__ void __launch_bounds__(32 * kSolveWarps) glp_update_solve_kernel(UpdA
         nan |= isnan(e);
         nrm = fmax(nrm, fabs(e));
         a.pc[o] = pn;
-        y[k] = narrow_rn(pn);
+        y[k] = float(pn);
       }
     }
     nrm = warp_max(nrm);
