@@ -86,6 +86,10 @@ def test_argument_checks_without_gpu():
     assert lib.gj_set_option(h, L.GJ_OPT_THREADS_PER_BLOCK, 64) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_PDL, 2) == L.GJ_EINVAL
     assert lib.gj_set_option(h, L.GJ_OPT_PDL, 0) == L.GJ_OK
+    assert lib.gj_set_option(h, L.GJ_OPT_GEMM_KSPLIT, 5) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_GEMM_KSPLIT, -1) == L.GJ_EINVAL
+    for v in range(5):
+        assert lib.gj_set_option(h, L.GJ_OPT_GEMM_KSPLIT, v) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 2) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(96, 1) == L.GJ_EINVAL
     # batch creation checks its arguments before touching the GPU
