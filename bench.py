@@ -103,30 +103,42 @@ MONGE_FLOPS_PER_DIM = 72
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms.
+
+    ``start`` waits (at most 3 s) for nvidia-smi's first sample, so that the
+    sampler runs when the timed region begins; ``stop`` keeps the samples that
+    arrived after ``start`` returned (all of them if none did)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
-        self.samples = []
+    def __init__(self, gpu_index=0, interval_ms=50):
+        self.samples = []  # (arrival time, fields)
         self.proc = None
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
+        self.t_mark = None
 
-    def start(self):
+    def start(self, wait_s=3.0):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.samples and self.proc.poll() is None and time.perf_counter() - t0 < wait_s:
+            time.sleep(0.005)
+        self.t_mark = time.perf_counter()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
+            self.samples.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
     def stop(self):
         if self.proc is None:
@@ -138,7 +150,8 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
+        timed = [s for t, s in self.samples if self.t_mark is not None and t >= self.t_mark]
+        for s in timed or [s for _, s in self.samples]:
             try:
                 sm.append(float(s[1]))
                 mx = float(s[2])
