@@ -767,6 +767,11 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
     for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_chol_cpw(lb, (int)value);
     return GJ_OK;
   }
+  if (key == GJ_OPT_GEMM_KSPLIT) {
+    if (value < 0 || value > 4) return fail(GJ_EINVAL, "K slices must be 0 (automatic) .. 4");
+    for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_gemm_ksplit(lb, (int)value);
+    return GJ_OK;
+  }
   return fail(GJ_EINVAL, "unknown batch option");
 }
 

@@ -355,7 +355,8 @@ typedef struct gj_batch gj_batch;
 int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
                         int32_t chains_per_posterior, int32_t num_streams, gj_batch** out);
 int32_t gj_batch_destroy(gj_batch* batch);
-/* GJ_OPT_CHOL_FP64 and GJ_OPT_CHOL_CHAINS_PER_WARP, for every posterior */
+/* GJ_OPT_CHOL_FP64, GJ_OPT_CHOL_CHAINS_PER_WARP and GJ_OPT_GEMM_KSPLIT, for
+ * every posterior */
 int32_t gj_batch_set_option(gj_batch* batch, int32_t key, int64_t value);
 int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_chain_state* state,
                             const float* z, const double* u, gj_info* info, void* stream);
