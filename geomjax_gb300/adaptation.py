@@ -72,19 +72,30 @@ def welford_init(d, diagonal=True, device="cpu"):
 
 
 def welford_update(s: WelfordState, value: torch.Tensor) -> WelfordState:
-    """mass_matrix.py:206-230, one sample per call; a [C, d] batch is folded
-    in row by row (the pooled estimator over chains)."""
+    """mass_matrix.py:206-230 (the pooled estimator over chains).
+
+    The reference folds in one sample per call.  A [C, d] batch of chain
+    positions is folded in at once by the pairwise combination of two
+    Welford states (Chan, Golub and LeVeque 1979): the batch's own mean and
+    sum of squared deviations, then n·n_b/(n + n_b)·δδᵀ for the shift
+    between the two means.  The result is the row-by-row recursion's up to
+    rounding, in a handful of kernels whatever C is."""
     value = value.double()
     if value.ndim == 1:
         value = value[None]
-    mean, m2, n = s.mean, s.m2, s.count
-    for x in value:
-        n += 1
-        delta = x - mean
-        mean = mean + delta / n
-        upd = x - mean
-        m2 = m2 + (delta * upd if m2.ndim == 1 else torch.outer(upd, delta))
-    return WelfordState(mean, m2, n)
+    n_b = value.shape[0]
+    if n_b == 0:
+        return s
+    mean_b = value.mean(0)
+    dev = value - mean_b
+    m2_b = (dev * dev).sum(0) if s.m2.ndim == 1 else dev.T @ dev
+    n = s.count
+    tot = n + n_b
+    delta = mean_b - s.mean
+    mean = s.mean + delta * (n_b / tot)
+    w = n * n_b / tot
+    m2 = s.m2 + m2_b + (delta * delta * w if s.m2.ndim == 1 else torch.outer(delta, delta) * w)
+    return WelfordState(mean, m2, tot)
 
 
 def welford_covariance(s: WelfordState):

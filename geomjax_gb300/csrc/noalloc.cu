@@ -4,15 +4,16 @@
 // cudaMalloc on every call.  Some callers cannot do that: a kernel embedded in
 // an XLA custom call runs while the framework's allocator owns nearly all
 // device memory (a stray cudaMalloc can fail, or fragment the pool it
-// reserved), and code recorded into a CUDA graph by stream capture may not
-// allocate at all.  This file serves them from one file-scope device array
-// that every GPU loading the library holds until the process exits.
+// reserved).  This file serves them from one file-scope device array that
+// every GPU loading the library holds until the process exits.
 //
 // The array is shared by every call: overlapping calls on the GPU (two
 // streams, or two host threads) race on it and must be serialised by the
 // caller.  Each call rewrites every element it reads (the split kernel also
-// writes the zero padding that the TMA boxes read), so a call never sees the
-// previous call's contents.
+// writes the zero padding that the TMA boxes read, and the error word in the
+// header is cleared first), so a call never sees the previous call's contents.
+#include <atomic>
+#include <mutex>
 #include <string>
 
 #include "gemm.cuh"
@@ -26,8 +27,14 @@ constexpr size_t kHeaderElems = 128;                 // 256 bytes
 constexpr size_t kScratchElems = size_t(4) << 20;    // 4,194,304 BF16 elements
 static __device__ __align__(256) bf16 g_scratch[kHeaderElems + kScratchElems];
 
+// Largest M, N or K accepted before any rounding (the capacity check below
+// rejects far smaller problems anyway; this bound keeps the rounding in range).
+constexpr int kMaxDim = 1 << 24;
+
 constexpr int kMaxDevices = 64;
-bf16* g_base[kMaxDevices];  // device address of g_scratch, per device
+// device address of g_scratch, per device; written once under g_setup_mu
+std::atomic<bf16*> g_base[kMaxDevices];
+std::mutex g_setup_mu;
 thread_local std::string g_err;
 
 inline int roundup(int x, int m) { return (x + m - 1) / m * m; }
@@ -60,14 +67,17 @@ int setup(int* dev_out) {
     g_err = "device index beyond the no-allocation entry point's table";
     return GJ_ENOTSUP;
   }
-  if (!g_base[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) {
-      g_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-      return GJ_ECUDA;
+  if (!g_base[dev].load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!g_base[dev].load(std::memory_order_relaxed)) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_scratch);
+      if (e != cudaSuccess || !p) {
+        g_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+        return GJ_ECUDA;
+      }
+      g_base[dev].store(static_cast<bf16*>(p), std::memory_order_release);
     }
-    g_base[dev] = static_cast<bf16*>(p);
   }
   *dev_out = dev;
   return GJ_OK;
@@ -86,6 +96,11 @@ int gemm_split_noalloc(int impl, int planes, int M, int N, int K, const float* A
     g_err = "bad arguments (impl 1 or 2, planes 2 or 3, positive sizes, device arrays)";
     return GJ_EINVAL;
   }
+  if (M > kMaxDim || N > kMaxDim || K > kMaxDim) {
+    g_err = "problem exceeds the no-allocation scratch: planes * (ceil128(M) + ceil128(N)) * "
+            "ceil64(K) must be <= 4194304";
+    return GJ_EINVAL;
+  }
   const int ld = roundup(K, 64);
   const size_t a_elems = (size_t)planes * roundup(M, 128) * ld;
   const size_t b_elems = (size_t)planes * roundup(N, 128) * ld;
@@ -97,10 +112,21 @@ int gemm_split_noalloc(int impl, int planes, int M, int N, int K, const float* A
   int dev = 0;
   int rc = setup(&dev);
   if (rc) return rc;
-  bf16* base = g_base[dev];
+  // the tcgen05 operands are checked before anything is enqueued, so a
+  // refused call leaves the stream untouched
+  TcOperand ta, tb;
+  bf16* base = g_base[dev].load(std::memory_order_acquire);
   int* err = reinterpret_cast<int*>(base);  // header
   SplitMat a{base + kHeaderElems, M, K, ld, roundup(M, 128), planes};
   SplitMat b{a.p + a_elems, N, K, ld, roundup(N, 128), planes};
+  if (impl == 2) {
+    const char* msg = "tcgen05 unavailable";
+    if (!tc_available() || gemm_tc_prepare() != cudaSuccess || !tc_operand_init(&ta, a, &msg) ||
+        !tc_operand_init(&tb, b, &msg)) {
+      g_err = msg;
+      return GJ_ENOTSUP;
+    }
+  }
   cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), st);
   if (e == cudaSuccess) {
     split_padded_kernel<<<304, 256, 0, st>>>(A, M, K, a);
@@ -119,13 +145,6 @@ int gemm_split_noalloc(int impl, int planes, int M, int N, int K, const float* A
   g.epi.ldd = N;
   if (e == cudaSuccess) {
     if (impl == 2) {
-      TcOperand ta, tb;
-      const char* msg = "tcgen05 unavailable";
-      if (!tc_available() || gemm_tc_prepare() != cudaSuccess || !tc_operand_init(&ta, a, &msg) ||
-          !tc_operand_init(&tb, b, &msg)) {
-        g_err = msg;
-        return GJ_ENOTSUP;
-      }
       e = gemm_tc(g, &ta, &tb, err, st);
     } else {
       e = gemm_simt(g, st);

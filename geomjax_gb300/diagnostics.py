@@ -42,12 +42,15 @@ def potential_scale_reduction(x, chain_axis=0, sample_axis=1):
     return torch.sqrt((B / W + n - 1) / n).squeeze()
 
 
-def effective_sample_size(x, chain_axis=0, sample_axis=1):
+def autocovariance_stats(x, chain_axis=0, sample_axis=1):
+    """The sufficient statistics of the ESS over a set of chains: the sum over
+    chains of each chain's centred FFT autocovariance (diagnostics.py:131-143),
+    [N, ...], and the chain means, [M, ...].  Sums from disjoint sets of chains
+    add, so ranks that hold different chains reduce these instead of
+    gathering their traces."""
     x = torch.as_tensor(x).double()
     x = torch.movedim(x, (chain_axis, sample_axis), (0, 1))
-    M, N = x.shape[0], x.shape[1]
-    if M < 2:
-        raise ValueError("effective_sample_size needs two or more chains")
+    N = x.shape[1]
     if N < 4:
         raise ValueError("effective_sample_size needs at least four samples per chain")
     mean = x.mean(dim=1, keepdim=True)
@@ -55,9 +58,19 @@ def effective_sample_size(x, chain_axis=0, sample_axis=1):
     m = _next_fast_len(2 * N)
     f = torch.fft.rfft(cen, n=m, dim=1)
     acov = torch.fft.irfft(f * f.conj(), n=m, dim=1)[:, :N] / N
-    mean_acov = acov.mean(dim=0)
+    return acov.sum(dim=0), mean[:, 0]
+
+
+def ess_from_stats(acov_sum, chain_means):
+    """ESS from ``autocovariance_stats`` (diagnostics.py:144-209): mean
+    autocovariance over chains, Geyer's initial positive then monotone
+    sequence, τ̂ floored at 1/log10(MN), ESS = MN/τ̂."""
+    M, N = chain_means.shape[0], acov_sum.shape[0]
+    if M < 2:
+        raise ValueError("effective_sample_size needs two or more chains")
+    mean_acov = acov_sum / M
     mean_var0 = mean_acov[0] * N / (N - 1.0)
-    weighted_var = mean_var0 * (N - 1.0) / N + mean[:, 0].var(dim=0, unbiased=True)
+    weighted_var = mean_var0 * (N - 1.0) / N + chain_means.var(dim=0, unbiased=True)
     n_even = N - N % 2
     rho = torch.cat([torch.ones_like(mean_var0)[None],
                      1.0 - (mean_var0[None] - mean_acov[1:n_even]) / weighted_var[None]], dim=0)
@@ -65,7 +78,7 @@ def effective_sample_size(x, chain_axis=0, sample_axis=1):
     T = rho_even.shape[0]
     mask0 = (rho_even + rho_odd) > 0.0
     mask = torch.cumprod(mask0.to(torch.int64), dim=0).bool()
-    tt = torch.arange(T, device=x.device).view((T,) + (1,) * (mask.ndim - 1))
+    tt = torch.arange(T, device=acov_sum.device).view((T,) + (1,) * (mask.ndim - 1))
     max_t = torch.where(mask, tt, torch.zeros_like(tt)).max(dim=0).values
     rho_odd = torch.where(mask, rho_odd, torch.zeros_like(rho_odd))
     idx = torch.clamp(max_t + 1, max=T - 1)
@@ -86,6 +99,13 @@ def effective_sample_size(x, chain_axis=0, sample_axis=1):
     tau = -1.0 + 2.0 * torch.sum(rho_even_f + rho_odd_f, dim=0) - last
     tau = torch.clamp(tau, min=1.0 / math.log10(ess_raw))
     return (ess_raw / tau).squeeze()
+
+
+def effective_sample_size(x, chain_axis=0, sample_axis=1):
+    x = torch.as_tensor(x)
+    if x.shape[chain_axis] < 2:
+        raise ValueError("effective_sample_size needs two or more chains")
+    return ess_from_stats(*autocovariance_stats(x, chain_axis, sample_axis))
 
 
 ess = effective_sample_size

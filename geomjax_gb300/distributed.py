@@ -3,10 +3,10 @@ multi-GPU run gives each rank its own chains and needs no collective while
 sampling.  Collectives appear only around the sampling phase:
 
 * the wall time of a measured phase is the maximum over ranks;
-* the min-ESS over all chains needs the ranks' traces together: each rank
-  contributes its [samples, chains, d] trace and the ESS is taken over the
-  concatenated chain axis (the reference's ESS over all chains,
-  ``diagnostics.py:78-209``).
+* the min-ESS over all chains (the reference's ESS over all chains,
+  ``diagnostics.py:78-209``) needs only two statistics of each rank's
+  chains: the sum of their autocovariances ([samples, d], one all-reduce)
+  and their means ([chains, d], one all-gather).  No trace leaves its rank.
 
 The functions take an initialised ``torch.distributed`` process group (NCCL
 on GPUs, gloo on CPU) and run on a single process without one.
@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import torch
 
-from .diagnostics import effective_sample_size
+from .diagnostics import autocovariance_stats, effective_sample_size, ess_from_stats
 
 
 def _dist():
@@ -61,7 +61,15 @@ def gather_chains(trace: torch.Tensor, chain_axis: int = 1) -> torch.Tensor:
 
 
 def global_min_ess(trace: torch.Tensor, chain_axis: int = 1, sample_axis: int = 0) -> float:
-    """min over dimensions of the ESS over all ranks' chains."""
-    full = gather_chains(trace, chain_axis)
-    return float(torch.min(effective_sample_size(full, chain_axis=chain_axis,
-                                                 sample_axis=sample_axis)).item())
+    """min over dimensions of the ESS over all ranks' chains.  Each rank
+    reduces its own trace to (Σ_c autocovariance_c, chain means); the sums
+    are all-reduced and the means all-gathered (chain counts may differ), so
+    the traffic is samples·d + chains·d doubles, not the traces."""
+    dist = _dist()
+    if dist is None or dist.get_world_size() == 1:
+        return float(torch.min(effective_sample_size(trace, chain_axis=chain_axis,
+                                                     sample_axis=sample_axis)).item())
+    acov_sum, means = autocovariance_stats(trace, chain_axis, sample_axis)
+    dist.all_reduce(acov_sum, op=dist.ReduceOp.SUM)
+    all_means = gather_chains(means, chain_axis=0)
+    return float(torch.min(ess_from_stats(acov_sum, all_means)).item())

@@ -206,10 +206,15 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
                   int32_t num_chains, gj_ctx** out);
 int32_t gj_destroy(gj_ctx* ctx);
 
-/* Selects the implementation of the dense-Fisher logistic-regression RMHMC
- * path in GJ_MIXED: 0 = automatic (batched tensor-core pipeline),
- * 1 = batched pipeline with the SIMT FP32 GEMM, 2 = batched pipeline with the
- * tcgen05 BF16 hi/lo GEMM, 3 = per-chain kernel. */
+/* Selects the implementation of the dense-Fisher logistic-regression paths.
+ * RMHMC: 0 = automatic (GJ_MIXED: batched tensor-core pipeline; GJ_FP64: one
+ * CTA per chain), 1 = batched pipeline with the SIMT FP32 GEMM, 2 = batched
+ * pipeline with the tcgen05 BF16 hi/lo GEMM, 3 = one thread per chain
+ * (d <= 32), 4 = one CTA per chain in either precision (d <= 64; shared
+ * memory of (3d(d+1)/2 + 16d + 276)·8 + (4N + max(N, 16d))·sizeof(T) +
+ * 16(d+1)·sizeof(T) bytes, at most 227 KB, else GJ_ENOTSUP).
+ * Dense LMC: 3 = one thread per chain (d <= 32), any other value = one CTA
+ * per chain (d <= 64). */
 int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
 #define GJ_OPT_LOGREG_PATH 1
 /* threads per block of the per-chain kernels: 32, 64, 96 or 128 (default) */
@@ -303,18 +308,19 @@ int32_t gj_gemm_split_bf16(int32_t impl, int32_t planes, int32_t M, int32_t N, i
 
 /* The same contraction as gj_gemm_split_bf16, for callers that cannot
  * allocate device memory: a JAX/XLA custom call, whose framework has
- * reserved nearly all device memory for its own pool, or work recorded by
- * stream capture.  It calls no cudaMalloc, cudaFree or allocating library
- * routine: its split planes live in one static device array of 8 MiB
- * (4,194,304 BF16 elements) that every GPU loading the library holds until
- * the process exits.  Limit: planes * (ceil128(M) + ceil128(N)) * ceil64(K)
- * <= 4194304, otherwise GJ_EINVAL.  All calls share the array: calls that
- * overlap on the GPU (other streams or host threads) race on it and must be
- * serialised by the caller; every call rewrites all of the array it reads.
- * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Synchronises the stream.  No counterpart in
- * the reference. */
+ * reserved nearly all device memory for its own pool, so that a cudaMalloc
+ * of its own can fail or fragment that pool.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: its split planes live in one
+ * static device array of 8 MiB (4,194,304 BF16 elements) that every GPU
+ * loading the library holds until the process exits.  Limit: planes *
+ * (ceil128(M) + ceil128(N)) * ceil64(K) <= 4194304, otherwise GJ_EINVAL.
+ * All calls share the array: calls that overlap on the GPU (other streams or
+ * host threads) race on it and must be serialised by the caller; every call
+ * rewrites all of the array it reads.  The first call on each device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Ends with a
+ * synchronisation of the stream (it reads the kernel's error word back).
+ * No counterpart in the reference. */
 int32_t gj_gemm_split_bf16_noalloc(int32_t impl, int32_t planes, int32_t M, int32_t N,
                                    int32_t K, const float* A, const float* B, float* D,
                                    void* stream);

@@ -60,6 +60,27 @@ def test_welford(diagonal):
     np.testing.assert_allclose(im, exp, rtol=1e-10)
 
 
+@pytest.mark.parametrize("diagonal", [True, False])
+def test_welford_batch_equals_one_sample_per_call(diagonal):
+    """Folding a [C, d] batch in at once gives the reference's one-sample
+    recursion (mass_matrix.py:206-230), restated here row by row."""
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((300, 5)) * 3.0 + 10.0
+    s = A.welford_init(5, diagonal)
+    for blk in (x[:1], x[1:130], x[130:131], x[131:]):
+        s = A.welford_update(s, torch.tensor(blk))
+    mean = np.zeros(5)
+    m2 = np.zeros(5) if diagonal else np.zeros((5, 5))
+    for n, v in enumerate(x, start=1):
+        delta = v - mean
+        mean = mean + delta / n
+        upd = v - mean
+        m2 = m2 + (delta * upd if diagonal else np.outer(upd, delta))
+    assert s.count == 300
+    np.testing.assert_allclose(s.mean.numpy(), mean, rtol=1e-13)
+    np.testing.assert_allclose(s.m2.numpy(), m2, rtol=1e-11)
+
+
 def test_gradient_step_size_adaptation_brackets_and_converges(monkeypatch):
     """The safeguarded Newton iteration on a synthetic acceptance curve: a
     smooth decreasing p(h) with a chain that diverges (contributing NaN)
