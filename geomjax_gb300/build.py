@@ -27,6 +27,7 @@ UNITS = [
     ("chain_kernels.cu", ["-DGJ_CHAIN_PREC=1"]),
     ("chain_kernels.cu", ["-DGJ_CHAIN_PREC=2"]),
     ("monge_warp.cu", []),
+    ("logreg_cta.cu", []),
     ("logreg_batched.cu", []),
     ("gemm_simt.cu", []),
     ("gemm_tc.cu", []),

@@ -233,7 +233,7 @@ int32_t gj_destroy(gj_ctx* ctx) {
 int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
   if (!ctx) return fail(GJ_EINVAL, "ctx is NULL");
   if (key == GJ_OPT_LOGREG_PATH) {
-    if (value < 0 || value > 3) return fail(GJ_EINVAL, "logreg path must be 0..3");
+    if (value < 0 || value > 4) return fail(GJ_EINVAL, "logreg path must be 0..4");
     ctx->logreg_path = (int)value;
     return GJ_OK;
   }
@@ -315,8 +315,9 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   // dense-Fisher logistic regression in mixed precision: batched pipeline
+  // (paths 0, 1, 2; 3 is one thread per chain, 4 one CTA per chain)
   if (ctx->precision == GJ_MIXED && t.family == GJ_LOGREG && t.metric == GJ_METRIC_DENSE_FISHER &&
-      ctx->logreg_path != 3) {
+      ctx->logreg_path != 3 && ctx->logreg_path != 4) {
     int rc = ensure_groups(ctx, t);
     if (rc) return rc;
     const int gemm = (ctx->logreg_path == 1) ? 1 : 2;
@@ -353,8 +354,26 @@ int32_t gj_rmhmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, c
           return fail(GJ_ECUDA, "stream wait failed");
     return GJ_OK;
   }
-  if (t.d > 32) return fail(GJ_ENOTSUP, "per-chain RMHMC supports d <= 32");
   cudaError_t e;
+  // dense-Fisher logistic regression, one CTA per chain: the plain FP64 form
+  // by default (path 0), either precision on request (path 4)
+  if (t.family == GJ_LOGREG && t.metric == GJ_METRIC_DENSE_FISHER &&
+      (ctx->logreg_path == 4 || (ctx->logreg_path == 0 && ctx->precision == GJ_FP64))) {
+    const bool mixed = ctx->precision == GJ_MIXED;
+    if (!gj::logreg_cta_supported(t.d, t.n, mixed, 0))
+      return fail(GJ_ENOTSUP, "CTA-per-chain logistic regression needs d <= 64 and the chain's "
+                              "shared memory within 227 KB");
+    if (!mixed)
+      e = gj::launch_logreg_cta<double>(GJ_SAMPLER_RMHMC, t, sp, (double*)s->position,
+                                        (double*)s->logdensity_grad, s->logdensity, nullptr,
+                                        (const double*)z, u, gj::to_dev<double>(info), ctx->C, cs);
+    else
+      e = gj::launch_logreg_cta<float>(GJ_SAMPLER_RMHMC, t, sp, (float*)s->position,
+                                       (float*)s->logdensity_grad, s->logdensity, nullptr,
+                                       (const float*)z, u, gj::to_dev<float>(info), ctx->C, cs);
+    return cuda_status(e, "gj_rmhmc_step");
+  }
+  if (t.d > 32) return fail(GJ_ENOTSUP, "per-chain RMHMC supports d <= 32");
   if (ctx->precision == GJ_FP64)
     e = gj::launch_rmhmc_chain<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
                                        s->logdensity, (const double*)z, u,
@@ -421,10 +440,29 @@ int32_t gj_lmc_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s, con
   if (st) return st;
   if (!z || !u) return fail(GJ_EINVAL, "z and u must be device arrays");
   const gj::TargetDev t = gj::to_dev(ctx->target);
-  if (t.d > 32) return fail(GJ_ENOTSUP, "dense LMC supports d <= 32");
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   cudaError_t e;
+  // dense-Fisher logistic regression: one CTA per chain (d <= 64), unless the
+  // thread-per-chain kernel is asked for (path 3)
+  if (t.family == GJ_LOGREG && t.metric == GJ_METRIC_DENSE_FISHER && ctx->logreg_path != 3) {
+    const bool mixed = ctx->precision == GJ_MIXED;
+    if (!gj::logreg_cta_supported(t.d, t.n, mixed, 1))
+      return fail(GJ_ENOTSUP, "CTA-per-chain dense LMC needs d <= 64 and the chain's shared "
+                              "memory within 227 KB");
+    if (!mixed)
+      e = gj::launch_logreg_cta<double>(GJ_SAMPLER_LMC, t, sp, (double*)s->position,
+                                        (double*)s->logdensity_grad, s->logdensity,
+                                        s->volume_adjustment, (const double*)z, u,
+                                        gj::to_dev<double>(info), ctx->C, cs);
+    else
+      e = gj::launch_logreg_cta<float>(GJ_SAMPLER_LMC, t, sp, (float*)s->position,
+                                       (float*)s->logdensity_grad, s->logdensity,
+                                       s->volume_adjustment, (const float*)z, u,
+                                       gj::to_dev<float>(info), ctx->C, cs);
+    return cuda_status(e, "gj_lmc_step");
+  }
+  if (t.d > 32) return fail(GJ_ENOTSUP, "dense LMC supports d <= 32");
   if (ctx->precision == GJ_FP64)
     e = gj::launch_lmc_chain<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
                                      s->logdensity, s->volume_adjustment, (const double*)z, u,

@@ -43,6 +43,17 @@ cudaError_t launch_gl_trajectory_jvp(const double* X, const double* y, int N, in
                                      double h, double lam, int L, int Kp, int Kq, int tangents,
                                      double* out, cudaStream_t st);
 
+// dense-Fisher logistic regression, one CTA per chain (logreg_cta.cu):
+// RMHMC (either integrator) or dense LMC for d <= 64 while the chain's shared
+// memory fits 227 KB; T = double is the plain FP64 form, T = float the mixed
+// form (FP32 per-datum arithmetic, FP64 factor, solves and iterates)
+size_t logreg_cta_smem(int d, int N, int mixed, int lmc);
+bool logreg_cta_supported(int d, int N, int mixed, int lmc);
+template <typename T>
+cudaError_t launch_logreg_cta(int sampler, const TargetDev& t, const StepDev& sp, T* pos, T* grad,
+                              double* ld, double* vol, const T* z, const double* u,
+                              const InfoDev<T>& info, int C, cudaStream_t st);
+
 // warp-per-chain LMC-Monge (monge_warp.cu), float32 state
 cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,
                               double* ld, double* vol, const float* z, const double* u,

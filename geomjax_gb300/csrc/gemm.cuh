@@ -77,21 +77,34 @@ struct Epi {
   const float* W;
 };
 
-__device__ __forceinline__ float softplus(float a) {
-  return a > 0.f ? a + log1pf(__expf(-a)) : log1pf(__expf(a));
+// σ(a), σ(−a) and log(1 + e^a) from one exponential, e = e^{−|a|}: neither
+// sigmoid is formed as 1 − the other, which in float32 loses the relative
+// accuracy of the small one (Λ = σ(a)σ(−a) at |a| = 7 would carry ~6e-5)
+struct Sig {
+  float sp, sm, softplus;
+};
+__device__ __forceinline__ Sig sig_pair(float a) {
+  const float e = __expf(-fabsf(a));
+  const float big = __fdividef(1.f, 1.f + e), small = e * big;
+  Sig s;
+  s.sp = a >= 0.f ? big : small;
+  s.sm = a >= 0.f ? small : big;
+  s.softplus = fmaxf(a, 0.f) + log1pf(e);
+  return s;
 }
 
 __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
   if (e.mode == EPI_STORE) {
     e.D[(size_t)m * e.ldd + n] = v;
   } else if (e.mode == EPI_SIGMOID) {
-    if (e.ld_acc) atomicAdd(&e.ld_acc[m], double(e.y[n] * v - softplus(v)));
-    const float sg = 1.f / (1.f + __expf(-v));
-    const float lam = sg * (1.f - sg);
+    const Sig sg = sig_pair(v);
+    const float yv = e.y[n];
+    if (e.ld_acc) atomicAdd(&e.ld_acc[m], double(yv * v - sg.softplus));
+    const float lam = sg.sp * sg.sm;
     split_store(e.lam, m, n, lam);
     if (e.lam_only) return;
-    e.lp[(size_t)m * e.lp_ld + n] = lam * (1.f - 2.f * sg);
-    split_store(e.r, m, n, e.y[n] - sg);
+    e.lp[(size_t)m * e.lp_ld + n] = lam * (sg.sm - sg.sp);
+    split_store(e.r, m, n, yv * sg.sm - (1.f - yv) * sg.sp);
   } else if (e.mode == EPI_TRACE) {
     const float s = e.S[(size_t)m * e.s_ld + n];
     const float r2 = e.lp[(size_t)m * e.lp_ld + n] * (v - s * s);

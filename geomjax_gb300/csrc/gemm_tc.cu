@@ -5,11 +5,18 @@
 //   warp 0      TMA producer: per 64-wide K chunk, one 128 x 64 BF16 box per
 //               plane of A and one BN x 64 box per plane of B (128B-swizzled)
 //               into a ring of 1-4 stages sized at launch
-//   warp 1      allocates max(32, BN) TMEM columns; one elected thread issues
-//               tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M = 128, N = BN,
-//               K = 16): the plane products A_i·B_j with i + j < planes per
-//               K step, and tcgen05.commit frees each stage / signals the
-//               accumulator
+//   warp 1      allocates NACC·max(32, BN) TMEM columns; one elected thread
+//               issues tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M = 128,
+//               N = BN, K = 16): the plane products A_i·B_j with i + j <
+//               planes per K step, and tcgen05.commit frees each stage /
+//               signals the accumulators.  The K blocks are cut into NACC
+//               contiguous ranges (1, 2 or 4), each with its own TMEM
+//               accumulator, and the epilogue adds the NACC partial tiles in
+//               FP32 registers: the tensor core's FP32 accumulation rounds
+//               low (measured mean relative bias −4.5e-6 at K = 1000 and
+//               −3.2e-5 at K = 5000 on positive operands, against ~0 for
+//               round-to-nearest FP32 FMAs), and the bias grows with the
+//               number of accumulation steps into one accumulator
 //   warps 2-9   epilogue: tcgen05.ld 32x32b (warp w reads TMEM lanes
 //               32·(w%4) .. +31 = output rows; the two warps of a lane
 //               quarter take alternate 32-column chunks), staged once through
@@ -219,11 +226,11 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
       double ld = 0.0;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        const float sg = __fdividef(1.f, 1.f + __expf(-a[k]));
-        lam[k] = sg * (1.f - sg);
-        lp[k] = lam[k] * (1.f - 2.f * sg);
-        r1[k] = yv[k] - sg;
-        if (e.ld_acc && n + k < N) ld += double(yv[k] * a[k] - softplus(a[k]));
+        const Sig sg = sig_pair(a[k]);
+        lam[k] = sg.sp * sg.sm;
+        lp[k] = lam[k] * (sg.sm - sg.sp);
+        r1[k] = yv[k] * sg.sm - (1.f - yv[k]) * sg.sp;  // y − σ(a)
+        if (e.ld_acc && n + k < N) ld += double(yv[k] * a[k] - sg.softplus);
       }
       if (m < M) {
         split8(e.lam, m, n, N, full, lam);
@@ -263,11 +270,13 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
 
 // STAGES (run time, 1 .. Cfg::MAX_STAGES) is the depth of the operand ring,
 // chosen by the host so that two CTAs share an SM where that fits.
+// NACC (run time, 1, 2 or 4) accumulators over contiguous K ranges; the
+// host keeps NACC·TMEM_COLS·(CTAs per SM) within the SM's 512 columns.
 template <int NPL, int BN>
 __global__ void __launch_bounds__(320, 2)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err, int STAGES,
-                   int a_row0) {
+                   int a_row0, int NACC) {
   using C = Cfg<NPL, BN>;
   constexpr int STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
@@ -287,6 +296,9 @@ __global__ void __launch_bounds__(320, 2)
   const int kper = (KB_all + (int)gridDim.z - 1) / (int)gridDim.z;
   const int kb_first = (int)blockIdx.z * kper;
   const int KB = max(0, min(KB_all, kb_first + kper) - kb_first);
+  // a K slice with fewer K blocks than accumulators uses one per block, so
+  // that no range is empty
+  const int nacc = max(1, min(NACC, KB));
 
   if (warp == 0 && lane == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -296,10 +308,11 @@ __global__ void __launch_bounds__(320, 2)
     mbar_init(accum, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  const uint32_t tmem_cols = (uint32_t)(TMEM_COLS * NACC);
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS)
+                 "r"(tmem_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -351,18 +364,22 @@ __global__ void __launch_bounds__(320, 2)
           db[q] = make_desc(sa + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES);
         }
         constexpr uint32_t ID = (uint32_t)C::IDESC;
+        // K range r = ⌊kb·nacc/KB⌋ accumulates into columns [r·TMEM_COLS, ..)
+        const int r = (kb * nacc) / KB;
+        const bool first = kb == (r * KB + nacc - 1) / nacc;  // the range's first K block
+        const uint32_t acc_t = tmem + (uint32_t)(r * TMEM_COLS);
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
           const uint64_t adv = (uint64_t)((k * 32) >> 4);  // 16 BF16 = 32 B along K
           // plane products with i + j <= NPL - 1 (the dropped ones are below
           // the last plane's resolution)
-          mma_bf16(tmem, da[0] + adv, db[0] + adv, ID, (kb > 0 || k > 0) ? 1u : 0u);
-          mma_bf16(tmem, da[0] + adv, db[1] + adv, ID, 1u);
-          mma_bf16(tmem, da[1] + adv, db[0] + adv, ID, 1u);
+          mma_bf16(acc_t, da[0] + adv, db[0] + adv, ID, (!first || k > 0) ? 1u : 0u);
+          mma_bf16(acc_t, da[0] + adv, db[1] + adv, ID, 1u);
+          mma_bf16(acc_t, da[1] + adv, db[0] + adv, ID, 1u);
           if (NPL == 3) {
-            mma_bf16(tmem, da[0] + adv, db[NPL - 1] + adv, ID, 1u);
-            mma_bf16(tmem, da[1] + adv, db[1] + adv, ID, 1u);
-            mma_bf16(tmem, da[NPL - 1] + adv, db[0] + adv, ID, 1u);
+            mma_bf16(acc_t, da[0] + adv, db[NPL - 1] + adv, ID, 1u);
+            mma_bf16(acc_t, da[1] + adv, db[1] + adv, ID, 1u);
+            mma_bf16(acc_t, da[NPL - 1] + adv, db[0] + adv, ID, 1u);
           }
         }
         mma_commit(&empty[s]);
@@ -389,6 +406,12 @@ __global__ void __launch_bounds__(320, 2)
         float v[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+        // the other K ranges' partial tiles, added in order (round to nearest)
+        for (int acc = 1; acc < nacc; ++acc) {
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TMEM_COLS + c0), r);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
+        }
         epi_chunk(epi, stg, lane, m0 + q * 32, n0 + c0, M, N, v);
       }
     }
@@ -401,7 +424,7 @@ __global__ void __launch_bounds__(320, 2)
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS)
+                 "r"(tmem_cols)
                  : "memory");
   }
 }
@@ -513,8 +536,14 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
     ns = std::min(ns, 3);
   const CUtensorMap& mb = BN == 128 ? b->map : (BN == 64 ? b->map64 : b->map32);
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.ksplit);
+  // K-range accumulators: up to 4, at least 2 K blocks each, and within the
+  // 512 TMEM columns of an SM for the CTAs that share it
+  const int kb_cta = (kb + g.ksplit - 1) / g.ksplit;
+  const int ctas = C::smem(ns) <= kTwoCtaSmem ? 2 : 1;
+  int nacc = 1;
+  while (nacc < 4 && 2 * nacc * 2 <= kb_cta && 2 * nacc * C::TMEM_COLS * ctas <= 512) nacc *= 2;
   return launch_k(g.pdl, gemm_tc_kernel<NPL, BN>, grid, dim3(320), (size_t)C::smem(ns), st, a->map,
-                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0);
+                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0, nacc);
 }
 
 template <int NPL>

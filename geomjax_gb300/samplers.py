@@ -32,7 +32,7 @@ from .targets import PRECISIONS, Target
 
 INTEGRATORS = {"implicit_midpoint": L.GJ_IMPLICIT_MIDPOINT,
                "generalized_leapfrog": L.GJ_GENERALIZED_LEAPFROG}
-LOGREG_PATHS = {"auto": 0, "simt": 1, "tcgen05": 2, "per_chain": 3}
+LOGREG_PATHS = {"auto": 0, "simt": 1, "tcgen05": 2, "per_chain": 3, "cta": 4}
 
 
 def _stream():
@@ -289,9 +289,12 @@ class lmc:
         return _init(target, position, True)
 
     @staticmethod
-    def build_kernel(divergence_threshold=1000.0):
-        """``lmcmc/lmc.py:114-182``."""
-        return Kernel(L.GJ_SAMPLER_LMC, divergence_threshold=divergence_threshold)
+    def build_kernel(divergence_threshold=1000.0, logreg_path="auto"):
+        """``lmcmc/lmc.py:114-182``.  ``logreg_path``: for the dense-Fisher
+        logistic regression, "per_chain" runs one thread per chain (d <= 32);
+        any other value one CTA per chain (d <= 64)."""
+        return Kernel(L.GJ_SAMPLER_LMC, divergence_threshold=divergence_threshold,
+                      logreg_path=logreg_path)
 
     def __new__(cls, target: Target, step_size: float, num_integration_steps: int, *,
                 divergence_threshold=1000.0):

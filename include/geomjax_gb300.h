@@ -211,10 +211,11 @@ int32_t gj_destroy(gj_ctx* ctx);
  * CTA per chain), 1 = batched pipeline with the SIMT FP32 GEMM, 2 = batched
  * pipeline with the tcgen05 BF16 hi/lo GEMM, 3 = one thread per chain
  * (d <= 32), 4 = one CTA per chain in either precision (d <= 64; shared
- * memory of (3d(d+1)/2 + 16d + 276)·8 + (4N + max(N, 16d))·sizeof(T) +
- * 16(d+1)·sizeof(T) bytes, at most 227 KB, else GJ_ENOTSUP).
+ * memory of (d(d+1) + 16d + 274)·8 + (4N + max(N, 16d) + 16(d+1))·sizeof(T)
+ * bytes, plus d(d+1)/2·4 in GJ_MIXED, at most 227 KB, else GJ_ENOTSUP).
  * Dense LMC: 3 = one thread per chain (d <= 32), any other value = one CTA
- * per chain (d <= 64). */
+ * per chain (d <= 64; also d(d+1)/2 + d² doubles and d ints of shared
+ * memory). */
 int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
 #define GJ_OPT_LOGREG_PATH 1
 /* threads per block of the per-chain kernels: 32, 64, 96 or 128 (default) */

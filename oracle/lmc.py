@@ -90,8 +90,15 @@ def metric_vector_product(target, q, v):
 
 
 def omega_tilde(target, q, v, h):
-    """metrics.py:158-179; returns Ω̃[l, j] per chain."""
+    """metrics.py:158-179; returns Ω̃[l, j] per chain.
+
+    For a family whose ∂G is fully symmetric (∂_kG_ij symmetric in i, j, k,
+    as Xᵀdiag(Λ'⊙X[:, k])X of logistic regression), the three einsums of
+    :174-176 all equal Σ_i v_i ∂_iG, so Ω̃ = G + h/4·Σ_i v_i ∂_iG, formed
+    without the d³ tensor (``dmetric_vec``)."""
     G = target.metric(q)
+    if getattr(target, "dmetric_fully_symmetric", False):
+        return G + 0.25 * h * target.dmetric_vec(q, v)
     dG = target.dmetric(q)
     if target.is_diagonal:
         # dG[c, a, k] = ∂G_a/∂q_k
@@ -114,6 +121,9 @@ def omega_tilde(target, q, v, h):
 def grad_logdetmetric(target, q):
     """metrics.py:181-189: ∂_k log det G = tr(G⁻¹ ∂_k G)."""
     G = target.metric(q)
+    if hasattr(target, "metric_trace_quad") and not target.is_diagonal:
+        Ginv = np.linalg.inv(G)
+        return target.metric_trace_quad(q, Ginv, np.zeros(q.shape))[0]
     dG = target.dmetric(q)
     if target.is_diagonal:
         return np.einsum("ca,cak->ck", 1.0 / G, dG)

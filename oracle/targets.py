@@ -140,6 +140,8 @@ class LogisticRegression:
 
     family = "logistic_regression"
     is_diagonal = False
+    # ∂_kG_ij = Σ_n Λ'_n x_ni x_nj x_nk is symmetric in (i, j, k)
+    dmetric_fully_symmetric = True
 
     def __init__(self, X, y, prior_var: float = 100.0):
         self.X = np.asarray(X, dtype=np.float64)
@@ -170,7 +172,8 @@ class LogisticRegression:
     def metric(self, q):
         s = _sigmoid(self._a(q))
         lam = s * (1.0 - s)
-        G = np.einsum("cn,ni,nj->cij", lam, self.X, self.X)
+        # Σ_n Λ_cn x_n x_nᵀ per chain, as one matmul per chain
+        G = np.matmul(np.swapaxes(lam[:, :, None] * self.X[None], 1, 2), self.X[None])
         G += np.eye(self.dim)[None] / self.prior_var
         return G
 
@@ -184,7 +187,7 @@ class LogisticRegression:
         """Return tr(G⁻¹∂_kG) and uᵀ∂_kG u for every k ([C, d] each)."""
         s = _sigmoid(self._a(q))
         lamp = s * (1.0 - s) * (1.0 - 2.0 * s)
-        w = np.einsum("ni,cij,nj->cn", self.X, Ginv, self.X)  # x_nᵀ G⁻¹ x_n
+        w = np.sum(np.matmul(self.X[None], Ginv) * self.X[None], axis=2)  # x_nᵀ G⁻¹ x_n
         xu = u @ self.X.T  # [C, N]
         tr = (lamp * w) @ self.X
         quad = (lamp * xu * xu) @ self.X
@@ -195,7 +198,8 @@ class LogisticRegression:
         s = _sigmoid(self._a(q))
         lamp = s * (1.0 - s) * (1.0 - 2.0 * s)
         xv = v @ self.X.T
-        return np.einsum("cn,ni,nj->cij", lamp * xv, self.X, self.X)
+        wgt = lamp * xv
+        return np.matmul(np.swapaxes(wgt[:, :, None] * self.X[None], 1, 2), self.X[None])
 
 
 class HierarchicalGaussian:

@@ -61,3 +61,16 @@ def rel_err(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return np.max(np.abs(a - b) / (np.abs(b) + 1.0))
+
+
+def laplace_draws(ot, C, seed, newton_iters=25):
+    """C positions drawn from the Laplace approximation of a logistic-regression
+    posterior: the mode by Newton steps β ← β + G(β)⁻¹∇ℓ(β) (the Fisher metric
+    is the negative Hessian of the log density for this family), then
+    β ~ N(mode, G(mode)⁻¹).  Chains started there are in the typical set."""
+    b = np.zeros((1, ot.dim))
+    for _ in range(newton_iters):
+        b = b + np.linalg.solve(ot.metric(b), ot.grad(b)[..., None])[..., 0]
+    L = np.linalg.cholesky(ot.metric(b)[0])
+    eps = np.random.default_rng(seed).standard_normal((C, ot.dim))
+    return b + np.linalg.solve(L.T, eps.T).T

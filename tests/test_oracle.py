@@ -69,6 +69,26 @@ def test_logreg_structured_contractions():
     np.testing.assert_allclose(tg.dmetric_vec(q, u), np.einsum("cabk,ck->cab", dG, u), rtol=1e-10)
 
 
+def test_lmc_logreg_structured_omega_matches_einsums():
+    """The dense-LMC oracle's logistic-regression shortcut (Ω̃ = G + h/4·Σ_i
+    v_i ∂_iG, tr(G⁻¹∂_kG) from the per-datum form) equals the three einsums of
+    lmcmc/metrics.py:174-176 and the trace of :181-189 over the full ∂G."""
+    X, y = T.make_logreg_data(40, 5, seed=4)
+    tg = T.LogisticRegression(X, y)
+    q = _q(tg)
+    v = np.random.default_rng(1).standard_normal(q.shape)
+    dG = tg.dmetric(q)
+    G = tg.metric(q)
+    for h in (0.1, -0.1):
+        p1 = np.einsum("ci,cjli->clj", v, dG)
+        p2 = np.einsum("ci,cilj->clj", v, dG)
+        p3 = np.einsum("ci,cijl->clj", v, dG)
+        full = G + 0.5 * h * 0.5 * (p1 + p2 - p3)
+        np.testing.assert_allclose(lmc.omega_tilde(tg, q, v, h), full, rtol=1e-12, atol=1e-12)
+    tr_full = np.einsum("cab,cbak->ck", np.linalg.inv(G), dG)
+    np.testing.assert_allclose(lmc.grad_logdetmetric(tg, q), tr_full, rtol=1e-10)
+
+
 def test_kinetic_grad_fd():
     for tg in _targets():
         q = _q(tg)
