@@ -281,11 +281,15 @@ def run_ours(args, wl):
     steps_per_s = ws * C * Lsteps * K / dev_s
     min_ess = float("nan")
     if K >= 4:
-        # ESS over every rank's chains (one gather of the traces; replicas
+        # ESS over every rank's chains (per-rank autocovariance sums; replicas
         # exchange nothing while sampling)
         from geomjax_gb300.distributed import global_min_ess
 
         min_ess = global_min_ess(trace, chain_axis=1, sample_axis=0)
+    ess_cmp = None
+    if rank == 0 and args.ess_transitions > 0 and wl["sampler"] in ("rmhmc", "lmcmonge"):
+        # rank 0 only: the plain arm is a baseline, not part of the weak-scaled value
+        ess_cmp = ess_comparison(args, wl, kern, target, state, info, extra, dev)
     # --- e2e through the public API with host buffers
     Zh = torch.empty(C, d, dtype=target.dtype).pin_memory()
     Uh = torch.empty(C, dtype=torch.float64).pin_memory()
@@ -368,8 +372,13 @@ def run_ours(args, wl):
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}", "autotune": tuned},
-        "min_ess_per_s": (round(min_ess / dev_s, 2) if K >= 4 else None),
-        "min_ess": (round(min_ess, 2) if K >= 4 else None),
+        # min-ESS/s from the post-burn-in trace of ess_comparison when it ran
+        # (the K timed transitions start out of equilibrium and are too short)
+        "min_ess_per_s": (ess_cmp["mixed"]["min_ess_per_s"] if ess_cmp else
+                          (round(min_ess / dev_s, 2) if K >= 4 else None)),
+        "min_ess": (ess_cmp["mixed"]["min_ess"] if ess_cmp else
+                    (round(min_ess, 2) if K >= 4 else None)),
+        "ess_comparison": ess_cmp,
         "mean_acceptance": round(float(acc_sum.mean().item()) / K, 4),
         "e2e": {"value": round(e2e, 1), "unit": "leapfrog steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
@@ -552,11 +561,116 @@ def run_jvp(args, wl):
     }
 
 
+def _moments_agreement(xm, xp, ess_p):
+    """Per-coordinate agreement of two traces [T, C, d] of the same chains:
+    |Δmean| and |Δvariance| in units of the plain trace's Monte Carlo
+    standard errors (mean: sqrt(var/ESS); variance: sqrt((m4 − var²)/ESS))."""
+    import torch
+
+    a = xm.double().reshape(-1, xm.shape[-1])
+    b = xp.double().reshape(-1, xp.shape[-1])
+    ma, mb = a.mean(0), b.mean(0)
+    va, vb = a.var(0), b.var(0)
+    m4 = ((b - mb) ** 4).mean(0)
+    se_m = torch.sqrt(vb / ess_p)
+    se_v = torch.sqrt(torch.clamp(m4 - vb * vb, min=0.0) / ess_p)
+    dm = (ma - mb).abs() / se_m
+    dv = (va - vb).abs() / se_v
+    return {"max_mean_dev_in_mcse": round(float(dm.max()), 4),
+            "max_var_dev_in_mcse": round(float(dv.max()), 4),
+            "coords_within_2_mcse": int(((dm < 2) & (dv < 2)).sum()), "coords": int(a.shape[1])}
+
+
+def ess_comparison(args, wl, kern, target, state, info, extra, dev):
+    """min-ESS/s of the batched mixed-precision form against the plain FP64
+    form on the same posterior.  After a burn-in of the mixed chains, both
+    arms run the same number of transitions from the same positions with
+    common random numbers (the same z and u; z is drawn in float32), each
+    transition timed with CUDA events on the launching stream and L2 flushed
+    between transitions.  The plain arm samples the first `plain_chains`
+    chains.  ESS is diagnostics.py:78-209 over each arm's trace."""
+    import torch
+
+    import geomjax_gb300 as gj
+
+    T, burn = args.ess_transitions, args.ess_burnin
+    C, d = state.position.shape
+    Lsteps, h = wl["L"], wl["h"]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(777)
+    for _ in range(burn):
+        kern.step_inplace(target, state, torch.randn(C, d, generator=gen, device=dev,
+                                                     dtype=target.dtype),
+                          torch.rand(C, generator=gen, device=dev, dtype=torch.float64), info, h,
+                          Lsteps, **extra)
+    start = state.position.detach().clone()
+    Z = torch.randn(T, C, d, generator=gen, device=dev, dtype=torch.float32)
+    U = torch.rand(T, C, generator=gen, device=dev, dtype=torch.float64)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def run(kern_, target_, st_, info_, extra_):
+        n = st_.position.shape[0]
+        tr = torch.empty(T, n, d, dtype=target_.dtype, device=dev)
+        acc = torch.empty(T, n, dtype=torch.uint8, device=dev)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(T)]
+        torch.cuda.synchronize()
+        for i in range(T):
+            z = Z[i, :n].to(target_.dtype)
+            flush.zero_()
+            evs[i][0].record(stream)
+            kern_.step_inplace(target_, st_, z, U[i, :n], info_, h, Lsteps, **extra_)
+            evs[i][1].record(stream)
+            tr[i].copy_(st_.position)
+            acc[i].copy_(info_["is_accepted"])
+        torch.cuda.synchronize()
+        return tr, acc, sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+    tr_m, acc_m, s_m = run(kern, target, state, info, extra)
+    Cp = min(C, args.plain_chains)
+    if wl["sampler"] == "rmhmc":
+        from geomjax_gb300.data import logreg_data
+
+        X, y = logreg_data(wl["N"], wl["d"], seed=0)
+        pt = gj.logistic_regression(X, y, precision="fp64", device=dev)
+        pk = gj.rmhmc.build_kernel(integrator=wl["integrator"])  # one CTA per chain
+        pst = gj.rmhmc.init(start[:Cp].double(), pt)
+        pextra = {}
+        form = "one CTA per chain, float64 throughout (data, state, Gram, factor, solves)"
+    else:
+        pt = gj.funnel(D=wl["D"], precision="fp64", device=dev)
+        pk = gj.lmcmonge.build_kernel()
+        pst = gj.lmcmonge.init(start[:Cp].double(), pt)
+        pextra = dict(alpha2=1.0, inverse_mass=torch.ones(d, dtype=torch.float64, device=dev))
+        form = "one thread per chain, float64 throughout"
+    pinfo = pk.new_info(Cp, d, pt, dev)
+    tr_p, acc_p, s_p = run(pk, pt, pst, pinfo, pextra)
+    ess_m = gj.effective_sample_size(tr_m, chain_axis=1, sample_axis=0)
+    ess_p = gj.effective_sample_size(tr_p, chain_axis=1, sample_axis=0)
+    ess_m_sub = gj.effective_sample_size(tr_m[:, :Cp], chain_axis=1, sample_axis=0)
+    mixed = {"chains": C, "min_ess": round(float(ess_m.min()), 2), "device_s": round(s_m, 4),
+             "min_ess_per_s": round(float(ess_m.min()) / s_m, 2),
+             "leapfrog_steps_per_s": round(C * Lsteps * T / s_m, 1)}
+    plain = {"chains": Cp, "form": form, "min_ess": round(float(ess_p.min()), 2),
+             "device_s": round(s_p, 4), "min_ess_per_s": round(float(ess_p.min()) / s_p, 2),
+             "leapfrog_steps_per_s": round(Cp * Lsteps * T / s_p, 1)}
+    agree = _moments_agreement(tr_m[:, :Cp], tr_p, ess_p)
+    agree["accept_agreement"] = round(float((acc_m[:, :Cp] == acc_p).double().mean()), 6)
+    agree["mixed_min_ess_same_chains"] = round(float(ess_m_sub.min()), 2)
+    return {"transitions": T, "burn_in": burn,
+            "draws": "common random numbers: the same z (float32) and u on both arms",
+            "mixed": mixed, "plain_fp64": plain,
+            "min_ess_ratio": round(mixed["min_ess_per_s"] / plain["min_ess_per_s"], 3),
+            "posterior_agreement": agree}
+
+
 def run_plain_fp64(args, wl):
-    """The plain per-chain FP64 CUDA form of the same workload: one thread
-    per chain, every vector and the metric algebra in float64.  For the
+    """The thread-per-chain FP64 form of the same workload: one thread per
+    chain, every vector and the metric algebra in float64.  For the
     dense-Fisher workload it runs on a bounded sample of chains (each chain
-    costs O(N·d²) FP64 per map evaluation)."""
+    costs O(N·d²) FP64 per map evaluation in one thread); the min-ESS/s
+    comparison uses the CTA-per-chain FP64 form instead (ess_comparison)."""
     import torch
 
     import geomjax_gb300 as gj
@@ -568,7 +682,7 @@ def run_plain_fp64(args, wl):
         C = min(wl["C"], 256)
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="fp64", device=dev)
-        kern = gj.rmhmc.build_kernel(integrator=wl["integrator"])
+        kern = gj.rmhmc.build_kernel(integrator=wl["integrator"], logreg_path="per_chain")
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(0),
@@ -775,7 +889,14 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="pick the GEMM tile policy and the factorisation's chains per warp by "
                          "timing the candidates before the warm-up (batched paths)")
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 per-chain arm")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the thread-per-chain plain FP64 arm")
+    ap.add_argument("--ess-transitions", type=int, default=200,
+                    help="transitions of the min-ESS/s comparison on each arm (0 = skip)")
+    ap.add_argument("--ess-burnin", type=int, default=100,
+                    help="untimed burn-in transitions of the mixed chains before it")
+    ap.add_argument("--plain-chains", type=int, default=1024,
+                    help="chains of the plain FP64 arm of the min-ESS/s comparison")
     ap.add_argument("--chains", type=int, default=None, help="override the chain count (small cases)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="fixed-point loop driver of the batched path (host: profilable by ncu)")
@@ -824,8 +945,15 @@ def main():
         return
     out = run_ours(args, wl)
     if rank == 0:
-        if not args.no_plain and wl["sampler"] != "rmhmc_funnel":  # that one is FP64 already
-            out["plain_fp64"] = run_plain_fp64(args, wl)
+        if out.get("ess_comparison"):
+            cmp_ = out["ess_comparison"]
+            out["plain_fp64"] = dict(cmp_["plain_fp64"], transitions=cmp_["transitions"])
+            out["min_ess_ratio"] = cmp_["min_ess_ratio"]
+        if not args.no_plain and wl["sampler"] == "rmhmc":
+            # the thread-per-chain FP64 form, kept for continuity
+            out["plain_fp64_thread_per_chain"] = run_plain_fp64(args, wl)
+            out["steps_ratio_vs_thread_per_chain"] = round(
+                out["value"] / out["plain_fp64_thread_per_chain"]["value"], 1)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(wl)
         print(json.dumps(out), flush=True)
