@@ -408,7 +408,8 @@ def run_batch(args, wl):
     Ns, ds = uneven_logreg_batch(B, seed=rank)
     t_setup = time.perf_counter()
     data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
-    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev, integrator=args.integrator)
+    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev, integrator=args.integrator,
+                        one_graph=not args.batch_pool)
     del data
     g0 = torch.Generator().manual_seed(rank)
     state = pb.init([0.01 * torch.randn(C, int(d), generator=g0) for d in ds])
@@ -477,6 +478,8 @@ def run_batch(args, wl):
         "data": "synthetic (seeded)",
         "config": {"workload": wl["name"], "posteriors": B, "chains_per_posterior": C,
                    "integration_steps": Lsteps, "step_size": h, "streams": args.streams,
+                   "launch": ("one graph per posterior on the stream pool" if args.batch_pool else
+                              "one CUDA graph per transition, every posterior a branch"),
                    "mean_N": float(np.mean(Ns)), "mean_d": float(np.mean(ds)),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}", "autotune": tuned},
@@ -486,7 +489,96 @@ def run_batch(args, wl):
                 "d2h_bytes_per_step": int(Ph.numel() * 4 + Ah.numel())},
         "graph_launches": B * K, "setup_s": round(t_setup, 1), "clocks": clk,
         "wall_s": round(t_wall, 3),
+        "plain_fp64": (batch_plain_comparison(args, wl, Ns, ds, dev)
+                       if rank == 0 and not args.no_plain else None),
     }
+
+
+def batch_plain_comparison(args, wl, Ns, ds, dev, T=4):
+    """The uneven batch's mixed pipeline against the plain FP64 form on the
+    same sample of posteriors: the first `args.plain_posteriors` posteriors
+    whose chains fit one CTA each (d <= 64 and the CTA's shared memory within
+    227 KB).  The mixed arm is a PosteriorBatch of those posteriors; the plain
+    arm runs each posterior's chains with the CTA-per-chain FP64 kernel, the
+    posteriors on concurrent streams.  Both are timed with CUDA events over
+    T transitions from the same start positions."""
+    import numpy as np
+    import torch
+
+    import geomjax_gb300 as gj
+    from geomjax_gb300.batch import PosteriorBatch
+    from geomjax_gb300.data import logreg_data
+    from geomjax_gb300.samplers import cta_supported
+
+    C, Lsteps, h = wl["C"], wl["L"], wl["h"]
+    pick = [i for i, (n, d) in enumerate(zip(Ns, ds)) if cta_supported(int(n), int(d), "fp64")]
+    pick = pick[: args.plain_posteriors]
+    if not pick:
+        return None
+    data = [logreg_data(int(Ns[i]), int(ds[i]), seed=1000 * 0 + i) for i in pick]
+    g0 = torch.Generator().manual_seed(17)
+    starts = [0.01 * torch.randn(C, int(ds[i]), generator=g0) for i in pick]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(18)
+    tot = sum(int(ds[i]) for i in pick) * C
+    Z = torch.randn(T, tot, generator=gen, device=dev)
+    U = torch.rand(T, len(pick) * C, generator=gen, device=dev, dtype=torch.float64)
+    stream = torch.cuda.current_stream()
+    # mixed: the batched pipeline over the sample
+    pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev, integrator=wl["integrator"])
+    st = pb.init(starts)
+    info = pb.new_info()
+    pb.step_inplace(st, Z[0], U[0], info, h, Lsteps)  # graph capture, untimed
+    st = pb.init(starts)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for t in range(T):
+        pb.step_inplace(st, Z[t], U[t], info, h, Lsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s_mixed = e0.elapsed_time(e1) / 1e3
+    # plain FP64: one CTA per chain, a stream per posterior
+    kern = gj.rmhmc.build_kernel(integrator=wl["integrator"])
+    tgs = [gj.logistic_regression(X, y, precision="fp64", device=dev) for X, y in data]
+    sts = [gj.rmhmc.init(q.double(), tg) for q, tg in zip(starts, tgs)]
+    infos = [kern.new_info(C, tg.dim, tg, dev) for tg in tgs]
+    streams = [torch.cuda.Stream(device=dev) for _ in range(min(len(pick), args.streams))]
+    offs, o = [], 0
+    for i in pick:
+        offs.append(o)
+        o += int(ds[i]) * C
+
+    def plain_transition(t):
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        for k, (tg, st_, inf) in enumerate(zip(tgs, sts, infos)):
+            s_ = streams[k % len(streams)]
+            s_.wait_event(ev)
+            with torch.cuda.stream(s_):
+                z = Z[t, offs[k]:offs[k] + tg.dim * C].view(C, tg.dim).double()
+                kern.step_inplace(tg, st_, z, U[t, k * C:(k + 1) * C], inf, h, Lsteps)
+        for s_ in streams:
+            stream.wait_stream(s_)
+
+    plain_transition(0)  # untimed
+    sts = [gj.rmhmc.init(q.double(), tg) for q, tg in zip(starts, tgs)]
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for t in range(T):
+        plain_transition(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    s_plain = e0.elapsed_time(e1) / 1e3
+    steps = len(pick) * C * Lsteps * T
+    return {"posteriors": len(pick), "chains_per_posterior": C, "transitions": T,
+            "sample": "the first posteriors of the batch with d <= 64 whose chains fit one CTA",
+            "mean_N": float(np.mean([Ns[i] for i in pick])),
+            "mean_d": float(np.mean([ds[i] for i in pick])),
+            "mixed_leapfrog_steps_per_s": round(steps / s_mixed, 1),
+            "plain_fp64_leapfrog_steps_per_s": round(steps / s_plain, 1),
+            "plain_form": "one CTA per chain, float64 throughout, a stream per posterior",
+            "steps_ratio": round(s_plain / s_mixed, 2)}
 
 
 def run_jvp(args, wl):
@@ -897,6 +989,8 @@ def main():
                     help="untimed burn-in transitions of the mixed chains before it")
     ap.add_argument("--plain-chains", type=int, default=1024,
                     help="chains of the plain FP64 arm of the min-ESS/s comparison")
+    ap.add_argument("--plain-posteriors", type=int, default=64,
+                    help="posteriors of the uneven batch's plain FP64 comparison")
     ap.add_argument("--chains", type=int, default=None, help="override the chain count (small cases)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="fixed-point loop driver of the batched path (host: profilable by ncu)")
@@ -914,6 +1008,9 @@ def main():
     ap.add_argument("--groups", type=int, default=0,
                     help="chain groups on concurrent streams (0 = automatic)")
     ap.add_argument("--streams", type=int, default=16, help="stream pool of the uneven batch")
+    ap.add_argument("--batch-pool", action="store_true",
+                    help="uneven batch: one graph per posterior on the stream pool instead of one "
+                         "graph holding every posterior")
     ap.add_argument("--posteriors", type=int, default=None, help="override the uneven batch size")
     ap.add_argument("--chol-cpw", type=int, default=0, choices=[0, 1, 2, 4, 8],
                     help="chains per warp in the metric factorisation (0 = automatic)")

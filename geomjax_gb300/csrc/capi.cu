@@ -714,6 +714,8 @@ int32_t gj_chees_statistics(int32_t precision, int32_t num_chains, int32_t dim,
 
 struct gj_batch {
   int B, C, S;
+  int one_graph;  // GJ_OPT_BATCH_GRAPH
+  gj::LogregBatchGraph* bg;
   std::vector<gj::LogregBatched*> lbs;
   std::vector<int> dims;
   std::vector<size_t> pos_off;  // [B + 1] offsets of each posterior's [C, d_b] block
@@ -725,6 +727,7 @@ struct gj_batch {
 namespace {
 
 void batch_free(gj_batch* b) {
+  gj::logreg_batch_graph_destroy(b->bg);
   for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_destroy(lb);
   for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
@@ -755,6 +758,8 @@ int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
   if (!b) return fail(GJ_ENOMEM, "host allocation failed");
   b->B = num_posteriors;
   b->C = chains_per_posterior;
+  b->one_graph = 1;
+  b->bg = nullptr;
   b->S = num_streams < num_posteriors ? num_streams : num_posteriors;
   b->fork = nullptr;
   b->pos_off.push_back(0);
@@ -810,6 +815,11 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
     for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_gemm_ksplit(lb, (int)value);
     return GJ_OK;
   }
+  if (key == GJ_OPT_BATCH_GRAPH) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "batch graph flag must be 0 or 1");
+    b->one_graph = (int)value;
+    return GJ_OK;
+  }
   return fail(GJ_EINVAL, "unknown batch option");
 }
 
@@ -825,6 +835,18 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const gj::InfoDev<float> inf = gj::to_dev<float>(info);
+  if (b->one_graph) {  // every posterior a branch of one graph, one launch
+    if (!b->bg) {
+      const int rc = gj::logreg_batch_graph_create(b->lbs.data(), b->B, b->C, b->pos_off.data(),
+                                                   &b->bg);
+      if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+    }
+    const int rc = gj::logreg_batch_graph_step(b->bg, sp, (float*)s->position,
+                                               (float*)s->logdensity_grad, s->logdensity, z, u,
+                                               inf, 2, cs);
+    if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+    return GJ_OK;
+  }
   if (cudaEventRecord(b->fork, cs) != cudaSuccess) return fail(GJ_ECUDA, "event record failed");
   for (int k = 0; k < b->S; ++k)
     if (cudaStreamWaitEvent(b->streams[k], b->fork, 0) != cudaSuccess)

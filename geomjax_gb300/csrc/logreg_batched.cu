@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -1705,16 +1706,15 @@ int graph_cfg(const LogregBatched* lb) {
          8192 * lb->gsplit_req;
 }
 
-// Capture one whole transition (all L steps, each fixed-point solve a
-// conditional WHILE node) into *out.  The graph reads and writes the
-// context's staging buffers; step parameters come from lb->spd.  With prop,
-// the energy factorisation also writes the proposal velocity.
-int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGraphExec_t* out) {
-  *out = nullptr;
+// Record one whole transition (all L steps, each fixed-point solve a
+// conditional WHILE node) into the capture that stream s takes part in.  The
+// kernels read and write the context's staging buffers; step parameters come
+// from lb->spd.  With prop, the energy factorisation also writes the
+// proposal velocity.  Returns the first error (the capture stays open).
+cudaError_t capture_transition(LogregBatched* lb, int L, int impl, bool prop, bool gl,
+                               cudaStream_t s) {
   const int C = lb->C, d = lb->d;
-  cudaStream_t s = lb->cap_main;
-  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return graph_fail("begin", e);
+  cudaError_t e = cudaSuccess;
   Runner R{lb, impl, s};
   R.spd = lb->spd;
   begin_kernel<<<(C + 127) / 128, 128, 0, s>>>(C, d, lb->pos_s, lb->q0, lb->qc, lb->qf, lb->Qb,
@@ -1815,17 +1815,24 @@ int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGrap
   inf.momentum = nullptr;
   inf.prop_q = lb->propq_s;
   R.accept(lb->ld_s, lb->u_s, 0.0, lb->pos_s, lb->grad_s, lb->ld_s, inf);
+  if (e == cudaSuccess) e = R.err;
+  return e;
+}
+
+// Capture one whole transition into *out (its own graph).
+int build_graph(LogregBatched* lb, int L, int impl, bool prop, bool gl, cudaGraphExec_t* out) {
+  *out = nullptr;
+  cudaStream_t s = lb->cap_main;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return graph_fail("begin", e);
+  e = capture_transition(lb, L, impl, prop, gl, s);
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(s, &g);
   if (e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
-    return graph_fail("conditional node", e);
+    return graph_fail("transition", e);
   }
   if (e2 != cudaSuccess) return graph_fail("end", e2);
-  if (R.err != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return graph_fail("kernels", R.err);
-  }
   e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
@@ -1986,6 +1993,236 @@ int gemm_split_test(int impl, int planes, int M, int N, int K, const float* A, c
   for (void* p : tmp.owned) cudaFree(p);
   tmp.owned.clear();
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// A batch of posteriors as one CUDA graph.  Every posterior's whole
+// transition (its conditional WHILE nodes included) is recorded as an
+// independent branch of one graph, so one launch advances every chain of
+// every posterior and the graph executor runs the branches concurrently as
+// the SMs allow.  One gather kernel before the launch copies the batch's
+// ragged state and draws into the posteriors' staging buffers and sets their
+// step parameters; one scatter kernel after it copies the results back.
+// Neither the batch's array addresses nor the step size are baked into the
+// graph, so one capture serves every call with the same number of steps,
+// integrator, GEMM path and factorisation set-up.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BatchStage {  // one posterior's staging buffers and its place in the batch arrays
+  float *pos_s, *grad_s, *z_s, *mom_s, *propq_s, *propv_s;
+  double *ld_s, *u_s, *acc_s, *energy_s;
+  uint8_t *accepted_s, *divergent_s, *status_s;
+  int* fpit_s;
+  StepDev* spd;
+  long long vec_off;  // the posterior's [C, d] block in the ragged vectors
+  int d;
+};
+
+__global__ void batch_gather_kernel(const BatchStage* S, int C, StepDev sp, const float* pos,
+                                    const float* grad, const double* ld, const float* z,
+                                    const double* u) {
+  const BatchStage st = S[blockIdx.x];
+  const size_t nv = (size_t)C * st.d, o = (size_t)st.vec_off, co = (size_t)blockIdx.x * C;
+  for (size_t i = threadIdx.x; i < nv; i += blockDim.x) {
+    st.pos_s[i] = pos[o + i];
+    st.grad_s[i] = grad[o + i];
+    st.z_s[i] = z[o + i];
+  }
+  for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    st.ld_s[i] = ld[co + i];
+    st.u_s[i] = u[co + i];
+  }
+  if (threadIdx.x == 0) *st.spd = sp;
+}
+
+__global__ void batch_scatter_kernel(const BatchStage* S, int C, float* pos, float* grad,
+                                     double* ld, InfoDev<float> info) {
+  const BatchStage st = S[blockIdx.x];
+  const size_t nv = (size_t)C * st.d, o = (size_t)st.vec_off, co = (size_t)blockIdx.x * C;
+  for (size_t i = threadIdx.x; i < nv; i += blockDim.x) {
+    pos[o + i] = st.pos_s[i];
+    grad[o + i] = st.grad_s[i];
+    if (info.momentum) info.momentum[o + i] = st.mom_s[i];
+    if (info.prop_q) info.prop_q[o + i] = st.propq_s[i];
+    if (info.prop_v) info.prop_v[o + i] = st.propv_s[i];
+  }
+  for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    ld[co + i] = st.ld_s[i];
+    if (info.acc_rate) info.acc_rate[co + i] = st.acc_s[i];
+    if (info.accepted) info.accepted[co + i] = st.accepted_s[i];
+    if (info.divergent) info.divergent[co + i] = st.divergent_s[i];
+    if (info.energy) info.energy[co + i] = st.energy_s[i];
+    if (info.fp_iters) info.fp_iters[co + i] = st.fpit_s[i];
+    if (info.status) info.status[co + i] = st.status_s[i];
+  }
+}
+
+constexpr size_t kMaxBatchGraphs = 8;
+
+}  // namespace
+
+struct LogregBatchGraph {
+  std::vector<LogregBatched*> lbs;
+  int C = 0;
+  BatchStage* stages = nullptr;  // device [B]
+  cudaStream_t cap_root = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  struct Entry {
+    int L, impl, cfg, prop;
+    cudaGraphExec_t exec;
+    unsigned long long used;
+  };
+  std::vector<Entry> graphs;
+  unsigned long long tick = 0;
+};
+
+void logreg_batch_graph_destroy(LogregBatchGraph* bg) {
+  if (!bg) return;
+  for (auto& g : bg->graphs) cudaGraphExecDestroy(g.exec);
+  if (bg->stages) cudaFree(bg->stages);
+  if (bg->cap_root) cudaStreamDestroy(bg->cap_root);
+  if (bg->fork) cudaEventDestroy(bg->fork);
+  if (bg->join) cudaEventDestroy(bg->join);
+  delete bg;
+}
+
+int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const size_t* vec_off,
+                              LogregBatchGraph** out) {
+  *out = nullptr;
+  LogregBatchGraph* bg = new (std::nothrow) LogregBatchGraph();
+  if (!bg) {
+    g_err = "host allocation failed";
+    return GJ_ENOMEM;
+  }
+  bg->lbs.assign(lbs, lbs + B);
+  bg->C = C;
+  std::vector<BatchStage> hs(B);
+  for (int b = 0; b < B; ++b) {
+    LogregBatched* lb = lbs[b];
+    if (lb->C != C) {
+      logreg_batch_graph_destroy(bg);
+      g_err = "every posterior of a batch graph has the same chain count";
+      return GJ_EINVAL;
+    }
+    BatchStage& st = hs[b];
+    st.pos_s = lb->pos_s;
+    st.grad_s = lb->grad_s;
+    st.z_s = lb->z_s;
+    st.mom_s = lb->mom_s;
+    st.propq_s = lb->propq_s;
+    st.propv_s = lb->propv_s;
+    st.ld_s = lb->ld_s;
+    st.u_s = lb->u_s;
+    st.acc_s = lb->acc_s;
+    st.energy_s = lb->energy_s;
+    st.accepted_s = lb->accepted_s;
+    st.divergent_s = lb->divergent_s;
+    st.status_s = lb->status_s;
+    st.fpit_s = lb->fpit_s;
+    st.spd = lb->spd;
+    st.vec_off = (long long)vec_off[b];
+    st.d = lb->d;
+  }
+  cudaError_t e = cudaMalloc(&bg->stages, sizeof(BatchStage) * (size_t)B);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(bg->stages, hs.data(), sizeof(BatchStage) * (size_t)B, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bg->cap_root, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->join, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    logreg_batch_graph_destroy(bg);
+    g_err = std::string("batch graph set-up: ") + cudaGetErrorString(e);
+    return GJ_ECUDA;
+  }
+  *out = bg;
+  return GJ_OK;
+}
+
+namespace {
+
+// Record every posterior's transition as one branch of one graph.
+int batch_capture(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
+                  cudaGraphExec_t* out) {
+  *out = nullptr;
+  cudaStream_t root = bg->cap_root;
+  cudaError_t e = cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return graph_fail("batch begin", e);
+  e = cudaEventRecord(bg->fork, root);
+  for (size_t b = 0; b < bg->lbs.size() && e == cudaSuccess; ++b) {
+    LogregBatched* lb = bg->lbs[b];
+    e = cudaStreamWaitEvent(lb->cap_main, bg->fork, 0);  // the branch starts at the fork
+    if (e == cudaSuccess) e = capture_transition(lb, L, impl, prop, gl, lb->cap_main);
+    if (e == cudaSuccess) e = cudaEventRecord(bg->join, lb->cap_main);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(root, bg->join, 0);  // and joins the root
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(root, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return graph_fail("batch capture", e != cudaSuccess ? e : e2);
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return graph_fail("batch instantiate", e);
+  }
+  return GJ_OK;
+}
+
+}  // namespace
+
+int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos, float* grad,
+                            double* logdens, const float* z, const double* u,
+                            const InfoDev<float>& info, int gemm_impl, cudaStream_t st) {
+  const bool gl = sp.integrator == GJ_GENERALIZED_LEAPFROG;
+  for (LogregBatched* lb : bg->lbs) {
+    if (gemm_impl == 2 && !lb->tc_ok) {
+      g_err = "tcgen05 GEMM unavailable (no sm_100-family device or tensor-map encoder)";
+      return GJ_ENOTSUP;
+    }
+    if (gl) {
+      const int rg = ensure_gl(lb);
+      if (rg) return rg;
+    }
+    lb->stats = LogregStats{};
+  }
+  const bool prop = info.prop_v != nullptr;
+  const int cfg = graph_cfg(bg->lbs[0]) + (gl ? (1 << 20) : 0);
+  cudaGraphExec_t exec = nullptr;
+  for (auto& g : bg->graphs)
+    if (g.L == sp.L && g.impl == gemm_impl && g.cfg == cfg && g.prop == (int)prop) {
+      g.used = ++bg->tick;
+      exec = g.exec;
+    }
+  if (!exec) {
+    // the capture streams must not see unfinished work of the caller's stream
+    cudaStreamSynchronize(st);
+    if (bg->graphs.size() >= kMaxBatchGraphs) {
+      size_t lru = 0;
+      for (size_t i = 1; i < bg->graphs.size(); ++i)
+        if (bg->graphs[i].used < bg->graphs[lru].used) lru = i;
+      cudaGraphExecDestroy(bg->graphs[lru].exec);
+      bg->graphs.erase(bg->graphs.begin() + lru);
+    }
+    const int rc = batch_capture(bg, sp.L, gemm_impl, prop, gl, &exec);
+    if (rc) return rc;
+    bg->graphs.push_back({sp.L, gemm_impl, cfg, (int)prop, exec, ++bg->tick});
+  }
+  const int B = (int)bg->lbs.size();
+  batch_gather_kernel<<<B, 256, 0, st>>>(bg->stages, bg->C, sp, pos, grad, logdens, z, u);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  if (e == cudaSuccess) {
+    batch_scatter_kernel<<<B, 256, 0, st>>>(bg->stages, bg->C, pos, grad, logdens, info);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    g_err = std::string("batch graph step: ") + cudaGetErrorString(e);
+    return GJ_ECUDA;
+  }
+  return GJ_OK;
 }
 
 }  // namespace gj

@@ -30,6 +30,22 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
                                     double* logdens, const float* z, const double* u,
                                     const InfoDev<float>& info, int gemm_impl, cudaStream_t st);
 
+// A batch of contexts (one per posterior, all with the same chain count)
+// advanced by one CUDA-graph launch per transition: every posterior's whole
+// transition is an independent branch of the graph.  vec_off[b]: offset of
+// posterior b's [C, d_b] block in the batch's ragged vectors; per-chain
+// scalars are [B·C].  One gather kernel before the launch and one scatter
+// kernel after it move the batch arrays in and out of the posteriors'
+// staging buffers.  Up to 8 captured graphs are kept (by number of steps,
+// GEMM path, factorisation set-up, integrator and proposal output).
+struct LogregBatchGraph;
+int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const size_t* vec_off,
+                              LogregBatchGraph** out);
+void logreg_batch_graph_destroy(LogregBatchGraph* bg);
+int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos, float* grad,
+                            double* logdens, const float* z, const double* u,
+                            const InfoDev<float>& info, int gemm_impl, cudaStream_t st);
+
 // Last-step statistics of the batched path (host-side counters).
 struct LogregStats {
   long long evals;           // fixed-point map evaluations issued (all chains)

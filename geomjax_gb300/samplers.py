@@ -35,6 +35,21 @@ INTEGRATORS = {"implicit_midpoint": L.GJ_IMPLICIT_MIDPOINT,
 LOGREG_PATHS = {"auto": 0, "simt": 1, "tcgen05": 2, "per_chain": 3, "cta": 4}
 
 
+def cta_supported(N: int, d: int, precision: str = "fp64", lmc: bool = False) -> bool:
+    """Whether one chain of an N x d logistic regression fits the
+    CTA-per-chain kernels (d <= 64 and the shared-memory layout of
+    csrc/logreg_cta.cu within 227 KB; the header gives the same formula)."""
+    if d < 1 or d > 64 or N < 1:
+        return False
+    P = d * (d + 1) // 2
+    t = 4 if precision == "mixed" else 8
+    nd = 2 * P + 16 * d + 274 + ((P + d * d) if lmc else 0)
+    b = nd * 8 + (P * 4 if t == 4 else 0) + (4 * N + max(N, 16 * d)) * t
+    b = (b + 15) // 16 * 16 + 16 * (d + 1) * t
+    b = (b + 15) // 16 * 16 + (4 * d if lmc else 0)
+    return (b + 15) // 16 * 16 <= 227 * 1024
+
+
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 

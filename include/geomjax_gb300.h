@@ -251,6 +251,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * and the consumers add the slices in order, so results do not depend on
  * scheduling. */
 #define GJ_OPT_GEMM_KSPLIT 8
+/* batches of posteriors (gj_batch_set_option): 1 (default) = one CUDA graph
+ * per transition holding every posterior's transition as an independent
+ * branch, launched once (plus one gather and one scatter kernel); 0 = one
+ * graph per posterior, spread over the batch's stream pool.  Results are
+ * bit-identical either way. */
+#define GJ_OPT_BATCH_GRAPH 9
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */
@@ -346,10 +352,13 @@ int32_t gj_metric_vjp(const gj_target* target, int32_t precision, int32_t num_ch
 /* ---- batches of independent posteriors ----------------------------------
  * A batch holds B dense-Fisher logistic-regression posteriors of any sizes
  * (n_data and dim may differ; dim <= 128), each sampled by C RMHMC chains
- * through the batched mixed-precision pipeline (either integrator).  Every
- * posterior's transition is one CUDA graph; the graphs are spread
- * round-robin over num_streams streams forked from and joined to the
- * caller's stream, so many small posteriors fill the GPU together.
+ * through the batched mixed-precision pipeline (either integrator).  By
+ * default one CUDA graph holds every posterior's transition as an
+ * independent branch, and one launch per transition advances them all
+ * (GJ_OPT_BATCH_GRAPH; the graph is captured at the first step with a given
+ * number of steps and kept); otherwise each posterior's transition is its
+ * own graph, spread round-robin over num_streams streams forked from and
+ * joined to the caller's stream.
  * The reference samples one posterior per kernel call; a batch is the
  * vmapped loop over posteriors a user would write around it.
  *
@@ -363,7 +372,7 @@ int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
                         int32_t chains_per_posterior, int32_t num_streams, gj_batch** out);
 int32_t gj_batch_destroy(gj_batch* batch);
 /* GJ_OPT_CHOL_FP64, GJ_OPT_CHOL_CHAINS_PER_WARP and GJ_OPT_GEMM_KSPLIT, for
- * every posterior */
+ * every posterior; GJ_OPT_BATCH_GRAPH for the batch */
 int32_t gj_batch_set_option(gj_batch* batch, int32_t key, int64_t value);
 int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_chain_state* state,
                             const float* z, const double* u, gj_info* info, void* stream);

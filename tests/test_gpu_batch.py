@@ -1,6 +1,7 @@
 """Batches of uneven logistic-regression posteriors (``gj_batch_*``): every
-posterior's chains follow the oracle step by step, and the batch (graphs on
-a stream pool) is bit-identical to running each posterior on its own."""
+posterior's chains follow the oracle step by step, and the batch (one CUDA
+graph holding every posterior as a branch, or one graph per posterior on a
+stream pool) is bit-identical to running each posterior on its own."""
 import numpy as np
 import pytest
 
@@ -69,13 +70,14 @@ def test_batch_matches_oracle_per_posterior(integrator):
             assert rel_err(eb, oi.energy) < 1e-4, (b, L)
 
 
-def test_batch_bitwise_equals_single_posterior_runs():
+@pytest.mark.parametrize("one_graph", [True, False])
+def test_batch_bitwise_equals_single_posterior_runs(one_graph):
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
     from geomjax_gb300.batch import PosteriorBatch
 
     data = _data()
-    pb = PosteriorBatch(data, C, num_streams=4)
+    pb = PosteriorBatch(data, C, num_streams=4, one_graph=one_graph)
     q0 = _starts()
     zs, us = _draws(11)
     st = pb.init(q0)
@@ -91,3 +93,34 @@ def test_batch_bitwise_equals_single_posterior_runs():
                                       _np(i1.is_accepted))
         np.testing.assert_array_equal(_np(info.fixed_point_iters)[b * C:(b + 1) * C],
                                       _np(i1.fixed_point_iters))
+
+
+@pytest.mark.parametrize("integrator", ["implicit_midpoint", "generalized_leapfrog"])
+def test_batch_one_graph_reused_across_calls(integrator):
+    """The one-graph batch over three transitions (the graph captured at the
+    first is reused, the step size changes between calls, the state arrays
+    move) equals the stream-pool batch bit for bit, info included."""
+    import torch
+    from geomjax_gb300.batch import PosteriorBatch
+
+    data = _data()
+    outs = []
+    for one in (True, False):
+        pb = PosteriorBatch(data, C, num_streams=3, one_graph=one, integrator=integrator)
+        st = pb.init(_starts())
+        info = pb.new_info()
+        g = torch.Generator(device="cuda").manual_seed(5)
+        n = int(pb.offsets[-1])
+        rec = []
+        for h in (0.05, 0.04, 0.06):
+            z = torch.randn(n, generator=g, device="cuda")
+            u = torch.rand(len(SIZES) * C, generator=g, device="cuda", dtype=torch.float64)
+            st = type(st)(*(t.clone() for t in st))  # new addresses every call
+            pb.step_inplace(st, z, u, info, h, 5)
+            rec.append([_np(st.position), _np(st.logdensity), _np(st.logdensity_grad)] +
+                       [_np(info[k]) for k in ("acceptance_rate", "is_accepted", "energy",
+                                               "fp_iters", "status", "momentum")])
+        outs.append(rec)
+    for a, b in zip(*outs):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
