@@ -487,7 +487,9 @@ def run_batch(args, wl):
         "e2e": {"value": round(ws * B * C * Lsteps * e2e_steps / e2e_s, 1), "unit": "leapfrog steps/s",
                 "h2d_bytes_per_step": int(Zh.numel() * 4 + Uh.numel() * 8),
                 "d2h_bytes_per_step": int(Ph.numel() * 4 + Ah.numel())},
-        "graph_launches": B * K, "setup_s": round(t_setup, 1), "clocks": clk,
+        "graph_launches": K if not args.batch_pool else B * K,
+        "gpu_launches": 3 * K if not args.batch_pool else None,
+        "setup_s": round(t_setup, 1), "clocks": clk,
         "wall_s": round(t_wall, 3),
         "plain_fp64": (batch_plain_comparison(args, wl, Ns, ds, dev)
                        if rank == 0 and not args.no_plain else None),
@@ -732,10 +734,10 @@ def ess_comparison(args, wl, kern, target, state, info, extra, dev):
         form = "one CTA per chain, float64 throughout (data, state, Gram, factor, solves)"
     else:
         pt = gj.funnel(D=wl["D"], precision="fp64", device=dev)
-        pk = gj.lmcmonge.build_kernel()
+        pk = gj.lmcmonge.build_kernel()  # one warp per chain
         pst = gj.lmcmonge.init(start[:Cp].double(), pt)
         pextra = dict(alpha2=1.0, inverse_mass=torch.ones(d, dtype=torch.float64, device=dev))
-        form = "one thread per chain, float64 throughout"
+        form = "one warp per chain, float64 throughout"
     pinfo = pk.new_info(Cp, d, pt, dev)
     tr_p, acc_p, s_p = run(pk, pt, pst, pinfo, pextra)
     ess_m = gj.effective_sample_size(tr_m, chain_axis=1, sample_axis=0)
@@ -784,7 +786,7 @@ def run_plain_fp64(args, wl):
         C = wl["C"]
         d = wl["D"]
         target = gj.funnel(D=d, precision="fp64", device=dev)
-        kern = gj.lmcmonge.build_kernel()
+        kern = gj.lmcmonge.build_kernel(warp=False)
         extra = dict(alpha2=1.0, inverse_mass=torch.ones(d, dtype=torch.float64, device=dev))
         state = gj.lmcmonge.init(torch.ones(C, d, dtype=torch.float64), target)
         K = args.steps
@@ -1046,7 +1048,7 @@ def main():
             cmp_ = out["ess_comparison"]
             out["plain_fp64"] = dict(cmp_["plain_fp64"], transitions=cmp_["transitions"])
             out["min_ess_ratio"] = cmp_["min_ess_ratio"]
-        if not args.no_plain and wl["sampler"] == "rmhmc":
+        if not args.no_plain and wl["sampler"] in ("rmhmc", "lmcmonge"):
             # the thread-per-chain FP64 form, kept for continuity
             out["plain_fp64_thread_per_chain"] = run_plain_fp64(args, wl)
             out["steps_ratio_vs_thread_per_chain"] = round(

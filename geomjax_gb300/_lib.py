@@ -25,6 +25,7 @@ GJ_OPT_LOGREG_PATH, GJ_OPT_THREADS_PER_BLOCK, GJ_OPT_LOOP, GJ_OPT_CHOL_FP64 = 1,
 GJ_OPT_CHOL_CHAINS_PER_WARP, GJ_OPT_CHAIN_GROUPS, GJ_OPT_PDL = 5, 6, 7
 GJ_OPT_GEMM_KSPLIT = 8
 GJ_OPT_BATCH_GRAPH = 9
+GJ_OPT_MONGE_WARP = 10
 
 
 class GjTarget(ctypes.Structure):

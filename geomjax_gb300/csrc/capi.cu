@@ -94,6 +94,7 @@ struct gj_ctx {
   int groups;     // GJ_OPT_CHAIN_GROUPS (0 = automatic)
   int pdl;        // GJ_OPT_PDL
   int ksplit;     // GJ_OPT_GEMM_KSPLIT (0 = automatic)
+  int monge_warp; // GJ_OPT_MONGE_WARP
   // batched dense-Fisher path: one context per chain group; in graph mode
   // the groups' transitions run on their own streams, forked from and joined
   // to the caller's stream by events, so one group's factorisation can share
@@ -219,6 +220,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->groups = 0;
   c->pdl = 0;
   c->ksplit = 0;
+  c->monge_warp = 1;
   *out = c;
   return GJ_OK;
 }
@@ -265,6 +267,11 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     if (value < 0 || value > 4) return fail(GJ_EINVAL, "K slices must be 0 (automatic) .. 4");
     ctx->ksplit = (int)value;
     for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_MONGE_WARP) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "LMC-Monge warp flag must be 0 or 1");
+    ctx->monge_warp = (int)value;
     return GJ_OK;
   }
   if (key == GJ_OPT_CHAIN_GROUPS) {
@@ -487,10 +494,15 @@ int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   cudaError_t e;
-  if (ctx->precision == GJ_MIXED && gj::monge_warp_supported(t)) {
-    e = gj::launch_monge_warp(t, sp, (float*)s->position, (float*)s->logdensity_grad,
-                              s->logdensity, s->volume_adjustment, (const float*)z, u,
-                              gj::to_dev<float>(info), ctx->C, cs);
+  if (ctx->monge_warp && gj::monge_warp_supported(t)) {  // one warp per chain
+    if (ctx->precision == GJ_MIXED)
+      e = gj::launch_monge_warp<float>(t, sp, (float*)s->position, (float*)s->logdensity_grad,
+                                       s->logdensity, s->volume_adjustment, (const float*)z, u,
+                                       gj::to_dev<float>(info), ctx->C, cs);
+    else
+      e = gj::launch_monge_warp<double>(t, sp, (double*)s->position, (double*)s->logdensity_grad,
+                                        s->logdensity, s->volume_adjustment, (const double*)z, u,
+                                        gj::to_dev<double>(info), ctx->C, cs);
     return cuda_status(e, "gj_lmcmonge_step");
   }
   if (t.d > 128) return fail(GJ_ENOTSUP, "per-chain LMC-Monge supports d <= 128");

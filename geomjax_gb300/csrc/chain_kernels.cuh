@@ -54,10 +54,12 @@ cudaError_t launch_logreg_cta(int sampler, const TargetDev& t, const StepDev& sp
                               double* ld, double* vol, const T* z, const double* u,
                               const InfoDev<T>& info, int C, cudaStream_t st);
 
-// warp-per-chain LMC-Monge (monge_warp.cu), float32 state
-cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,
-                              double* ld, double* vol, const float* z, const double* u,
-                              const InfoDev<float>& info, int C, cudaStream_t st);
+// warp-per-chain LMC-Monge (monge_warp.cu): R = float (mixed form, float32
+// state) or R = double (plain FP64 form)
+template <typename R>
+cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, R* pos, R* grad, double* ld,
+                              double* vol, const R* z, const double* u, const InfoDev<R>& info,
+                              int C, cudaStream_t st);
 bool monge_warp_supported(const TargetDev& t);
 
 // q_L and ∂q_L/∂α² of one LMC-Monge transition, forward mode in float64

@@ -1,4 +1,5 @@
-// LMC on a Monge patch, one WARP per chain, float32 state (mixed precision).
+// LMC on a Monge patch, one WARP per chain: float32 state (the mixed form) or
+// float64 throughout (the plain form; R = double below).
 //
 // Restates lmcmonge/lmc.py:151-236 (kernel: L, normalised gradient, weighted
 // gradient, two HVPs, velocity draw, momentum), lmc_proposal :472-536,
@@ -12,33 +13,34 @@
 // uses the O(d) closed-form Cholesky factor of diag(M⁻¹) − α²·w·wᵀ (rank-one
 // modification, Gill, Golub, Murray & Saunders 1974) instead of the
 // reference's dense d x d Cholesky (lmcmonge/metrics.py:162-166).
-// FP64: the volume adjustment J across transitions (a transition's
-// increments are summed in FP32), the log density at the proposal and the
-// Hamiltonian difference; nothing in the step loop runs on the FP64 pipe.
+// Mixed form (R = float) FP64: the volume adjustment J across transitions (a
+// transition's increments are summed in FP32), the log density at the
+// proposal and the Hamiltonian difference; nothing in its step loop runs on
+// the FP64 pipe.  The plain form (R = double) is the same code in float64.
 #include "chain_kernels.cuh"
 
 namespace gj {
 
 namespace {
 
-template <int E>
+template <int E, typename R>
 struct WVec {
-  float x[E];
+  R x[E];
 };
 
-template <int E>
-__device__ __forceinline__ float wdot(const WVec<E>& a, const WVec<E>& b) {
-  float s = 0.f;
+template <int E, typename R>
+__device__ __forceinline__ R wdot(const WVec<E, R>& a, const WVec<E, R>& b) {
+  R s = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) s = fmaf(a.x[k], b.x[k], s);
+  for (int k = 0; k < E; ++k) s = fma(a.x[k], b.x[k], s);
   return warp_sum(s);
 }
 
 // broadcast element i (runtime) of a warp vector to all lanes
-template <int E>
-__device__ __forceinline__ float wget(const WVec<E>& a, int i) {
+template <int E, typename R>
+__device__ __forceinline__ R wget(const WVec<E, R>& a, int i) {
   const int slot = i >> 5, lane = i & 31;
-  float v = 0.f;
+  R v = R(0);
 #pragma unroll
   for (int k = 0; k < E; ++k)
     if (k == slot) v = a.x[k];
@@ -49,34 +51,36 @@ __device__ __forceinline__ float wget(const WVec<E>& a, int i) {
 // The scale constants are precomputed once per transition: on GB300 an FP64
 // division or logarithm inside the step loop costs more than the whole FP32
 // step (the FP64 pipe was 85 % busy with them in the loop).
+template <typename R>
 struct WarpTarget {
   TargetDev t;
   int lane;
-  float inv_a2, inv_b2;   // funnel: 1/σ² (a); hier: 1/σ_μ² (a), 1/σ_v² (b)
+  R inv_a2, inv_b2;   // funnel: 1/σ² (a); hier: 1/σ_μ² (a), 1/σ_v² (b)
   double inv_a2d, inv_b2d;  // the same in FP64, for the log density
   double ld_const;          // the log density's constant terms
 };
 
-__device__ inline WarpTarget make_warp_target(const TargetDev& t, int lane) {
-  WarpTarget W;
+template <typename R>
+__device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, int lane) {
+  WarpTarget<R> W;
   W.t = t;
   W.lane = lane;
   if (t.family == GJ_FUNNEL) {
     W.inv_a2d = 1.0 / (t.p0 * t.p0);
     W.inv_b2d = 0.0;
-    W.inv_a2 = float(W.inv_a2d);
-    W.inv_b2 = 0.f;
+    W.inv_a2 = R(W.inv_a2d);
+    W.inv_b2 = R(0);
     W.ld_const = -log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
   } else {
     const int J = t.n;
-    const float* sg = static_cast<const float*>(t.s);
+    const R* sg = static_cast<const R*>(t.s);
     double c = 0.0;
     for (int i = lane; i < J; i += 32) c += -log(double(sg[i])) - 0.5 * kLog2Pi;
     c = warp_sum(c);
     W.inv_a2d = 1.0 / (t.p0 * t.p0);
     W.inv_b2d = 1.0 / (t.p1 * t.p1);
-    W.inv_a2 = float(W.inv_a2d);
-    W.inv_b2 = float(W.inv_b2d);
+    W.inv_a2 = R(W.inv_a2d);
+    W.inv_b2 = R(W.inv_b2d);
     W.ld_const = c - J * 0.5 * kLog2Pi - log(t.p0) - 0.5 * kLog2Pi - log(t.p1) - 0.5 * kLog2Pi;
   }
   return W;
@@ -85,27 +89,27 @@ __device__ inline WarpTarget make_warp_target(const TargetDev& t, int lane) {
 // funnel: v = θ[d−1]
 // The FP64 log density is formed only when need_ld (the proposal's, after
 // the last step); the gradient is FP32.
-template <int E>
-__device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<E>& g, float* sx_out,
+template <int E, typename R>
+__device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q, WVec<E, R>& g, R* sx_out,
                                     bool need_ld = true) {
   const TargetDev& t = W.t;
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
-    const float v = wget<E>(q, d - 1);
-    const float ev = expf(-v);
-    float sx = 0.f;
+    const R v = wget<E>(q, d - 1);
+    const R ev = exp(-v);
+    R sx = R(0);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
-      const float x = (i < d - 1) ? q.x[k] : 0.f;
-      sx = fmaf(x, x, sx);
+      const R x = (i < d - 1) ? q.x[k] : R(0);
+      sx = fma(x, x, sx);
     }
     sx = warp_sum(sx);
-    const float gv = -v * W.inv_a2 - 0.5f * float(d - 1) + 0.5f * ev * sx;
+    const R gv = -v * W.inv_a2 - R(0.5) * R(d - 1) + R(0.5) * ev * sx;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
-      g.x[k] = (i < d - 1) ? -q.x[k] * ev : ((i == d - 1) ? gv : 0.f);
+      g.x[k] = (i < d - 1) ? -q.x[k] * ev : ((i == d - 1) ? gv : R(0));
     }
     *sx_out = sx;
     if (!need_ld) return 0.0;
@@ -114,33 +118,33 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
   }
   // hierarchical Gaussian: θ = [θ_1..θ_J, μ, v]
   const int J = t.n;
-  const float* y = static_cast<const float*>(t.y);
-  const float* sg = static_cast<const float*>(t.s);
-  const float mu = wget<E>(q, J), v = wget<E>(q, J + 1);
-  const float ev = expf(-v);
-  float sr = 0.f, srr = 0.f;
+  const R* y = static_cast<const R*>(t.y);
+  const R* sg = static_cast<const R*>(t.s);
+  const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
+  const R ev = exp(-v);
+  R sr = R(0), srr = R(0);
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
     if (i < J) {
-      const float r = q.x[k] - mu;
-      const float e = y[i] - q.x[k];
-      const float is2 = 1.f / (sg[i] * sg[i]);
+      const R r = q.x[k] - mu;
+      const R e = y[i] - q.x[k];
+      const R is2 = R(1) / (sg[i] * sg[i]);
       g.x[k] = e * is2 - r * ev;
       sr += r;
-      srr = fmaf(r, r, srr);
+      srr = fma(r, r, srr);
     }
   }
   sr = warp_sum(sr);
   srr = warp_sum(srr);
-  const float gmu = sr * ev - mu * W.inv_a2;
-  const float gvv = 0.5f * ev * srr - 0.5f * J - v * W.inv_b2;
+  const R gmu = sr * ev - mu * W.inv_a2;
+  const R gvv = R(0.5) * ev * srr - R(0.5) * J - v * W.inv_b2;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
     if (i == J) g.x[k] = gmu;
     if (i == J + 1) g.x[k] = gvv;
-    if (i > J + 1) g.x[k] = 0.f;
+    if (i > J + 1) g.x[k] = R(0);
   }
   *sx_out = srr;
   if (!need_ld) return 0.0;
@@ -160,67 +164,67 @@ __device__ double w_logdensity_grad(const WarpTarget& W, const WVec<E>& q, WVec<
 
 // Hessian-vector product; `sx` is the Σx² (funnel) / Σr² (hier) of the
 // last gradient evaluation at the same q.
-template <int E>
-__device__ void w_hvp(const WarpTarget& W, const WVec<E>& q, const WVec<E>& u, float sx, WVec<E>& out) {
+template <int E, typename R>
+__device__ void w_hvp(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E, R>& u, R sx, WVec<E, R>& out) {
   const TargetDev& t = W.t;
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
-    const float v = wget<E>(q, d - 1);
-    const float ev = expf(-v);
-    const float uv = wget<E>(u, d - 1);
-    float xu = 0.f;
+    const R v = wget<E>(q, d - 1);
+    const R ev = exp(-v);
+    const R uv = wget<E>(u, d - 1);
+    R xu = R(0);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
-      if (i < d - 1) xu = fmaf(q.x[k], u.x[k], xu);
+      if (i < d - 1) xu = fma(q.x[k], u.x[k], xu);
     }
     xu = warp_sum(xu);
-    const float ov = ev * xu + (-W.inv_a2 - 0.5f * ev * sx) * uv;
+    const R ov = ev * xu + (-W.inv_a2 - R(0.5) * ev * sx) * uv;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
-      out.x[k] = (i < d - 1) ? ev * (-u.x[k] + q.x[k] * uv) : ((i == d - 1) ? ov : 0.f);
+      out.x[k] = (i < d - 1) ? ev * (-u.x[k] + q.x[k] * uv) : ((i == d - 1) ? ov : R(0));
     }
     return;
   }
   const int J = t.n;
-  const float* sg = static_cast<const float*>(t.s);
-  const float mu = wget<E>(q, J), v = wget<E>(q, J + 1);
-  const float ev = expf(-v);
-  const float um = wget<E>(u, J), uv = wget<E>(u, J + 1);
-  float sr = 0.f, sut = 0.f, sru = 0.f;
+  const R* sg = static_cast<const R*>(t.s);
+  const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
+  const R ev = exp(-v);
+  const R um = wget<E>(u, J), uv = wget<E>(u, J + 1);
+  R sr = R(0), sut = R(0), sru = R(0);
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
     if (i < J) {
-      const float r = q.x[k] - mu;
+      const R r = q.x[k] - mu;
       sr += r;
       sut += u.x[k];
-      sru = fmaf(r, u.x[k], sru);
-      out.x[k] = -(1.f / (sg[i] * sg[i]) + ev) * u.x[k] + ev * um + r * ev * uv;
+      sru = fma(r, u.x[k], sru);
+      out.x[k] = -(R(1) / (sg[i] * sg[i]) + ev) * u.x[k] + ev * um + r * ev * uv;
     }
   }
   sr = warp_sum(sr);
   sut = warp_sum(sut);
   sru = warp_sum(sru);
-  const float om = ev * sut + (-float(J) * ev - W.inv_a2) * um - ev * sr * uv;
-  const float ovv = ev * sru - ev * sr * um + (-0.5f * ev * sx - W.inv_b2) * uv;
+  const R om = ev * sut + (-R(J) * ev - W.inv_a2) * um - ev * sr * uv;
+  const R ovv = ev * sru - ev * sr * um + (-R(0.5) * ev * sx - W.inv_b2) * uv;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
     if (i == J) out.x[k] = om;
     if (i == J + 1) out.x[k] = ovv;
-    if (i > J + 1) out.x[k] = 0.f;
+    if (i > J + 1) out.x[k] = R(0);
   }
 }
 
 // half_step_omega (lmcmonge/integrators.py:158-194), im = diag(M⁻¹).  dJ
 // accumulates this transition's volume-term increments in FP32 (each is
 // ≈ 1e-3; 4 per step); the caller adds the sum to the FP64 J once.
-template <int E>
-__device__ void w_half(float a2, WVec<E>& v, float* dJ, const WVec<E>& gn, const WVec<E>& hv, float L,
-                       const WVec<E>& im, const WVec<E>& Hdl, float eps, int fix) {
-  WVec<E> dl_ig, igH;
+template <int E, typename R>
+__device__ void w_half(R a2, WVec<E, R>& v, R* dJ, const WVec<E, R>& gn, const WVec<E, R>& hv, R L,
+                       const WVec<E, R>& im, const WVec<E, R>& Hdl, R eps, int fix) {
+  WVec<E, R> dl_ig, igH;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     dl_ig.x[k] = im.x[k] * gn.x[k];
@@ -228,43 +232,45 @@ __device__ void w_half(float a2, WVec<E>& v, float* dJ, const WVec<E>& gn, const
   }
   // log|det1| and log|1 − ½εα²(Hdl·v)| as FP32 log1p of the small terms
   // (det1 is an FP32 value, so an FP64 logarithm adds nothing)
-  const float x1 = 0.5f * eps * a2 * wdot<E>(hv, dl_ig);
-  const float det1 = 1.f + x1;
-  *dJ -= x1 > -1.f ? log1pf(x1) : logf(fabsf(det1));
-  const float sL = sqrtf(L);
+  const R x1 = R(0.5) * eps * a2 * wdot<E>(hv, dl_ig);
+  const R det1 = R(1) + x1;
+  *dJ -= x1 > -R(1) ? log1p(x1) : log(fabs(det1));
+  const R sL = sqrt(L);
   // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
-  float pd = 0.f;
+  R pd = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) pd = fmaf(-gn.x[k] + a2 * Hdl.x[k] / sL, dl_ig.x[k], pd);
+  for (int k = 0; k < E; ++k) pd = fma(-gn.x[k] + a2 * Hdl.x[k] / sL, dl_ig.x[k], pd);
   pd = warp_sum(pd);
-  WVec<E> vt;
+  WVec<E, R> vt;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
-    const float dphi_ig = -dl_ig.x[k] + a2 * igH.x[k] / sL;
-    vt.x[k] = v.x[k] - 0.5f * eps * sL * (dphi_ig - a2 * pd * dl_ig.x[k]);
+    const R dphi_ig = -dl_ig.x[k] + a2 * igH.x[k] / sL;
+    vt.x[k] = v.x[k] - R(0.5) * eps * sL * (dphi_ig - a2 * pd * dl_ig.x[k]);
   }
-  float corr = 0.5f * eps * wdot<E>(vt, hv) / det1;
+  R corr = R(0.5) * eps * wdot<E>(vt, hv) / det1;
   if (fix) corr *= a2;
 #pragma unroll
   for (int k = 0; k < E; ++k) v.x[k] = vt.x[k] - corr * dl_ig.x[k];
-  const float x2 = -0.5f * eps * a2 * wdot<E>(Hdl, v);
-  *dJ += x2 > -1.f ? log1pf(x2) : logf(fabsf(1.f + x2));
+  const R x2 = -R(0.5) * eps * a2 * wdot<E>(Hdl, v);
+  *dJ += x2 > -R(1) ? log1p(x2) : log(fabs(R(1) + x2));
 }
 
 // inclusive warp scan (ascending lane order)
-__device__ __forceinline__ float warp_incl_scan(float x, int lane) {
+template <typename R>
+__device__ __forceinline__ R warp_incl_scan(R x, int lane) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const float y = __shfl_up_sync(0xffffffffu, x, o);
+    const R y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
   return x;
 }
 // inclusive warp scan in descending lane order (suffix sums)
-__device__ __forceinline__ float warp_incl_rscan(float x, int lane) {
+template <typename R>
+__device__ __forceinline__ R warp_incl_rscan(R x, int lane) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const float y = __shfl_down_sync(0xffffffffu, x, o);
+    const R y = __shfl_down_sync(0xffffffffu, x, o);
     if (lane + o < 32) x += y;
   }
   return x;
@@ -274,47 +280,47 @@ __device__ __forceinline__ float warp_incl_rscan(float x, int lane) {
 // is bound by the latency of its warp reductions, and 24 warps per SM hide
 // it better than 16 (D = 100 ran 0.28 ms per transition at 80 registers,
 // 0.36 ms at the 120 the compiler picks unbounded)
-template <int E>
-__global__ void __launch_bounds__(256, 3) monge_warp_kernel(TargetDev t, StepDev sp, float* pos,
-                                                         float* grad, double* logdens, double* vol,
-                                                         const float* z, const double* uacc,
-                                                         InfoDev<float> info, int C) {
+template <int E, typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel(TargetDev t, StepDev sp, R* pos,
+                                                         R* grad, double* logdens, double* vol,
+                                                         const R* z, const double* uacc,
+                                                         InfoDev<R> info, int C) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= C) return;  // whole warp exits together
   const int d = t.d;
-  const WarpTarget W = make_warp_target(t, lane);
-  const float a2 = float(sp.alpha2);
-  const float eps = float(sp.h);
-  const float* imv = static_cast<const float*>(sp.inv_mass);
-  WVec<E> q, g, im, gn, Hdl, hv, v;
+  const WarpTarget<R> W = make_warp_target<R>(t, lane);
+  const R a2 = R(sp.alpha2);
+  const R eps = R(sp.h);
+  const R* imv = static_cast<const R*>(sp.inv_mass);
+  WVec<E, R> q, g, im, gn, Hdl, hv, v;
   double slm_part = 0.0;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
     const bool in = i < d;
-    q.x[k] = in ? pos[(size_t)c * d + i] : 0.f;
-    g.x[k] = in ? grad[(size_t)c * d + i] : 0.f;
-    im.x[k] = in ? (imv ? imv[i] : 1.f) : 0.f;
-    if (in) slm_part += -double(logf(im.x[k]));  // cancels in H1 − H0
+    q.x[k] = in ? pos[(size_t)c * d + i] : R(0);
+    g.x[k] = in ? grad[(size_t)c * d + i] : R(0);
+    im.x[k] = in ? (imv ? imv[i] : R(1)) : R(0);
+    if (in) slm_part += -double(log(im.x[k]));  // cancels in H1 − H0
   }
   const double slm = warp_sum(slm_part);  // Σ log M
   const double ld0 = logdens[c];
   const double J0 = vol[c];
-  float sx;
+  R sx;
   // ---- setup (lmc.py:177-208)
-  float L = 0.f;
+  R L = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) L = fmaf(im.x[k] * g.x[k], g.x[k], L);
-  L = 1.f + a2 * warp_sum(L);
-  float sL = sqrtf(L);
+  for (int k = 0; k < E; ++k) L = fma(im.x[k] * g.x[k], g.x[k], L);
+  L = R(1) + a2 * warp_sum(L);
+  R sL = sqrt(L);
   {
     // Σx² at the current q for the HVPs (one extra gradient pass is avoided by
     // recomputing only the reduction)
-    WVec<E> gtmp;
+    WVec<E, R> gtmp;
     (void)w_logdensity_grad<E>(W, q, gtmp, &sx, false);
   }
-  WVec<E> dl_ig;
+  WVec<E, R> dl_ig;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     gn.x[k] = g.x[k] / sL;
@@ -325,33 +331,33 @@ __global__ void __launch_bounds__(256, 3) monge_warp_kernel(TargetDev t, StepDev
   for (int k = 0; k < E; ++k) Hdl.x[k] /= sL;
   // ---- velocity: closed-form factor (τ_j = 1/L + α² Σ_{k≥j} u_k², u = w/sqrt(M⁻¹))
   {
-    WVec<E> u, zz;
-    float tot_after = 0.f;  // Σ over slots > k of u²
-    float tau[E], taun[E];
+    WVec<E, R> u, zz;
+    R tot_after = R(0);  // Σ over slots > k of u²
+    R tau[E], taun[E];
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
-      u.x[k] = (i < d) ? dl_ig.x[k] * rsqrtf(im.x[k]) : 0.f;
-      zz.x[k] = (i < d) ? z[(size_t)c * d + i] : 0.f;
+      u.x[k] = (i < d) ? dl_ig.x[k] * rsqrt(im.x[k]) : R(0);
+      zz.x[k] = (i < d) ? z[(size_t)c * d + i] : R(0);
     }
 #pragma unroll
     for (int k = E - 1; k >= 0; --k) {
-      const float u2 = u.x[k] * u.x[k];
-      const float r = warp_incl_rscan(u2, lane);
-      const float suf = r + tot_after;  // Σ_{j≥i}
-      tau[k] = 1.f / L + a2 * suf;
+      const R u2 = u.x[k] * u.x[k];
+      const R r = warp_incl_rscan(u2, lane);
+      const R suf = r + tot_after;  // Σ_{j≥i}
+      tau[k] = R(1) / L + a2 * suf;
       taun[k] = tau[k] - a2 * u2;
       tot_after += __shfl_sync(0xffffffffu, r, 0);
     }
-    float pre_before = 0.f;  // Σ over slots < k
+    R pre_before = R(0);  // Σ over slots < k
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
-      const float tk = (i < d) ? u.x[k] * zz.x[k] * rsqrtf(tau[k] * taun[k]) : 0.f;
-      const float incl = warp_incl_scan(tk, lane);
-      const float pre = pre_before + incl - tk;  // Σ_{j<i}
-      const float y = sqrtf(taun[k] / tau[k]) * zz.x[k] - a2 * u.x[k] * pre;
-      v.x[k] = (i < d) ? sqrtf(im.x[k]) * y : 0.f;
+      const R tk = (i < d) ? u.x[k] * zz.x[k] * rsqrt(tau[k] * taun[k]) : R(0);
+      const R incl = warp_incl_scan(tk, lane);
+      const R pre = pre_before + incl - tk;  // Σ_{j<i}
+      const R y = sqrt(taun[k] / tau[k]) * zz.x[k] - a2 * u.x[k] * pre;
+      v.x[k] = (i < d) ? sqrt(im.x[k]) * y : R(0);
       pre_before += __shfl_sync(0xffffffffu, incl, 31);
       if (info.momentum && i < d) info.momentum[(size_t)c * d + i] = v.x[k];
     }
@@ -359,13 +365,13 @@ __global__ void __launch_bounds__(256, 3) monge_warp_kernel(TargetDev t, StepDev
   w_hvp<E>(W, q, v, sx, hv);
 #pragma unroll
   for (int k = 0; k < E; ++k) hv.x[k] /= sL;
-  auto kinetic = [&](float Lc) -> double {  // lmcmonge/metrics.py:168-186
-    float vmv = 0.f, vg = 0.f;
+  auto kinetic = [&](R Lc) -> double {  // lmcmonge/metrics.py:168-186
+    R vmv = R(0), vg = R(0);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
-      const float m = (im.x[k] > 0.f) ? 1.f / im.x[k] : 0.f;
-      vmv = fmaf(m * v.x[k], v.x[k], vmv);
-      vg = fmaf(v.x[k], gn.x[k], vg);
+      const R m = (im.x[k] > R(0)) ? R(1) / im.x[k] : R(0);
+      vmv = fma(m * v.x[k], v.x[k], vmv);
+      vg = fma(v.x[k], gn.x[k], vg);
     }
     vmv = warp_sum(vmv);
     vg = warp_sum(vg);
@@ -374,17 +380,17 @@ __global__ void __launch_bounds__(256, 3) monge_warp_kernel(TargetDev t, StepDev
   };
   const double H0 = -ld0 + kinetic(L) - J0;
   double ld = ld0;
-  float dJ = 0.f;  // this transition's volume-term increments
+  R dJ = R(0);  // this transition's volume-term increments
   for (int s = 0; s < sp.L; ++s) {  // lan_integrator.one_step
     w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
 #pragma unroll
-    for (int k = 0; k < E; ++k) q.x[k] = fmaf(eps, v.x[k], q.x[k]);
+    for (int k = 0; k < E; ++k) q.x[k] = fma(eps, v.x[k], q.x[k]);
     ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1);
-    float Ls = 0.f;
+    R Ls = R(0);
 #pragma unroll
-    for (int k = 0; k < E; ++k) Ls = fmaf(im.x[k] * g.x[k], g.x[k], Ls);
-    L = 1.f + a2 * warp_sum(Ls);
-    sL = sqrtf(L);
+    for (int k = 0; k < E; ++k) Ls = fma(im.x[k] * g.x[k], g.x[k], Ls);
+    L = R(1) + a2 * warp_sum(Ls);
+    sL = sqrt(L);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       gn.x[k] = g.x[k] / sL;
@@ -445,22 +451,30 @@ bool monge_warp_supported(const TargetDev& t) {
   return (t.family == GJ_FUNNEL || t.family == GJ_HIERGAUSS) && t.d >= 2 && t.d <= 256;
 }
 
-cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, float* pos, float* grad,
-                              double* ld, double* vol, const float* z, const double* u,
-                              const InfoDev<float>& info, int C, cudaStream_t st) {
+template <typename R>
+cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, R* pos, R* grad, double* ld,
+                              double* vol, const R* z, const double* u, const InfoDev<R>& info,
+                              int C, cudaStream_t st) {
   const int tpb = 256;
   const dim3 grid((unsigned)(((size_t)C * 32 + tpb - 1) / tpb));
   if (t.d <= 32)
-    monge_warp_kernel<1><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<1, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 64)
-    monge_warp_kernel<2><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<2, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 128)
-    monge_warp_kernel<4><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<4, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 256)
-    monge_warp_kernel<8><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<8, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
+
+template cudaError_t launch_monge_warp<float>(const TargetDev&, const StepDev&, float*, float*,
+                                              double*, double*, const float*, const double*,
+                                              const InfoDev<float>&, int, cudaStream_t);
+template cudaError_t launch_monge_warp<double>(const TargetDev&, const StepDev&, double*, double*,
+                                               double*, double*, const double*, const double*,
+                                               const InfoDev<double>&, int, cudaStream_t);
 
 }  // namespace gj

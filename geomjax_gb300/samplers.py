@@ -273,11 +273,15 @@ class lmcmonge:
         return _init(target, position, True)
 
     @staticmethod
-    def build_kernel(divergence_threshold=1000.0, alpha2_fix=False):
+    def build_kernel(divergence_threshold=1000.0, alpha2_fix=False, warp=True):
         """``lmcmonge/lmc.py:130-237``; kernel(rng_key, state, target,
-        step_size, num_integration_steps, alpha2=..., inverse_mass_matrix=...)."""
-        return Kernel(L.GJ_SAMPLER_LMCMONGE, divergence_threshold=divergence_threshold,
-                      alpha2_fix=alpha2_fix)
+        step_size, num_integration_steps, alpha2=..., inverse_mass_matrix=...).
+        ``warp``: one warp per chain (default, either precision) or one thread
+        per chain."""
+        k = Kernel(L.GJ_SAMPLER_LMCMONGE, divergence_threshold=divergence_threshold,
+                   alpha2_fix=alpha2_fix)
+        k.options[L.GJ_OPT_MONGE_WARP] = 1 if warp else 0
+        return k
 
     def __new__(cls, target: Target, step_size: float, inverse_mass_matrix, num_integration_steps:
                 int, *, alpha2: float = 0.001, divergence_threshold=1000.0, alpha2_fix=False):

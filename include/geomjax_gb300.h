@@ -257,6 +257,10 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * graph per posterior, spread over the batch's stream pool.  Results are
  * bit-identical either way. */
 #define GJ_OPT_BATCH_GRAPH 9
+/* LMC-Monge (funnel and hierarchical Gaussian, d <= 256): 1 (default) = one
+ * warp per chain in either precision (float64 throughout for GJ_FP64),
+ * 0 = one thread per chain */
+#define GJ_OPT_MONGE_WARP 10
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */

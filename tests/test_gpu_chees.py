@@ -167,7 +167,7 @@ def test_lmc_proposal_matches_oracle(precision):
 
 @pytest.mark.parametrize("precision,D", [("fp64", 7), ("mixed", 100)])
 def test_lmcmonge_proposal_matches_oracle(precision, D):
-    """FP64 runs the per-chain kernel, mixed D = 100 the warp-per-chain one."""
+    """FP64 at D = 7 and mixed at D = 100, both on the warp-per-chain kernel."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
