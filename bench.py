@@ -196,6 +196,7 @@ def run_ours(args, wl):
     C, Lsteps, h = wl["C"], wl["L"], wl["h"]
     L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else
                                        (1 if args.gemm_two_cta else -1)))
+    L.check(L.lib().gj_set_gemm_accumulators(args.gemm_accumulators))
     if wl["sampler"] == "rmhmc":
         X, y = logreg_data(wl["N"], wl["d"], seed=0)
         target = gj.logistic_regression(X, y, precision="mixed", device=dev)
@@ -369,6 +370,7 @@ def run_ours(args, wl):
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
                    "gemm_ksplit": args.gemm_ksplit or "auto",
+                   "gemm_accumulators": args.gemm_accumulators,
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}", "autotune": tuned},
@@ -405,6 +407,7 @@ def run_batch(args, wl):
     B, C, Lsteps, h = wl["B"], wl["C"], wl["L"], wl["h"]
     L.check(L.lib().gj_set_gemm_tiling(args.gemm_tile_n, 0 if args.gemm_one_cta else
                                        (1 if args.gemm_two_cta else -1)))
+    L.check(L.lib().gj_set_gemm_accumulators(args.gemm_accumulators))
     Ns, ds = uneven_logreg_batch(B, seed=rank)
     t_setup = time.perf_counter()
     data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
@@ -722,7 +725,10 @@ def ess_comparison(args, wl, kern, target, state, info, extra, dev):
         return tr, acc, sum(a.elapsed_time(b) for a, b in evs) / 1e3
 
     tr_m, acc_m, s_m = run(kern, target, state, info, extra)
-    Cp = min(C, args.plain_chains)
+    # the warp-per-chain Monge form needs every chain to fill the GPU (8192
+    # chains are 1024 CTAs); the CTA-per-chain logistic form fills it with
+    # plain_chains and costs ~60x more per chain
+    Cp = C if wl["sampler"] == "lmcmonge" else min(C, args.plain_chains)
     if wl["sampler"] == "rmhmc":
         from geomjax_gb300.data import logreg_data
 
@@ -798,7 +804,6 @@ def run_plain_fp64(args, wl):
         kern.step_inplace(target, state, torch.randn(C, d, generator=gen, device=dev, dtype=torch.float64),
                           torch.rand(C, generator=gen, device=dev, dtype=torch.float64), info, h, Lsteps,
                           **extra)
-    trace = torch.empty(K, C, d, dtype=torch.float64, device=dev)
     Z = torch.randn(K, C, d, generator=gen, device=dev, dtype=torch.float64)
     U = torch.rand(K, C, generator=gen, device=dev, dtype=torch.float64)
     stream = torch.cuda.current_stream()
@@ -808,16 +813,13 @@ def run_plain_fp64(args, wl):
         evs[i][0].record(stream)
         kern.step_inplace(target, state, Z[i], U[i], info, h, Lsteps, **extra)
         evs[i][1].record(stream)
-        trace[i].copy_(state.position)
     torch.cuda.synchronize()
     dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-    out = {"value": round(C * Lsteps * K / dev_s, 1), "unit": "leapfrog steps/s", "chains": C,
-           "transitions": K, "ms_per_step": round(1e3 * dev_s / K, 3),
-           "form": "one thread per chain, float64 throughout"}
-    if K >= 4:
-        ess = gj.effective_sample_size(trace, chain_axis=1, sample_axis=0)
-        out["min_ess_per_s"] = round(float(torch.min(ess).item()) / dev_s, 2)
-    return out
+    # leapfrog steps/s only: its few transitions start out of equilibrium, so
+    # an ESS of them would not be a min-ESS/s (ess_comparison has that)
+    return {"value": round(C * Lsteps * K / dev_s, 1), "unit": "leapfrog steps/s", "chains": C,
+            "transitions": K, "ms_per_step": round(1e3 * dev_s / K, 3),
+            "form": "one thread per chain, float64 throughout"}
 
 
 def cpu_baseline(wl, budget_s=12.0):
@@ -1003,6 +1005,8 @@ def main():
                     help="deep operand ring, one CTA per SM, for every GEMM")
     ap.add_argument("--gemm-two-cta", action="store_true",
                     help="operand ring cut back to two CTAs per SM for every GEMM")
+    ap.add_argument("--gemm-accumulators", type=int, default=4, choices=[1, 2, 4],
+                    help="most K-range TMEM accumulators per tcgen05 GEMM CTA")
     ap.add_argument("--gemm-ksplit", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="K slices of the gradient contraction (0 = automatic)")
     ap.add_argument("--pdl", action="store_true",

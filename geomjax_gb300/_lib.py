@@ -152,6 +152,7 @@ SIGNATURES = {
                                          POINTER(GjStepParams), c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_void_p]),
     "gj_fma_peak": (c_int32, [c_int32, POINTER(c_double), c_void_p]),
+    "gj_set_gemm_accumulators": (c_int32, [c_int32]),
     "gj_chees_workspace_size": (c_int64, [c_int32, c_int32]),
     "gj_chees_statistics": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

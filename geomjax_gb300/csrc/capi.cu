@@ -882,6 +882,13 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
   return GJ_OK;
 }
 
+int32_t gj_set_gemm_accumulators(int32_t max_ranges) {
+  if (max_ranges != 1 && max_ranges != 2 && max_ranges != 4)
+    return fail(GJ_EINVAL, "K-range accumulators must be 1, 2 or 4");
+  gj::gemm_tc_set_accumulators(max_ranges);
+  return GJ_OK;
+}
+
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm) {
   if (tile_n_wide != 0 && tile_n_wide != 64 && tile_n_wide != 128)
     return fail(GJ_EINVAL, "tile width must be 0 (automatic), 64 or 128");

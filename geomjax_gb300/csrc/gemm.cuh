@@ -187,6 +187,10 @@ void gemm_tc_set_tuning(int bn_wide, int two_ctas);
 // a small integer identifying the current tile policy (part of the key of
 // captured graphs, whose launches keep the tiles they were captured with)
 int gemm_tc_tuning_code();
+// most K-range accumulators a CTA may use (1, 2 or 4; default 4): more
+// ranges shorten the tensor core's low-rounding accumulation runs, and cost
+// the epilogue one TMEM read per range
+void gemm_tc_set_accumulators(int max_ranges);
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
 

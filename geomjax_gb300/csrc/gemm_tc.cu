@@ -518,6 +518,7 @@ namespace {
 struct TcTuning {
   int bn_wide = 0;         // tile width for N > 64: 0 = automatic, 64 or 128
   int two_ctas = -1;       // -1 = automatic, 1 = prefer two CTAs per SM, 0 = deep ring
+  int max_nacc = 4;        // most K-range accumulators per CTA: 1, 2 or 4
 };
 TcTuning g_tune;
 
@@ -541,7 +542,8 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   const int kb_cta = (kb + g.ksplit - 1) / g.ksplit;
   const int ctas = C::smem(ns) <= kTwoCtaSmem ? 2 : 1;
   int nacc = 1;
-  while (nacc < 4 && 2 * nacc * 2 <= kb_cta && 2 * nacc * C::TMEM_COLS * ctas <= 512) nacc *= 2;
+  while (nacc < g_tune.max_nacc && 2 * nacc * 2 <= kb_cta && 2 * nacc * C::TMEM_COLS * ctas <= 512)
+    nacc *= 2;
   return launch_k(g.pdl, gemm_tc_kernel<NPL, BN>, grid, dim3(320), (size_t)C::smem(ns), st, a->map,
                   mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0, nacc);
 }
@@ -558,7 +560,13 @@ cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOper
 
 }  // namespace
 
-int gemm_tc_tuning_code() { return (g_tune.bn_wide / 64) * 3 + (g_tune.two_ctas + 1); }
+int gemm_tc_tuning_code() {
+  return (g_tune.bn_wide / 64) * 3 + (g_tune.two_ctas + 1) + 16 * g_tune.max_nacc;
+}
+
+void gemm_tc_set_accumulators(int max_ranges) {
+  g_tune.max_nacc = (max_ranges == 1 || max_ranges == 2) ? max_ranges : 4;
+}
 
 void gemm_tc_set_tuning(int bn_wide, int two_ctas) {
   g_tune.bn_wide = (bn_wide == 64 || bn_wide == 128) ? bn_wide : 0;

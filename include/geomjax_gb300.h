@@ -42,7 +42,7 @@
  *                      (adaptation/chees_adaptation_riemanian.py:145-190,
  *                      chees_adaptation_lmcmonge.py:151-236)
  *   gj_gemm_split_bf16, gj_gemm_split_bf16_noalloc, gj_stats, gj_profile,
- *   gj_fma_peak, gj_set_option, gj_set_gemm_tiling
+ *   gj_fma_peak, gj_set_option, gj_set_gemm_tiling, gj_set_gemm_accumulators
  *                      no reference counterpart: the split-BF16 contraction
  *                      as a test hook, measurement and tuning
  *
@@ -389,6 +389,16 @@ int32_t gj_batch_rmhmc_step(gj_batch* batch, const gj_step_params* params, gj_ch
  * one captured graph per policy, so changing it (as the autotuner of
  * geomjax_gb300.autotune does) captures anew. */
 int32_t gj_set_gemm_tiling(int32_t tile_n_wide, int32_t two_ctas_per_sm);
+
+/* Process-wide: the most K-range accumulators a tcgen05 GEMM CTA uses (1, 2
+ * or 4; default 4).  The K blocks of a CTA are cut into up to that many
+ * contiguous ranges, each accumulated in its own TMEM tile and added in FP32
+ * registers by the epilogue: the tensor core's FP32 accumulation rounds low
+ * and its bias grows with the accumulation run (−4.5e-6 relative over
+ * K = 1000 and −3.2e-5 over K = 5000 with one range).  Like
+ * gj_set_gemm_tiling it applies to later launches and graph captures.  No
+ * counterpart in the reference (accuracy / speed tuning). */
+int32_t gj_set_gemm_accumulators(int32_t max_ranges);
 
 /* Derivatives of one RMHMC transition with the generalized leapfrog, for a
  * GJ_LOGREG target with float64 data: with respect to the step size h and
