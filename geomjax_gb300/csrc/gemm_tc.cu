@@ -401,14 +401,19 @@ __global__ void __launch_bounds__(320, 2)
 #pragma unroll 1
       for (int c0 = 32 * half; c0 < BN; c0 += 64) {
         if (n0 + c0 >= N) break;  // warp-uniform
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         float v[32];
+        {
+          uint32_t r[32];
+          tmem_ld32(ta, r);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+        }
         // the other K ranges' partial tiles, added in order (round to nearest)
+#pragma unroll 1
         for (int acc = 1; acc < nacc; ++acc) {
-          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TMEM_COLS + c0), r);
+          uint32_t r[32];
+          tmem_ld32(ta + (uint32_t)(acc * TMEM_COLS), r);
 #pragma unroll
           for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
         }
