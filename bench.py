@@ -64,6 +64,8 @@ WORKLOADS = {
                             d=64, C=1024, L=20, h=0.02, lam=0.01, sampler="jvp"),
     "uneven": dict(name="uneven_logreg_2048posteriors_N200-5000_d8-128_64chains", B=2048, C=64,
                    L=8, h=0.05, sampler="batch"),
+    "nuts": dict(name="funnel_D2_nuts_rmhmc_diag_fisher_fp64_4096chains", D=2, C=4096, h=0.1,
+                 M=6, sampler="nuts"),
 }
 
 
@@ -586,6 +588,62 @@ def batch_plain_comparison(args, wl, Ns, ds, dev, T=4):
             "steps_ratio": round(s_plain / s_mixed, 2)}
 
 
+def run_nuts(args, wl):
+    """Iterative NUTS with the RMHMC dynamics (rmhmc/nuts.py) on the funnel
+    D = 2 with the diagonal Fisher metric, plain FP64, one thread per chain:
+    every chain builds its own tree (up to 2^M states).  A "step" is one NUTS
+    transition of every chain; the unit counts the integration steps the
+    trees actually took."""
+    import torch
+
+    import geomjax_gb300 as gj
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    C, d, h, M = wl["C"], wl["D"], wl["h"], wl["M"]
+    tg = gj.funnel(D=d, metric="diag", precision="fp64", device=dev)
+    kern = gj.nutsrmhmc.build_kernel(integrator="generalized_leapfrog", max_iters=6)
+    st = gj.nutsrmhmc.init(torch.ones(C, d, dtype=torch.float64), tg)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(31 + rank)
+    K, W = args.steps, args.warmup
+    for _ in range(W + 50):  # warm-up and burn-in
+        st, _ = kern(gen, st, tg, h, M)
+    trace = torch.empty(K, C, d, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(K)]
+    nsteps = torch.zeros((), dtype=torch.int64, device=dev)
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    for i in range(K):
+        evs[i][0].record(stream)
+        st, info = kern(gen, st, tg, h, M)
+        evs[i][1].record(stream)
+        trace[i].copy_(st.position)
+        nsteps += info.num_integration_steps.sum()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev_s = _barrier_max(sum(a.elapsed_time(b) for a, b in evs) / 1e3, ws)
+    steps = float(nsteps.item())
+    ess = gj.effective_sample_size(trace, chain_axis=1, sample_axis=0) if K >= 4 else None
+    return {
+        "metric": "leapfrog steps/s of iterative NUTS-RMHMC (integration steps the trees took), 1 GB300",
+        "value": round(ws * steps / dev_s, 1), "unit": "leapfrog steps/s", "n_gpus": ws,
+        "steps": K, "warmup": W, "ms_per_step": round(1e3 * dev_s / K, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["name"], "chains": C, "step_size": h, "max_num_doublings": M,
+                   "integrator": "generalized_leapfrog", "max_iters": 6,
+                   "form": "one thread per chain, float64"},
+        "mean_tree_steps": round(steps / (C * K), 2),
+        "min_ess_per_s": (round(float(ess.min()) / dev_s, 2) if ess is not None else None),
+        "gpu_launches": K, "clocks": clk,
+    }
+
+
 def run_jvp(args, wl):
     """Differentiated trajectory: per chain, p_accept and ΔH of one
     generalized-leapfrog transition of L steps with their derivatives with
@@ -891,6 +949,41 @@ def run_reference(args, wl):
     if wl["sampler"] == "jvp":
         return {"impl": "reference", "unavailable": "the reference differentiates trajectories with "
                 "JAX autodiff, and JAX is not installable here; the float64 oracle has no derivative"}
+    if wl["sampler"] == "nuts":
+        from oracle import nuts as O_nuts
+
+        ot = OT.Funnel(D=wl["D"], metric="diag")
+        d, C, M = wl["D"], 16, wl["M"]
+        s = O_rm.init(ot, np.ones((C, d)))
+        counted = {"n": 0}
+
+        def step(s):
+            s2, infos = O_nuts.kernel(ot, s, rng.standard_normal((C, d)),
+                                      rng.random((C, O_nuts.num_uniforms(M))), wl["h"], M,
+                                      integrator="generalized_leapfrog", max_iters=6)
+            counted["n"] += int(sum(i.num_integration_steps for i in infos))
+            return s2
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            s = step(s)
+        counted["n"] = 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s = step(s)
+        dt = time.perf_counter() - t0
+        v = counted["n"] / dt
+        return {
+            "metric": "leapfrog steps/s of iterative NUTS-RMHMC (integration steps the trees took)",
+            "value": round(v, 2), "unit": "leapfrog steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": wl["name"], "chains_sampled": C},
+            "cpu_baseline": {"value": round(v, 2), "unit": "leapfrog steps/s", "cores": cores,
+                             "kind": "port", "sample": f"{C} chains per step, float64 NumPy "
+                                                       "restatement in oracle/"},
+            "e2e": {"value": round(v, 2), "unit": "leapfrog steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
     if wl["sampler"] == "rmhmc_funnel":
         ot = OT.Funnel(D=wl["D"], metric="diag")
         d, C = wl["D"], wl["C"]
@@ -1041,8 +1134,8 @@ def main():
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if wl["sampler"] in ("batch", "jvp"):
-        out = run_batch(args, wl) if wl["sampler"] == "batch" else run_jvp(args, wl)
+    if wl["sampler"] in ("batch", "jvp", "nuts"):
+        out = {"batch": run_batch, "jvp": run_jvp, "nuts": run_nuts}[wl["sampler"]](args, wl)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
