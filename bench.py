@@ -46,12 +46,11 @@ sys.path.insert(0, ROOT)
 METRIC = "min-ESS/s and leapfrog steps/s, batched mixed-precision vs plain FP64 CUDA, 1 GB300"
 
 # DRAM bytes (read + write) per GEMM launch on the default logistic-regression
-# workload (4096 chains), averaged over the five GEMMs of one implicit-midpoint
-# map evaluation (Xβ, Gram, S, trace, gradient), from one cold-cache ncu
-# capture (profiles/gemm_tc_and_chol_logreg_N1000_d25_C4096_ncu.md).  The
-# generalized leapfrog launches the same kernels in another mix.  Reported
-# only for that chain count.
-NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 23.9e6}
+# workload (4096 chains), averaged over three consecutive GEMM launches of the
+# generalized leapfrog's momentum loop (r₂·X, Xβ / S, r₂·X), from one
+# cold-cache ncu capture (profiles/gemm_tc_logreg_N1000_d25_C4096_ncu.md).
+# Reported only for that chain count.
+NCU_TRAFFIC_PER_GEMM_LAUNCH = {("logistic_regression_N1000_d25_rmhmc_fisher_4096chains", 4096): 28.7e6}
 
 WORKLOADS = {
     "logreg": dict(name="logistic_regression_N1000_d25_rmhmc_fisher_4096chains", N=1000, d=25,

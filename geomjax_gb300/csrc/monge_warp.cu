@@ -23,6 +23,25 @@ namespace gj {
 
 namespace {
 
+// math on the kernel's real type R: the float forms call the float32
+// functions explicitly (a bare rsqrt / log1p / log / fabs of a float may
+// resolve to the double overload and run on the FP64 pipe)
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ float m_log(float x) { return logf(x); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ float m_log1p(float x) { return log1pf(x); }
+__device__ __forceinline__ double m_log1p(double x) { return log1p(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double m_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double m_fma(double a, double b, double c) { return fma(a, b, c); }
+
+
 template <int E, typename R>
 struct WVec {
   R x[E];
@@ -32,7 +51,7 @@ template <int E, typename R>
 __device__ __forceinline__ R wdot(const WVec<E, R>& a, const WVec<E, R>& b) {
   R s = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) s = fma(a.x[k], b.x[k], s);
+  for (int k = 0; k < E; ++k) s = m_fma(a.x[k], b.x[k], s);
   return warp_sum(s);
 }
 
@@ -70,18 +89,18 @@ __device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, int lane) {
     W.inv_b2d = 0.0;
     W.inv_a2 = R(W.inv_a2d);
     W.inv_b2 = R(0);
-    W.ld_const = -log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
+    W.ld_const = -m_log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
   } else {
     const int J = t.n;
     const R* sg = static_cast<const R*>(t.s);
     double c = 0.0;
-    for (int i = lane; i < J; i += 32) c += -log(double(sg[i])) - 0.5 * kLog2Pi;
+    for (int i = lane; i < J; i += 32) c += -m_log(double(sg[i])) - 0.5 * kLog2Pi;
     c = warp_sum(c);
     W.inv_a2d = 1.0 / (t.p0 * t.p0);
     W.inv_b2d = 1.0 / (t.p1 * t.p1);
     W.inv_a2 = R(W.inv_a2d);
     W.inv_b2 = R(W.inv_b2d);
-    W.ld_const = c - J * 0.5 * kLog2Pi - log(t.p0) - 0.5 * kLog2Pi - log(t.p1) - 0.5 * kLog2Pi;
+    W.ld_const = c - J * 0.5 * kLog2Pi - m_log(t.p0) - 0.5 * kLog2Pi - m_log(t.p1) - 0.5 * kLog2Pi;
   }
   return W;
 }
@@ -96,13 +115,13 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
     const R v = wget<E>(q, d - 1);
-    const R ev = exp(-v);
+    const R ev = m_exp(-v);
     R sx = R(0);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
       const R x = (i < d - 1) ? q.x[k] : R(0);
-      sx = fma(x, x, sx);
+      sx = m_fma(x, x, sx);
     }
     sx = warp_sum(sx);
     const R gv = -v * W.inv_a2 - R(0.5) * R(d - 1) + R(0.5) * ev * sx;
@@ -121,7 +140,7 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
   const R* y = static_cast<const R*>(t.y);
   const R* sg = static_cast<const R*>(t.s);
   const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
-  const R ev = exp(-v);
+  const R ev = m_exp(-v);
   R sr = R(0), srr = R(0);
 #pragma unroll
   for (int k = 0; k < E; ++k) {
@@ -132,7 +151,7 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
       const R is2 = R(1) / (sg[i] * sg[i]);
       g.x[k] = e * is2 - r * ev;
       sr += r;
-      srr = fma(r, r, srr);
+      srr = m_fma(r, r, srr);
     }
   }
   sr = warp_sum(sr);
@@ -170,13 +189,13 @@ __device__ void w_hvp(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E,
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
     const R v = wget<E>(q, d - 1);
-    const R ev = exp(-v);
+    const R ev = m_exp(-v);
     const R uv = wget<E>(u, d - 1);
     R xu = R(0);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
-      if (i < d - 1) xu = fma(q.x[k], u.x[k], xu);
+      if (i < d - 1) xu = m_fma(q.x[k], u.x[k], xu);
     }
     xu = warp_sum(xu);
     const R ov = ev * xu + (-W.inv_a2 - R(0.5) * ev * sx) * uv;
@@ -190,7 +209,7 @@ __device__ void w_hvp(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E,
   const int J = t.n;
   const R* sg = static_cast<const R*>(t.s);
   const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
-  const R ev = exp(-v);
+  const R ev = m_exp(-v);
   const R um = wget<E>(u, J), uv = wget<E>(u, J + 1);
   R sr = R(0), sut = R(0), sru = R(0);
 #pragma unroll
@@ -200,7 +219,7 @@ __device__ void w_hvp(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E,
       const R r = q.x[k] - mu;
       sr += r;
       sut += u.x[k];
-      sru = fma(r, u.x[k], sru);
+      sru = m_fma(r, u.x[k], sru);
       out.x[k] = -(R(1) / (sg[i] * sg[i]) + ev) * u.x[k] + ev * um + r * ev * uv;
     }
   }
@@ -234,12 +253,12 @@ __device__ void w_half(R a2, WVec<E, R>& v, R* dJ, const WVec<E, R>& gn, const W
   // (det1 is an FP32 value, so an FP64 logarithm adds nothing)
   const R x1 = R(0.5) * eps * a2 * wdot<E>(hv, dl_ig);
   const R det1 = R(1) + x1;
-  *dJ -= x1 > -R(1) ? log1p(x1) : log(fabs(det1));
-  const R sL = sqrt(L);
+  *dJ -= x1 > -R(1) ? m_log1p(x1) : m_log(m_abs(det1));
+  const R sL = m_sqrt(L);
   // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
   R pd = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) pd = fma(-gn.x[k] + a2 * Hdl.x[k] / sL, dl_ig.x[k], pd);
+  for (int k = 0; k < E; ++k) pd = m_fma(-gn.x[k] + a2 * Hdl.x[k] / sL, dl_ig.x[k], pd);
   pd = warp_sum(pd);
   WVec<E, R> vt;
 #pragma unroll
@@ -252,7 +271,7 @@ __device__ void w_half(R a2, WVec<E, R>& v, R* dJ, const WVec<E, R>& gn, const W
 #pragma unroll
   for (int k = 0; k < E; ++k) v.x[k] = vt.x[k] - corr * dl_ig.x[k];
   const R x2 = -R(0.5) * eps * a2 * wdot<E>(Hdl, v);
-  *dJ += x2 > -R(1) ? log1p(x2) : log(fabs(R(1) + x2));
+  *dJ += x2 > -R(1) ? m_log1p(x2) : m_log(m_abs(R(1) + x2));
 }
 
 // inclusive warp scan (ascending lane order)
@@ -302,7 +321,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     q.x[k] = in ? pos[(size_t)c * d + i] : R(0);
     g.x[k] = in ? grad[(size_t)c * d + i] : R(0);
     im.x[k] = in ? (imv ? imv[i] : R(1)) : R(0);
-    if (in) slm_part += -double(log(im.x[k]));  // cancels in H1 − H0
+    if (in) slm_part += -double(m_log(im.x[k]));  // cancels in H1 − H0
   }
   const double slm = warp_sum(slm_part);  // Σ log M
   const double ld0 = logdens[c];
@@ -311,9 +330,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   // ---- setup (lmc.py:177-208)
   R L = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) L = fma(im.x[k] * g.x[k], g.x[k], L);
+  for (int k = 0; k < E; ++k) L = m_fma(im.x[k] * g.x[k], g.x[k], L);
   L = R(1) + a2 * warp_sum(L);
-  R sL = sqrt(L);
+  R sL = m_sqrt(L);
   {
     // Σx² at the current q for the HVPs (one extra gradient pass is avoided by
     // recomputing only the reduction)
@@ -329,7 +348,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   w_hvp<E>(W, q, dl_ig, sx, Hdl);
 #pragma unroll
   for (int k = 0; k < E; ++k) Hdl.x[k] /= sL;
-  // ---- velocity: closed-form factor (τ_j = 1/L + α² Σ_{k≥j} u_k², u = w/sqrt(M⁻¹))
+  // ---- velocity: closed-form factor (τ_j = 1/L + α² Σ_{k≥j} u_k², u = w/m_sqrt(M⁻¹))
   {
     WVec<E, R> u, zz;
     R tot_after = R(0);  // Σ over slots > k of u²
@@ -337,7 +356,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
-      u.x[k] = (i < d) ? dl_ig.x[k] * rsqrt(im.x[k]) : R(0);
+      u.x[k] = (i < d) ? dl_ig.x[k] * m_rsqrt(im.x[k]) : R(0);
       zz.x[k] = (i < d) ? z[(size_t)c * d + i] : R(0);
     }
 #pragma unroll
@@ -353,11 +372,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = lane + 32 * k;
-      const R tk = (i < d) ? u.x[k] * zz.x[k] * rsqrt(tau[k] * taun[k]) : R(0);
+      const R tk = (i < d) ? u.x[k] * zz.x[k] * m_rsqrt(tau[k] * taun[k]) : R(0);
       const R incl = warp_incl_scan(tk, lane);
       const R pre = pre_before + incl - tk;  // Σ_{j<i}
-      const R y = sqrt(taun[k] / tau[k]) * zz.x[k] - a2 * u.x[k] * pre;
-      v.x[k] = (i < d) ? sqrt(im.x[k]) * y : R(0);
+      const R y = m_sqrt(taun[k] / tau[k]) * zz.x[k] - a2 * u.x[k] * pre;
+      v.x[k] = (i < d) ? m_sqrt(im.x[k]) * y : R(0);
       pre_before += __shfl_sync(0xffffffffu, incl, 31);
       if (info.momentum && i < d) info.momentum[(size_t)c * d + i] = v.x[k];
     }
@@ -370,12 +389,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const R m = (im.x[k] > R(0)) ? R(1) / im.x[k] : R(0);
-      vmv = fma(m * v.x[k], v.x[k], vmv);
-      vg = fma(v.x[k], gn.x[k], vg);
+      vmv = m_fma(m * v.x[k], v.x[k], vmv);
+      vg = m_fma(v.x[k], gn.x[k], vg);
     }
     vmv = warp_sum(vmv);
     vg = warp_sum(vg);
-    return -0.5 * (log(double(Lc)) + slm) + 0.5 * double(vmv) +
+    return -0.5 * (m_log(double(Lc)) + slm) + 0.5 * double(vmv) +
            0.5 * double(Lc) * double(a2) * double(vg) * double(vg);
   };
   const double H0 = -ld0 + kinetic(L) - J0;
@@ -384,13 +403,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   for (int s = 0; s < sp.L; ++s) {  // lan_integrator.one_step
     w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
 #pragma unroll
-    for (int k = 0; k < E; ++k) q.x[k] = fma(eps, v.x[k], q.x[k]);
+    for (int k = 0; k < E; ++k) q.x[k] = m_fma(eps, v.x[k], q.x[k]);
     ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1);
     R Ls = R(0);
 #pragma unroll
-    for (int k = 0; k < E; ++k) Ls = fma(im.x[k] * g.x[k], g.x[k], Ls);
+    for (int k = 0; k < E; ++k) Ls = m_fma(im.x[k] * g.x[k], g.x[k], Ls);
     L = R(1) + a2 * warp_sum(Ls);
-    sL = sqrt(L);
+    sL = m_sqrt(L);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       gn.x[k] = g.x[k] / sL;
