@@ -81,7 +81,7 @@ struct Epi {
 // sigmoid is formed as 1 − the other, which in float32 loses the relative
 // accuracy of the small one (Λ = σ(a)σ(−a) at |a| = 7 would carry ~6e-5)
 struct Sig {
-  float sp, sm, softplus;
+  float sp, sm, e;  // e = e^{−|a|}
 };
 __device__ __forceinline__ Sig sig_pair(float a) {
   const float e = __expf(-fabsf(a));
@@ -89,8 +89,12 @@ __device__ __forceinline__ Sig sig_pair(float a) {
   Sig s;
   s.sp = a >= 0.f ? big : small;
   s.sm = a >= 0.f ? small : big;
-  s.softplus = fmaxf(a, 0.f) + log1pf(e);
+  s.e = e;
   return s;
+}
+// log(1 + e^a) from the pair's e (only where the log density is summed)
+__device__ __forceinline__ float sig_softplus(float a, const Sig& s) {
+  return fmaxf(a, 0.f) + log1pf(s.e);
 }
 
 __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
@@ -99,7 +103,7 @@ __device__ __forceinline__ void epi_apply(const Epi& e, int m, int n, float v) {
   } else if (e.mode == EPI_SIGMOID) {
     const Sig sg = sig_pair(v);
     const float yv = e.y[n];
-    if (e.ld_acc) atomicAdd(&e.ld_acc[m], double(yv * v - sg.softplus));
+    if (e.ld_acc) atomicAdd(&e.ld_acc[m], double(yv * v - sig_softplus(v, sg)));
     const float lam = sg.sp * sg.sm;
     split_store(e.lam, m, n, lam);
     if (e.lam_only) return;

@@ -230,7 +230,7 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
         lam[k] = sg.sp * sg.sm;
         lp[k] = lam[k] * (sg.sm - sg.sp);
         r1[k] = yv[k] * sg.sm - (1.f - yv[k]) * sg.sp;  // y − σ(a)
-        if (e.ld_acc && n + k < N) ld += double(yv[k] * a[k] - sg.softplus);
+        if (e.ld_acc && n + k < N) ld += double(yv[k] * a[k] - sig_softplus(a[k], sg));
       }
       if (m < M) {
         split8(e.lam, m, n, N, full, lam);

@@ -263,15 +263,16 @@ __device__ void w_half(R a2, WVec<E, R>& v, R* dJ, const WVec<E, R>& gn, const W
   const R det1 = R(1) + x1;
   *dJ -= x1 > -R(1) ? m_log1p(x1) : m_log(m_abs(det1));
   const R sL = m_sqrt(L);
+  const R isL = R(1) / sL;  // one division, then products
   // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
   R pd = R(0);
 #pragma unroll
-  for (int k = 0; k < E; ++k) pd = m_fma(-gn.x[k] + a2 * Hdl.x[k] / sL, dl_ig.x[k], pd);
+  for (int k = 0; k < E; ++k) pd = m_fma(-gn.x[k] + a2 * Hdl.x[k] * isL, dl_ig.x[k], pd);
   pd = warp_sum(pd);
   WVec<E, R> vt;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
-    const R dphi_ig = -dl_ig.x[k] + a2 * igH.x[k] / sL;
+    const R dphi_ig = -dl_ig.x[k] + a2 * igH.x[k] * isL;
     vt.x[k] = v.x[k] - R(0.5) * eps * sL * (dphi_ig - a2 * pd * dl_ig.x[k]);
   }
   R corr = R(0.5) * eps * wdot<E>(vt, hv) / det1;
@@ -341,6 +342,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   for (int k = 0; k < E; ++k) L = m_fma(im.x[k] * g.x[k], g.x[k], L);
   L = R(1) + a2 * warp_sum(L);
   R sL = m_sqrt(L);
+  R isL = R(1) / sL;
   {
     // Σx² at the current q for the HVPs (one extra gradient pass is avoided by
     // recomputing only the reduction)
@@ -350,12 +352,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   WVec<E, R> dl_ig;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
-    gn.x[k] = g.x[k] / sL;
+    gn.x[k] = g.x[k] * isL;
     dl_ig.x[k] = im.x[k] * gn.x[k];
   }
   w_hvp<E>(W, q, dl_ig, sx, Hdl);
 #pragma unroll
-  for (int k = 0; k < E; ++k) Hdl.x[k] /= sL;
+  for (int k = 0; k < E; ++k) Hdl.x[k] *= isL;
   // ---- velocity: closed-form factor (τ_j = 1/L + α² Σ_{k≥j} u_k², u = w/m_sqrt(M⁻¹))
   {
     WVec<E, R> u, zz;
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   }
   w_hvp<E>(W, q, v, sx, hv);
 #pragma unroll
-  for (int k = 0; k < E; ++k) hv.x[k] /= sL;
+  for (int k = 0; k < E; ++k) hv.x[k] *= isL;
   auto kinetic = [&](R Lc) -> double {  // lmcmonge/metrics.py:168-186
     R vmv = R(0), vg = R(0);
 #pragma unroll
@@ -418,22 +420,23 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     for (int k = 0; k < E; ++k) Ls = m_fma(im.x[k] * g.x[k], g.x[k], Ls);
     L = R(1) + a2 * warp_sum(Ls);
     sL = m_sqrt(L);
+    isL = R(1) / sL;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
-      gn.x[k] = g.x[k] / sL;
+      gn.x[k] = g.x[k] * isL;
       dl_ig.x[k] = im.x[k] * gn.x[k];
     }
     w_hvp<E>(W, q, v, sx, hv);
     w_hvp<E>(W, q, dl_ig, sx, Hdl);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
-      hv.x[k] /= sL;
-      Hdl.x[k] /= sL;
+      hv.x[k] *= isL;
+      Hdl.x[k] *= isL;
     }
     w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
     w_hvp<E>(W, q, v, sx, hv);
 #pragma unroll
-    for (int k = 0; k < E; ++k) hv.x[k] /= sL;
+    for (int k = 0; k < E; ++k) hv.x[k] *= isL;
   }
   const double J = J0 + double(dJ);
   const double H1 = -ld + kinetic(L) - J;

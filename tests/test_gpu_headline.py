@@ -165,3 +165,25 @@ def test_c4_largest_posterior_per_step():
         st, _ = kern(Draws(z, u), st0, dt, h, step)
         e = rel_err(_np(st.position)[S], traj[step - 1].position)
         assert e < 1e-5, f"step {step}: position error {e}"
+
+
+@pytest.mark.parametrize("N,d,path,bound", [
+    (1000, 25, "tcgen05", 3e-5), (1000, 25, "simt", 3e-5), (1000, 25, "cta", 1e-6),
+    (2000, 64, "cta", 1e-5)])
+def test_momentum_draw_accuracy_by_path(N, d, path, bound):
+    """The drawn momentum chol(G)·z against the oracle's, by implementation:
+    the batched paths carry their FP32 Gram's rounding through the factor
+    (≈ 1e-5 at d = 25, growing with d); the CTA form sums its Gram's 16-row
+    tiles in float64 (≈ 3e-7 at d = 25, 2e-6 at d = 64)."""
+    import geomjax_gb300 as gj
+    from geomjax_gb300.base import Draws
+
+    ot, dt = _targets(N=N, d=d)
+    Cb = 64
+    S = np.arange(0, Cb, 8)
+    q0 = _f32(laplace_draws(ot, Cb, seed=1))
+    z = _f32(np.random.default_rng(2).standard_normal((Cb, d)))
+    kern = gj.rmhmc.build_kernel(logreg_path=path, integrator=GL, loop="host")
+    _, info = kern(Draws(z, -np.ones(Cb)), gj.rmhmc.init(q0, dt), dt, 0.05, 1)
+    ref = O_rm.momentum_from_normals(ot, q0[S], z[S])
+    assert rel_err(_np(info.momentum)[S], ref) < bound
