@@ -17,6 +17,8 @@
 // transition's increments are summed in FP32), the log density at the
 // proposal and the Hamiltonian difference; nothing in its step loop runs on
 // the FP64 pipe.  The plain form (R = double) is the same code in float64.
+#include <cmath>
+
 #include "chain_kernels.cuh"
 
 namespace gj {
@@ -87,28 +89,46 @@ struct WarpTarget {
   double ld_const;          // the log density's constant terms
 };
 
+// The target's scale constants, computed once on the host: an FP64 division
+// or logarithm costs every warp tens of FP64-pipe instructions (1/64 of the
+// FP32 rate on GB300), which a transition of 16 steps cannot amortise.
+struct WarpConst {
+  double inv_a2d, inv_b2d;  // funnel: 1/σ²; hier: 1/σ_μ², 1/σ_v²
+  double ld_const;          // the log density's constant terms but the hier σ_j sum
+};
+
+inline WarpConst warp_const_host(const TargetDev& t) {
+  WarpConst k;
+  if (t.family == GJ_FUNNEL) {
+    k.inv_a2d = 1.0 / (t.p0 * t.p0);
+    k.inv_b2d = 0.0;
+    k.ld_const = -std::log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
+  } else {
+    const int J = t.n;
+    k.inv_a2d = 1.0 / (t.p0 * t.p0);
+    k.inv_b2d = 1.0 / (t.p1 * t.p1);
+    // J · (−½ log 2π) from the data terms and as many from the latent terms
+    k.ld_const = -J * kLog2Pi - std::log(t.p0) - 0.5 * kLog2Pi - std::log(t.p1) - 0.5 * kLog2Pi;
+  }
+  return k;
+}
+
 template <typename R>
-__device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, int lane) {
+__device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, const WarpConst& k, int lane) {
   WarpTarget<R> W;
   W.t = t;
   W.lane = lane;
-  if (t.family == GJ_FUNNEL) {
-    W.inv_a2d = 1.0 / (t.p0 * t.p0);
-    W.inv_b2d = 0.0;
-    W.inv_a2 = R(W.inv_a2d);
-    W.inv_b2 = R(0);
-    W.ld_const = -m_log(t.p0) - 0.5 * kLog2Pi - (t.d - 1) * 0.5 * kLog2Pi;
-  } else {
+  W.inv_a2d = k.inv_a2d;
+  W.inv_b2d = k.inv_b2d;
+  W.inv_a2 = R(k.inv_a2d);
+  W.inv_b2 = R(k.inv_b2d);
+  W.ld_const = k.ld_const;
+  if (t.family != GJ_FUNNEL) {  // hier: −Σ_j log σ_j (the data's scales, on the device)
     const int J = t.n;
     const R* sg = static_cast<const R*>(t.s);
     double c = 0.0;
-    for (int i = lane; i < J; i += 32) c += -m_log(double(sg[i])) - 0.5 * kLog2Pi;
-    c = warp_sum(c);
-    W.inv_a2d = 1.0 / (t.p0 * t.p0);
-    W.inv_b2d = 1.0 / (t.p1 * t.p1);
-    W.inv_a2 = R(W.inv_a2d);
-    W.inv_b2 = R(W.inv_b2d);
-    W.ld_const = c - J * 0.5 * kLog2Pi - m_log(t.p0) - 0.5 * kLog2Pi - m_log(t.p1) - 0.5 * kLog2Pi;
+    for (int i = lane; i < J; i += 32) c += -m_log(double(sg[i]));
+    W.ld_const += warp_sum(c);
   }
   return W;
 }
@@ -309,7 +329,7 @@ __device__ __forceinline__ R warp_incl_rscan(R x, int lane) {
 // it better than 16 (D = 100 ran 0.28 ms per transition at 80 registers,
 // 0.36 ms at the 120 the compiler picks unbounded)
 template <int E, typename R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel(TargetDev t, StepDev sp, R* pos,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel(TargetDev t, WarpConst wc, StepDev sp, R* pos,
                                                          R* grad, double* logdens, double* vol,
                                                          const R* z, const double* uacc,
                                                          InfoDev<R> info, int C) {
@@ -317,7 +337,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= C) return;  // whole warp exits together
   const int d = t.d;
-  const WarpTarget<R> W = make_warp_target<R>(t, lane);
+  const WarpTarget<R> W = make_warp_target<R>(t, wc, lane);
   const R a2 = R(sp.alpha2);
   const R eps = R(sp.h);
   const R* imv = static_cast<const R*>(sp.inv_mass);
@@ -404,7 +424,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     }
     vmv = warp_sum(vmv);
     vg = warp_sum(vg);
-    return -0.5 * (m_log(double(Lc)) + slm) + 0.5 * double(vmv) +
+    // log L in float32: L is a float32 value, so a float64 logarithm adds
+    // no accuracy (and costs tens of FP64-pipe instructions)
+    return -0.5 * (double(m_log(Lc)) + slm) + 0.5 * double(vmv) +
            0.5 * double(Lc) * double(a2) * double(vg) * double(vg);
   };
   const double H0 = -ld0 + kinetic(L) - J0;
@@ -487,14 +509,15 @@ cudaError_t launch_monge_warp(const TargetDev& t, const StepDev& sp, R* pos, R* 
                               int C, cudaStream_t st) {
   const int tpb = 256;
   const dim3 grid((unsigned)(((size_t)C * 32 + tpb - 1) / tpb));
+  const WarpConst wc = warp_const_host(t);
   if (t.d <= 32)
-    monge_warp_kernel<1, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<1, R><<<grid, tpb, 0, st>>>(t, wc, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 64)
-    monge_warp_kernel<2, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<2, R><<<grid, tpb, 0, st>>>(t, wc, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 128)
-    monge_warp_kernel<4, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<4, R><<<grid, tpb, 0, st>>>(t, wc, sp, pos, grad, ld, vol, z, u, info, C);
   else if (t.d <= 256)
-    monge_warp_kernel<8, R><<<grid, tpb, 0, st>>>(t, sp, pos, grad, ld, vol, z, u, info, C);
+    monge_warp_kernel<8, R><<<grid, tpb, 0, st>>>(t, wc, sp, pos, grad, ld, vol, z, u, info, C);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
