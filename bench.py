@@ -205,7 +205,8 @@ def run_ours(args, wl):
                                      integrator=args.integrator, cholesky=args.cholesky,
                                      chol_chains_per_warp=args.chol_cpw,
                                      chain_groups=args.groups, pdl=args.pdl,
-                                     gemm_ksplit=args.gemm_ksplit)
+                                     gemm_ksplit=args.gemm_ksplit,
+                                     fuse_r2x=not args.no_fuse_r2x)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -371,6 +372,7 @@ def run_ours(args, wl):
                    "cholesky": args.cholesky, "chol_chains_per_warp": args.chol_cpw or "auto",
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
                    "gemm_ksplit": args.gemm_ksplit or "auto",
+                   "fuse_r2x": not args.no_fuse_r2x,
                    "gemm_accumulators": args.gemm_accumulators,
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
@@ -1101,6 +1103,9 @@ def main():
                     help="most K-range TMEM accumulators per tcgen05 GEMM CTA")
     ap.add_argument("--gemm-ksplit", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="K slices of the gradient contraction (0 = automatic)")
+    ap.add_argument("--no-fuse-r2x", action="store_true",
+                    help="store r2 and contract it by its own GEMM in the momentum evaluations "
+                         "(default: r2·X inside the S GEMM's epilogue)")
     ap.add_argument("--pdl", action="store_true",
                     help="launch the batched pipeline's kernels with programmatic dependent launch")
     ap.add_argument("--groups", type=int, default=0,

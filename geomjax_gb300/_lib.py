@@ -26,6 +26,7 @@ GJ_OPT_CHOL_CHAINS_PER_WARP, GJ_OPT_CHAIN_GROUPS, GJ_OPT_PDL = 5, 6, 7
 GJ_OPT_GEMM_KSPLIT = 8
 GJ_OPT_BATCH_GRAPH = 9
 GJ_OPT_MONGE_WARP = 10
+GJ_OPT_FUSE_R2X = 11
 
 
 class GjTarget(ctypes.Structure):

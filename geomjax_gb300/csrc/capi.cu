@@ -95,6 +95,7 @@ struct gj_ctx {
   int pdl;        // GJ_OPT_PDL
   int ksplit;     // GJ_OPT_GEMM_KSPLIT (0 = automatic)
   int monge_warp; // GJ_OPT_MONGE_WARP
+  int fuse_r2x;   // GJ_OPT_FUSE_R2X
   // batched dense-Fisher path: one context per chain group; in graph mode
   // the groups' transitions run on their own streams, forked from and joined
   // to the caller's stream by events, so one group's factorisation can share
@@ -162,6 +163,7 @@ int ensure_groups(gj_ctx* ctx, const gj::TargetDev& t) {
     gj::logreg_batched_set_chol_cpw(lb, ctx->chol_cpw);
     gj::logreg_batched_set_pdl(lb, ctx->pdl);
     gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
+    gj::logreg_batched_set_fuse_r2x(lb, ctx->fuse_r2x);
     // every group makes the automatic choices of the whole context, so that
     // results do not depend on the group count
     gj::logreg_batched_set_auto_chains(lb, ctx->C);
@@ -221,6 +223,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->pdl = 0;
   c->ksplit = 0;
   c->monge_warp = 1;
+  c->fuse_r2x = 1;
   *out = c;
   return GJ_OK;
 }
@@ -267,6 +270,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     if (value < 0 || value > 4) return fail(GJ_EINVAL, "K slices must be 0 (automatic) .. 4");
     ctx->ksplit = (int)value;
     for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_FUSE_R2X) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "fused r2·X flag must be 0 or 1");
+    ctx->fuse_r2x = (int)value;
+    for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_fuse_r2x(lb, ctx->fuse_r2x);
     return GJ_OK;
   }
   if (key == GJ_OPT_MONGE_WARP) {
@@ -825,6 +834,11 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
   if (key == GJ_OPT_GEMM_KSPLIT) {
     if (value < 0 || value > 4) return fail(GJ_EINVAL, "K slices must be 0 (automatic) .. 4");
     for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_gemm_ksplit(lb, (int)value);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_FUSE_R2X) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "fused r2·X flag must be 0 or 1");
+    for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_fuse_r2x(lb, (int)value);
     return GJ_OK;
   }
   if (key == GJ_OPT_BATCH_GRAPH) {

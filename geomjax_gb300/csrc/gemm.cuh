@@ -15,7 +15,7 @@ namespace gj {
 
 using bf16 = __nv_bfloat16;
 
-enum EpiMode : int { EPI_STORE = 0, EPI_SIGMOID = 1, EPI_TRACE = 2, EPI_R2W = 3 };
+enum EpiMode : int { EPI_STORE = 0, EPI_SIGMOID = 1, EPI_TRACE = 2, EPI_R2W = 3, EPI_R2G = 4 };
 
 // A split BF16 matrix, `rows` x `kdim`, as `planes` BF16 planes whose sum is
 // the value: x0 = bf16(x), x1 = bf16(x − x0) and, with three planes,
@@ -42,6 +42,8 @@ __device__ __forceinline__ void split_store(const SplitMat& s, int r, int k, flo
   if (s.planes == 3)
     s.p[(size_t)(2 * s.rpad + r) * s.ld + k] = __float2bfloat16_rn(r0 - __bfloat162float(b1));
 }
+
+struct TcOperand;
 
 struct Epi {
   int mode;
@@ -75,6 +77,20 @@ struct Epi {
   // w read from W[m, n] (stride s_ld): the momentum-only re-evaluation of
   // the generalized leapfrog, where w = x_nᵀG⁻¹x_n is fixed
   const float* W;
+  // EPI_R2G (tcgen05 path only; three planes, 128-wide tiles, K <= 64):
+  // EPI_R2W's r2, split into three BF16 planes in shared memory and
+  // contracted with Xᵀ (the operand xt: x_d <= 32 rows, the observations
+  // along K, plane pitch xt_rpad) by a second tcgen05 MMA in the same CTA
+  // instead of being stored: the CTA of N tile t writes
+  // g2[t·g2_slice + m·g2_ld + k] = Σ_{n in tile t} r2[m, n]·X[n, k] for
+  // k < x_d (rounded up to a multiple of 4; 16-byte aligned rows); the
+  // consumer adds the ⌈N / 128⌉ tile partials in tile order
+  const TcOperand* xt;
+  int xt_rpad;
+  int x_d;
+  float* g2;
+  int g2_ld;
+  size_t g2_slice;
 };
 
 // σ(a), σ(−a) and log(1 + e^a) from one exponential, e = e^{−|a|}: neither
@@ -197,6 +213,9 @@ int gemm_tc_tuning_code();
 void gemm_tc_set_accumulators(int max_ranges);
 cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err_flag,
                     cudaStream_t st);
+// the output tile width (32, 64 or 128) a launch with these planes, N and K
+// takes under the current tile policy
+int gemm_tc_bn(int planes, int N, int K);
 
 // noalloc.cu: the same contraction with the split planes in a static device
 // array (no cudaMalloc / cudaFree); capacity in BF16 elements.

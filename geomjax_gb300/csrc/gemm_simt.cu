@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(GemmArgs g) {
 
 cudaError_t gemm_simt(const GemmArgs& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return cudaSuccess;
-  if (g.ksplit != 1 || g.a_row0 != 0) return cudaErrorInvalidValue;  // tcgen05 path only
+  // tcgen05 path only: K slices, A row offsets, the fused r2·X epilogue
+  if (g.ksplit != 1 || g.a_row0 != 0 || g.epi.mode == EPI_R2G) return cudaErrorInvalidValue;
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM);
   gemm_simt_kernel<<<grid, 256, 0, st>>>(g);
   return cudaGetLastError();

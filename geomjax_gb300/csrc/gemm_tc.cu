@@ -268,15 +268,172 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
   __syncwarp();  // the tile is reused by the warp's next chunk
 }
 
+// One 32-column chunk of the accumulator for this warp's lane quarter (lane
+// l = row 32·q + l), the NACC K-range partial tiles added in order.
+__device__ __forceinline__ void load_acc(uint32_t tmem, int q, int c0, int nacc, int tmem_cols,
+                                         float (&v)[32]) {
+  const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+  {
+    uint32_t r[32];
+    tmem_ld32(ta, r);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+  }
+  // the other K ranges' partial tiles, added in order (round to nearest)
+#pragma unroll 1
+  for (int acc = 1; acc < nacc; ++acc) {
+    uint32_t r[32];
+    tmem_ld32(ta + (uint32_t)(acc * tmem_cols), r);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
+  }
+}
+
+// EPI_R2G layout in the operand ring, free once the S accumulator is
+// complete: the r2 tile of one 64-wide K half as three BF16 planes
+// (128 rows x 64, 16 KB each, 128B-swizzled K-major like a TMA-loaded A
+// box), then the six Xᵀ boxes (two K halves x three planes, 32 rows x 64).
+constexpr int R2G_A_BYTES = 3 * A_TILE_BYTES;
+constexpr int R2G_XT_BOX = 32 * BK * 2;
+constexpr int R2G_SMEM = R2G_A_BYTES + 6 * R2G_XT_BOX;
+constexpr uint32_t R2G_TMEM_COL = 128;  // the gradient accumulator's columns
+constexpr uint32_t R2G_TMEM_ALLOC = 256;
+constexpr uint32_t R2G_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) |
+                               ((uint32_t)(BM >> 4) << 24);  // M = 128, N = 32
+
+// EPI_R2G, one epilogue warp (see Epi; BN = 128, 3 planes, one K block).
+// For each 64-wide K half of the tile: lane l (tile row 32·q + l) forms
+// r2 = Λ'(w − s²) over this warp's 32 columns of that half, splits it into
+// three BF16 planes and stores them swizzled into the A tile; after a
+// named barrier of the 256 epilogue threads one thread issues the plane
+// products r2_i · Xᵀ_j (i + j <= 2) as tcgen05 MMAs, M = 128, N = 32,
+// K = 64, into the TMEM columns after S's.  The second half waits for the
+// first half's MMAs before overwriting the A tile.  Every epilogue thread
+// reaches both barriers and all waits whatever the outcome of its own
+// waits, and every wait is bounded.
+__device__ __forceinline__ void epi_r2g(const Epi& e, unsigned char* base, uint64_t* xfull,
+                                        uint64_t* gdone, uint32_t tmem, int warp, int lane,
+                                        bool ok, int m0, int n0, int M, int N, int* err) {
+  const int q = warp & 3, half = (warp - 2) >> 2;
+  const int row = q * 32 + lane;  // tile row of this lane
+  const int m = m0 + row;
+  unsigned char* At = base;
+  const uint32_t a_s = smem_u32(At), x_s = smem_u32(base + R2G_A_BYTES);
+#pragma unroll 1
+  for (int kh = 0; kh < 2; ++kh) {
+    const int c0 = 64 * kh + 32 * half;  // this warp's 32 columns
+    if (kh == 1 && !mbar_wait(gdone, 0) && lane == 0) atomicExch(err, 5);
+    float r2[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r2[j] = 0.f;
+    if (ok && n0 + c0 < N) {  // warp-uniform
+      float sv[32];
+      {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sv[j] = __uint_as_float(r[j]);
+      }
+      if (m < M) {
+        const int n = n0 + c0;
+        const bool full = n + 32 <= N;
+#pragma unroll
+        for (int j8 = 0; j8 < 4; ++j8) {
+          float wv[8], lv[8];
+          const int nj = n + 8 * j8;
+          load8(e.W + (size_t)m * e.s_ld + nj, nj, N, full && aligned16(e.W, e.s_ld), wv);
+          load8(e.lp + (size_t)m * e.lp_ld + nj, nj, N, full && aligned16(e.lp, e.lp_ld), lv);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const float s = sv[8 * j8 + k];
+            r2[8 * j8 + k] = lv[k] * (wv[k] - s * s);
+          }
+        }
+      }
+    }
+    // three planes, one 16-byte chunk (8 columns) per plane and store; the
+    // 128B swizzle puts chunk c of row r at chunk c ^ (r mod 8)
+#pragma unroll
+    for (int j8 = 0; j8 < 4; ++j8) {
+      uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const float xa = r2[8 * j8 + 2 * t], xb = r2[8 * j8 + 2 * t + 1];
+        const __nv_bfloat162 h = __floats2bfloat162_rn(xa, xb);
+        const float2 hf = __bfloat1622float2(h);
+        const float ra = xa - hf.x, rb = xb - hf.y;
+        const __nv_bfloat162 md = __floats2bfloat162_rn(ra, rb);
+        const float2 mf = __bfloat1622float2(md);
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(ra - mf.x, rb - mf.y);
+        w0[t] = *reinterpret_cast<const uint32_t*>(&h);
+        w1[t] = *reinterpret_cast<const uint32_t*>(&md);
+        w2[t] = *reinterpret_cast<const uint32_t*>(&lo);
+      }
+      const int chunk = (4 * half + j8) ^ (row & 7);
+      unsigned char* p = At + row * 128 + chunk * 16;
+      *reinterpret_cast<uint4*>(p) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+      *reinterpret_cast<uint4*>(p + A_TILE_BYTES) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+      *reinterpret_cast<uint4*>(p + 2 * A_TILE_BYTES) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+    }
+    // the tensor core reads shared memory through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+    if (warp == 2 && lane == 0) {
+      bool go = ok;
+      if (kh == 0 && !mbar_wait(xfull, 0)) {
+        atomicExch(err, 6);
+        go = false;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (go) {
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          const uint64_t adv = (uint64_t)((k * 32) >> 4);
+          uint64_t da[3], db[3];
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            da[p] = make_desc(a_s + p * A_TILE_BYTES) + adv;
+            db[p] = make_desc(x_s + (kh * 3 + p) * R2G_XT_BOX) + adv;
+          }
+          const uint32_t acc_t = tmem + R2G_TMEM_COL;
+          mma_bf16(acc_t, da[0], db[0], R2G_IDESC, (kh > 0 || k > 0) ? 1u : 0u);
+          mma_bf16(acc_t, da[0], db[1], R2G_IDESC, 1u);
+          mma_bf16(acc_t, da[1], db[0], R2G_IDESC, 1u);
+          mma_bf16(acc_t, da[0], db[2], R2G_IDESC, 1u);
+          mma_bf16(acc_t, da[1], db[1], R2G_IDESC, 1u);
+          mma_bf16(acc_t, da[2], db[0], R2G_IDESC, 1u);
+        }
+      }
+      mma_commit(gdone);  // arrives also when nothing was issued
+    }
+    __syncwarp();
+  }
+  const bool done = __all_sync(0xffffffffu, mbar_wait(gdone, 1));
+  if (!done && lane == 0) atomicExch(err, 7);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  uint32_t r[32];
+  tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + R2G_TMEM_COL, r);
+  if (ok && done && m < M) {  // the row's partial gradient for this N tile
+    float* out = e.g2 + (size_t)blockIdx.x * e.g2_slice + (size_t)m * e.g2_ld;
+    const int k4n = (e.x_d + 3) >> 2;
+#pragma unroll
+    for (int k4 = 0; k4 < 8; ++k4)
+      if (k4 < k4n)
+        reinterpret_cast<float4*>(out)[k4] =
+            make_float4(__uint_as_float(r[4 * k4]), __uint_as_float(r[4 * k4 + 1]),
+                        __uint_as_float(r[4 * k4 + 2]), __uint_as_float(r[4 * k4 + 3]));
+  }
+}
+
 // STAGES (run time, 1 .. Cfg::MAX_STAGES) is the depth of the operand ring,
 // chosen by the host so that two CTAs share an SM where that fits.
 // NACC (run time, 1, 2 or 4) accumulators over contiguous K ranges; the
 // host keeps NACC·TMEM_COLS·(CTAs per SM) within the SM's 512 columns.
-template <int NPL, int BN>
+template <int NPL, int BN, bool R2G = false>  // R2G: the EPI_R2G epilogue
 __global__ void __launch_bounds__(320, 2)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                   int rpadA, int rpadB, int M, int N, int K, Epi epi, int* err, int STAGES,
-                   int a_row0, int NACC) {
+                   const __grid_constant__ CUtensorMap mapXT, int rpadA, int rpadB, int M, int N,
+                   int K, Epi epi, int* err, int STAGES, int a_row0, int NACC) {
   using C = Cfg<NPL, BN>;
   constexpr int STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
@@ -287,7 +444,9 @@ __global__ void __launch_bounds__(320, 2)
   uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* xfull = accum + 1;  // EPI_R2G: the Xᵀ boxes have landed
+  uint64_t* gdone = accum + 2;  // EPI_R2G: a K half's gradient MMAs are complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 3);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -306,9 +465,12 @@ __global__ void __launch_bounds__(320, 2)
       mbar_init(&empty[s], 1);
     }
     mbar_init(accum, 1);
+    mbar_init(xfull, 1);
+    mbar_init(gdone, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  const uint32_t tmem_cols = (uint32_t)(TMEM_COLS * NACC);
+  // EPI_R2G adds 32 gradient columns after S's 128 (one accumulator)
+  const uint32_t tmem_cols = R2G ? R2G_TMEM_ALLOC : (uint32_t)(TMEM_COLS * NACC);
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
@@ -341,6 +503,18 @@ __global__ void __launch_bounds__(320, 2)
           tma_load_2d(st + q * A_TILE_BYTES, &mapA, &full[s], x, q * rpadA + a_row0 + m0);
           tma_load_2d(st + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES, &mapB, &full[s], x,
                       q * rpadB + n0);
+        }
+      }
+      if constexpr (R2G) {  // the Xᵀ boxes of the tile's two K halves, into
+        // the ring once the S accumulator (its last reader) is complete
+        if (mbar_wait(accum, 0)) {
+          mbar_expect_tx(xfull, 6 * R2G_XT_BOX);
+          for (int kh = 0; kh < 2; ++kh)
+            for (int q = 0; q < 3; ++q)
+              tma_load_2d(base + R2G_A_BYTES + (kh * 3 + q) * R2G_XT_BOX, &mapXT, xfull,
+                          n0 + 64 * kh, q * epi.xt_rpad);
+        } else {
+          atomicExch(err, 4);
         }
       }
     }
@@ -394,29 +568,17 @@ __global__ void __launch_bounds__(320, 2)
     const bool ok = __all_sync(0xffffffffu, mbar_wait(accum, 0));
     if (!ok && lane == 0) atomicExch(err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && KB > 0) {
+    if constexpr (R2G) {  // the host keeps K in one unsplit block (KB = 1)
+      epi_r2g(epi, base, xfull, gdone, tmem, warp, lane, ok && KB > 0, m0, n0, M, N, err);
+    } else if (ok && KB > 0) {
       // the operand ring is free once the accumulator is complete: each
       // epilogue warp stages its chunks in its own 32 x 33 float tile
       float* stg = reinterpret_cast<float*>(base) + (warp - 2) * (32 * 33);
 #pragma unroll 1
       for (int c0 = 32 * half; c0 < BN; c0 += 64) {
         if (n0 + c0 >= N) break;  // warp-uniform
-        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         float v[32];
-        {
-          uint32_t r[32];
-          tmem_ld32(ta, r);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-        }
-        // the other K ranges' partial tiles, added in order (round to nearest)
-#pragma unroll 1
-        for (int acc = 1; acc < nacc; ++acc) {
-          uint32_t r[32];
-          tmem_ld32(ta + (uint32_t)(acc * TMEM_COLS), r);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
-        }
+        load_acc(tmem, q, c0, nacc, TMEM_COLS, v);
         epi_chunk(epi, stg, lane, m0 + q * 32, n0 + c0, M, N, v);
       }
     }
@@ -491,8 +653,13 @@ namespace {
 
 template <int NPL, int BN>
 cudaError_t set_smem_limit() {
-  return cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<NPL, BN>::smem(Cfg<NPL, BN>::MAX_STAGES));
+  const int bytes = Cfg<NPL, BN>::smem(Cfg<NPL, BN>::MAX_STAGES);
+  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if constexpr (NPL == 3 && BN == 128)  // the fused r2·X form (launched with these only)
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
 }
 
 }  // namespace
@@ -549,21 +716,44 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   int nacc = 1;
   while (nacc < g_tune.max_nacc && 2 * nacc * 2 <= kb_cta && 2 * nacc * C::TMEM_COLS * ctas <= 512)
     nacc *= 2;
-  return launch_k(g.pdl, gemm_tc_kernel<NPL, BN>, grid, dim3(320), (size_t)C::smem(ns), st, a->map,
-                  mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0, nacc);
+  if (g.epi.mode == EPI_R2G) {
+    // three planes, 128-wide tiles, one K block (one accumulator) and a
+    // ring that holds the r2 tile and the Xᵀ boxes
+    if constexpr (NPL == 3 && BN == 128) {
+      const TcOperand* xt = g.epi.xt;
+      if (kb != 1 || ns * C::STAGE_BYTES < R2G_SMEM || !xt || xt->s.planes != 3 ||
+          xt->s.rows > 32 || g.epi.xt_rpad != xt->s.rpad)
+        return cudaErrorInvalidValue;
+      return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, true>, grid, dim3(320), (size_t)C::smem(ns),
+                      st, a->map, mb, xt->map32, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err,
+                      ns, g.a_row0, 1);
+    }
+    return cudaErrorInvalidValue;
+  }
+  return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, false>, grid, dim3(320), (size_t)C::smem(ns), st,
+                  a->map, mb, mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0,
+                  nacc);
+}
+
+int tile_bn(int planes, int N, int K) {
+  if (N <= 32) return 32;
+  const int kb = (K + BK - 1) / BK;
+  const bool narrow = g_tune.bn_wide == 0 ? (planes == 2 && kb <= 8) : g_tune.bn_wide == 64;
+  return (N <= 64 || narrow) ? 64 : 128;
 }
 
 template <int NPL>
 cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
                              cudaStream_t st) {
-  if (g.N <= 32) return launch_tc<NPL, 32>(g, a, b, err, st);
-  const int kb = (g.K + BK - 1) / BK;
-  const bool narrow = g_tune.bn_wide == 0 ? (NPL == 2 && kb <= 8) : g_tune.bn_wide == 64;
-  if (g.N <= 64 || narrow) return launch_tc<NPL, 64>(g, a, b, err, st);
+  const int bn = tile_bn(NPL, g.N, g.K);
+  if (bn == 32) return launch_tc<NPL, 32>(g, a, b, err, st);
+  if (bn == 64) return launch_tc<NPL, 64>(g, a, b, err, st);
   return launch_tc<NPL, 128>(g, a, b, err, st);
 }
 
 }  // namespace
+
+int gemm_tc_bn(int planes, int N, int K) { return tile_bn(planes, N, K); }
 
 int gemm_tc_tuning_code() {
   return (g_tune.bn_wide / 64) * 3 + (g_tune.two_ctas + 1) + 16 * g_tune.max_nacc;
@@ -587,6 +777,11 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
     return cudaErrorInvalidValue;
   if (g.ksplit != 1 && (g.epi.mode != EPI_STORE || !gemm_ksplit_valid(g.K, g.ksplit) ||
                         (g.epi.d_slice & 3)))
+    return cudaErrorInvalidValue;
+  if (g.epi.mode == EPI_R2G &&
+      (g.epi.x_d < 1 || g.epi.x_d > 32 || g.epi.g2_ld < 4 * ((g.epi.x_d + 3) / 4) ||
+       (g.epi.g2_ld & 3) || (g.epi.g2_slice & 3) || !g.epi.g2 ||
+       (reinterpret_cast<uintptr_t>(g.epi.g2) & 15) || g.ksplit != 1 || g.a_row0 != 0))
     return cudaErrorInvalidValue;
   return a->s.planes == 3 ? launch_tc_planes<3>(g, a, b, err, st)
                           : launch_tc_planes<2>(g, a, b, err, st);

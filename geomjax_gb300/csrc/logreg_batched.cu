@@ -568,6 +568,12 @@ struct UpdArgs {
   int ldo;
   int gs;          // K slices of the gradient contraction (summed here)
   size_t gstride;  // elements between slices
+  // when set (the momentum updates of the generalized leapfrog after fused
+  // evaluations): the r₂·X rows come from these g2s N-tile partials,
+  // [tile][C][ldo], g2stride elements apart, instead of Gout's rows [C, 2C)
+  const float* G2;
+  int g2s;
+  size_t g2stride;
   const double* u;
   const double* u0;           // generalized leapfrog: G(q0)⁻¹p½
   double *q0, *p0, *qc, *pc;  // FP64 fixed-point iterates
@@ -832,7 +838,8 @@ __global__ void __launch_bounds__(32 * kSolveWarps) glp_update_solve_kernel(UpdA
         const double g = double(slice_sum(a.Gout, (size_t)c * a.ldo + i, a.gs, a.gstride)) -
                          a.qc[o] * a.prior_inv;
         const double dK =
-            0.5 * double(slice_sum(a.Gout, (size_t)(a.C + c) * a.ldo + i, a.gs, a.gstride));
+            0.5 * double(a.G2 ? slice_sum(a.G2, (size_t)c * a.ldo + i, a.g2s, a.g2stride)
+                              : slice_sum(a.Gout, (size_t)(a.C + c) * a.ldo + i, a.gs, a.gstride));
         const double pn = a.p0[o] - hh * (dK - g);
         const double e = pn - a.pc[o];
         nan |= isnan(e);
@@ -973,6 +980,12 @@ struct LogregBatched {
   // w = x_nᵀG⁻¹x_n at the step's start position, and G(q0)⁻¹p½
   double *Lf, *u0;
   float *W, *Lf32;
+  // the momentum evaluations' fused r₂·X partials, [tile][C][dpad] for up
+  // to g2_tiles N tiles (allocated with the other generalized-leapfrog
+  // buffers)
+  float* G2;
+  int g2_tiles;
+  int fuse_r2x;  // logreg_batched_set_fuse_r2x
   int *iters, *iters_total, *n_active_d;
   int* n_active_h;  // pinned
   uint8_t *active, *notconv, *bad;
@@ -1020,6 +1033,7 @@ void logreg_batched_set_chol_fp64(LogregBatched* lb, int on) { lb->chol_fp64 = o
 void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw) { lb->chol_cpw = cpw; }
 void logreg_batched_set_pdl(LogregBatched* lb, int on) { lb->pdl = on; }
 void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k) { lb->gsplit_req = k; }
+void logreg_batched_set_fuse_r2x(LogregBatched* lb, int on) { lb->fuse_r2x = on ? 1 : 0; }
 void logreg_batched_set_auto_chains(LogregBatched* lb, int C) { lb->auto_C = C > 0 ? C : lb->C; }
 
 // K slices of the gradient contractions [r₁; r₂]·X (M = 2C) and r₂·X
@@ -1088,6 +1102,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->chol_cpw = 0;
   lb->pdl = 0;
   lb->gsplit_req = 0;
+  lb->fuse_r2x = 1;
   lb->auto_C = C;
   lb->sms = 0;
   {
@@ -1443,9 +1458,36 @@ struct Runner {
     solve(lb->pc, nullptr, true, false, true);
     p_contract();
   }
+  // the fused form: r₂·X in the S GEMM's epilogue, one partial per N tile
+  int g2_tiles_used() const {
+    const int bn = gemm_tc_bn(3, lb->N, lb->d);
+    return (lb->N + bn - 1) / bn;
+  }
+  bool fused_r2x() const {
+    return impl == 2 && lb->fuse_r2x && lb->d <= 32 && lb->G2 && lb->tXTb &&
+           gemm_tc_bn(3, lb->N, lb->d) == 128 && g2_tiles_used() <= lb->g2_tiles;
+  }
   // s = x_nᵀu and r₂ = Λ'(w − s²) from the split u, then r₂·X
   void p_contract() {
     LogregBatched& L = *lb;
+    if (fused_r2x()) {
+      Epi f{};
+      f.mode = EPI_R2G;
+      f.W = L.W;
+      f.s_ld = L.Npad;
+      f.lp = L.Lp;
+      f.lp_ld = L.Npad;
+      f.xt = L.tXTb;
+      f.xt_rpad = L.XTb.rpad;
+      f.x_d = L.d;
+      f.g2 = L.G2;
+      f.g2_ld = L.dpad;
+      f.g2_slice = (size_t)L.C * L.dpad;
+      gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, f);
+      L.stats.gemm_flops += 2.0 * L.C * L.N * L.d;  // the in-kernel r₂·X MMAs
+      L.stats.evals++;
+      return;
+    }
     Epi s{};
     s.mode = EPI_R2W;
     s.W = L.W;
@@ -1515,6 +1557,11 @@ struct Runner {
     a.ldo = L.dpad;
     a.gs = gsplit();
     a.gstride = gstride();
+    if ((mode == UP_GLP0 || mode == UP_GLPN) && fused_r2x()) {
+      a.G2 = L.G2;
+      a.g2s = g2_tiles_used();
+      a.g2stride = (size_t)L.C * L.dpad;
+    }
     a.u = L.u;
     a.u0 = L.u0;
     a.q0 = L.q0;
@@ -1556,6 +1603,10 @@ static int ensure_gl(LogregBatched* lb) {
   lb->u0 = dalloc<double>((size_t)lb->C * lb->d, lb->owned, &ok);
   lb->W = dalloc<float>((size_t)lb->C * lb->Npad, lb->owned, &ok);
   lb->Lf32 = dalloc<float>((size_t)lb->C * lb->P, lb->owned, &ok);
+  // the fused r₂·X partials: one per N tile, whose width is at least 64
+  // for N > 64 (one tile for N <= 64)
+  lb->g2_tiles = lb->N <= 64 ? 1 : (lb->N + 63) / 64;
+  lb->G2 = dalloc<float>((size_t)lb->g2_tiles * lb->C * lb->dpad, lb->owned, &ok);
   if (!ok) {
     g_err = "device allocation failed for the generalized leapfrog's buffers";
     return GJ_ENOMEM;
@@ -1701,9 +1752,15 @@ int graph_fail(const char* what, cudaError_t e) {
 
 constexpr size_t kMaxGraphs = 64;
 
+// every setting a captured transition depends on, in mixed radix (each
+// field below its radix: chol_cpw <= 8, tuning code < 128, K slices <= 4)
 int graph_cfg(const LogregBatched* lb) {
-  return lb->chol_fp64 * 16 + lb->chol_cpw + 256 * lb->pdl + 512 * gemm_tc_tuning_code() +
-         8192 * lb->gsplit_req;
+  int k = lb->chol_fp64;
+  k = k * 16 + lb->chol_cpw;
+  k = k * 2 + lb->pdl;
+  k = k * 128 + gemm_tc_tuning_code();
+  k = k * 8 + lb->gsplit_req;
+  return k * 2 + lb->fuse_r2x;
 }
 
 // Record one whole transition (all L steps, each fixed-point solve a

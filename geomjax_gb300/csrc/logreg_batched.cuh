@@ -67,6 +67,11 @@ void logreg_batched_set_pdl(LogregBatched* lb, int on);
 // K slices of the gradient contraction [r₁; r₂]·X on the tcgen05 path:
 // 1 .. 4, or 0 (automatic: enough slices to fill the SMs once)
 void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k);
+// 1 (default): the generalized leapfrog's momentum evaluations contract
+// r₂ = Λ'(w − s²) with X inside the S = U·Xᵀ GEMM's epilogue (tcgen05 path,
+// d <= 32), one partial gradient per N tile; 0: r₂ is stored as split BF16
+// planes and contracted by its own GEMM
+void logreg_batched_set_fuse_r2x(LogregBatched* lb, int on);
 // the chain count the automatic rules (K slices of the gradient contraction,
 // chains per warp of the factorisation) size their grids for (default: the
 // context's own; the chain groups of one sampler pass the sampler's total,

@@ -126,9 +126,9 @@ __device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, const WarpC
   if (t.family != GJ_FUNNEL) {  // hier: −Σ_j log σ_j (the data's scales, on the device)
     const int J = t.n;
     const R* sg = static_cast<const R*>(t.s);
-    double c = 0.0;
-    for (int i = lane; i < J; i += 32) c += -m_log(double(sg[i]));
-    W.ld_const += warp_sum(c);
+    R c = R(0);
+    for (int i = lane; i < J; i += 32) c -= m_log(sg[i]);
+    W.ld_const += double(warp_sum(c));
   }
   return W;
 }
@@ -201,12 +201,32 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
     const int i = W.lane + 32 * k;
     if (i < J) {
       const double e = double(y[i]) - double(q.x[k]);
-      se += e * e / (double(sg[i]) * double(sg[i]));
+      se += e * e * double(R(1) / (sg[i] * sg[i]));
     }
   }
   se = warp_sum(se);
   return W.ld_const - 0.5 * se - 0.5 * double(ev) * double(srr) - J * 0.5 * double(v) -
          0.5 * double(mu) * double(mu) * W.inv_a2d - 0.5 * double(v) * double(v) * W.inv_b2d;
+}
+
+// Metropolis accept (mcmc/proposal.py: p = min(1, e^{H0−H1}), accept when
+// u < p) with the exponential in R: the energy difference is formed in
+// float64, and in the float32 form e^w carries a relative error near 1e-7,
+// so a decision changes only for a uniform within that of the threshold.
+template <typename R>
+__device__ __forceinline__ AcceptOut metropolis_r(double H0, double H1, double u, double div_thr) {
+  if constexpr (sizeof(R) == 8) {
+    return metropolis(H0, H1, u, div_thr);
+  } else {
+    AcceptOut a;
+    float w = float(H0 - H1);
+    if (isnan(w)) w = -INFINITY;
+    a.w = w;
+    a.p_acc = double(fminf(m_exp(w), 1.0f));
+    a.accept = u < a.p_acc;
+    a.divergent = -w > float(div_thr);
+    return a;
+  }
 }
 
 // Hessian-vector product; `sx` is the Σx² (funnel) / Σr² (hier) of the
@@ -342,7 +362,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
   const R eps = R(sp.h);
   const R* imv = static_cast<const R*>(sp.inv_mass);
   WVec<E, R> q, g, im, gn, Hdl, hv, v;
-  double slm_part = 0.0;
+  R slm_part = R(0);
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = lane + 32 * k;
@@ -350,9 +370,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     q.x[k] = in ? pos[(size_t)c * d + i] : R(0);
     g.x[k] = in ? grad[(size_t)c * d + i] : R(0);
     im.x[k] = in ? (imv ? imv[i] : R(1)) : R(0);
-    if (in) slm_part += -double(m_log(im.x[k]));  // cancels in H1 − H0
+    if (in) slm_part -= m_log(im.x[k]);  // cancels in H1 − H0
   }
-  const double slm = warp_sum(slm_part);  // Σ log M
+  const double slm = double(warp_sum(slm_part));  // Σ log M
   const double ld0 = logdens[c];
   const double J0 = vol[c];
   R sx;
@@ -424,10 +444,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     }
     vmv = warp_sum(vmv);
     vg = warp_sum(vg);
-    // log L in float32: L is a float32 value, so a float64 logarithm adds
-    // no accuracy (and costs tens of FP64-pipe instructions)
-    return -0.5 * (double(m_log(Lc)) + slm) + 0.5 * double(vmv) +
-           0.5 * double(Lc) * double(a2) * double(vg) * double(vg);
+    // in the state's type R: every factor is an R value, and each FP64
+    // instruction costs 64 FP32 ones on GB300
+    const R kin = R(0.5) * (vmv - m_log(Lc)) + R(0.5) * Lc * a2 * vg * vg;
+    return double(kin) - 0.5 * slm;
   };
   const double H0 = -ld0 + kinetic(L) - J0;
   double ld = ld0;
@@ -472,7 +492,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
       }
     }
   }
-  const AcceptOut a = metropolis(H0, H1, uacc[c], sp.div_threshold);
+  const AcceptOut a = metropolis_r<R>(H0, H1, uacc[c], sp.div_threshold);
   if (a.accept) {
 #pragma unroll
     for (int k = 0; k < E; ++k) {

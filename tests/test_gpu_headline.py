@@ -187,3 +187,37 @@ def test_momentum_draw_accuracy_by_path(N, d, path, bound):
     _, info = kern(Draws(z, -np.ones(Cb)), gj.rmhmc.init(q0, dt), dt, 0.05, 1)
     ref = O_rm.momentum_from_normals(ot, q0[S], z[S])
     assert rel_err(_np(info.momentum)[S], ref) < bound
+
+
+@pytest.mark.parametrize("N,d", [(1000, 25), (300, 9), (400, 32), (100, 8)])
+def test_fused_r2x_matches_stored_r2(N, d):
+    """The momentum evaluations' r₂·X formed in the S = U·Xᵀ GEMM's epilogue
+    (FP32 FMAs on the CUDA cores, one partial gradient per N tile, added in
+    tile order) against r₂ stored as three BF16 planes and contracted on the
+    tensor cores: both within 1e-5 of the oracle per step over 10
+    generalized-leapfrog steps, and within 2e-6 of each other."""
+    import geomjax_gb300 as gj
+    from geomjax_gb300.base import Draws
+
+    ot, dt = _targets(N=N, d=d)
+    Cb = 256
+    S = np.arange(0, Cb, 16)
+    q0 = _f32(laplace_draws(ot, Cb, seed=11))
+    z = _f32(np.random.default_rng(12).standard_normal((Cb, d)))
+    u = -np.ones(Cb)
+    h, L = 0.05, 10
+    traj = []
+    O_rm.kernel(ot, O_rm.init(ot, q0[S]), z[S], u[S], h, L, trajectory=traj, integrator=GL)
+    kf = gj.rmhmc.build_kernel(logreg_path="tcgen05", integrator=GL, fuse_r2x=True)
+    ks = gj.rmhmc.build_kernel(logreg_path="tcgen05", integrator=GL, fuse_r2x=False)
+    st0 = gj.rmhmc.init(q0, dt)
+    for step in (1, 5, 10):
+        sf, inf_f = kf(Draws(z, u), st0, dt, h, step)
+        ss, inf_s = ks(Draws(z, u), st0, dt, h, step)
+        pf, ps = _np(sf.position), _np(ss.position)
+        ef, es = (rel_err(pf[S], traj[step - 1].position),
+                  rel_err(ps[S], traj[step - 1].position))
+        assert rel_err(pf, ps) < 2e-6, (step, rel_err(pf, ps), ef, es)
+        assert ef < 1e-5 and es < 1e-5, (step, ef, es)
+    diff = np.abs(_np(inf_f.fixed_point_iters) - _np(inf_s.fixed_point_iters))
+    assert diff.mean() < 1.0, diff.mean()
