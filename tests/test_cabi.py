@@ -91,6 +91,10 @@ def test_argument_checks_without_gpu():
     for v in range(5):
         assert lib.gj_set_option(h, L.GJ_OPT_GEMM_KSPLIT, v) == L.GJ_OK
     assert lib.gj_set_option(h, L.GJ_OPT_CHAIN_GROUPS, 2) == L.GJ_OK
+    assert lib.gj_set_option(h, L.GJ_OPT_FUSE_R2X, 2) == L.GJ_EINVAL
+    assert lib.gj_set_option(h, L.GJ_OPT_FUSE_R2X, -1) == L.GJ_EINVAL
+    for v in (0, 1):
+        assert lib.gj_set_option(h, L.GJ_OPT_FUSE_R2X, v) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(96, 1) == L.GJ_EINVAL
     # batch creation checks its arguments before touching the GPU
     bh = ctypes.c_void_p()
