@@ -22,6 +22,11 @@
 //               quarter take alternate 32-column chunks), staged once through
 //               shared memory and processed as row segments (8 values of one
 //               row per lane, 16-byte global accesses)
+// The R2G instantiation (EPI_R2G: three planes, BN = 128, one K block) then
+// contracts its r2 = Λ'(w − s²) with Xᵀ in the same CTA: r2 goes into the
+// freed operand ring as swizzled BF16 planes, the producer warp TMA-loads
+// the Xᵀ boxes, and one epilogue thread issues a second set of MMAs into 32
+// more TMEM columns (see epi_r2g).
 // Every mbarrier wait is bounded; on timeout the kernel records an error code
 // in *err and skips the rest of its work, releasing TMEM before exit.
 #include <cuda.h>
