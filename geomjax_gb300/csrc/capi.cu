@@ -735,7 +735,7 @@ int32_t gj_chees_statistics(int32_t precision, int32_t num_chains, int32_t dim,
 
 struct gj_batch {
   int B, C, S;
-  int one_graph;  // GJ_OPT_BATCH_GRAPH
+  int one_graph;  // GJ_OPT_BATCH_GRAPH: 0 stream pool, 1 a branch per posterior, 2 grouped
   gj::LogregBatchGraph* bg;
   std::vector<gj::LogregBatched*> lbs;
   std::vector<int> dims;
@@ -842,8 +842,9 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
     return GJ_OK;
   }
   if (key == GJ_OPT_BATCH_GRAPH) {
-    if (value < 0 || value > 1) return fail(GJ_EINVAL, "batch graph flag must be 0 or 1");
+    if (value < 0 || value > 2) return fail(GJ_EINVAL, "batch graph mode must be 0, 1 or 2");
     b->one_graph = (int)value;
+    if (b->bg) gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2);
     return GJ_OK;
   }
   return fail(GJ_EINVAL, "unknown batch option");
@@ -866,6 +867,7 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
       const int rc = gj::logreg_batch_graph_create(b->lbs.data(), b->B, b->C, b->pos_off.data(),
                                                    &b->bg);
       if (rc) return fail(rc, "%s", gj::logreg_batched_error());
+      gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2);
     }
     const int rc = gj::logreg_batch_graph_step(b->bg, sp, (float*)s->position,
                                                (float*)s->logdensity_grad, s->logdensity, z, u,

@@ -200,6 +200,21 @@ __device__ __forceinline__ T dsigmoid(T a) {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
 
+// Grouped launches run many independent launches of one kernel as one grid:
+// item i owns blocks [prefix[i], prefix[i + 1]) (prefix[0] = 0, n items).
+// Returns the item that holds block b (b < prefix[n]).
+__device__ __forceinline__ int group_item(const int* __restrict__ prefix, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(prefix + mid) <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_k(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                             cudaStream_t st, Args... args) {

@@ -91,6 +91,11 @@ struct Epi {
   float* g2;
   int g2_ld;
   size_t g2_slice;
+  // tcgen05 path, when set: output row m (a chain) is wanted only while
+  // active_rows[m] != 0, and a CTA whose 128 rows are all inactive does
+  // nothing (the fixed-point loop bodies, whose converged chains' outputs
+  // are not read again before the evaluation that follows the loop)
+  const uint8_t* active_rows;
 };
 
 // σ(a), σ(−a) and log(1 + e^a) from one exponential, e = e^{−|a|}: neither
@@ -216,6 +221,26 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
 // the output tile width (32, 64 or 128) a launch with these planes, N and K
 // takes under the current tile policy
 int gemm_tc_bn(int planes, int N, int K);
+
+// One contraction of a grouped launch: its tensor maps, epilogue, error
+// flag and launch parameters (the ring depth, K-range accumulators and grid
+// gemm_tc would use).  The tensor maps (64-byte aligned, so the item is)
+// are read by the kernel from global memory.
+struct GemmItem {
+  CUtensorMap mapA, mapB, mapXT;
+  Epi epi;
+  int* err;
+  int rpadA, rpadB, M, N, K, stages, a_row0, nacc, gx, gy, gz;
+};
+// The launch gemm_tc would make, described instead of made: the item, the
+// kernel variant (planes, tile width, fused r2·X epilogue), the CTA count
+// and the dynamic shared memory.  The same checks as gemm_tc.
+cudaError_t gemm_tc_describe(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                             GemmItem* item, int* variant, int* blocks, size_t* smem);
+// One grid over n described items of one variant; items and the prefix sums
+// of their CTA counts (n + 1 entries, prefix[n] = blocks) in device memory.
+cudaError_t gemm_tc_grouped(int variant, const GemmItem* items, const int* prefix, int n, int blocks,
+                            size_t smem, cudaStream_t st);
 
 // noalloc.cu: the same contraction with the split planes in a static device
 // array (no cudaMalloc / cudaFree); capacity in BF16 elements.

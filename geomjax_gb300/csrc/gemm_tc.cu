@@ -109,6 +109,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// Acquire a tensor map that the host copied into global memory (grouped
+// launches), before the TMA unit reads it: the copy is not ordered with the
+// tensor-map proxy otherwise; system scope for a host-side write.
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(m) : "memory");
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y) {
   asm volatile(
@@ -210,7 +217,7 @@ __device__ __forceinline__ void split8(const SplitMat& S, int row, int n, int N,
 }
 
 __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, int m_base, int n_base,
-                                          int M, int N, const float* v) {
+                                          int M, int N, const float* v, int kslice) {
   stage_row(stg, lane, v);
   const int cc = (lane & 3) * 8;
   const int n = n_base + cc;
@@ -223,7 +230,7 @@ __device__ __forceinline__ void epi_chunk(const Epi& e, float* stg, int lane, in
 #pragma unroll
     for (int k = 0; k < 8; ++k) a[k] = stg[rr * 33 + cc + k];
     if (e.mode == EPI_STORE) {
-      float* D = e.D + (size_t)blockIdx.z * e.d_slice;  // K slice (0 unless split)
+      float* D = e.D + (size_t)kslice * e.d_slice;  // K slice (0 unless split)
       if (m < M) store8(D + (size_t)m * e.ldd + n, n, N, full && aligned16(D, e.ldd), a);
     } else if (e.mode == EPI_SIGMOID) {
       float yv[8], lam[8], lp[8], r1[8];
@@ -318,7 +325,8 @@ constexpr uint32_t R2G_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) 
 // waits, and every wait is bounded.
 __device__ __forceinline__ void epi_r2g(const Epi& e, unsigned char* base, uint64_t* xfull,
                                         uint64_t* gdone, uint32_t tmem, int warp, int lane,
-                                        bool ok, int m0, int n0, int M, int N, int* err) {
+                                        bool ok, int m0, int n0, int M, int N, int* err,
+                                        int ntile) {
   const int q = warp & 3, half = (warp - 2) >> 2;
   const int row = q * 32 + lane;  // tile row of this lane
   const int m = m0 + row;
@@ -419,7 +427,7 @@ __device__ __forceinline__ void epi_r2g(const Epi& e, unsigned char* base, uint6
   uint32_t r[32];
   tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + R2G_TMEM_COL, r);
   if (ok && done && m < M) {  // the row's partial gradient for this N tile
-    float* out = e.g2 + (size_t)blockIdx.x * e.g2_slice + (size_t)m * e.g2_ld;
+    float* out = e.g2 + (size_t)ntile * e.g2_slice + (size_t)m * e.g2_ld;
     const int k4n = (e.x_d + 3) >> 2;
 #pragma unroll
     for (int k4 = 0; k4 < 8; ++k4)
@@ -434,11 +442,15 @@ __device__ __forceinline__ void epi_r2g(const Epi& e, unsigned char* base, uint6
 // chosen by the host so that two CTAs share an SM where that fits.
 // NACC (run time, 1, 2 or 4) accumulators over contiguous K ranges; the
 // host keeps NACC·TMEM_COLS·(CTAs per SM) within the SM's 512 columns.
-template <int NPL, int BN, bool R2G = false>  // R2G: the EPI_R2G epilogue
-__global__ void __launch_bounds__(320, 2)
-    gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                   const __grid_constant__ CUtensorMap mapXT, int rpadA, int rpadB, int M, int N,
-                   int K, Epi epi, int* err, int STAGES, int a_row0, int NACC) {
+// The CTA's work as a device function: block (bx, by, bz) of a grid with gz
+// K slices, tensor maps by address (kernel parameters of gemm_tc_kernel, or
+// the items of a grouped launch in global memory).
+template <int NPL, int BN, bool R2G>  // R2G: the EPI_R2G epilogue
+__device__ __forceinline__ void gemm_tc_body(const CUtensorMap* mapA, const CUtensorMap* mapB,
+                                             const CUtensorMap* mapXT, int rpadA, int rpadB, int M,
+                                             int N, int K, const Epi& epi, int* err, int STAGES,
+                                             int a_row0, int NACC, int bx, int by, int bz, int gz,
+                                             bool maps_in_global) {
   using C = Cfg<NPL, BN>;
   constexpr int STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
@@ -454,11 +466,11 @@ __global__ void __launch_bounds__(320, 2)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 3);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int m0 = by * BM, n0 = bx * BN;
   // this CTA's contiguous range of K blocks (the whole K unless split)
   const int KB_all = (K + BK - 1) / BK;
-  const int kper = (KB_all + (int)gridDim.z - 1) / (int)gridDim.z;
-  const int kb_first = (int)blockIdx.z * kper;
+  const int kper = (KB_all + gz - 1) / gz;
+  const int kb_first = bz * kper;
   const int KB = max(0, min(KB_all, kb_first + kper) - kb_first);
   // a K slice with fewer K blocks than accumulators uses one per block, so
   // that no range is empty
@@ -490,9 +502,24 @@ __global__ void __launch_bounds__(320, 2)
   // barriers and TMEM are set up; the operands and epilogue inputs come from
   // the preceding kernels
   pdl_wait();
+  // a tile whose chains have all converged is skipped (whole CTA)
+  bool work = true;
+  if (epi.active_rows) {
+    bool any = false;
+    for (int r = (int)threadIdx.x; r < BM; r += (int)blockDim.x)
+      any |= (m0 + r < M) && epi.active_rows[m0 + r] != 0;
+    work = __syncthreads_or(any) != 0;
+  }
 
-  if (warp == 0) {
+  if (!work) {
+    // nothing issued, nothing to wait for
+  } else if (warp == 0) {
     if (lane == 0) {
+      if (maps_in_global) {
+        tensormap_acquire(mapA);
+        tensormap_acquire(mapB);
+        if (R2G) tensormap_acquire(mapXT);
+      }
       for (int kb = 0; kb < KB; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (kb / STAGES) & 1;
@@ -505,8 +532,8 @@ __global__ void __launch_bounds__(320, 2)
         const int x = (kb_first + kb) * BK;
 #pragma unroll
         for (int q = 0; q < NPL; ++q) {
-          tma_load_2d(st + q * A_TILE_BYTES, &mapA, &full[s], x, q * rpadA + a_row0 + m0);
-          tma_load_2d(st + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES, &mapB, &full[s], x,
+          tma_load_2d(st + q * A_TILE_BYTES, mapA, &full[s], x, q * rpadA + a_row0 + m0);
+          tma_load_2d(st + NPL * A_TILE_BYTES + q * C::B_TILE_BYTES, mapB, &full[s], x,
                       q * rpadB + n0);
         }
       }
@@ -516,7 +543,7 @@ __global__ void __launch_bounds__(320, 2)
           mbar_expect_tx(xfull, 6 * R2G_XT_BOX);
           for (int kh = 0; kh < 2; ++kh)
             for (int q = 0; q < 3; ++q)
-              tma_load_2d(base + R2G_A_BYTES + (kh * 3 + q) * R2G_XT_BOX, &mapXT, xfull,
+              tma_load_2d(base + R2G_A_BYTES + (kh * 3 + q) * R2G_XT_BOX, mapXT, xfull,
                           n0 + 64 * kh, q * epi.xt_rpad);
         } else {
           atomicExch(err, 4);
@@ -574,7 +601,7 @@ __global__ void __launch_bounds__(320, 2)
     if (!ok && lane == 0) atomicExch(err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if constexpr (R2G) {  // the host keeps K in one unsplit block (KB = 1)
-      epi_r2g(epi, base, xfull, gdone, tmem, warp, lane, ok && KB > 0, m0, n0, M, N, err);
+      epi_r2g(epi, base, xfull, gdone, tmem, warp, lane, ok && KB > 0, m0, n0, M, N, err, bx);
     } else if (ok && KB > 0) {
       // the operand ring is free once the accumulator is complete: each
       // epilogue warp stages its chunks in its own 32 x 33 float tile
@@ -584,7 +611,7 @@ __global__ void __launch_bounds__(320, 2)
         if (n0 + c0 >= N) break;  // warp-uniform
         float v[32];
         load_acc(tmem, q, c0, nacc, TMEM_COLS, v);
-        epi_chunk(epi, stg, lane, m0 + q * 32, n0 + c0, M, N, v);
+        epi_chunk(epi, stg, lane, m0 + q * 32, n0 + c0, M, N, v, bz);
       }
     }
   }
@@ -599,6 +626,32 @@ __global__ void __launch_bounds__(320, 2)
                  "r"(tmem_cols)
                  : "memory");
   }
+}
+
+template <int NPL, int BN, bool R2G = false>
+__global__ void __launch_bounds__(320, 2)
+    gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const __grid_constant__ CUtensorMap mapXT, int rpadA, int rpadB, int M, int N,
+                   int K, Epi epi, int* err, int STAGES, int a_row0, int NACC) {
+  gemm_tc_body<NPL, BN, R2G>(&mapA, &mapB, &mapXT, rpadA, rpadB, M, N, K, epi, err, STAGES, a_row0,
+                             NACC, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
+                             (int)gridDim.z, false);
+}
+
+// Grouped launch: many independent contractions of one tile shape in one
+// grid, each CTA finding its item (its own operands, tensor maps, epilogue
+// and grid) by its block index.
+template <int NPL, int BN, bool R2G>
+__global__ void __launch_bounds__(320, 2)
+    gemm_tc_grouped_kernel(const GemmItem* __restrict__ items, const int* __restrict__ prefix,
+                           int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  const GemmItem& it = items[i];
+  const int local = (int)blockIdx.x - __ldg(prefix + i);
+  const int bx = local % it.gx, by = (local / it.gx) % it.gy, bz = local / (it.gx * it.gy);
+  gemm_tc_body<NPL, BN, R2G>(&it.mapA, &it.mapB, &it.mapXT, it.rpadA, it.rpadB, it.M, it.N, it.K,
+                             it.epi, it.err, it.stages, it.a_row0, it.nacc, bx, by, bz, it.gz,
+                             true);
 }
 
 }  // namespace
@@ -661,6 +714,13 @@ cudaError_t set_smem_limit() {
   const int bytes = Cfg<NPL, BN>::smem(Cfg<NPL, BN>::MAX_STAGES);
   cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(gemm_tc_grouped_kernel<NPL, BN, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if constexpr (NPL == 3 && BN == 128)
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gemm_tc_grouped_kernel<NPL, BN, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if constexpr (NPL == 3 && BN == 128)  // the fused r2·X form (launched with these only)
     if (e == cudaSuccess) e = cudaFuncSetAttribute(gemm_tc_kernel<NPL, BN, true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -701,9 +761,14 @@ TcTuning g_tune;
 
 constexpr int kTwoCtaSmem = 113 * 1024;
 
+constexpr int variant_of(int npl, int bn, bool r2g) {
+  return (npl - 2) * 6 + (bn == 32 ? 0 : (bn == 64 ? 1 : 2)) * 2 + (r2g ? 1 : 0);
+}
+
+// The launch parameters of one contraction with this tile shape.
 template <int NPL, int BN>
-cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
-                      cudaStream_t st) {
+cudaError_t plan_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                    GemmItem* it, int* variant, size_t* smem) {
   using C = Cfg<NPL, BN>;
   const int kb = (g.K + BK - 1) / BK;
   int ns = std::max(1, std::min(C::MAX_STAGES, kb));
@@ -713,7 +778,6 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   else
     ns = std::min(ns, 3);
   const CUtensorMap& mb = BN == 128 ? b->map : (BN == 64 ? b->map64 : b->map32);
-  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.ksplit);
   // K-range accumulators: up to 4, at least 2 K blocks each, and within the
   // 512 TMEM columns of an SM for the CTAs that share it
   const int kb_cta = (kb + g.ksplit - 1) / g.ksplit;
@@ -721,23 +785,57 @@ cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b,
   int nacc = 1;
   while (nacc < g_tune.max_nacc && 2 * nacc * 2 <= kb_cta && 2 * nacc * C::TMEM_COLS * ctas <= 512)
     nacc *= 2;
-  if (g.epi.mode == EPI_R2G) {
+  const bool r2g = g.epi.mode == EPI_R2G;
+  it->mapA = a->map;
+  it->mapB = mb;
+  it->mapXT = mb;
+  if (r2g) {
     // three planes, 128-wide tiles, one K block (one accumulator) and a
     // ring that holds the r2 tile and the Xᵀ boxes
-    if constexpr (NPL == 3 && BN == 128) {
-      const TcOperand* xt = g.epi.xt;
-      if (kb != 1 || ns * C::STAGE_BYTES < R2G_SMEM || !xt || xt->s.planes != 3 ||
-          xt->s.rows > 32 || g.epi.xt_rpad != xt->s.rpad)
-        return cudaErrorInvalidValue;
-      return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, true>, grid, dim3(320), (size_t)C::smem(ns),
-                      st, a->map, mb, xt->map32, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err,
-                      ns, g.a_row0, 1);
-    }
+    const TcOperand* xt = g.epi.xt;
+    if (NPL != 3 || BN != 128 || kb != 1 || ns * C::STAGE_BYTES < R2G_SMEM || !xt ||
+        xt->s.planes != 3 || xt->s.rows > 32 || g.epi.xt_rpad != xt->s.rpad)
+      return cudaErrorInvalidValue;
+    it->mapXT = xt->map32;
+    nacc = 1;
+  }
+  it->epi = g.epi;
+  it->err = err;
+  it->rpadA = a->s.rpad;
+  it->rpadB = b->s.rpad;
+  it->M = g.M;
+  it->N = g.N;
+  it->K = g.K;
+  it->stages = ns;
+  it->a_row0 = g.a_row0;
+  it->nacc = nacc;
+  it->gx = (g.N + BN - 1) / BN;
+  it->gy = (g.M + BM - 1) / BM;
+  it->gz = g.ksplit;
+  *variant = variant_of(NPL, BN, r2g);
+  *smem = (size_t)C::smem(ns);
+  return cudaSuccess;
+}
+
+template <int NPL, int BN>
+cudaError_t launch_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                      cudaStream_t st) {
+  GemmItem it;
+  int variant = 0;
+  size_t smem = 0;
+  const cudaError_t e = plan_tc<NPL, BN>(g, a, b, err, &it, &variant, &smem);
+  if (e != cudaSuccess) return e;
+  const dim3 grid(it.gx, it.gy, it.gz);
+  if (g.epi.mode == EPI_R2G) {
+    if constexpr (NPL == 3 && BN == 128)
+      return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, true>, grid, dim3(320), smem, st, it.mapA,
+                      it.mapB, it.mapXT, it.rpadA, it.rpadB, g.M, g.N, g.K, g.epi, err, it.stages,
+                      g.a_row0, 1);
     return cudaErrorInvalidValue;
   }
-  return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, false>, grid, dim3(320), (size_t)C::smem(ns), st,
-                  a->map, mb, mb, a->s.rpad, b->s.rpad, g.M, g.N, g.K, g.epi, err, ns, g.a_row0,
-                  nacc);
+  return launch_k(g.pdl, gemm_tc_kernel<NPL, BN, false>, grid, dim3(320), smem, st, it.mapA,
+                  it.mapB, it.mapB, it.rpadA, it.rpadB, g.M, g.N, g.K, g.epi, err, it.stages,
+                  g.a_row0, it.nacc);
 }
 
 int tile_bn(int planes, int N, int K) {
@@ -754,6 +852,15 @@ cudaError_t launch_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOper
   if (bn == 32) return launch_tc<NPL, 32>(g, a, b, err, st);
   if (bn == 64) return launch_tc<NPL, 64>(g, a, b, err, st);
   return launch_tc<NPL, 128>(g, a, b, err, st);
+}
+
+template <int NPL>
+cudaError_t plan_tc_planes(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                           GemmItem* it, int* variant, size_t* smem) {
+  const int bn = tile_bn(NPL, g.N, g.K);
+  if (bn == 32) return plan_tc<NPL, 32>(g, a, b, err, it, variant, smem);
+  if (bn == 64) return plan_tc<NPL, 64>(g, a, b, err, it, variant, smem);
+  return plan_tc<NPL, 128>(g, a, b, err, it, variant, smem);
 }
 
 }  // namespace
@@ -773,9 +880,9 @@ void gemm_tc_set_tuning(int bn_wide, int two_ctas) {
   g_tune.two_ctas = two_ctas < 0 ? -1 : (two_ctas ? 1 : 0);
 }
 
-cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
-                    cudaStream_t st) {
-  if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+namespace {
+
+cudaError_t check_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b) {
   // every box must lie inside the padded planes
   if (g.a_row0 < 0 || g.a_row0 + g.M > a->s.rpad || g.N > b->s.rpad || g.K > a->s.ld ||
       g.K > b->s.ld || a->s.planes != b->s.planes)
@@ -788,8 +895,47 @@ cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, i
        (g.epi.g2_ld & 3) || (g.epi.g2_slice & 3) || !g.epi.g2 ||
        (reinterpret_cast<uintptr_t>(g.epi.g2) & 15) || g.ksplit != 1 || g.a_row0 != 0))
     return cudaErrorInvalidValue;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t gemm_tc(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                    cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0) return cudaSuccess;
+  const cudaError_t e = check_tc(g, a, b);
+  if (e != cudaSuccess) return e;
   return a->s.planes == 3 ? launch_tc_planes<3>(g, a, b, err, st)
                           : launch_tc_planes<2>(g, a, b, err, st);
+}
+
+cudaError_t gemm_tc_describe(const GemmArgs& g, const TcOperand* a, const TcOperand* b, int* err,
+                             GemmItem* item, int* variant, int* blocks, size_t* smem) {
+  if (g.M <= 0 || g.N <= 0) return cudaErrorInvalidValue;
+  if (g.pdl) return cudaErrorInvalidValue;  // grouped launches are plain stream order
+  cudaError_t e = check_tc(g, a, b);
+  if (e != cudaSuccess) return e;
+  e = a->s.planes == 3 ? plan_tc_planes<3>(g, a, b, err, item, variant, smem)
+                       : plan_tc_planes<2>(g, a, b, err, item, variant, smem);
+  if (e == cudaSuccess) *blocks = item->gx * item->gy * item->gz;
+  return e;
+}
+
+cudaError_t gemm_tc_grouped(int variant, const GemmItem* items, const int* prefix, int n, int blocks,
+                            size_t smem, cudaStream_t st) {
+  if (n < 1 || blocks < 1) return cudaErrorInvalidValue;
+  const dim3 grid((unsigned)blocks), th(320);
+  switch (variant) {
+    case variant_of(2, 32, false): gemm_tc_grouped_kernel<2, 32, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(2, 64, false): gemm_tc_grouped_kernel<2, 64, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(2, 128, false): gemm_tc_grouped_kernel<2, 128, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(3, 32, false): gemm_tc_grouped_kernel<3, 32, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(3, 64, false): gemm_tc_grouped_kernel<3, 64, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(3, 128, false): gemm_tc_grouped_kernel<3, 128, false><<<grid, th, smem, st>>>(items, prefix, n); break;
+    case variant_of(3, 128, true): gemm_tc_grouped_kernel<3, 128, true><<<grid, th, smem, st>>>(items, prefix, n); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace gj

@@ -26,9 +26,11 @@
 // evaluated per chain in FP32 with an FP64 sum.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "chain_kernels.cuh"
@@ -136,8 +138,9 @@ struct CholArgs {
 // consecutive packed entries fall in distinct banks.
 struct CholCfg {
   int cpw;       // chains per warp
-  int lpc;       // lanes per chain (32 / cpw)
+  int lpc;       // lanes per chain (32 / cpw; 128: one chain per CTA of 4 warps)
   int warps;     // warps per CTA
+  int chains;    // chains per CTA
   size_t stride; // bytes per chain
   size_t tab;    // bytes of the pair table
   size_t smem;   // dynamic shared memory per CTA
@@ -176,6 +179,18 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) 
   // as many of those warps as fit 200 KB (large d: one warp of one chain)
   while (c.warps > 1 && c.tab + (size_t)c.warps * c.cpw * c.stride > 200 * 1024) --c.warps;
   c.smem = c.tab + (size_t)c.warps * c.cpw * c.stride;
+  c.chains = c.warps * c.cpw;
+  // One chain per warp, and four such chains would not let two CTAs share an
+  // SM (d >= 64): each warp alone on its scheduler leaves the other FP64
+  // units idle and exposes every latency of the chain's d dependent column
+  // steps.  Such a chain gets a CTA of four warps (its trailing updates
+  // spread over 128 lanes), one chain per CTA.
+  if (c.cpw == 1 && c.tab + 4 * c.stride > 113 * 1024) {
+    c.lpc = 128;
+    c.warps = 4;
+    c.chains = 1;
+    c.smem = c.tab + c.stride;
+  }
   return c;
 }
 
@@ -242,18 +257,71 @@ __device__ __forceinline__ bool group_any(bool b) {
   return v != 0;
 }
 
+// A chain's barrier and reductions: its sub-group of a warp (LPC <= 32) or
+// its whole CTA (LPC > 32, LPC / 32 warps; reductions through shared memory,
+// warps added in order)
+template <int LPC>
+__device__ __forceinline__ void chain_sync() {
+  if constexpr (LPC > 32)
+    __syncthreads();
+  else
+    __syncwarp();
+}
+template <int LPC>
+__device__ __forceinline__ double chain_sum(double v) {
+  if constexpr (LPC <= 32) {
+    return group_sum<LPC>(v);
+  } else {
+    __shared__ double red[LPC / 32];
+    v = group_sum<32>(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < LPC / 32; ++w) t += red[w];
+    __syncthreads();
+    return t;
+  }
+}
+template <int LPC>
+__device__ __forceinline__ double chain_max(double v) {
+  if constexpr (LPC <= 32) {
+    return group_max<LPC>(v);
+  } else {
+    __shared__ double red[LPC / 32];
+    v = group_max<32>(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = red[0];
+#pragma unroll
+    for (int w = 1; w < LPC / 32; ++w) t = fmax(t, red[w]);
+    __syncthreads();
+    return t;
+  }
+}
+template <int LPC>
+__device__ __forceinline__ bool chain_any(bool b) {
+  if constexpr (LPC <= 32) return group_any<LPC>(b);
+  else return __syncthreads_or(b ? 1 : 0) != 0;
+}
+
+// block bx of the factorisation (chol_kernel, or an item of a grouped launch)
+// LPC = 128: one chain per CTA of four warps (large d, where one warp per
+// chain leaves most of an SM's FP64 units idle); its barrier is the CTA's.
 template <typename F, int LPC>  // factorisation type (double / float), lanes per chain
-__global__ void chol_kernel(CholArgs a, int stride) {
+__device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int CPW = 32 / LPC;
+  constexpr bool kCta = LPC > 32;
+  constexpr int CPW = kCta ? 1 : 32 / LPC;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
-  const int sub = lane / LPC, sl = lane % LPC;
-  const int c = (blockIdx.x * nwarps + warp) * CPW + sub;
+  const int sub = kCta ? 0 : lane / LPC, sl = kCta ? (int)threadIdx.x : lane % LPC;
+  const int c = kCta ? bx : (bx * nwarps + warp) * CPW + sub;
   const int d = a.d;
   const int P = a.P;
   uint32_t* tab = reinterpret_cast<uint32_t*>(smem_raw);
-  unsigned char* base = smem_raw + chol_table_bytes(d) + (size_t)(warp * CPW + sub) * stride;
+  unsigned char* base =
+      smem_raw + chol_table_bytes(d) + (size_t)(kCta ? 0 : warp * CPW + sub) * stride;
   F* L = reinterpret_cast<F*>(base);  // packed lower, column-major
   F* y = L + P;
   F* xv = y + d;
@@ -280,7 +348,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     }
     L[t] = g;
   }
-  __syncwarp();
+  chain_sync<LPC>();
   // right-looking Cholesky; log det G = log Π pivots, accumulated as
   // mantissa · 2^exponent so that one logarithm is taken per chain.  Outside
   // DRAW the right-hand side p is known, so y = L⁻¹p rides along as a
@@ -310,14 +378,14 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     const F djj = L[cj];
     const F inv = pivot_rsqrt(djj, bad);  // 1/L_jj
     if (want_ld) ld_accumulate(pm, pe, double(djj));
-    __syncwarp();
+    chain_sync<LPC>();
     if (sl == 0) {
       if (a.mode == CH_DRAW) L[cj] = djj * inv;  // L_jj, read only by p = L z
       rdiag[j] = inv;
       if (border) y[j] *= inv;
     }
     for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
-    __syncwarp();
+    chain_sync<LPC>();
     return inv;
   };
   constexpr bool kRank2 = sizeof(F) == sizeof(float);
@@ -339,7 +407,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
         tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
       }
       cj = cj1;
-      __syncwarp();
+      chain_sync<LPC>();
       continue;
     }
     // column j + 1 (rows j + 1 ..) and y_{j+1} reduced by column j
@@ -348,7 +416,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       for (int i = j + 1 + sl; i < d; i += LPC) L[cj1 + i - j - 1] -= L[cj + i - j] * l10;
       if (border && sl == 0) y[j + 1] -= y[j] * l10;
     }
-    __syncwarp();
+    chain_sync<LPC>();
     pivot(j + 1, cj1);
     // trailing triangle (columns k >= j + 2): both columns are read-only
     // here and disjoint from the entries written
@@ -367,7 +435,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       tr[t] -= c0[i] * c0[k] + c1[i] * c1[k];
     }
     cj = cn;
-    __syncwarp();
+    chain_sync<LPC>();
   }
   pdl_trigger();  // the factorisation is done; the successor may be scheduled
   if (sl == 0 && live) {
@@ -388,7 +456,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   // column-oriented forward substitution
   if (a.mode == CH_DRAW) {
     for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
-    __syncwarp();
+    chain_sync<LPC>();
     double zz = 0.0;
     for (int i = sl; i < d; i += LPC) {
       F sacc = 0;
@@ -404,28 +472,28 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       }
       zz += double(y[i]) * double(y[i]);
     }
-    zz = group_sum<LPC>(zz);
+    zz = chain_sum<LPC>(zz);
     if (sl == 0 && live) a.quad[c] = zz;
   } else {  // y = L⁻¹p was formed with the factor
     if (a.mode == CH_ENERGY) {
       double q = 0.0;
       for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
-      q = group_sum<LPC>(q);
+      q = chain_sum<LPC>(q);
       if (sl == 0 && live) a.quad[c] = q;
       if (!a.vel_info) return;  // uniform: the proposal velocity was not asked for
     }
   }
-  __syncwarp();
+  chain_sync<LPC>();
   // u = L⁻ᵀ y, column-oriented backward substitution (row j of L is
   // L(j, i) at colstart(i) + j − i)
   for (int i = sl; i < d; i += LPC) xv[i] = y[i];
-  __syncwarp();
+  chain_sync<LPC>();
   for (int j = d - 1; j >= 0; --j) {
     const F xj = xv[j] * rdiag[j];
-    __syncwarp();
+    chain_sync<LPC>();
     if (sl == 0) xv[j] = xj;
     for (int i = sl; i < j; i += LPC) xv[i] -= L[colstart(i, d) + j - i] * xj;
-    __syncwarp();
+    chain_sync<LPC>();
   }
   if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
     if (live)
@@ -458,8 +526,8 @@ __global__ void chol_kernel(CholArgs a, int stride) {
           split_store(a.Qb, c, i, float(qn));
         }
       }
-      nrm = group_max<LPC>(nrm);
-      if (group_any<LPC>(nan)) nrm = NAN;
+      nrm = chain_max<LPC>(nrm);
+      if (chain_any<LPC>(nan)) nrm = NAN;
       bool act = false;
       if (live) {
         const int it = a.iters[c] + 1;
@@ -482,7 +550,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
     const uint32_t ik = tab[t];
     Li[t] = (ik & 0xffffu) == (ik >> 16) ? 1.f : 0.f;
   }
-  __syncwarp();
+  chain_sync<LPC>();
   // two rows at a time: rows k and k + 1 are made final (row k scaled; row
   // k + 1 reduced by row k, then scaled), then rows i > k + 1 are reduced
   // by both in one pass
@@ -490,7 +558,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   for (int k = 0; k < d; k += 2) {
     const float ikk = float(rdiag[k]);
     for (int cc = sl; cc <= k; cc += LPC) Li[colstart(cc, d) + k - cc] *= ikk;
-    __syncwarp();
+    chain_sync<LPC>();
     const int ck1 = ck + (d - k);  // colstart(k + 1)
     if (k + 1 == d) break;
     const float l10 = float(L[ck + 1]);  // L(k + 1, k)
@@ -500,7 +568,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       const float v = (cc <= k) ? Li[o + k + 1 - cc] - l10 * Li[o + k - cc] : Li[o];
       Li[o + k + 1 - cc] = v * ik1;
     }
-    __syncwarp();
+    chain_sync<LPC>();
     for (int i = k + 2 + sl; i < d; i += LPC) {
       const float li0 = float(L[ck + i - k]);       // L(i, k)
       const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
@@ -512,7 +580,7 @@ __global__ void chol_kernel(CholArgs a, int stride) {
       Li[cc0 + i - k - 1] -= li1 * Li[cc0];  // cc = k + 1: Li(k, k + 1) = 0
     }
     ck = ck1 + (d - k - 1);
-    __syncwarp();
+    chain_sync<LPC>();
   }
   // G⁻¹ = L⁻ᵀL⁻¹ packed as Z-coefficients (row-major upper triangle, whose
   // index for (k, i), k <= i, is the packed index t of (i, k)); the
@@ -529,6 +597,23 @@ __global__ void chol_kernel(CholArgs a, int stride) {
   }
 }
 
+template <typename F, int LPC>
+__global__ void chol_kernel(CholArgs a, int stride) {
+  chol_body<F, LPC>(a, stride, (int)blockIdx.x);
+}
+
+// a grouped launch of factorisations: one item per posterior
+struct CholItem {
+  CholArgs a;
+  int stride;
+};
+template <typename F, int LPC>
+__global__ void chol_grouped_kernel(const CholItem* __restrict__ items,
+                                    const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  chol_body<F, LPC>(items[i].a, items[i].stride, (int)blockIdx.x - __ldg(prefix + i));
+}
+
 template <typename F>
 cudaError_t chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, bool pdl,
                         cudaStream_t st) {
@@ -538,6 +623,7 @@ cudaError_t chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, bool pd
     case 4: return launch_k(pdl, chol_kernel<F, 4>, grid, th, cf.smem, st, a, stride);
     case 8: return launch_k(pdl, chol_kernel<F, 8>, grid, th, cf.smem, st, a, stride);
     case 16: return launch_k(pdl, chol_kernel<F, 16>, grid, th, cf.smem, st, a, stride);
+    case 128: return launch_k(pdl, chol_kernel<F, 128>, grid, th, cf.smem, st, a, stride);
     default: return launch_k(pdl, chol_kernel<F, 32>, grid, th, cf.smem, st, a, stride);
   }
 }
@@ -545,6 +631,16 @@ cudaError_t chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, bool pd
 template <typename F>
 cudaError_t chol_set_smem(int smax) {
   cudaError_t e = cudaSuccess, r;
+  const void* grouped[6] = {(const void*)chol_grouped_kernel<F, 4>,
+                            (const void*)chol_grouped_kernel<F, 8>,
+                            (const void*)chol_grouped_kernel<F, 16>,
+                            (const void*)chol_grouped_kernel<F, 32>,
+                            (const void*)chol_grouped_kernel<F, 128>,
+                            (const void*)chol_kernel<F, 128>};
+  for (const void* k : grouped) {
+    r = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (r != cudaSuccess) e = r;
+  }
   r = cudaFuncSetAttribute(chol_kernel<F, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
   if (r != cudaSuccess) e = r;
   r = cudaFuncSetAttribute(chol_kernel<F, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
@@ -598,10 +694,10 @@ __device__ __forceinline__ float slice_sum(const float* p, size_t off, int ns, s
 // one warp per chain, lanes over coordinates.  *n_active is only a flag
 // (> 0 while some chain iterates): one plain store per block that has an
 // active chain, instead of an atomic per chain on one address.
-__global__ void update_kernel(UpdArgs a) {
+__device__ __forceinline__ void update_body(const UpdArgs& a, int bx) {
   pdl_wait();
   const int lane = threadIdx.x & 31;
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int c = (bx * blockDim.x + threadIdx.x) >> 5;
   bool act = false;
   if (a.mode >= UP_GLP0) {  // generalized leapfrog (grid-uniform)
     if (c < a.C && !(upd_iterated(a.mode) && !a.active[c])) {  // warp-uniform
@@ -776,14 +872,14 @@ constexpr int kStageEntries = 528; // packed entries of a factor with d = 32
 
 // Inactive chains (active set, flag 0) are skipped.
 template <typename T, int E>
-__global__ void __launch_bounds__(32 * kSolveWarps) solve_kernel(int C, int d, int P,
-                                                    const T* __restrict__ Lf,
-                                                    const double* __restrict__ rhs, double* u,
-                                                    SplitMat Ub, int split, const uint8_t* active) {
+__device__ __forceinline__ void solve_body(int C, int d, int P, const T* __restrict__ Lf,
+                                           const double* __restrict__ rhs, double* u,
+                                           const SplitMat& Ub, int split, const uint8_t* active,
+                                           int bx) {
   __shared__ T stage[E == 1 ? kSolveWarps * kStageEntries : 1];
   pdl_wait();
   const int lane = threadIdx.x & 31;
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int c = (bx * blockDim.x + threadIdx.x) >> 5;
   if (c >= C || (active && !active[c])) return;  // warp-uniform
   FactorStage<T, E> sg;
   if constexpr (E == 1) sg.buf = stage + (threadIdx.x >> 5) * kStageEntries;
@@ -812,13 +908,13 @@ __global__ void __launch_bounds__(32 * kSolveWarps) solve_kernel(int C, int d, i
 // Converged chains solve nothing, so the loop body that follows needs no
 // solve of its own.
 template <int E>
-__global__ void __launch_bounds__(32 * kSolveWarps) glp_update_solve_kernel(UpdArgs a,
-                                                                            const float* __restrict__ Lf,
-                                                                            int P, SplitMat Ub) {
+__device__ __forceinline__ void glp_update_solve_body(const UpdArgs& a,
+                                                      const float* __restrict__ Lf, int P,
+                                                      const SplitMat& Ub, int bx) {
   __shared__ float stage[E == 1 ? kSolveWarps * kStageEntries : 1];
   pdl_wait();
   const int lane = threadIdx.x & 31;
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int c = (bx * blockDim.x + threadIdx.x) >> 5;
   bool act = false;
   if (c < a.C && !(a.mode == UP_GLPN && !a.active[c])) {  // warp-uniform
     const int d = a.d;
@@ -875,9 +971,25 @@ __global__ void __launch_bounds__(32 * kSolveWarps) glp_update_solve_kernel(UpdA
   if (__syncthreads_or(act) && threadIdx.x == 0) *a.n_active = 1;
 }
 
-__global__ void begin_kernel(int C, int d, const float* pos, double* q0, double* qc, float* qf,
-                             SplitMat Qb, int* iters_total, uint8_t* notconv, uint8_t* bad) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+struct BeginArgs {
+  int C, d;
+  const float* pos;
+  double *q0, *qc;
+  float* qf;
+  SplitMat Qb;
+  int* iters_total;
+  uint8_t *notconv, *bad;
+};
+
+__device__ __forceinline__ void begin_body(const BeginArgs& a, int bx) {
+  const int C = a.C, d = a.d;
+  const float* pos = a.pos;
+  double *q0 = a.q0, *qc = a.qc;
+  float* qf = a.qf;
+  const SplitMat& Qb = a.Qb;
+  int* iters_total = a.iters_total;
+  uint8_t *notconv = a.notconv, *bad = a.bad;
+  const int c = bx * blockDim.x + threadIdx.x;
   if (c >= C) return;
   for (int i = 0; i < d; ++i) {
     const float q = pos[(size_t)c * d + i];
@@ -893,16 +1005,41 @@ __global__ void begin_kernel(int C, int d, const float* pos, double* q0, double*
 
 // Accept: H = −ℓ + ½pᵀG⁻¹p + ½ log det G + d/2 log 2π (rmhmc/metrics.py:60-74,
 // mcmc/metrics.py:160-166), ℓ at the proposal = data row sums + the prior.
-__global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q,
-                              const double* logdet0, const double* ldsum, const double* quad1,
-                              const double* logdet1, const double* uacc, double div_thr,
-                              const StepDev* spd, double prior_var, const double* qc,
-                              const float* Gout, int ldo, int gs, size_t gstride, float* pos,
-                              float* grad,
-                              double* logdens, InfoDev<float> info, const int* iters_total,
-                              const uint8_t* notconv, const uint8_t* bad) {
+struct AcceptArgs {
+  int C, d;
+  const double *ld0, *H0q, *logdet0, *ldsum, *quad1, *logdet1, *uacc;
+  double div_thr;
+  const StepDev* spd;
+  double prior_var;
+  const double* qc;
+  const float* Gout;
+  int ldo, gs;
+  size_t gstride;
+  float *pos, *grad;
+  double* logdens;
+  InfoDev<float> info;
+  const int* iters_total;
+  const uint8_t *notconv, *bad;
+};
+
+__device__ __forceinline__ void accept_body(const AcceptArgs& A, int bx) {
+  const int C = A.C, d = A.d;
+  const double *ld0 = A.ld0, *H0q = A.H0q, *logdet0 = A.logdet0, *ldsum = A.ldsum,
+               *quad1 = A.quad1, *logdet1 = A.logdet1, *uacc = A.uacc;
+  const double div_thr = A.div_thr;
+  const StepDev* spd = A.spd;
+  const double prior_var = A.prior_var;
+  const double* qc = A.qc;
+  const float* Gout = A.Gout;
+  const int ldo = A.ldo, gs = A.gs;
+  const size_t gstride = A.gstride;
+  float *pos = A.pos, *grad = A.grad;
+  double* logdens = A.logdens;
+  const InfoDev<float>& info = A.info;
+  const int* iters_total = A.iters_total;
+  const uint8_t *notconv = A.notconv, *bad = A.bad;
   pdl_wait();
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = bx * blockDim.x + threadIdx.x;
   if (c >= C) return;
   const double cst = 0.5 * d * kLog2Pi;
   double qq = 0.0;
@@ -930,6 +1067,89 @@ __global__ void accept_kernel(int C, int d, const double* ld0, const double* H0q
   if (info.status)
     info.status[c] = (notconv[c] ? GJ_CHAIN_FP_NOT_CONVERGED : 0u) |
                      (isfinite(H1) ? 0u : GJ_CHAIN_NONFINITE) | (bad[c] ? GJ_CHAIN_NOT_SPD : 0u);
+}
+
+// The pipeline's per-chain kernels: ordinary launches, and grouped launches
+// over items (one per posterior) in one grid.
+__global__ void update_kernel(UpdArgs a) { update_body(a, (int)blockIdx.x); }
+__global__ void update_grouped_kernel(const UpdArgs* __restrict__ items,
+                                      const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  update_body(items[i], (int)blockIdx.x - __ldg(prefix + i));
+}
+
+struct SolveItem {
+  int C, d, P;
+  const void* Lf;
+  const double* rhs;
+  double* u;
+  SplitMat Ub;
+  int split;
+  const uint8_t* active;
+};
+template <typename T, int E>
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    solve_kernel(int C, int d, int P, const T* __restrict__ Lf, const double* __restrict__ rhs,
+                 double* u, SplitMat Ub, int split, const uint8_t* active) {
+  solve_body<T, E>(C, d, P, Lf, rhs, u, Ub, split, active, (int)blockIdx.x);
+}
+template <typename T, int E>
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    solve_grouped_kernel(const SolveItem* __restrict__ items, const int* __restrict__ prefix,
+                         int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  const SolveItem& it = items[i];
+  solve_body<T, E>(it.C, it.d, it.P, static_cast<const T*>(it.Lf), it.rhs, it.u, it.Ub, it.split,
+                   it.active, (int)blockIdx.x - __ldg(prefix + i));
+}
+
+struct GlpItem {
+  UpdArgs a;
+  const float* Lf;
+  int P;
+  SplitMat Ub;
+};
+template <int E>
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    glp_update_solve_kernel(UpdArgs a, const float* __restrict__ Lf, int P, SplitMat Ub) {
+  glp_update_solve_body<E>(a, Lf, P, Ub, (int)blockIdx.x);
+}
+template <int E>
+__global__ void __launch_bounds__(32 * kSolveWarps)
+    glp_update_solve_grouped_kernel(const GlpItem* __restrict__ items,
+                                    const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  glp_update_solve_body<E>(items[i].a, items[i].Lf, items[i].P, items[i].Ub,
+                           (int)blockIdx.x - __ldg(prefix + i));
+}
+
+__global__ void begin_kernel(BeginArgs a) { begin_body(a, (int)blockIdx.x); }
+__global__ void begin_grouped_kernel(const BeginArgs* __restrict__ items,
+                                     const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  begin_body(items[i], (int)blockIdx.x - __ldg(prefix + i));
+}
+
+__global__ void accept_kernel(AcceptArgs a) { accept_body(a, (int)blockIdx.x); }
+__global__ void accept_grouped_kernel(const AcceptArgs* __restrict__ items,
+                                      const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  accept_body(items[i], (int)blockIdx.x - __ldg(prefix + i));
+}
+
+// zero fill of `words` 4-byte words (a grouped launch's memsets)
+struct ZeroItem {
+  uint32_t* p;
+  long long words;
+};
+constexpr int kZeroPerBlock = 4096;  // words per block of zero_grouped_kernel
+__global__ void zero_grouped_kernel(const ZeroItem* __restrict__ items,
+                                    const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  const ZeroItem it = items[i];
+  const long long w0 = (long long)((int)blockIdx.x - __ldg(prefix + i)) * kZeroPerBlock;
+  for (long long w = w0 + threadIdx.x; w < it.words && w < w0 + kZeroPerBlock; w += blockDim.x)
+    it.p[w] = 0u;
 }
 
 // Sets the WHILE condition of the fixed-point loop node: iterate while a
@@ -1236,6 +1456,56 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
 
 namespace {
 
+// A recorded launch of the pipeline.  A batch of posteriors records each
+// posterior's transition as such a list (the same list for every posterior
+// up to sizes and addresses), then replays the lists side by side: every
+// op becomes one grouped launch over the posteriors' items (one per kernel
+// variant present), every loop one conditional WHILE node for the batch.
+enum OpKind : int {
+  OP_GEMM,
+  OP_CHOL,
+  OP_SOLVE,
+  OP_UPDATE,
+  OP_GLPUS,
+  OP_BEGIN,
+  OP_ACCEPT,
+  OP_ZERO,
+  OP_FLAG_CLEAR,   // the active-chain flag := 0
+  OP_TRIPS_CLEAR,  // the loop trip counter := 0
+  OP_LOOP_BEGIN,   // condition kernel, then the WHILE node's body starts
+  OP_LOOP_END      // condition kernel at the end of the body
+};
+struct Op {
+  int kind = 0;
+  int variant = 0;  // kernel template selector
+  int blocks = 0;   // CTAs
+  int threads = 0;
+  size_t smem = 0;  // dynamic shared memory
+  std::vector<unsigned char> item;  // the kernel's item (argument struct) bytes
+};
+struct Recorder {
+  std::vector<Op> ops;
+  int* flag = nullptr;   // the batch's active-chain flag, shared by its posteriors
+  template <typename T>
+  void push(int kind, int variant, int blocks, int threads, size_t smem, const T& it) {
+    static_assert(std::is_trivially_copyable<T>::value, "items are copied as bytes");
+    Op o;
+    o.kind = kind;
+    o.variant = variant;
+    o.blocks = blocks;
+    o.threads = threads;
+    o.smem = smem;
+    o.item.resize(sizeof(T));
+    std::memcpy(o.item.data(), &it, sizeof(T));
+    ops.push_back(std::move(o));
+  }
+  void mark(int kind) {
+    Op o;
+    o.kind = kind;
+    ops.push_back(std::move(o));
+  }
+};
+
 struct Runner {
   LogregBatched* lb;
   int impl;
@@ -1243,6 +1513,34 @@ struct Runner {
   cudaError_t err = cudaSuccess;
   const StepDev* spd = nullptr;  // graph path: step parameters in device memory
   StepDev hsp{};                 // host path: the step parameters
+  Recorder* rec = nullptr;       // record instead of launching (grouped batches)
+  // inside a fixed-point loop body: contractions skip the tiles whose chains
+  // have all converged (their outputs are not read before the evaluation
+  // after the loop, which recomputes them)
+  bool loop_body = false;
+  const uint8_t* rows_active() const { return loop_body ? lb->active : nullptr; }
+
+  int* active_flag() const { return rec ? rec->flag : lb->n_active_d; }
+  // zero `bytes` (a multiple of 4) at p
+  void zero(void* p, size_t bytes) {
+    if (rec) {
+      ZeroItem z{static_cast<uint32_t*>(p), (long long)(bytes / 4)};
+      rec->push(OP_ZERO, 0, (int)((z.words + kZeroPerBlock - 1) / kZeroPerBlock), 256, 0, z);
+      return;
+    }
+    check(cudaMemsetAsync(p, 0, bytes, st));
+  }
+  // the transition's start: positions into the FP64 iterates and the split Q
+  void begin(const float* pos) {
+    LogregBatched& L = *lb;
+    BeginArgs b{L.C, L.d, pos, L.q0, L.qc, L.qf, L.Qb, L.iters_total, L.notconv, L.bad};
+    if (rec) {
+      rec->push(OP_BEGIN, 0, (L.C + 127) / 128, 128, 0, b);
+      return;
+    }
+    begin_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(b);
+    check(cudaGetLastError());
+  }
 
   void gemm(const SplitMat& A, const TcOperand* ta, const SplitMat& B, const TcOperand* tb, int M,
             int N, int K, const Epi& e, int ksplit = 1, int a_row0 = 0) {
@@ -1257,6 +1555,18 @@ struct Runner {
     g.pdl = lb->pdl != 0;
     g.ksplit = ksplit;
     g.a_row0 = a_row0;
+    if (rec) {
+      GemmItem it;
+      int variant = 0, blocks = 0;
+      size_t smem = 0;
+      g.pdl = false;
+      err = impl == 2 ? gemm_tc_describe(g, ta, tb, lb->tc_err, &it, &variant, &blocks, &smem)
+                      : cudaErrorNotSupported;
+      if (err == cudaSuccess) rec->push(OP_GEMM, variant, blocks, 320, smem, it);
+      lb->stats.gemm_launches++;
+      lb->stats.gemm_flops += 2.0 * M * N * K;
+      return;
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (lb->prof) {
       while (lb->ev.size() < lb->ev_used + 2) {
@@ -1301,6 +1611,7 @@ struct Runner {
     o.D = L.Gout + (size_t)row0 * L.dpad;
     o.ldd = L.dpad;
     o.d_slice = gstride();
+    if (M == L.C) o.active_rows = rows_active();  // output row m is chain m
     gemm(L.Rb, L.tRb, L.XTb, L.tXTb, M, L.d, L.N, o, gsplit(), row0);
   }
 
@@ -1317,11 +1628,13 @@ struct Runner {
     e.lp = L.Lp;
     e.lp_ld = L.Npad;
     e.r = L.Rb;
+    e.active_rows = rows_active();
     gemm(L.Qb, L.tQb, L.Xb, L.tXb, L.C, L.N, L.d, e);
     Epi g{};
     g.mode = EPI_STORE;
     g.D = L.Gv;
     g.ldd = L.Pp;
+    g.active_rows = rows_active();
     gemm(L.Lam, L.tLam, L.Zt, L.tZt, L.C, L.P, L.N, g);
   }
 
@@ -1389,8 +1702,14 @@ struct Runner {
     L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + solves * dd * dd);
     const CholCfg cf =
         chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
-    const int per_cta = cf.warps * cf.cpw;
+    const int per_cta = cf.chains;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
+    if (rec) {
+      if (a.q_update) a.n_active = rec->flag;
+      CholItem it{a, (int)cf.stride};
+      rec->push(OP_CHOL, (L.chol_fp64 ? 100 : 0) + cf.lpc, (int)grid.x, 32 * cf.warps, cf.smem, it);
+      return;
+    }
     // the dynamic shared-memory limit was raised at context creation
     check(L.chol_fp64 ? chol_launch<double>(cf, grid, a, L.pdl, st)
                       : chol_launch<float>(cf, grid, a, L.pdl, st));
@@ -1404,9 +1723,11 @@ struct Runner {
     s.mode = EPI_STORE;
     s.D = L.S;
     s.ldd = L.Npad;
+    s.active_rows = rows_active();
     gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
     Epi w{};
     w.mode = EPI_TRACE;
+    w.active_rows = rows_active();
     w.w_out = w_out;
     w.S = L.S;
     w.s_ld = L.Npad;
@@ -1429,6 +1750,12 @@ struct Runner {
     LogregBatched& L = *lb;
     // one warp per chain, kSolveWarps warps per block (the staging buffers)
     const dim3 th(32 * kSolveWarps), grid((unsigned)(((size_t)L.C + kSolveWarps - 1) / kSolveWarps));
+    if (rec) {
+      SolveItem it{L.C, L.d, L.P, Lf, rhs, out, L.Ub, split ? 1 : 0, act};
+      const int E = L.d <= 32 ? 1 : (L.d <= 64 ? 2 : 4);
+      rec->push(OP_SOLVE, (sizeof(T) == sizeof(double) ? 10 : 0) + E, (int)grid.x, (int)th.x, 0, it);
+      return;
+    }
     if (L.d <= 32)
       check(launch_k(L.pdl, solve_kernel<T, 1>, grid, th, 0, st, L.C, L.d, L.P, Lf, rhs, out,
                      L.Ub, split ? 1 : 0, act));
@@ -1483,9 +1810,13 @@ struct Runner {
       f.g2 = L.G2;
       f.g2_ld = L.dpad;
       f.g2_slice = (size_t)L.C * L.dpad;
+      f.active_rows = rows_active();
       gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, f);
       L.stats.gemm_flops += 2.0 * L.C * L.N * L.d;  // the in-kernel r₂·X MMAs
       L.stats.evals++;
+      // a grouped batch replays the posteriors' launch lists side by side:
+      // an empty launch stands where the stored form has its r₂·X GEMM
+      if (rec) rec->push(OP_GEMM, -1, 0, 320, 0, GemmItem{});
       return;
     }
     Epi s{};
@@ -1496,6 +1827,7 @@ struct Runner {
     s.lp_ld = L.Npad;
     s.r = L.Rb;
     s.r_off = L.C;
+    s.active_rows = rows_active();
     gemm(L.Ub, L.tUb, L.Xb, L.tXb, L.C, L.N, L.d, s);
     grad_gemm(L.C, L.C);
     L.stats.evals++;
@@ -1527,7 +1859,7 @@ struct Runner {
   // with vel_out, also the flipped proposal velocity −G⁻¹p
   void energy(float* vel_out) {
     LogregBatched& L = *lb;
-    check(cudaMemsetAsync(L.ldnew, 0, sizeof(double) * L.C, st));
+    zero(L.ldnew, sizeof(double) * L.C);
     metric_gram(L.ldnew);
     chol(CH_ENERGY, nullptr, L.logdet1, L.quad1, nullptr, false, vel_out);
     grad_gemm(0, L.C);
@@ -1536,10 +1868,15 @@ struct Runner {
   void accept(const double* ld0, const double* u, double div_thr, float* pos, float* grad,
               double* logdens, const InfoDev<float>& info) {
     LogregBatched& L = *lb;
-    accept_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(
-        L.C, L.d, ld0, L.quad0, L.logdet0, L.ldnew, L.quad1, L.logdet1, u, div_thr, spd,
-        L.t.p0, L.qc, L.Gout, L.dpad, gsplit(), gstride(), pos, grad, logdens, info,
-        L.iters_total, L.notconv, L.bad);
+    const AcceptArgs A{L.C,      L.d,         ld0,          L.quad0,   L.logdet0, L.ldnew,
+                       L.quad1,  L.logdet1,   u,            div_thr,   spd,       L.t.p0,
+                       L.qc,     L.Gout,      L.dpad,       gsplit(),  gstride(), pos,
+                       grad,     logdens,     info,         L.iters_total, L.notconv, L.bad};
+    if (rec) {
+      rec->push(OP_ACCEPT, 0, (L.C + 127) / 128, 128, 0, A);
+      return;
+    }
+    accept_kernel<<<(L.C + 127) / 128, 128, 0, st>>>(A);
     check(cudaGetLastError());
   }
 
@@ -1575,10 +1912,19 @@ struct Runner {
     a.active = L.active;
     a.notconv = L.notconv;
     a.Qb = L.Qb;
-    a.n_active = L.n_active_d;
+    a.n_active = active_flag();
     a.spd = spd;
     static_assert(32 * kSolveWarps == 256, "the fused update stages one factor per warp");
     const dim3 grid((unsigned)(((size_t)L.C * 32 + 255) / 256)), th(256);
+    if (rec) {
+      if (mode == UP_GLP0 || mode == UP_GLPN) {
+        GlpItem it{a, L.Lf32, L.P, L.Ub};
+        rec->push(OP_GLPUS, L.d <= 32 ? 1 : (L.d <= 64 ? 2 : 4), (int)grid.x, 256, 0, it);
+      } else {
+        rec->push(OP_UPDATE, 0, (int)grid.x, 256, 0, a);
+      }
+      return;
+    }
     if (mode == UP_GLP0 || mode == UP_GLPN) {  // with the next evaluation's solve
       if (L.d <= 32)
         check(launch_k(L.pdl, glp_update_solve_kernel<1>, grid, th, 0, st, a, L.Lf32, L.P, L.Ub));
@@ -1632,9 +1978,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   Runner R{lb, gemm_impl, st};
   R.hsp = sp;
   const int C = lb->C, d = lb->d;
-  begin_kernel<<<(C + 127) / 128, 128, 0, st>>>(C, d, pos, lb->q0, lb->qc, lb->qf, lb->Qb,
-                                                 lb->iters_total, lb->notconv, lb->bad);
-  R.check(cudaGetLastError());
+  R.begin(pos);
   // a fixed-point solve driven from the host: the eager update, then body +
   // update while some chain is active (at most max_iters + 1 bodies); with
   // iterated < 0 the body updates the iterate itself
@@ -1647,7 +1991,9 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
       R.check(cudaStreamSynchronize(st));
       if (R.err != cudaSuccess || *lb->n_active_h == 0 || guard > sp.max_iters) break;
       R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
+      R.loop_body = true;
       body();
+      R.loop_body = false;
       if (iterated >= 0) R.update(iterated, sp);
     }
   };
@@ -1686,9 +2032,11 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
       if (R.err != cudaSuccess) break;
       if (*lb->n_active_h == 0 || guard > sp.max_iters + 1) break;
       ++guard;
+      R.loop_body = true;
       R.metric_gram();
       R.chol(CH_EVAL, nullptr, lb->logdet1, lb->quad1, nullptr, true);
       R.trace_grad();
+      R.loop_body = false;
       R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), st));
       R.update(UP_FPN, sp);
       lb->stats.evals++;
@@ -1768,60 +2116,16 @@ int graph_cfg(const LogregBatched* lb) {
 // kernels read and write the context's staging buffers; step parameters come
 // from lb->spd.  With prop, the energy factorisation also writes the
 // proposal velocity.  Returns the first error (the capture stays open).
-cudaError_t capture_transition(LogregBatched* lb, int L, int impl, bool prop, bool gl,
-                               cudaStream_t s) {
-  const int C = lb->C, d = lb->d;
+// The transition's sequence of stages, shared by the capture of one
+// posterior's graph and the recording of a grouped batch: add_solve(eager,
+// body, iterated) emits one fixed-point solve (the eager update, then body +
+// the iterated update while some chain is active).
+template <typename AddSolve>
+cudaError_t transition_script(Runner& R, LogregBatched* lb, int L, bool prop, bool gl,
+                              AddSolve&& add_solve) {
   cudaError_t e = cudaSuccess;
-  Runner R{lb, impl, s};
-  R.spd = lb->spd;
-  begin_kernel<<<(C + 127) / 128, 128, 0, s>>>(C, d, lb->pos_s, lb->q0, lb->qc, lb->qf, lb->Qb,
-                                                lb->iters_total, lb->notconv, lb->bad);
   StepDev dummy{};
-  // one fixed-point solve: the eager update, then a conditional WHILE node
-  // whose body is `body` + the iterated update (none when iterated < 0: the
-  // body updates the iterate itself), repeated while some chain is active
-  // (at most max_iters + 1 times)
-  auto add_solve = [&](int eager, auto body, int iterated) -> cudaError_t {
-    R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), s));
-    R.update(eager, dummy);
-    R.check(cudaMemsetAsync(lb->trips, 0, sizeof(int), s));
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t cg = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t nd = 0;
-    cudaError_t r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    if (r != cudaSuccess) return r;
-    cudaGraphConditionalHandle h;
-    r = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
-    if (r != cudaSuccess) return r;
-    loop_cond_kernel<<<1, 1, 0, s>>>(h, lb->n_active_d, lb->trips, lb->spd);
-    r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    if (r != cudaSuccess) return r;
-    cudaGraphNodeParams np{};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    r = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
-    if (r != cudaSuccess) return r;
-    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
-    r = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-    if (r != cudaSuccess) return r;
-    r = cudaStreamBeginCaptureToGraph(lb->cap_body, bodyg, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal);
-    if (r != cudaSuccess) return r;
-    Runner B{lb, impl, lb->cap_body};
-    B.spd = lb->spd;
-    body(B);
-    if (iterated >= 0) B.update(iterated, dummy);
-    loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
-    B.check(cudaGetLastError());
-    cudaGraph_t bout = nullptr;
-    r = cudaStreamEndCapture(lb->cap_body, &bout);
-    if (r == cudaSuccess && B.err != cudaSuccess) r = B.err;
-    return r;
-  };
+  R.begin(lb->pos_s);
   for (int st = 0; st < L && R.err == cudaSuccess && e == cudaSuccess; ++st) {
     if (gl) {
       // generalized leapfrog: momentum solve at the fixed position, position
@@ -1874,6 +2178,83 @@ cudaError_t capture_transition(LogregBatched* lb, int L, int impl, bool prop, bo
   R.accept(lb->ld_s, lb->u_s, 0.0, lb->pos_s, lb->grad_s, lb->ld_s, inf);
   if (e == cudaSuccess) e = R.err;
   return e;
+}
+
+cudaError_t capture_transition(LogregBatched* lb, int L, int impl, bool prop, bool gl,
+                               cudaStream_t s) {
+  Runner R{lb, impl, s};
+  R.spd = lb->spd;
+  StepDev dummy{};
+  // one fixed-point solve: the eager update, then a conditional WHILE node
+  // whose body is `body` + the iterated update (none when iterated < 0: the
+  // body updates the iterate itself), repeated while some chain is active
+  // (at most max_iters + 1 times)
+  auto add_solve = [&](int eager, auto body, int iterated) -> cudaError_t {
+    R.check(cudaMemsetAsync(lb->n_active_d, 0, sizeof(int), s));
+    R.update(eager, dummy);
+    R.check(cudaMemsetAsync(lb->trips, 0, sizeof(int), s));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (r != cudaSuccess) return r;
+    cudaGraphConditionalHandle h;
+    r = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+    if (r != cudaSuccess) return r;
+    loop_cond_kernel<<<1, 1, 0, s>>>(h, lb->n_active_d, lb->trips, lb->spd);
+    r = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (r != cudaSuccess) return r;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    r = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+    if (r != cudaSuccess) return r;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    r = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (r != cudaSuccess) return r;
+    r = cudaStreamBeginCaptureToGraph(lb->cap_body, bodyg, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) return r;
+    Runner B{lb, impl, lb->cap_body};
+    B.spd = lb->spd;
+    B.loop_body = true;
+    body(B);
+    B.loop_body = false;
+    if (iterated >= 0) B.update(iterated, dummy);
+    loop_cond_kernel<<<1, 1, 0, lb->cap_body>>>(h, lb->n_active_d, lb->trips, lb->spd);
+    B.check(cudaGetLastError());
+    cudaGraph_t bout = nullptr;
+    r = cudaStreamEndCapture(lb->cap_body, &bout);
+    if (r == cudaSuccess && B.err != cudaSuccess) r = B.err;
+    return r;
+  };
+  return transition_script(R, lb, L, prop, gl, add_solve);
+}
+
+// Record one transition of one posterior as launches (grouped batches).
+cudaError_t record_transition(LogregBatched* lb, int L, int impl, bool prop, bool gl,
+                              Recorder* rec) {
+  Runner R{lb, impl, nullptr};
+  R.spd = lb->spd;
+  R.rec = rec;
+  StepDev dummy{};
+  auto add_solve = [&](int eager, auto body, int iterated) -> cudaError_t {
+    rec->mark(OP_FLAG_CLEAR);
+    R.update(eager, dummy);
+    rec->mark(OP_TRIPS_CLEAR);
+    rec->mark(OP_LOOP_BEGIN);
+    R.loop_body = true;
+    body(R);
+    R.loop_body = false;
+    if (iterated >= 0) R.update(iterated, dummy);
+    rec->mark(OP_LOOP_END);
+    return R.err;
+  };
+  return transition_script(R, lb, L, prop, gl, add_solve);
 }
 
 // Capture one whole transition into *out (its own graph).
@@ -2124,20 +2505,35 @@ struct LogregBatchGraph {
   int C = 0;
   BatchStage* stages = nullptr;  // device [B]
   cudaStream_t cap_root = nullptr;
+  cudaStream_t cap_body = nullptr;  // grouped: the WHILE bodies' capture
   cudaEvent_t fork = nullptr, join = nullptr;
+  int grouped = 0;       // logreg_batch_graph_set_grouped
+  int* flag = nullptr;   // grouped: the batch's active-chain flag
+  int* trips = nullptr;  // grouped: the batch's loop trip counter
   struct Entry {
     int L, impl, cfg, prop;
     cudaGraphExec_t exec;
     unsigned long long used;
+    std::vector<void*> bufs;  // grouped: the launches' items and prefix sums
   };
   std::vector<Entry> graphs;
   unsigned long long tick = 0;
 };
 
+static void free_entry(LogregBatchGraph::Entry& g) {
+  cudaGraphExecDestroy(g.exec);
+  for (void* p : g.bufs) cudaFree(p);
+  g.bufs.clear();
+}
+
+void logreg_batch_graph_set_grouped(LogregBatchGraph* bg, int on) { bg->grouped = on ? 1 : 0; }
+
 void logreg_batch_graph_destroy(LogregBatchGraph* bg) {
   if (!bg) return;
-  for (auto& g : bg->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& g : bg->graphs) free_entry(g);
   if (bg->stages) cudaFree(bg->stages);
+  if (bg->flag) cudaFree(bg->flag);
+  if (bg->cap_body) cudaStreamDestroy(bg->cap_body);
   if (bg->cap_root) cudaStreamDestroy(bg->cap_root);
   if (bg->fork) cudaEventDestroy(bg->fork);
   if (bg->join) cudaEventDestroy(bg->join);
@@ -2185,6 +2581,10 @@ int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const siz
   if (e == cudaSuccess)
     e = cudaMemcpy(bg->stages, hs.data(), sizeof(BatchStage) * (size_t)B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bg->cap_root, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bg->cap_body, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&bg->flag, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(bg->flag, 0, 2 * sizeof(int));
+  if (e == cudaSuccess) bg->trips = bg->flag + 1;
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
@@ -2228,6 +2628,238 @@ int batch_capture(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
   return GJ_OK;
 }
 
+// One grouped launch: the items of the posteriors whose op has this kernel
+// variant and block size, in device memory.
+struct GroupLaunch {
+  int kind, variant, threads, n, blocks;
+  size_t smem;
+  const void* items;
+  const int* prefix;
+};
+
+cudaError_t launch_group(const GroupLaunch& g, cudaStream_t s) {
+  if (g.blocks < 1) return cudaSuccess;
+  const dim3 grid((unsigned)g.blocks), th((unsigned)g.threads);
+  const int* pf = g.prefix;
+  const int n = g.n;
+  switch (g.kind) {
+    case OP_GEMM:
+      return gemm_tc_grouped(g.variant, static_cast<const GemmItem*>(g.items), pf, n, g.blocks,
+                             g.smem, s);
+    case OP_CHOL: {
+      const CholItem* it = static_cast<const CholItem*>(g.items);
+      switch (g.variant) {
+        case 104: chol_grouped_kernel<double, 4><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 108: chol_grouped_kernel<double, 8><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 116: chol_grouped_kernel<double, 16><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 132: chol_grouped_kernel<double, 32><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 228: chol_grouped_kernel<double, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 128: chol_grouped_kernel<float, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 4: chol_grouped_kernel<float, 4><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 8: chol_grouped_kernel<float, 8><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 16: chol_grouped_kernel<float, 16><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 32: chol_grouped_kernel<float, 32><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        default: return cudaErrorInvalidValue;
+      }
+      break;
+    }
+    case OP_SOLVE: {
+      const SolveItem* it = static_cast<const SolveItem*>(g.items);
+      switch (g.variant) {
+        case 1: solve_grouped_kernel<float, 1><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 2: solve_grouped_kernel<float, 2><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 4: solve_grouped_kernel<float, 4><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 11: solve_grouped_kernel<double, 1><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 12: solve_grouped_kernel<double, 2><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 14: solve_grouped_kernel<double, 4><<<grid, th, 0, s>>>(it, pf, n); break;
+        default: return cudaErrorInvalidValue;
+      }
+      break;
+    }
+    case OP_GLPUS: {
+      const GlpItem* it = static_cast<const GlpItem*>(g.items);
+      switch (g.variant) {
+        case 1: glp_update_solve_grouped_kernel<1><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 2: glp_update_solve_grouped_kernel<2><<<grid, th, 0, s>>>(it, pf, n); break;
+        case 4: glp_update_solve_grouped_kernel<4><<<grid, th, 0, s>>>(it, pf, n); break;
+        default: return cudaErrorInvalidValue;
+      }
+      break;
+    }
+    case OP_UPDATE:
+      update_grouped_kernel<<<grid, th, 0, s>>>(static_cast<const UpdArgs*>(g.items), pf, n);
+      break;
+    case OP_BEGIN:
+      begin_grouped_kernel<<<grid, th, 0, s>>>(static_cast<const BeginArgs*>(g.items), pf, n);
+      break;
+    case OP_ACCEPT:
+      accept_grouped_kernel<<<grid, th, 0, s>>>(static_cast<const AcceptArgs*>(g.items), pf, n);
+      break;
+    case OP_ZERO:
+      zero_grouped_kernel<<<grid, th, 0, s>>>(static_cast<const ZeroItem*>(g.items), pf, n);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+bool is_kernel_op(int kind) { return kind <= OP_ZERO; }
+
+// The whole batch as grouped launches: every posterior's transition is
+// recorded as a list of launches (the lists match op by op: same stages,
+// same loops), then each op runs as one grid per kernel variant over all
+// posteriors, and each fixed-point solve as one WHILE node whose condition
+// is the batch's shared active-chain flag.  A posterior whose chains have
+// all converged runs the loop's remaining bodies without changing state:
+// the updates and factorisations skip inactive chains, and the
+// contractions recompute the same values from unchanged inputs.
+int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
+                          cudaGraphExec_t* out, std::vector<void*>* bufs) {
+  *out = nullptr;
+  if (impl != 2) {
+    g_err = "grouped batch launches need the tcgen05 GEMM path";
+    return GJ_ENOTSUP;
+  }
+  const int B = (int)bg->lbs.size();
+  std::vector<Recorder> recs(B);
+  for (int b = 0; b < B; ++b) {
+    recs[b].flag = bg->flag;
+    const cudaError_t e = record_transition(bg->lbs[b], L, impl, prop, gl, &recs[b]);
+    if (e != cudaSuccess) return graph_fail("batch record", e);
+  }
+  const size_t nops = recs[0].ops.size();
+  for (int b = 1; b < B; ++b) {
+    bool same = recs[b].ops.size() == nops;
+    for (size_t i = 0; same && i < nops; ++i)
+      same = recs[b].ops[i].kind == recs[0].ops[i].kind &&
+             recs[b].ops[i].item.size() == recs[0].ops[i].item.size();
+    if (!same) {
+      g_err = "grouped batch: the posteriors' transitions differ in structure";
+      return GJ_EINVAL;
+    }
+  }
+  // the grouped launches of every op, their items uploaded before the capture
+  std::vector<std::vector<GroupLaunch>> plan(nops);
+  auto fail_alloc = [&](cudaError_t e) { return graph_fail("batch items", e); };
+  for (size_t i = 0; i < nops; ++i) {
+    if (!is_kernel_op(recs[0].ops[i].kind)) continue;
+    std::vector<int> order(B);
+    for (int b = 0; b < B; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      const Op &ox = recs[x].ops[i], &oy = recs[y].ops[i];
+      return ox.variant != oy.variant ? ox.variant < oy.variant : ox.threads < oy.threads;
+    });
+    const size_t isz = recs[0].ops[i].item.size();
+    for (size_t k = 0; k < order.size();) {
+      const Op& o0 = recs[order[k]].ops[i];
+      size_t k1 = k;
+      std::vector<unsigned char> items;
+      std::vector<int> prefix(1, 0);
+      GroupLaunch g{o0.kind, o0.variant, o0.threads, 0, 0, 0, nullptr, nullptr};
+      while (k1 < order.size() && recs[order[k1]].ops[i].variant == o0.variant &&
+             recs[order[k1]].ops[i].threads == o0.threads) {
+        const Op& o = recs[order[k1]].ops[i];
+        items.insert(items.end(), o.item.begin(), o.item.end());
+        prefix.push_back(prefix.back() + o.blocks);
+        g.smem = std::max(g.smem, o.smem);
+        ++k1;
+      }
+      g.n = (int)(k1 - k);
+      g.blocks = prefix.back();
+      void* di = nullptr;
+      void* dp = nullptr;
+      cudaError_t e = cudaMalloc(&di, isz * (size_t)g.n);
+      if (e == cudaSuccess) bufs->push_back(di);
+      if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(int) * prefix.size());
+      if (e == cudaSuccess) bufs->push_back(dp);
+      if (e == cudaSuccess) e = cudaMemcpy(di, items.data(), items.size(), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(dp, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail_alloc(e);
+      g.items = di;
+      g.prefix = static_cast<const int*>(dp);
+      plan[i].push_back(g);
+      k = k1;
+    }
+  }
+  const StepDev* spd = bg->lbs[0]->spd;  // every posterior gets the same step parameters
+  cudaStream_t root = bg->cap_root, cur = root;
+  cudaError_t e = cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return graph_fail("grouped begin", e);
+  cudaGraphConditionalHandle h{};
+  for (size_t i = 0; i < nops && e == cudaSuccess; ++i) {
+    const int kind = recs[0].ops[i].kind;
+    if (is_kernel_op(kind)) {
+      for (const GroupLaunch& g : plan[i])
+        if (e == cudaSuccess) e = launch_group(g, cur);
+      continue;
+    }
+    if (kind == OP_FLAG_CLEAR) {
+      e = cudaMemsetAsync(bg->flag, 0, sizeof(int), cur);
+    } else if (kind == OP_TRIPS_CLEAR) {
+      e = cudaMemsetAsync(bg->trips, 0, sizeof(int), cur);
+    } else if (kind == OP_LOOP_BEGIN) {
+      if (cur != root) {
+        e = cudaErrorInvalidValue;  // loops do not nest
+        break;
+      }
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t cg = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(root, &cs, nullptr, &cg, &deps, nullptr, &nd);
+      if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+      if (e != cudaSuccess) break;
+      loop_cond_kernel<<<1, 1, 0, root>>>(h, bg->flag, bg->trips, spd);
+      e = cudaStreamGetCaptureInfo(root, &cs, nullptr, &cg, &deps, nullptr, &nd);
+      if (e != cudaSuccess) break;
+      cudaGraphNodeParams np{};
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+      if (e == cudaSuccess)
+        e = cudaStreamUpdateCaptureDependencies(root, &node, nullptr, 1,
+                                                cudaStreamSetCaptureDependencies);
+      if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(bg->cap_body, np.conditional.phGraph_out[0], nullptr,
+                                          nullptr, 0, cudaStreamCaptureModeThreadLocal);
+      cur = bg->cap_body;
+    } else if (kind == OP_LOOP_END) {
+      if (cur != bg->cap_body) {
+        e = cudaErrorInvalidValue;
+        break;
+      }
+      loop_cond_kernel<<<1, 1, 0, cur>>>(h, bg->flag, bg->trips, spd);
+      e = cudaGetLastError();
+      cudaGraph_t bout = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(bg->cap_body, &bout);
+      if (e == cudaSuccess) e = e2;
+      cur = root;
+    }
+  }
+  if (cur != root) {  // an error inside a loop body: close its capture
+    cudaGraph_t bout = nullptr;
+    cudaStreamEndCapture(bg->cap_body, &bout);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(root, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return graph_fail("grouped capture", e != cudaSuccess ? e : e2);
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return graph_fail("grouped instantiate", e);
+  }
+  return GJ_OK;
+}
+
 }  // namespace
 
 int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos, float* grad,
@@ -2246,7 +2878,7 @@ int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos,
     lb->stats = LogregStats{};
   }
   const bool prop = info.prop_v != nullptr;
-  const int cfg = graph_cfg(bg->lbs[0]) + (gl ? (1 << 20) : 0);
+  const int cfg = graph_cfg(bg->lbs[0]) + (gl ? (1 << 20) : 0) + (bg->grouped ? (1 << 21) : 0);
   cudaGraphExec_t exec = nullptr;
   for (auto& g : bg->graphs)
     if (g.L == sp.L && g.impl == gemm_impl && g.cfg == cfg && g.prop == (int)prop) {
@@ -2260,12 +2892,18 @@ int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos,
       size_t lru = 0;
       for (size_t i = 1; i < bg->graphs.size(); ++i)
         if (bg->graphs[i].used < bg->graphs[lru].used) lru = i;
-      cudaGraphExecDestroy(bg->graphs[lru].exec);
+      free_entry(bg->graphs[lru]);
       bg->graphs.erase(bg->graphs.begin() + lru);
     }
-    const int rc = batch_capture(bg, sp.L, gemm_impl, prop, gl, &exec);
-    if (rc) return rc;
-    bg->graphs.push_back({sp.L, gemm_impl, cfg, (int)prop, exec, ++bg->tick});
+    std::vector<void*> bufs;
+    const int rc = bg->grouped
+                       ? batch_capture_grouped(bg, sp.L, gemm_impl, prop, gl, &exec, &bufs)
+                       : batch_capture(bg, sp.L, gemm_impl, prop, gl, &exec);
+    if (rc) {
+      for (void* p : bufs) cudaFree(p);
+      return rc;
+    }
+    bg->graphs.push_back({sp.L, gemm_impl, cfg, (int)prop, exec, ++bg->tick, std::move(bufs)});
   }
   const int B = (int)bg->lbs.size();
   batch_gather_kernel<<<B, 256, 0, st>>>(bg->stages, bg->C, sp, pos, grad, logdens, z, u);

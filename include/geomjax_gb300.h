@@ -253,9 +253,13 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
 #define GJ_OPT_GEMM_KSPLIT 8
 /* batches of posteriors (gj_batch_set_option): 1 (default) = one CUDA graph
  * per transition holding every posterior's transition as an independent
- * branch, launched once (plus one gather and one scatter kernel); 0 = one
- * graph per posterior, spread over the batch's stream pool.  Results are
- * bit-identical either way. */
+ * branch, launched once (plus one gather and one scatter kernel); 2 = one
+ * CUDA graph per transition of grouped launches: every stage of the
+ * transition is one grid (per kernel variant) over all posteriors, whose
+ * blocks find their posterior in a list of per-posterior items, and every
+ * fixed-point solve one WHILE node for the batch (tcgen05 GEMM path);
+ * 0 = one graph per posterior, spread over the batch's stream pool.
+ * Results are bit-identical in every mode. */
 #define GJ_OPT_BATCH_GRAPH 9
 /* LMC-Monge (funnel and hierarchical Gaussian, d <= 256): 1 (default) = one
  * warp per chain in either precision (float64 throughout for GJ_FP64),

@@ -1,7 +1,8 @@
 """Batches of uneven logistic-regression posteriors (``gj_batch_*``): every
 posterior's chains follow the oracle step by step, and the batch (one CUDA
-graph holding every posterior as a branch, or one graph per posterior on a
-stream pool) is bit-identical to running each posterior on its own."""
+graph holding every posterior as a branch, one CUDA graph of grouped
+launches over all posteriors, or one graph per posterior on a stream pool)
+is bit-identical to running each posterior on its own."""
 import numpy as np
 import pytest
 
@@ -70,14 +71,14 @@ def test_batch_matches_oracle_per_posterior(integrator):
             assert rel_err(eb, oi.energy) < 1e-4, (b, L)
 
 
-@pytest.mark.parametrize("one_graph", [True, False])
-def test_batch_bitwise_equals_single_posterior_runs(one_graph):
+@pytest.mark.parametrize("one_graph,grouped", [(True, False), (True, True), (False, False)])
+def test_batch_bitwise_equals_single_posterior_runs(one_graph, grouped):
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
     from geomjax_gb300.batch import PosteriorBatch
 
     data = _data()
-    pb = PosteriorBatch(data, C, num_streams=4, one_graph=one_graph)
+    pb = PosteriorBatch(data, C, num_streams=4, one_graph=one_graph, grouped=grouped)
     q0 = _starts()
     zs, us = _draws(11)
     st = pb.init(q0)
@@ -97,16 +98,18 @@ def test_batch_bitwise_equals_single_posterior_runs(one_graph):
 
 @pytest.mark.parametrize("integrator", ["implicit_midpoint", "generalized_leapfrog"])
 def test_batch_one_graph_reused_across_calls(integrator):
-    """The one-graph batch over three transitions (the graph captured at the
-    first is reused, the step size changes between calls, the state arrays
-    move) equals the stream-pool batch bit for bit, info included."""
+    """The one-graph batch, as branches and as grouped launches, over three
+    transitions (the graph captured at the first is reused, the step size
+    changes between calls, the state arrays move) equals the stream-pool
+    batch bit for bit, info included."""
     import torch
     from geomjax_gb300.batch import PosteriorBatch
 
     data = _data()
     outs = []
-    for one in (True, False):
-        pb = PosteriorBatch(data, C, num_streams=3, one_graph=one, integrator=integrator)
+    for one, grouped in ((True, False), (True, True), (False, False)):
+        pb = PosteriorBatch(data, C, num_streams=3, one_graph=one, grouped=grouped,
+                            integrator=integrator)
         st = pb.init(_starts())
         info = pb.new_info()
         g = torch.Generator(device="cuda").manual_seed(5)
@@ -121,6 +124,7 @@ def test_batch_one_graph_reused_across_calls(integrator):
                        [_np(info[k]) for k in ("acceptance_rate", "is_accepted", "energy",
                                                "fp_iters", "status", "momentum")])
         outs.append(rec)
-    for a, b in zip(*outs):
-        for x, y in zip(a, b):
-            np.testing.assert_array_equal(x, y)
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y)
