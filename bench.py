@@ -415,7 +415,8 @@ def run_batch(args, wl):
     t_setup = time.perf_counter()
     data = [logreg_data(int(n), int(d), seed=1000 * rank + i) for i, (n, d) in enumerate(zip(Ns, ds))]
     pb = PosteriorBatch(data, C, num_streams=args.streams, device=dev, integrator=args.integrator,
-                        one_graph=not args.batch_pool, grouped=args.batch_grouped)
+                        one_graph=not args.batch_pool, grouped=not args.batch_branches,
+                        buckets=args.batch_buckets)
     if args.cholesky == "fp32":
         pb.set_option(L.GJ_OPT_CHOL_FP64, 0)
     del data
@@ -487,10 +488,13 @@ def run_batch(args, wl):
         "config": {"workload": wl["name"], "posteriors": B, "chains_per_posterior": C,
                    "integration_steps": Lsteps, "step_size": h, "streams": args.streams,
                    "launch": ("one graph per posterior on the stream pool" if args.batch_pool else
-                              ("one CUDA graph per transition of grouped launches (every stage "
-                               "one grid over all posteriors)" if args.batch_grouped else
-                               "one CUDA graph per transition, every posterior a branch")),
+                              ("one CUDA graph per transition, every posterior a branch"
+                               if args.batch_branches else
+                               "one CUDA graph per transition of grouped launches: every stage "
+                               "one grid over a bucket of posteriors, each bucket a branch")),
                    "cholesky": args.cholesky,
+                   "buckets": None if (args.batch_branches or args.batch_pool) else
+                              (args.batch_buckets or "auto"),
                    "mean_N": float(np.mean(Ns)), "mean_d": float(np.mean(ds)),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{ws}", "autotune": tuned},
@@ -1116,8 +1120,11 @@ def main():
     ap.add_argument("--groups", type=int, default=0,
                     help="chain groups on concurrent streams (0 = automatic)")
     ap.add_argument("--streams", type=int, default=16, help="stream pool of the uneven batch")
-    ap.add_argument("--batch-grouped", action="store_true",
-                    help="uneven batch: grouped launches (every stage one grid over all posteriors)")
+    ap.add_argument("--batch-branches", action="store_true",
+                    help="uneven batch: every posterior its own branch of the graph "
+                         "(default: grouped launches over buckets of posteriors)")
+    ap.add_argument("--batch-buckets", type=int, default=0,
+                    help="uneven batch, grouped launches: buckets of posteriors (0 = automatic)")
     ap.add_argument("--batch-pool", action="store_true",
                     help="uneven batch: one graph per posterior on the stream pool instead of one "
                          "graph holding every posterior")

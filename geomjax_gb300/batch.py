@@ -55,7 +55,7 @@ class PosteriorBatch:
                  num_streams: int = 16, max_iters: int = 100, tol: float = 1e-6,
                  divergence_threshold: float = 1000.0, device="cuda",
                  integrator: str = "implicit_midpoint", one_graph: bool = True,
-                 grouped: bool = False):
+                 grouped: bool = True, buckets: int = 0):
         self.lib = L.lib()
         self.device = torch.device(device)
         self.targets = [logistic_regression(X, y, prior_var=prior_var, precision="mixed",
@@ -74,10 +74,13 @@ class PosteriorBatch:
         L.check(self.lib.gj_batch_create(ctypes.cast(descs, ctypes.c_void_p), self.B, self.C,
                                          int(num_streams), ctypes.byref(h)))
         self.h = h
-        # one CUDA graph for the whole batch (every posterior a branch, or with
-        # ``grouped`` every stage one grid over all posteriors), or one graph
-        # per posterior on the stream pool
+        # one CUDA graph for the whole batch (with ``grouped``, the default,
+        # every stage one grid over a bucket of posteriors, each bucket a
+        # branch; otherwise every posterior a branch), or one graph per
+        # posterior on the stream pool
         self.set_option(L.GJ_OPT_BATCH_GRAPH, (2 if grouped else 1) if one_graph else 0)
+        if buckets:
+            self.set_option(L.GJ_OPT_BATCH_BUCKETS, int(buckets))
 
     def __del__(self):
         if getattr(self, "h", None) is not None and self.h.value:

@@ -736,6 +736,7 @@ int32_t gj_chees_statistics(int32_t precision, int32_t num_chains, int32_t dim,
 struct gj_batch {
   int B, C, S;
   int one_graph;  // GJ_OPT_BATCH_GRAPH: 0 stream pool, 1 a branch per posterior, 2 grouped
+  int buckets;    // GJ_OPT_BATCH_BUCKETS (0 = automatic)
   gj::LogregBatchGraph* bg;
   std::vector<gj::LogregBatched*> lbs;
   std::vector<int> dims;
@@ -779,7 +780,8 @@ int32_t gj_batch_create(const gj_target* targets, int32_t num_posteriors,
   if (!b) return fail(GJ_ENOMEM, "host allocation failed");
   b->B = num_posteriors;
   b->C = chains_per_posterior;
-  b->one_graph = 1;
+  b->one_graph = 2;
+  b->buckets = 0;
   b->bg = nullptr;
   b->S = num_streams < num_posteriors ? num_streams : num_posteriors;
   b->fork = nullptr;
@@ -841,10 +843,16 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
     for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_fuse_r2x(lb, (int)value);
     return GJ_OK;
   }
+  if (key == GJ_OPT_BATCH_BUCKETS) {
+    if (value < 0 || value > 256) return fail(GJ_EINVAL, "batch buckets must be 0 (automatic) .. 256");
+    b->buckets = (int)value;
+    if (b->bg) gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2, b->buckets);
+    return GJ_OK;
+  }
   if (key == GJ_OPT_BATCH_GRAPH) {
     if (value < 0 || value > 2) return fail(GJ_EINVAL, "batch graph mode must be 0, 1 or 2");
     b->one_graph = (int)value;
-    if (b->bg) gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2);
+    if (b->bg) gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2, b->buckets);
     return GJ_OK;
   }
   return fail(GJ_EINVAL, "unknown batch option");
@@ -867,7 +875,7 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
       const int rc = gj::logreg_batch_graph_create(b->lbs.data(), b->B, b->C, b->pos_off.data(),
                                                    &b->bg);
       if (rc) return fail(rc, "%s", gj::logreg_batched_error());
-      gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2);
+      gj::logreg_batch_graph_set_grouped(b->bg, b->one_graph == 2, b->buckets);
     }
     const int rc = gj::logreg_batch_graph_step(b->bg, sp, (float*)s->position,
                                                (float*)s->logdensity_grad, s->logdensity, z, u,

@@ -2497,6 +2497,17 @@ __global__ void batch_scatter_kernel(const BatchStage* S, int C, float* pos, flo
 }
 
 constexpr size_t kMaxBatchGraphs = 8;
+constexpr int kMaxBuckets = 256;  // grouped batches: most buckets of posteriors
+
+// One grouped launch: the items of the posteriors whose op has this kernel
+// variant and block size, in device memory.
+struct GroupLaunch {
+  int kind, variant, threads, n, blocks;
+  size_t smem;
+  const void* items;
+  const int* prefix;
+};
+
 
 }  // namespace
 
@@ -2508,8 +2519,17 @@ struct LogregBatchGraph {
   cudaStream_t cap_body = nullptr;  // grouped: the WHILE bodies' capture
   cudaEvent_t fork = nullptr, join = nullptr;
   int grouped = 0;       // logreg_batch_graph_set_grouped
-  int* flag = nullptr;   // grouped: the batch's active-chain flag
-  int* trips = nullptr;  // grouped: the batch's loop trip counter
+  int buckets = 0;       // grouped: buckets of posteriors (0 = automatic)
+  int* flag = nullptr;   // grouped: each bucket's active-chain flag and trip counter
+                         // (kMaxBuckets pairs, allocated once: captured graphs keep them)
+  std::vector<cudaStream_t> bucket_main, bucket_body;  // grouped: capture streams
+  struct Pending {  // a recorded bucket, between its recording and its capture
+    std::vector<std::vector<GroupLaunch>> plan;
+    std::vector<int> kinds;
+    int* flag;
+    int* trips;
+  };
+  std::vector<Pending> pending;
   struct Entry {
     int L, impl, cfg, prop;
     cudaGraphExec_t exec;
@@ -2526,13 +2546,18 @@ static void free_entry(LogregBatchGraph::Entry& g) {
   g.bufs.clear();
 }
 
-void logreg_batch_graph_set_grouped(LogregBatchGraph* bg, int on) { bg->grouped = on ? 1 : 0; }
+void logreg_batch_graph_set_grouped(LogregBatchGraph* bg, int on, int buckets) {
+  bg->grouped = on ? 1 : 0;
+  bg->buckets = buckets > 0 ? buckets : 0;
+}
 
 void logreg_batch_graph_destroy(LogregBatchGraph* bg) {
   if (!bg) return;
   for (auto& g : bg->graphs) free_entry(g);
   if (bg->stages) cudaFree(bg->stages);
   if (bg->flag) cudaFree(bg->flag);
+  for (cudaStream_t x : bg->bucket_main) cudaStreamDestroy(x);
+  for (cudaStream_t x : bg->bucket_body) cudaStreamDestroy(x);
   if (bg->cap_body) cudaStreamDestroy(bg->cap_body);
   if (bg->cap_root) cudaStreamDestroy(bg->cap_root);
   if (bg->fork) cudaEventDestroy(bg->fork);
@@ -2582,9 +2607,8 @@ int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const siz
     e = cudaMemcpy(bg->stages, hs.data(), sizeof(BatchStage) * (size_t)B, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bg->cap_root, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bg->cap_body, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&bg->flag, 2 * sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(bg->flag, 0, 2 * sizeof(int));
-  if (e == cudaSuccess) bg->trips = bg->flag + 1;
+  if (e == cudaSuccess) e = cudaMalloc(&bg->flag, 2 * sizeof(int) * kMaxBuckets);
+  if (e == cudaSuccess) e = cudaMemset(bg->flag, 0, 2 * sizeof(int) * kMaxBuckets);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bg->join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
@@ -2627,15 +2651,6 @@ int batch_capture(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
   }
   return GJ_OK;
 }
-
-// One grouped launch: the items of the posteriors whose op has this kernel
-// variant and block size, in device memory.
-struct GroupLaunch {
-  int kind, variant, threads, n, blocks;
-  size_t smem;
-  const void* items;
-  const int* prefix;
-};
 
 cudaError_t launch_group(const GroupLaunch& g, cudaStream_t s) {
   if (g.blocks < 1) return cudaSuccess;
@@ -2706,27 +2721,37 @@ cudaError_t launch_group(const GroupLaunch& g, cudaStream_t s) {
 
 bool is_kernel_op(int kind) { return kind <= OP_ZERO; }
 
-// The whole batch as grouped launches: every posterior's transition is
-// recorded as a list of launches (the lists match op by op: same stages,
-// same loops), then each op runs as one grid per kernel variant over all
-// posteriors, and each fixed-point solve as one WHILE node whose condition
-// is the batch's shared active-chain flag.  A posterior whose chains have
-// all converged runs the loop's remaining bodies without changing state:
-// the updates and factorisations skip inactive chains, and the
-// contractions recompute the same values from unchanged inputs.
-int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
-                          cudaGraphExec_t* out, std::vector<void*>* bufs) {
-  *out = nullptr;
-  if (impl != 2) {
-    g_err = "grouped batch launches need the tcgen05 GEMM path";
-    return GJ_ENOTSUP;
+// One bucket of posteriors as grouped launches: every posterior's transition
+// is recorded as a list of launches (the lists match op by op: same stages,
+// same loops), then each op becomes one grid per kernel variant over the
+// bucket's posteriors, and each fixed-point solve one WHILE node whose
+// condition is the bucket's shared active-chain flag.  A posterior whose
+// chains have all converged runs the loop's remaining bodies without
+// changing state: the updates and factorisations skip inactive chains, and
+// the contractions skip tiles with no active chain.  The items are uploaded
+// here; emit_bucket records the launches into a capture.
+// capture streams for nb buckets (their flags are allocated with the batch)
+cudaError_t ensure_buckets(LogregBatchGraph* bg, int nb) {
+  cudaError_t e = cudaSuccess;
+  while ((int)bg->bucket_main.size() < nb && e == cudaSuccess) {
+    cudaStream_t a = nullptr, b = nullptr;
+    e = cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking);
+    if (a) bg->bucket_main.push_back(a);
+    if (b) bg->bucket_body.push_back(b);
   }
-  const int B = (int)bg->lbs.size();
+  return e;
+}
+
+cudaError_t capture_bucket(LogregBatchGraph* bg, const std::vector<int>& members, int* flag,
+                           int* trips, int L, int impl, bool prop, bool gl,
+                           std::vector<void*>* bufs) {
+  const int B = (int)members.size();
   std::vector<Recorder> recs(B);
   for (int b = 0; b < B; ++b) {
-    recs[b].flag = bg->flag;
-    const cudaError_t e = record_transition(bg->lbs[b], L, impl, prop, gl, &recs[b]);
-    if (e != cudaSuccess) return graph_fail("batch record", e);
+    recs[b].flag = flag;
+    const cudaError_t e = record_transition(bg->lbs[members[b]], L, impl, prop, gl, &recs[b]);
+    if (e != cudaSuccess) return e;
   }
   const size_t nops = recs[0].ops.size();
   for (int b = 1; b < B; ++b) {
@@ -2734,14 +2759,10 @@ int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool
     for (size_t i = 0; same && i < nops; ++i)
       same = recs[b].ops[i].kind == recs[0].ops[i].kind &&
              recs[b].ops[i].item.size() == recs[0].ops[i].item.size();
-    if (!same) {
-      g_err = "grouped batch: the posteriors' transitions differ in structure";
-      return GJ_EINVAL;
-    }
+    if (!same) return cudaErrorInvalidValue;  // the transitions differ in structure
   }
   // the grouped launches of every op, their items uploaded before the capture
   std::vector<std::vector<GroupLaunch>> plan(nops);
-  auto fail_alloc = [&](cudaError_t e) { return graph_fail("batch items", e); };
   for (size_t i = 0; i < nops; ++i) {
     if (!is_kernel_op(recs[0].ops[i].kind)) continue;
     std::vector<int> order(B);
@@ -2776,43 +2797,48 @@ int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool
       if (e == cudaSuccess) e = cudaMemcpy(di, items.data(), items.size(), cudaMemcpyHostToDevice);
       if (e == cudaSuccess)
         e = cudaMemcpy(dp, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) return fail_alloc(e);
+      if (e != cudaSuccess) return e;
       g.items = di;
       g.prefix = static_cast<const int*>(dp);
       plan[i].push_back(g);
       k = k1;
     }
   }
-  const StepDev* spd = bg->lbs[0]->spd;  // every posterior gets the same step parameters
-  cudaStream_t root = bg->cap_root, cur = root;
-  cudaError_t e = cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return graph_fail("grouped begin", e);
+  bg->pending.push_back({std::move(plan), std::vector<int>(), flag, trips});
+  auto& pk = bg->pending.back();
+  pk.kinds.reserve(nops);
+  for (size_t i = 0; i < nops; ++i) pk.kinds.push_back(recs[0].ops[i].kind);
+  return cudaSuccess;
+}
+
+// Emit one recorded bucket into the capture stream s (loop bodies on sb).
+cudaError_t emit_bucket(const LogregBatchGraph::Pending& pk, const StepDev* spd, cudaStream_t s,
+                        cudaStream_t sb) {
+  cudaStream_t cur = s;
+  cudaError_t e = cudaSuccess;
   cudaGraphConditionalHandle h{};
-  for (size_t i = 0; i < nops && e == cudaSuccess; ++i) {
-    const int kind = recs[0].ops[i].kind;
+  for (size_t i = 0; i < pk.kinds.size() && e == cudaSuccess; ++i) {
+    const int kind = pk.kinds[i];
     if (is_kernel_op(kind)) {
-      for (const GroupLaunch& g : plan[i])
+      for (const GroupLaunch& g : pk.plan[i])
         if (e == cudaSuccess) e = launch_group(g, cur);
       continue;
     }
     if (kind == OP_FLAG_CLEAR) {
-      e = cudaMemsetAsync(bg->flag, 0, sizeof(int), cur);
+      e = cudaMemsetAsync(pk.flag, 0, sizeof(int), cur);
     } else if (kind == OP_TRIPS_CLEAR) {
-      e = cudaMemsetAsync(bg->trips, 0, sizeof(int), cur);
+      e = cudaMemsetAsync(pk.trips, 0, sizeof(int), cur);
     } else if (kind == OP_LOOP_BEGIN) {
-      if (cur != root) {
-        e = cudaErrorInvalidValue;  // loops do not nest
-        break;
-      }
+      if (cur != s) return cudaErrorInvalidValue;  // loops do not nest
       cudaStreamCaptureStatus cs;
       cudaGraph_t cg = nullptr;
       const cudaGraphNode_t* deps = nullptr;
       size_t nd = 0;
-      e = cudaStreamGetCaptureInfo(root, &cs, nullptr, &cg, &deps, nullptr, &nd);
+      e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
       if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
       if (e != cudaSuccess) break;
-      loop_cond_kernel<<<1, 1, 0, root>>>(h, bg->flag, bg->trips, spd);
-      e = cudaStreamGetCaptureInfo(root, &cs, nullptr, &cg, &deps, nullptr, &nd);
+      loop_cond_kernel<<<1, 1, 0, s>>>(h, pk.flag, pk.trips, spd);
+      e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
       if (e != cudaSuccess) break;
       cudaGraphNodeParams np{};
       np.type = cudaGraphNodeTypeConditional;
@@ -2822,29 +2848,83 @@ int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool
       cudaGraphNode_t node;
       e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
       if (e == cudaSuccess)
-        e = cudaStreamUpdateCaptureDependencies(root, &node, nullptr, 1,
+        e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
                                                 cudaStreamSetCaptureDependencies);
       if (e == cudaSuccess)
-        e = cudaStreamBeginCaptureToGraph(bg->cap_body, np.conditional.phGraph_out[0], nullptr,
-                                          nullptr, 0, cudaStreamCaptureModeThreadLocal);
-      cur = bg->cap_body;
+        e = cudaStreamBeginCaptureToGraph(sb, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+      cur = sb;
     } else if (kind == OP_LOOP_END) {
-      if (cur != bg->cap_body) {
-        e = cudaErrorInvalidValue;
-        break;
-      }
-      loop_cond_kernel<<<1, 1, 0, cur>>>(h, bg->flag, bg->trips, spd);
+      if (cur != sb) return cudaErrorInvalidValue;
+      loop_cond_kernel<<<1, 1, 0, cur>>>(h, pk.flag, pk.trips, spd);
       e = cudaGetLastError();
       cudaGraph_t bout = nullptr;
-      const cudaError_t e2 = cudaStreamEndCapture(bg->cap_body, &bout);
+      const cudaError_t e2 = cudaStreamEndCapture(sb, &bout);
       if (e == cudaSuccess) e = e2;
-      cur = root;
+      cur = s;
     }
   }
-  if (cur != root) {  // an error inside a loop body: close its capture
+  if (cur != s) {  // an error inside a loop body: close its capture
     cudaGraph_t bout = nullptr;
-    cudaStreamEndCapture(bg->cap_body, &bout);
+    cudaStreamEndCapture(sb, &bout);
   }
+  return e;
+}
+
+// The whole batch as grouped launches in buckets: the posteriors, sorted by
+// (d, N), are cut into nb buckets of consecutive sizes; each bucket is one
+// branch of the graph (its own loops and active-chain flag), so a bucket
+// waits only for its own slowest chain and the branches overlap as the SMs
+// allow.
+int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool gl,
+                          cudaGraphExec_t* out, std::vector<void*>* bufs) {
+  *out = nullptr;
+  if (impl != 2) {
+    g_err = "grouped batch launches need the tcgen05 GEMM path";
+    return GJ_ENOTSUP;
+  }
+  const int B = (int)bg->lbs.size();
+  // automatic: buckets of 16 posteriors (2048 posteriors: 128 buckets, the
+  // measured optimum; fewer, larger buckets wait longer for their slowest
+  // chain at every loop)
+  const int want = bg->buckets > 0 ? bg->buckets : (B + 15) / 16;
+  const int nb = std::max(1, std::min(std::min(want, B), kMaxBuckets));
+  cudaError_t e = ensure_buckets(bg, nb);
+  if (e != cudaSuccess) return graph_fail("bucket set-up", e);
+  std::vector<int> order(B);
+  for (int b = 0; b < B; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const LogregBatched *a = bg->lbs[x], *c = bg->lbs[y];
+    return a->d != c->d ? a->d < c->d : a->N < c->N;
+  });
+  bg->pending.clear();
+  for (int k = 0; k < nb; ++k) {
+    const int b0 = (int)((long long)B * k / nb), b1 = (int)((long long)B * (k + 1) / nb);
+    std::vector<int> members(order.begin() + b0, order.begin() + b1);
+    e = capture_bucket(bg, members, bg->flag + 2 * k, bg->flag + 2 * k + 1, L, impl, prop, gl,
+                       bufs);
+    if (e != cudaSuccess) {
+      bg->pending.clear();
+      if (e == cudaErrorInvalidValue) {
+        g_err = "grouped batch: the posteriors' transitions differ in structure";
+        return GJ_EINVAL;
+      }
+      return graph_fail("batch record", e);
+    }
+  }
+  const StepDev* spd = bg->lbs[0]->spd;  // every posterior gets the same step parameters
+  cudaStream_t root = bg->cap_root;
+  e = cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return graph_fail("grouped begin", e);
+  e = cudaEventRecord(bg->fork, root);
+  for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+    cudaStream_t sk = bg->bucket_main[k], sbk = bg->bucket_body[k];
+    e = cudaStreamWaitEvent(sk, bg->fork, 0);
+    if (e == cudaSuccess) e = emit_bucket(bg->pending[k], spd, sk, sbk);
+    if (e == cudaSuccess) e = cudaEventRecord(bg->join, sk);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(root, bg->join, 0);
+  }
+  bg->pending.clear();
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(root, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -2878,7 +2958,8 @@ int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos,
     lb->stats = LogregStats{};
   }
   const bool prop = info.prop_v != nullptr;
-  const int cfg = graph_cfg(bg->lbs[0]) + (gl ? (1 << 20) : 0) + (bg->grouped ? (1 << 21) : 0);
+  const int cfg = graph_cfg(bg->lbs[0]) + (gl ? (1 << 20) : 0) +
+                  (bg->grouped ? (1 << 21) * (1 + std::min(bg->buckets, 255)) : 0);
   cudaGraphExec_t exec = nullptr;
   for (auto& g : bg->graphs)
     if (g.L == sp.L && g.impl == gemm_impl && g.cfg == cfg && g.prop == (int)prop) {

@@ -42,11 +42,13 @@ struct LogregBatchGraph;
 int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const size_t* vec_off,
                               LogregBatchGraph** out);
 void logreg_batch_graph_destroy(LogregBatchGraph* bg);
-// 1: the batch's graph holds grouped launches instead of one branch per
-// posterior: each stage of the transition is one grid (per kernel variant)
-// over all posteriors, each fixed-point solve one WHILE node for the batch
-// (tcgen05 GEMM path only); 0 (default): a branch per posterior
-void logreg_batch_graph_set_grouped(LogregBatchGraph* bg, int on);
+// on = 1: the batch's graph holds grouped launches instead of one branch per
+// posterior: the posteriors, sorted by size, are cut into `buckets` buckets
+// (0 = automatic, 16 posteriors each); each bucket is a branch in which every stage of the transition
+// is one grid (per kernel variant) over the bucket's posteriors and every
+// fixed-point solve one WHILE node (tcgen05 GEMM path only).  on = 0
+// (default): a branch per posterior.
+void logreg_batch_graph_set_grouped(LogregBatchGraph* bg, int on, int buckets);
 int logreg_batch_graph_step(LogregBatchGraph* bg, const StepDev& sp, float* pos, float* grad,
                             double* logdens, const float* z, const double* u,
                             const InfoDev<float>& info, int gemm_impl, cudaStream_t st);

@@ -251,15 +251,17 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * and the consumers add the slices in order, so results do not depend on
  * scheduling. */
 #define GJ_OPT_GEMM_KSPLIT 8
-/* batches of posteriors (gj_batch_set_option): 1 (default) = one CUDA graph
- * per transition holding every posterior's transition as an independent
- * branch, launched once (plus one gather and one scatter kernel); 2 = one
- * CUDA graph per transition of grouped launches: every stage of the
- * transition is one grid (per kernel variant) over all posteriors, whose
- * blocks find their posterior in a list of per-posterior items, and every
- * fixed-point solve one WHILE node for the batch (tcgen05 GEMM path);
- * 0 = one graph per posterior, spread over the batch's stream pool.
- * Results are bit-identical in every mode. */
+/* batches of posteriors (gj_batch_set_option): 2 (default) = one CUDA graph
+ * per transition of grouped launches: the posteriors, in buckets of similar
+ * size (GJ_OPT_BATCH_BUCKETS), each bucket a branch of the graph, every stage
+ * of the transition one grid (per kernel variant) over the bucket's
+ * posteriors, whose blocks find their posterior in a list of per-posterior
+ * items, and every fixed-point solve one WHILE node per bucket (tcgen05 GEMM
+ * path); 1 = one CUDA graph per transition holding every posterior's
+ * transition as its own branch; 0 = one graph per posterior, spread over the
+ * batch's stream pool.  Each mode is launched once per transition (plus one
+ * gather and one scatter kernel), and results are bit-identical in every
+ * mode. */
 #define GJ_OPT_BATCH_GRAPH 9
 /* LMC-Monge (funnel and hierarchical Gaussian, d <= 256): 1 (default) = one
  * warp per chain in either precision (float64 throughout for GJ_FP64),
@@ -272,6 +274,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * the momentum update); 0 = r2 is stored as three BF16 planes and contracted
  * by its own tensor-core GEMM */
 #define GJ_OPT_FUSE_R2X 11
+/* batches with GJ_OPT_BATCH_GRAPH = 2 (gj_batch_set_option): the posteriors,
+ * sorted by (d, N), are cut into this many buckets of consecutive sizes,
+ * 1 .. 256 (0 = automatic: 16 posteriors per bucket); each bucket is one branch of the graph with its
+ * own grouped launches and fixed-point loops, so a bucket waits only for its
+ * own slowest chain and the branches overlap */
+#define GJ_OPT_BATCH_BUCKETS 12
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */

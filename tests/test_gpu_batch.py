@@ -98,8 +98,8 @@ def test_batch_bitwise_equals_single_posterior_runs(one_graph, grouped):
 
 @pytest.mark.parametrize("integrator", ["implicit_midpoint", "generalized_leapfrog"])
 def test_batch_one_graph_reused_across_calls(integrator):
-    """The one-graph batch, as branches and as grouped launches, over three
-    transitions (the graph captured at the first is reused, the step size
+    """The one-graph batch, as branches and as grouped launches (one bucket
+    and three buckets of posteriors), over three transitions (the graph captured at the first is reused, the step size
     changes between calls, the state arrays move) equals the stream-pool
     batch bit for bit, info included."""
     import torch
@@ -107,9 +107,10 @@ def test_batch_one_graph_reused_across_calls(integrator):
 
     data = _data()
     outs = []
-    for one, grouped in ((True, False), (True, True), (False, False)):
+    for one, grouped, buckets in ((True, False, 0), (True, True, 0), (True, True, 3),
+                                  (False, False, 0)):
         pb = PosteriorBatch(data, C, num_streams=3, one_graph=one, grouped=grouped,
-                            integrator=integrator)
+                            buckets=buckets, integrator=integrator)
         st = pb.init(_starts())
         info = pb.new_info()
         g = torch.Generator(device="cuda").manual_seed(5)
