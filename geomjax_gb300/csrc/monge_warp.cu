@@ -76,6 +76,22 @@ __device__ __forceinline__ R wget(const WVec<E, R>& a, int i) {
   return __shfl_sync(0xffffffffu, v, lane);
 }
 
+// N independent warp sums in one butterfly: the N shuffles of a stage issue
+// together, so the round costs the latency of one sum (every lane ends with
+// the same, bit-identical totals: each stage adds a pair in both orders,
+// which float addition makes equal)
+template <int N, typename R>
+__device__ __forceinline__ void warp_sum_n(R (&v)[N]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R t[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) t[i] = __shfl_xor_sync(0xffffffffu, v[i], o);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] += t[i];
+  }
+}
+
 // warp-level target: log density + gradient and HVP for funnel / hier.
 // The scale constants are precomputed once per transition: on GB300 an FP64
 // division or logarithm inside the step loop costs more than the whole FP32
@@ -135,29 +151,39 @@ __device__ inline WarpTarget<R> make_warp_target(const TargetDev& t, const WarpC
 
 // funnel: v = θ[d−1]
 // The FP64 log density is formed only when need_ld (the proposal's, after
-// the last step); the gradient is FP32.
+// the last step); the gradient is FP32.  With Lout, the normalising constant
+// L = 1 + α² Σ_i M⁻¹_i g_i² (lmcmonge/metrics.py:193-197) is formed from the
+// same reduction round (its sum over the coordinates whose gradient is
+// local, plus the one or two coordinates whose gradient needs the sums).
 template <int E, typename R>
-__device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q, WVec<E, R>& g, R* sx_out,
-                                    bool need_ld = true) {
+__device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q, WVec<E, R>& g,
+                                    R* sx_out, bool need_ld = true, const WVec<E, R>* im = nullptr,
+                                    R a2 = R(0), R* Lout = nullptr) {
   const TargetDev& t = W.t;
   const int d = t.d;
   if (t.family == GJ_FUNNEL) {
     const R v = wget<E>(q, d - 1);
     const R ev = m_exp(-v);
-    R sx = R(0);
+    R p[2] = {R(0), R(0)};  // Σx², Σ M⁻¹x²
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
       const R x = (i < d - 1) ? q.x[k] : R(0);
-      sx = m_fma(x, x, sx);
+      p[0] = m_fma(x, x, p[0]);
+      if (Lout) p[1] = m_fma(im->x[k] * x, x, p[1]);
     }
-    sx = warp_sum(sx);
+    if (Lout)
+      warp_sum_n<2>(p);
+    else
+      p[0] = warp_sum(p[0]);
+    const R sx = p[0];
     const R gv = -v * W.inv_a2 - R(0.5) * R(d - 1) + R(0.5) * ev * sx;
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       const int i = W.lane + 32 * k;
       g.x[k] = (i < d - 1) ? -q.x[k] * ev : ((i == d - 1) ? gv : R(0));
     }
+    if (Lout) *Lout = R(1) + a2 * (ev * ev * p[1] + wget<E>(*im, d - 1) * gv * gv);
     *sx_out = sx;
     if (!need_ld) return 0.0;
     return W.ld_const - 0.5 * double(v) * double(v) * W.inv_a2d - 0.5 * double(ev) * double(sx) -
@@ -169,7 +195,7 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
   const R* sg = static_cast<const R*>(t.s);
   const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
   const R ev = m_exp(-v);
-  R sr = R(0), srr = R(0);
+  R p[3] = {R(0), R(0), R(0)};  // Σr, Σr², Σ_{j<J} M⁻¹g_j²
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int i = W.lane + 32 * k;
@@ -178,12 +204,20 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
       const R e = y[i] - q.x[k];
       const R is2 = R(1) / (sg[i] * sg[i]);
       g.x[k] = e * is2 - r * ev;
-      sr += r;
-      srr = m_fma(r, r, srr);
+      p[0] += r;
+      p[1] = m_fma(r, r, p[1]);
+      if (Lout) p[2] = m_fma(im->x[k] * g.x[k], g.x[k], p[2]);
     }
   }
-  sr = warp_sum(sr);
-  srr = warp_sum(srr);
+  if (Lout) {
+    warp_sum_n<3>(p);
+  } else {
+    R p2[2] = {p[0], p[1]};
+    warp_sum_n<2>(p2);
+    p[0] = p2[0];
+    p[1] = p2[1];
+  }
+  const R sr = p[0], srr = p[1];
   const R gmu = sr * ev - mu * W.inv_a2;
   const R gvv = R(0.5) * ev * srr - R(0.5) * J - v * W.inv_b2;
 #pragma unroll
@@ -193,6 +227,8 @@ __device__ double w_logdensity_grad(const WarpTarget<R>& W, const WVec<E, R>& q,
     if (i == J + 1) g.x[k] = gvv;
     if (i > J + 1) g.x[k] = R(0);
   }
+  if (Lout)
+    *Lout = R(1) + a2 * (p[2] + wget<E>(*im, J) * gmu * gmu + wget<E>(*im, J + 1) * gvv * gvv);
   *sx_out = srr;
   if (!need_ld) return 0.0;
   double se = 0.0;  // Σ (y_j − θ_j)² / σ_j², in FP64 as the initial log density
@@ -285,41 +321,136 @@ __device__ void w_hvp(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E,
   }
 }
 
+// Two Hessian-vector products at the same q (H·u1, H·u2) with one reduction
+// round: the same arithmetic as two w_hvp calls.
+template <int E, typename R>
+__device__ void w_hvp2(const WarpTarget<R>& W, const WVec<E, R>& q, const WVec<E, R>& u1,
+                       const WVec<E, R>& u2, R sx, WVec<E, R>& o1, WVec<E, R>& o2) {
+  const TargetDev& t = W.t;
+  const int d = t.d;
+  if (t.family == GJ_FUNNEL) {
+    const R v = wget<E>(q, d - 1);
+    const R ev = m_exp(-v);
+    const R uv1 = wget<E>(u1, d - 1), uv2 = wget<E>(u2, d - 1);
+    R p[2] = {R(0), R(0)};
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = W.lane + 32 * k;
+      if (i < d - 1) {
+        p[0] = m_fma(q.x[k], u1.x[k], p[0]);
+        p[1] = m_fma(q.x[k], u2.x[k], p[1]);
+      }
+    }
+    warp_sum_n<2>(p);
+    const R cv = -W.inv_a2 - R(0.5) * ev * sx;
+    const R ov1 = ev * p[0] + cv * uv1, ov2 = ev * p[1] + cv * uv2;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = W.lane + 32 * k;
+      o1.x[k] = (i < d - 1) ? ev * (-u1.x[k] + q.x[k] * uv1) : ((i == d - 1) ? ov1 : R(0));
+      o2.x[k] = (i < d - 1) ? ev * (-u2.x[k] + q.x[k] * uv2) : ((i == d - 1) ? ov2 : R(0));
+    }
+    return;
+  }
+  const int J = t.n;
+  const R* sg = static_cast<const R*>(t.s);
+  const R mu = wget<E>(q, J), v = wget<E>(q, J + 1);
+  const R ev = m_exp(-v);
+  const R um1 = wget<E>(u1, J), uv1 = wget<E>(u1, J + 1);
+  const R um2 = wget<E>(u2, J), uv2 = wget<E>(u2, J + 1);
+  R p[5] = {R(0), R(0), R(0), R(0), R(0)};  // Σr, Σu1, Σr·u1, Σu2, Σr·u2
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = W.lane + 32 * k;
+    if (i < J) {
+      const R r = q.x[k] - mu;
+      const R is2 = R(1) / (sg[i] * sg[i]);
+      p[0] += r;
+      p[1] += u1.x[k];
+      p[2] = m_fma(r, u1.x[k], p[2]);
+      p[3] += u2.x[k];
+      p[4] = m_fma(r, u2.x[k], p[4]);
+      o1.x[k] = -(is2 + ev) * u1.x[k] + ev * um1 + r * ev * uv1;
+      o2.x[k] = -(is2 + ev) * u2.x[k] + ev * um2 + r * ev * uv2;
+    }
+  }
+  warp_sum_n<5>(p);
+  const R sr = p[0];
+  const R om1 = ev * p[1] + (-R(J) * ev - W.inv_a2) * um1 - ev * sr * uv1;
+  const R ovv1 = ev * p[2] - ev * sr * um1 + (-R(0.5) * ev * sx - W.inv_b2) * uv1;
+  const R om2 = ev * p[3] + (-R(J) * ev - W.inv_a2) * um2 - ev * sr * uv2;
+  const R ovv2 = ev * p[4] - ev * sr * um2 + (-R(0.5) * ev * sx - W.inv_b2) * uv2;
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = W.lane + 32 * k;
+    if (i == J) {
+      o1.x[k] = om1;
+      o2.x[k] = om2;
+    }
+    if (i == J + 1) {
+      o1.x[k] = ovv1;
+      o2.x[k] = ovv2;
+    }
+    if (i > J + 1) {
+      o1.x[k] = R(0);
+      o2.x[k] = R(0);
+    }
+  }
+}
+
 // half_step_omega (lmcmonge/integrators.py:158-194), im = diag(M⁻¹).  dJ
 // accumulates this transition's volume-term increments in FP32 (each is
 // ≈ 1e-3; 4 per step); the caller adds the sum to the FP64 J once.
+//
+// The reference's four dot products depend on one another (dφ·dl_ig, then
+// v_tmp·Hv, then Hdl_ig·v'), so each would be its own warp reduction.  They
+// are all linear in seven sums of the step's inputs, taken in one round:
+//   S_dh = Σ hv·dl_ig, S_gd = Σ gn·dl_ig, S_Hd = Σ Hdl·dl_ig, S_vh = Σ v·hv,
+//   S_gh = Σ igH·hv,  S_Hv = Σ Hdl·v,   S_HH = Σ Hdl·igH    (igH = M⁻¹Hdl)
+// with dφ_ig = −dl_ig + α²·igH/√L and c1 = ½ε√L:
+//   dφ·dl_ig  = −S_gd + α² S_Hd/√L
+//   v_tmp·hv  = S_vh − c1 (−S_dh + α² S_gh/√L − α² (dφ·dl_ig) S_dh)
+//   Hdl·v'    = S_Hv − c1 (−S_Hd + α² S_HH/√L − α² (dφ·dl_ig) S_Hd) − corr S_Hd
+// (v' = v_tmp − corr·dl_ig); each leading sum dominates its correction, so
+// the rewriting loses nothing to cancellation.
 template <int E, typename R>
 __device__ void w_half(R a2, WVec<E, R>& v, R* dJ, const WVec<E, R>& gn, const WVec<E, R>& hv, R L,
                        const WVec<E, R>& im, const WVec<E, R>& Hdl, R eps, int fix) {
   WVec<E, R> dl_ig, igH;
+  R p[7] = {R(0), R(0), R(0), R(0), R(0), R(0), R(0)};
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     dl_ig.x[k] = im.x[k] * gn.x[k];
     igH.x[k] = im.x[k] * Hdl.x[k];
+    p[0] = m_fma(hv.x[k], dl_ig.x[k], p[0]);
+    p[1] = m_fma(gn.x[k], dl_ig.x[k], p[1]);
+    p[2] = m_fma(Hdl.x[k], dl_ig.x[k], p[2]);
+    p[3] = m_fma(v.x[k], hv.x[k], p[3]);
+    p[4] = m_fma(igH.x[k], hv.x[k], p[4]);
+    p[5] = m_fma(Hdl.x[k], v.x[k], p[5]);
+    p[6] = m_fma(Hdl.x[k], igH.x[k], p[6]);
   }
+  warp_sum_n<7>(p);
   // log|det1| and log|1 − ½εα²(Hdl·v)| as FP32 log1p of the small terms
   // (det1 is an FP32 value, so an FP64 logarithm adds nothing)
-  const R x1 = R(0.5) * eps * a2 * wdot<E>(hv, dl_ig);
+  const R x1 = R(0.5) * eps * a2 * p[0];
   const R det1 = R(1) + x1;
   *dJ -= x1 > -R(1) ? m_log1p(x1) : m_log(m_abs(det1));
   const R sL = m_sqrt(L);
   const R isL = R(1) / sL;  // one division, then products
-  // dphi·dl_ig with dphi = −dl + α² Hdl_ig / sL
-  R pd = R(0);
-#pragma unroll
-  for (int k = 0; k < E; ++k) pd = m_fma(-gn.x[k] + a2 * Hdl.x[k] * isL, dl_ig.x[k], pd);
-  pd = warp_sum(pd);
-  WVec<E, R> vt;
+  const R pd = -p[1] + a2 * isL * p[2];  // dφ·dl_ig
+  const R c1 = R(0.5) * eps * sL;
+  const R vt_hv = p[3] - c1 * (-p[0] + a2 * isL * p[4] - a2 * pd * p[0]);
+  R corr = R(0.5) * eps * vt_hv / det1;
+  if (fix) corr *= a2;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const R dphi_ig = -dl_ig.x[k] + a2 * igH.x[k] * isL;
-    vt.x[k] = v.x[k] - R(0.5) * eps * sL * (dphi_ig - a2 * pd * dl_ig.x[k]);
+    const R vt = v.x[k] - c1 * (dphi_ig - a2 * pd * dl_ig.x[k]);
+    v.x[k] = vt - corr * dl_ig.x[k];
   }
-  R corr = R(0.5) * eps * wdot<E>(vt, hv) / det1;
-  if (fix) corr *= a2;
-#pragma unroll
-  for (int k = 0; k < E; ++k) v.x[k] = vt.x[k] - corr * dl_ig.x[k];
-  const R x2 = -R(0.5) * eps * a2 * wdot<E>(Hdl, v);
+  const R hdl_v = p[5] - c1 * (-p[2] + a2 * isL * p[6] - a2 * pd * p[2]) - corr * p[2];
+  const R x2 = -R(0.5) * eps * a2 * hdl_v;
   *dJ += x2 > -R(1) ? m_log1p(x2) : m_log(m_abs(R(1) + x2));
 }
 
@@ -442,8 +573,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
       vmv = m_fma(m * v.x[k], v.x[k], vmv);
       vg = m_fma(v.x[k], gn.x[k], vg);
     }
-    vmv = warp_sum(vmv);
-    vg = warp_sum(vg);
+    R p[2] = {vmv, vg};
+    warp_sum_n<2>(p);
+    vmv = p[0];
+    vg = p[1];
     // in the state's type R: every factor is an R value, and each FP64
     // instruction costs 64 FP32 ones on GB300
     const R kin = R(0.5) * (vmv - m_log(Lc)) + R(0.5) * Lc * a2 * vg * vg;
@@ -456,11 +589,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
     w_half<E>(a2, v, &dJ, gn, hv, L, im, Hdl, eps, sp.alpha2_fix);
 #pragma unroll
     for (int k = 0; k < E; ++k) q.x[k] = m_fma(eps, v.x[k], q.x[k]);
-    ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1);
-    R Ls = R(0);
-#pragma unroll
-    for (int k = 0; k < E; ++k) Ls = m_fma(im.x[k] * g.x[k], g.x[k], Ls);
-    L = R(1) + a2 * warp_sum(Ls);
+    ld = w_logdensity_grad<E>(W, q, g, &sx, s == sp.L - 1, &im, a2, &L);
     sL = m_sqrt(L);
     isL = R(1) / sL;
 #pragma unroll
@@ -468,8 +597,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 1) monge_warp_kernel
       gn.x[k] = g.x[k] * isL;
       dl_ig.x[k] = im.x[k] * gn.x[k];
     }
-    w_hvp<E>(W, q, v, sx, hv);
-    w_hvp<E>(W, q, dl_ig, sx, Hdl);
+    w_hvp2<E>(W, q, v, dl_ig, sx, hv, Hdl);
 #pragma unroll
     for (int k = 0; k < E; ++k) {
       hv.x[k] *= isL;
