@@ -419,6 +419,8 @@ def run_batch(args, wl):
                         buckets=args.batch_buckets)
     if args.cholesky == "fp32":
         pb.set_option(L.GJ_OPT_CHOL_FP64, 0)
+    if args.chol_cpw:
+        pb.set_option(L.GJ_OPT_CHOL_CHAINS_PER_WARP, args.chol_cpw)
     del data
     g0 = torch.Generator().manual_seed(rank)
     state = pb.init([0.01 * torch.randn(C, int(d), generator=g0) for d in ds])
@@ -493,6 +495,7 @@ def run_batch(args, wl):
                                "one CUDA graph per transition of grouped launches: every stage "
                                "one grid over a bucket of posteriors, each bucket a branch")),
                    "cholesky": args.cholesky,
+                   "chol_chains_per_warp": args.chol_cpw or "auto",
                    "buckets": None if (args.batch_branches or args.batch_pool) else
                               (args.batch_buckets or "auto"),
                    "mean_N": float(np.mean(Ns)), "mean_d": float(np.mean(ds)),
