@@ -2530,6 +2530,7 @@ struct LogregBatchGraph {
     int* trips;
   };
   std::vector<Pending> pending;
+  std::vector<unsigned char> staging;  // grouped: the items of a capture, uploaded at once
   struct Entry {
     int L, impl, cfg, prop;
     cudaGraphExec_t exec;
@@ -2728,8 +2729,9 @@ bool is_kernel_op(int kind) { return kind <= OP_ZERO; }
 // condition is the bucket's shared active-chain flag.  A posterior whose
 // chains have all converged runs the loop's remaining bodies without
 // changing state: the updates and factorisations skip inactive chains, and
-// the contractions skip tiles with no active chain.  The items are uploaded
-// here; emit_bucket records the launches into a capture.
+// the contractions skip tiles with no active chain.  The items are staged
+// here (batch_capture_grouped uploads them at once); emit_bucket records the
+// launches into a capture.
 // capture streams for nb buckets (their flags are allocated with the batch)
 cudaError_t ensure_buckets(LogregBatchGraph* bg, int nb) {
   cudaError_t e = cudaSuccess;
@@ -2744,8 +2746,7 @@ cudaError_t ensure_buckets(LogregBatchGraph* bg, int nb) {
 }
 
 cudaError_t capture_bucket(LogregBatchGraph* bg, const std::vector<int>& members, int* flag,
-                           int* trips, int L, int impl, bool prop, bool gl,
-                           std::vector<void*>* bufs) {
+                           int* trips, int L, int impl, bool prop, bool gl) {
   const int B = (int)members.size();
   std::vector<Recorder> recs(B);
   for (int b = 0; b < B; ++b) {
@@ -2788,18 +2789,18 @@ cudaError_t capture_bucket(LogregBatchGraph* bg, const std::vector<int>& members
       }
       g.n = (int)(k1 - k);
       g.blocks = prefix.back();
-      void* di = nullptr;
-      void* dp = nullptr;
-      cudaError_t e = cudaMalloc(&di, isz * (size_t)g.n);
-      if (e == cudaSuccess) bufs->push_back(di);
-      if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(int) * prefix.size());
-      if (e == cudaSuccess) bufs->push_back(dp);
-      if (e == cudaSuccess) e = cudaMemcpy(di, items.data(), items.size(), cudaMemcpyHostToDevice);
-      if (e == cudaSuccess)
-        e = cudaMemcpy(dp, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) return e;
-      g.items = di;
-      g.prefix = static_cast<const int*>(dp);
+      // staged in the capture's one upload buffer; the offsets become device
+      // addresses once it is allocated (64-byte aligned: items may hold
+      // tensor maps)
+      auto stage = [&](const void* src, size_t bytes) {
+        std::vector<unsigned char>& h = bg->staging;
+        const size_t off = (h.size() + 63) / 64 * 64;
+        h.resize(off + bytes);
+        std::memcpy(h.data() + off, src, bytes);
+        return off;
+      };
+      g.items = reinterpret_cast<const void*>(stage(items.data(), items.size()));
+      g.prefix = reinterpret_cast<const int*>(stage(prefix.data(), sizeof(int) * prefix.size()));
       plan[i].push_back(g);
       k = k1;
     }
@@ -2898,11 +2899,11 @@ int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool
     return a->d != c->d ? a->d < c->d : a->N < c->N;
   });
   bg->pending.clear();
+  bg->staging.clear();
   for (int k = 0; k < nb; ++k) {
     const int b0 = (int)((long long)B * k / nb), b1 = (int)((long long)B * (k + 1) / nb);
     std::vector<int> members(order.begin() + b0, order.begin() + b1);
-    e = capture_bucket(bg, members, bg->flag + 2 * k, bg->flag + 2 * k + 1, L, impl, prop, gl,
-                       bufs);
+    e = capture_bucket(bg, members, bg->flag + 2 * k, bg->flag + 2 * k + 1, L, impl, prop, gl);
     if (e != cudaSuccess) {
       bg->pending.clear();
       if (e == cudaErrorInvalidValue) {
@@ -2911,6 +2912,25 @@ int batch_capture_grouped(LogregBatchGraph* bg, int L, int impl, bool prop, bool
       }
       return graph_fail("batch record", e);
     }
+  }
+  {  // one upload of every launch's items and prefix sums
+    void* dbuf = nullptr;
+    e = cudaMalloc(&dbuf, std::max<size_t>(bg->staging.size(), 64));
+    if (e == cudaSuccess) bufs->push_back(dbuf);
+    if (e == cudaSuccess && !bg->staging.empty())
+      e = cudaMemcpy(dbuf, bg->staging.data(), bg->staging.size(), cudaMemcpyHostToDevice);
+    std::vector<unsigned char>().swap(bg->staging);
+    if (e != cudaSuccess) {
+      bg->pending.clear();
+      return graph_fail("batch items", e);
+    }
+    unsigned char* d0 = static_cast<unsigned char*>(dbuf);
+    for (auto& pk : bg->pending)
+      for (auto& launches : pk.plan)
+        for (GroupLaunch& g : launches) {
+          g.items = d0 + reinterpret_cast<size_t>(g.items);
+          g.prefix = reinterpret_cast<const int*>(d0 + reinterpret_cast<size_t>(g.prefix));
+        }
   }
   const StepDev* spd = bg->lbs[0]->spd;  // every posterior gets the same step parameters
   cudaStream_t root = bg->cap_root;
