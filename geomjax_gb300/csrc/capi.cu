@@ -870,7 +870,7 @@ int32_t gj_batch_rmhmc_step(gj_batch* b, const gj_step_params* p, gj_chain_state
   const gj::StepDev sp = gj::to_dev(*p);
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const gj::InfoDev<float> inf = gj::to_dev<float>(info);
-  if (b->one_graph) {  // every posterior a branch of one graph, one launch
+  if (b->one_graph) {  // one graph launch: grouped launches or a branch per posterior
     if (!b->bg) {
       const int rc = gj::logreg_batch_graph_create(b->lbs.data(), b->B, b->C, b->pos_off.data(),
                                                    &b->bg);

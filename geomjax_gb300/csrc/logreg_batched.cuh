@@ -32,12 +32,13 @@ int logreg_batched_rmhmc_step_graph(LogregBatched* lb, const StepDev& sp, float*
 
 // A batch of contexts (one per posterior, all with the same chain count)
 // advanced by one CUDA-graph launch per transition: every posterior's whole
-// transition is an independent branch of the graph.  vec_off[b]: offset of
+// transition an independent branch of the graph, or grouped launches over
+// buckets of posteriors (logreg_batch_graph_set_grouped).  vec_off[b]: offset of
 // posterior b's [C, d_b] block in the batch's ragged vectors; per-chain
 // scalars are [B·C].  One gather kernel before the launch and one scatter
 // kernel after it move the batch arrays in and out of the posteriors'
 // staging buffers.  Up to 8 captured graphs are kept (by number of steps,
-// GEMM path, factorisation set-up, integrator and proposal output).
+// GEMM path, factorisation set-up, integrator, proposal output and form).
 struct LogregBatchGraph;
 int logreg_batch_graph_create(LogregBatched* const* lbs, int B, int C, const size_t* vec_off,
                               LogregBatchGraph** out);

@@ -267,12 +267,13 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * warp per chain in either precision (float64 throughout for GJ_FP64),
  * 0 = one thread per chain */
 #define GJ_OPT_MONGE_WARP 10
-/* batched path, tcgen05 GEMMs, d <= 32 (contexts and batches): 1 (default)
- * = the generalized leapfrog's momentum evaluations contract
- * r2 = Λ'(w − s²) with X in the epilogue of the S = U·Xᵀ GEMM (FP32 FMAs on
- * the CUDA cores, one partial gradient per N tile, added in tile order by
- * the momentum update); 0 = r2 is stored as three BF16 planes and contracted
- * by its own tensor-core GEMM */
+/* batched path, tcgen05 GEMMs, d <= 32 and N > 64 (contexts and batches):
+ * 1 (default) = the generalized leapfrog's momentum evaluations contract
+ * r2 = Λ'(w − s²) with X inside the CTA of the S = U·Xᵀ GEMM (r2 as three
+ * BF16 planes in shared memory, a second tcgen05 MMA against the Xᵀ tile,
+ * one partial gradient per N tile, added in tile order by the momentum
+ * update); 0 = r2 is stored as three BF16 planes in global memory and
+ * contracted by its own tensor-core GEMM */
 #define GJ_OPT_FUSE_R2X 11
 /* batches with GJ_OPT_BATCH_GRAPH = 2 (gj_batch_set_option): the posteriors,
  * sorted by (d, N), are cut into this many buckets of consecutive sizes,
