@@ -61,6 +61,11 @@ WORKLOADS = {
                      max_iters=6, sampler="rmhmc_funnel"),
     "trajectory_grad": dict(name="logistic_regression_N2000_d64_gl20_dh_dlambda_1024chains", N=2000,
                             d=64, C=1024, L=20, h=0.02, lam=0.01, sampler="jvp"),
+    # the uneven batch's largest posterior as one context (its factorisation
+    # takes a CTA of four warps per chain); no plain or ESS arms (the plain
+    # CTA-per-chain form stops at d = 64)
+    "logreg_large": dict(name="logistic_regression_N5000_d128_rmhmc_fisher_1024chains", N=5000,
+                         d=128, C=1024, L=8, h=0.02, sampler="rmhmc", comparisons=False),
     "uneven": dict(name="uneven_logreg_2048posteriors_N200-5000_d8-128_64chains", B=2048, C=64,
                    L=8, h=0.05, sampler="batch"),
     "nuts": dict(name="funnel_D2_nuts_rmhmc_diag_fisher_fp64_4096chains", D=2, C=4096, h=0.1,
@@ -290,7 +295,8 @@ def run_ours(args, wl):
 
         min_ess = global_min_ess(trace, chain_axis=1, sample_axis=0)
     ess_cmp = None
-    if rank == 0 and args.ess_transitions > 0 and wl["sampler"] in ("rmhmc", "lmcmonge"):
+    if (rank == 0 and args.ess_transitions > 0 and wl["sampler"] in ("rmhmc", "lmcmonge")
+            and wl.get("comparisons", True)):
         # rank 0 only: the plain arm is a baseline, not part of the weak-scaled value
         ess_cmp = ess_comparison(args, wl, kern, target, state, info, extra, dev)
     # --- e2e through the public API with host buffers
@@ -1166,7 +1172,8 @@ def main():
             cmp_ = out["ess_comparison"]
             out["plain_fp64"] = dict(cmp_["plain_fp64"], transitions=cmp_["transitions"])
             out["min_ess_ratio"] = cmp_["min_ess_ratio"]
-        if not args.no_plain and wl["sampler"] in ("rmhmc", "lmcmonge"):
+        if (not args.no_plain and wl["sampler"] in ("rmhmc", "lmcmonge")
+                and wl.get("comparisons", True)):
             # the thread-per-chain FP64 form, kept for continuity
             out["plain_fp64_thread_per_chain"] = run_plain_fp64(args, wl)
             out["steps_ratio_vs_thread_per_chain"] = round(

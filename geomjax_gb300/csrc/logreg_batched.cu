@@ -138,7 +138,7 @@ struct CholArgs {
 // consecutive packed entries fall in distinct banks.
 struct CholCfg {
   int cpw;       // chains per warp
-  int lpc;       // lanes per chain (32 / cpw; 128: one chain per CTA of 4 warps)
+  int lpc;       // lanes per chain (32 / cpw; 128 / 256: one chain per CTA of 4 / 8 warps)
   int warps;     // warps per CTA
   int chains;    // chains per CTA
   size_t stride; // bytes per chain
@@ -190,6 +190,12 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) 
     c.warps = 4;
     c.chains = 1;
     c.smem = c.tab + c.stride;
+    // when even one such chain leaves no room for a second CTA (d >= ~110),
+    // the SM holds four warps only: the chain gets eight
+    if (c.smem > 113 * 1024) {
+      c.lpc = 256;
+      c.warps = 8;
+    }
   }
   return c;
 }
@@ -306,8 +312,9 @@ __device__ __forceinline__ bool chain_any(bool b) {
 }
 
 // block bx of the factorisation (chol_kernel, or an item of a grouped launch)
-// LPC = 128: one chain per CTA of four warps (large d, where one warp per
-// chain leaves most of an SM's FP64 units idle); its barrier is the CTA's.
+// LPC = 128 / 256: one chain per CTA of four / eight warps (large d, where
+// one warp per chain leaves most of an SM's FP64 units idle); its barrier is
+// the CTA's.
 template <typename F, int LPC>  // factorisation type (double / float), lanes per chain
 __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -615,28 +622,31 @@ __global__ void chol_grouped_kernel(const CholItem* __restrict__ items,
 }
 
 template <typename F>
-cudaError_t chol_launch(const CholCfg& cf, dim3 grid, const CholArgs& a, bool pdl,
+cudaError_t chol_launch(const CholCfg& cf, size_t smem, dim3 grid, const CholArgs& a, bool pdl,
                         cudaStream_t st) {
   const dim3 th(32 * cf.warps);
   const int stride = (int)cf.stride;
   switch (cf.lpc) {
-    case 4: return launch_k(pdl, chol_kernel<F, 4>, grid, th, cf.smem, st, a, stride);
-    case 8: return launch_k(pdl, chol_kernel<F, 8>, grid, th, cf.smem, st, a, stride);
-    case 16: return launch_k(pdl, chol_kernel<F, 16>, grid, th, cf.smem, st, a, stride);
-    case 128: return launch_k(pdl, chol_kernel<F, 128>, grid, th, cf.smem, st, a, stride);
-    default: return launch_k(pdl, chol_kernel<F, 32>, grid, th, cf.smem, st, a, stride);
+    case 4: return launch_k(pdl, chol_kernel<F, 4>, grid, th, smem, st, a, stride);
+    case 8: return launch_k(pdl, chol_kernel<F, 8>, grid, th, smem, st, a, stride);
+    case 16: return launch_k(pdl, chol_kernel<F, 16>, grid, th, smem, st, a, stride);
+    case 128: return launch_k(pdl, chol_kernel<F, 128>, grid, th, smem, st, a, stride);
+    case 256: return launch_k(pdl, chol_kernel<F, 256>, grid, th, smem, st, a, stride);
+    default: return launch_k(pdl, chol_kernel<F, 32>, grid, th, smem, st, a, stride);
   }
 }
 
 template <typename F>
 cudaError_t chol_set_smem(int smax) {
   cudaError_t e = cudaSuccess, r;
-  const void* grouped[6] = {(const void*)chol_grouped_kernel<F, 4>,
+  const void* grouped[8] = {(const void*)chol_grouped_kernel<F, 4>,
                             (const void*)chol_grouped_kernel<F, 8>,
                             (const void*)chol_grouped_kernel<F, 16>,
                             (const void*)chol_grouped_kernel<F, 32>,
                             (const void*)chol_grouped_kernel<F, 128>,
-                            (const void*)chol_kernel<F, 128>};
+                            (const void*)chol_kernel<F, 128>,
+                            (const void*)chol_grouped_kernel<F, 256>,
+                            (const void*)chol_kernel<F, 256>};
   for (const void* k : grouped) {
     r = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     if (r != cudaSuccess) e = r;
@@ -1704,15 +1714,20 @@ struct Runner {
         chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
     const int per_cta = cf.chains;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
+    // one chain per CTA (lpc >= 128) without the inverse: the FP32 L⁻¹ at the
+    // end of the chain's block is never touched, so it is not allocated
+    // (d = 128: two CTAs per SM instead of one)
+    const size_t smem = (cf.lpc >= 128 && no_inverse) ? cf.smem - (size_t)L.P * sizeof(float)
+                                                      : cf.smem;
     if (rec) {
       if (a.q_update) a.n_active = rec->flag;
       CholItem it{a, (int)cf.stride};
-      rec->push(OP_CHOL, (L.chol_fp64 ? 100 : 0) + cf.lpc, (int)grid.x, 32 * cf.warps, cf.smem, it);
+      rec->push(OP_CHOL, (L.chol_fp64 ? 100 : 0) + cf.lpc, (int)grid.x, 32 * cf.warps, smem, it);
       return;
     }
     // the dynamic shared-memory limit was raised at context creation
-    check(L.chol_fp64 ? chol_launch<double>(cf, grid, a, L.pdl, st)
-                      : chol_launch<float>(cf, grid, a, L.pdl, st));
+    check(L.chol_fp64 ? chol_launch<double>(cf, smem, grid, a, L.pdl, st)
+                      : chol_launch<float>(cf, smem, grid, a, L.pdl, st));
     if (e1) cudaEventRecord(e1, st);
   }
 
@@ -2671,6 +2686,8 @@ cudaError_t launch_group(const GroupLaunch& g, cudaStream_t s) {
         case 132: chol_grouped_kernel<double, 32><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 228: chol_grouped_kernel<double, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 128: chol_grouped_kernel<float, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 356: chol_grouped_kernel<double, 256><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 256: chol_grouped_kernel<float, 256><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 4: chol_grouped_kernel<float, 4><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 8: chol_grouped_kernel<float, 8><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 16: chol_grouped_kernel<float, 16><<<grid, th, g.smem, s>>>(it, pf, n); break;
