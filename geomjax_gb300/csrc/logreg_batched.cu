@@ -382,6 +382,24 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   // bordered y_j (all lanes compute the same scalars; lane 0 of the chain
   // writes them)
   auto pivot = [&](int j, int cj) -> F {
+    if constexpr (kCta) {
+      // a CTA per chain: thread 0 alone takes the pivot (the FP64 pipe issues
+      // each warp's copy of it at full cost) and publishes 1/L_jj; bad, pm
+      // and pe, read only by thread 0 at the end, stay its own
+      if (sl == 0) {
+        const F djj = L[cj];
+        const F inv = pivot_rsqrt(djj, bad);
+        if (want_ld) ld_accumulate(pm, pe, double(djj));
+        if (a.mode == CH_DRAW) L[cj] = djj * inv;  // L_jj, read only by p = L z
+        rdiag[j] = inv;
+        if (border) y[j] *= inv;
+      }
+      chain_sync<LPC>();
+      const F inv = rdiag[j];
+      for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
+      chain_sync<LPC>();
+      return inv;
+    }
     const F djj = L[cj];
     const F inv = pivot_rsqrt(djj, bad);  // 1/L_jj
     if (want_ld) ld_accumulate(pm, pe, double(djj));
