@@ -189,13 +189,15 @@ inline CholCfg chol_config(int d, size_t fsz, int cpw_req = 0, int C = 1 << 30) 
     c.lpc = 128;
     c.warps = 4;
     c.chains = 1;
-    c.smem = c.tab + c.stride;
-    // when even one such chain leaves no room for a second CTA (d >= ~110),
-    // the SM holds four warps only: the chain gets eight
-    if (c.smem > 113 * 1024) {
+    // when even one such chain's full layout leaves no room for a second
+    // CTA (d >= ~110), the SM would hold four warps only: the chain gets eight
+    if (c.tab + c.stride > 113 * 1024) {
       c.lpc = 256;
       c.warps = 8;
     }
+    // the chain's FP32 L⁻¹ (the end of its block) lives in the pair table's
+    // place (d = 128: 102 KB, two CTAs per SM)
+    c.smem = c.tab + c.stride - (size_t)d * (d + 1) / 2 * sizeof(float);
   }
   return c;
 }
@@ -333,7 +335,9 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   F* y = L + P;
   F* xv = y + d;
   F* rdiag = xv + d;  // 1 / L_jj
-  float* Li = reinterpret_cast<float*>(rdiag + d);  // L⁻¹, packed like L
+  // L⁻¹, packed like L; a CTA's single chain keeps it in the pair table's
+  // place (the table is not read after the factorisation and its bytes)
+  float* Li = kCta ? reinterpret_cast<float*>(smem_raw) : reinterpret_cast<float*>(rdiag + d);
   for (int k = threadIdx.x; k < d; k += blockDim.x) {
     int off = colstart(k, d);
     for (int i = k; i < d; ++i, ++off) tab[off] = (uint32_t)i | ((uint32_t)k << 16);
@@ -571,9 +575,16 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   }
   // L⁻¹ in FP32 by forward substitution of the identity, all columns at
   // once: row k is final once scaled, then rows i > k are reduced by it
-  for (int t = sl; t < P; t += LPC) {
-    const uint32_t ik = tab[t];
-    Li[t] = (ik & 0xffffu) == (ik >> 16) ? 1.f : 0.f;
+  if constexpr (kCta) {
+    chain_sync<LPC>();  // the table's last readers are done: L⁻¹ takes its place
+    for (int t = sl; t < P; t += LPC) Li[t] = 0.f;
+    chain_sync<LPC>();
+    for (int cc = sl; cc < d; cc += LPC) Li[colstart(cc, d)] = 1.f;
+  } else {
+    for (int t = sl; t < P; t += LPC) {
+      const uint32_t ik = tab[t];
+      Li[t] = (ik & 0xffffu) == (ik >> 16) ? 1.f : 0.f;
+    }
   }
   chain_sync<LPC>();
   // two rows at a time: rows k and k + 1 are made final (row k scaled; row
@@ -594,15 +605,35 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
       Li[o + k + 1 - cc] = v * ik1;
     }
     chain_sync<LPC>();
-    for (int i = k + 2 + sl; i < d; i += LPC) {
-      const float li0 = float(L[ck + i - k]);       // L(i, k)
-      const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
-      int cc0 = 0;  // colstart(cc)
-      for (int cc = 0; cc <= k; ++cc) {
-        Li[cc0 + i - cc] -= li0 * Li[cc0 + k - cc] + li1 * Li[cc0 + k + 1 - cc];
-        cc0 += d - cc;
+    if constexpr (kCta) {
+      // a CTA's chain: warps over the columns cc of L⁻¹, lanes over the rows
+      // (each row a serial loop over the columns leaves most threads idle at
+      // d = 128 and exposes every load's latency).  Columns k and k + 1 of L
+      // are converted to FP32 once, into y's and x's space (free by now)
+      float* lc = reinterpret_cast<float*>(y);  // lc[i] = L(i, k), lc[d + i] = L(i, k + 1)
+      for (int i = k + 2 + sl; i < d; i += LPC) {
+        lc[i] = float(L[ck + i - k]);
+        lc[d + i] = float(L[ck1 + i - k - 1]);
       }
-      Li[cc0 + i - k - 1] -= li1 * Li[cc0];  // cc = k + 1: Li(k, k + 1) = 0
+      chain_sync<LPC>();
+      const int nw = LPC / 32, w = sl >> 5, ln = sl & 31;
+      for (int cc = w; cc <= k + 1; cc += nw) {
+        const int o = colstart(cc, d) - cc;  // Li(m, cc) at o + m
+        const float a0 = cc <= k ? Li[o + k] : 0.f;  // Li(k, cc); Li(k, k + 1) = 0
+        const float a1 = Li[o + k + 1];              // Li(k + 1, cc)
+        for (int i = k + 2 + ln; i < d; i += 32) Li[o + i] -= lc[i] * a0 + lc[d + i] * a1;
+      }
+    } else {
+      for (int i = k + 2 + sl; i < d; i += LPC) {
+        const float li0 = float(L[ck + i - k]);       // L(i, k)
+        const float li1 = float(L[ck1 + i - k - 1]);  // L(i, k + 1)
+        int cc0 = 0;  // colstart(cc)
+        for (int cc = 0; cc <= k; ++cc) {
+          Li[cc0 + i - cc] -= li0 * Li[cc0 + k - cc] + li1 * Li[cc0 + k + 1 - cc];
+          cc0 += d - cc;
+        }
+        Li[cc0 + i - k - 1] -= li1 * Li[cc0];  // cc = k + 1: Li(k, k + 1) = 0
+      }
     }
     ck = ck1 + (d - k - 1);
     chain_sync<LPC>();
@@ -611,14 +642,43 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   // index for (k, i), k <= i, is the packed index t of (i, k)); the
   // off-diagonal coefficients are doubled
   if (!live) return;
-  for (int t = sl; t < P; t += LPC) {
-    const uint32_t ik = tab[t];
-    const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
-    const float* li = Li + colstart(i, d) - i;  // li[m] = L⁻¹(m, i)
-    const float* lk = Li + colstart(k, d) - k;  // lk[m] = L⁻¹(m, k)
-    float sacc = 0.f;
-    for (int m = i; m < d; ++m) sacc += lk[m] * li[m];
-    split_store(a.Giv, c, t, (i == k) ? sacc : 2.f * sacc);
+  if constexpr (kCta) {
+    // a CTA's chain: the same per-thread dot products over entries t = sl +
+    // LPC·u, with (i, k) walked along the packed columns (the pair table's
+    // place holds L⁻¹ now); the walk stops at the last column
+    int i = 0, k = 0;  // (i, k) of entry t
+    auto advance = [&](int delta) {
+      while (delta > 0 && k < d) {
+        const int left = d - i;  // entries of column k from row i on
+        if (delta < left) {
+          i += delta;
+          delta = 0;
+        } else {
+          delta -= left;
+          ++k;
+          i = k;
+        }
+      }
+    };
+    advance(sl);
+    for (int t = sl; t < P; t += LPC) {
+      const float* li = Li + colstart(i, d) - i;  // li[m] = L⁻¹(m, i)
+      const float* lk = Li + colstart(k, d) - k;  // lk[m] = L⁻¹(m, k)
+      float sacc = 0.f;
+      for (int m = i; m < d; ++m) sacc += lk[m] * li[m];
+      split_store(a.Giv, c, t, (i == k) ? sacc : 2.f * sacc);
+      advance(LPC);
+    }
+  } else {
+    for (int t = sl; t < P; t += LPC) {
+      const uint32_t ik = tab[t];
+      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+      const float* li = Li + colstart(i, d) - i;  // li[m] = L⁻¹(m, i)
+      const float* lk = Li + colstart(k, d) - k;  // lk[m] = L⁻¹(m, k)
+      float sacc = 0.f;
+      for (int m = i; m < d; ++m) sacc += lk[m] * li[m];
+      split_store(a.Giv, c, t, (i == k) ? sacc : 2.f * sacc);
+    }
   }
 }
 
@@ -1732,11 +1792,7 @@ struct Runner {
         chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
     const int per_cta = cf.chains;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
-    // one chain per CTA (lpc >= 128) without the inverse: the FP32 L⁻¹ at the
-    // end of the chain's block is never touched, so it is not allocated
-    // (d = 128: two CTAs per SM instead of one)
-    const size_t smem = (cf.lpc >= 128 && no_inverse) ? cf.smem - (size_t)L.P * sizeof(float)
-                                                      : cf.smem;
+    const size_t smem = cf.smem;
     if (rec) {
       if (a.q_update) a.n_active = rec->flag;
       CholItem it{a, (int)cf.stride};
