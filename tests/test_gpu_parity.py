@@ -286,16 +286,22 @@ IM, GL = "implicit_midpoint", "generalized_leapfrog"
     # position solves, the explicit final momentum
     ("tcgen05", "graph", "fp64", 9, 160, GL), ("tcgen05", "host", "fp64", 9, 160, GL),
     ("simt", "host", "fp64", 9, 160, GL), ("tcgen05", "graph", "fp64", 40, 37, GL),
-    ("tcgen05", "graph", "fp32", 9, 160, GL)])
+    ("tcgen05", "graph", "fp32", 9, 160, GL),
+    # a CTA per chain in the factorisation: 4 warps at d = 100 (FP64 and
+    # FP32), 8 at d = 120 (FP64), with L⁻¹ in the pair table's place
+    ("tcgen05", "graph", "fp64", 100, 16, GL), ("tcgen05", "host", "fp32", 100, 16, GL),
+    ("tcgen05", "graph", "fp64", 120, 16, GL)])
 def test_logreg_batched_per_step(path, loop, chol, d, C, integrator):
     """The batched dense-Fisher path (split-BF16 contractions, FP64 fixed-point
     iterates, FP64 or FP32 factorisation, host-driven loop or one CUDA-graph
     launch, either integrator) against the oracle: per-step positions over
-    10 steps within 1e-5."""
+    10 steps within 1e-5 (1e-4 for the FP32 factorisation at d >= 64, whose
+    rounding grows with d)."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
-    kw = dict(N=300 if d < 32 else 500, d=d, seed=3)
+    kw = dict(N=300 if d < 32 else (500 if d < 64 else 1500), d=d, seed=3)
+    tol = 1e-4 if (chol == "fp32" and d >= 64) else 1e-5
     ot = oracle_target("logreg", **kw)
     dt = device_target("logreg", "mixed", **kw)
     h, L = 0.05, 10
@@ -311,8 +317,8 @@ def test_logreg_batched_per_step(path, loop, chol, d, C, integrator):
     for step in (1, 2, 5, 10):
         st, info = kern(Draws(z, u), st0, dt, h, step)
         e = rel_err(_np(st.position), traj[step - 1].position)
-        assert e < 1e-5, f"step {step}: {e}"
-    assert rel_err(_np(info.energy), oinfo.energy) < 1e-4
+        assert e < tol, f"step {step}: {e}"
+    assert rel_err(_np(info.energy), oinfo.energy) < 10 * tol
     # iteration counts over the 10 solves agree up to solves whose norm lands
     # next to the tolerance (FP32-level rounding of the map, more of it at
     # larger d); no solve may run away towards max_iters
