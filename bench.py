@@ -211,7 +211,8 @@ def run_ours(args, wl):
                                      chol_chains_per_warp=args.chol_cpw,
                                      chain_groups=args.groups, pdl=args.pdl,
                                      gemm_ksplit=args.gemm_ksplit,
-                                     fuse_r2x=not args.no_fuse_r2x)
+                                     fuse_r2x=not args.no_fuse_r2x,
+                                     refine_iterates=not args.no_refine)
         d = wl["d"]
         extra = {}
         state = gj.rmhmc.init(torch.zeros(C, d) + 0.01 * torch.randn(C, d, generator=torch.Generator().manual_seed(rank)), target)
@@ -248,10 +249,10 @@ def run_ours(args, wl):
     acc_sum = torch.zeros(C, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    stats = np.zeros(8, dtype=np.int64)
+    stats = np.zeros(10, dtype=np.int64)
     import ctypes
 
-    buf = (ctypes.c_int64 * 8)()
+    buf = (ctypes.c_int64 * 10)()
     clocks = ClockSampler(local)
     if ws > 1:
         import torch.distributed as dist
@@ -267,21 +268,21 @@ def run_ours(args, wl):
         evs[i][1].record(stream)
         trace[i].copy_(state.position)
         acc_sum += info["acceptance_rate"]
-        n = ctx.lib.gj_stats(ctx.h, buf, 8)
-        stats += np.array(buf[:8], dtype=np.int64)
+        n = ctx.lib.gj_stats(ctx.h, buf, 10)
+        stats += np.array(buf[:10], dtype=np.int64)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     # dominant-kernel timing: the same transitions with CUDA events around every
     # GEMM launch (profiling switches the batched path to its host-driven loop)
-    prof = np.zeros(8, dtype=np.int64)
+    prof = np.zeros(10, dtype=np.int64)
     if wl["sampler"] == "rmhmc":
         L.check(ctx.lib.gj_profile(ctx.h, 1))
         for i in range(min(K, 3)):
             flush.zero_()
             kern.step_inplace(target, state, Z[W + i], U[W + i], info, h, Lsteps, **extra)
-            ctx.lib.gj_stats(ctx.h, buf, 8)
-            prof += np.array(buf[:8], dtype=np.int64)
+            ctx.lib.gj_stats(ctx.h, buf, 10)
+            prof += np.array(buf[:10], dtype=np.int64)
         L.check(ctx.lib.gj_profile(ctx.h, 0))
         torch.cuda.synchronize()
     dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
@@ -351,6 +352,13 @@ def run_ours(args, wl):
                 "nominal_peak": 1.25,
                 "ms_per_transition": round(prof[7] * 1e-6 / min(K, 3), 3),
                 "launches_per_transition": int(prof[5] // min(K, 3))}
+        if prof[8] > 0:
+            # the position iterates' solves by FP32 factor + FP64 refinement
+            # (same kernel, not part of the FP64 rate above)
+            roof["refined_iterate_solves"] = {
+                "kernel": "chol_kernel (FP32 factor, FP64-residual refinement)",
+                "ms_per_transition": round(prof[9] * 1e-6 / min(K, 3), 3),
+                "launches_per_transition": int(prof[8] // min(K, 3))}
     elif wl["sampler"] == "lmcmonge":
         # the warp-per-chain Monge kernel runs on the FP32 pipe: algorithmic
         # flops (MONGE_FLOPS_PER_DIM·D per chain and step) against the FP32
@@ -379,6 +387,7 @@ def run_ours(args, wl):
                    "chain_groups": args.groups or "auto", "pdl": args.pdl, "gemm_tile_n": args.gemm_tile_n or "auto",
                    "gemm_ksplit": args.gemm_ksplit or "auto",
                    "fuse_r2x": not args.no_fuse_r2x,
+                   "refine_iterates": not args.no_refine and args.cholesky == "fp64",
                    "gemm_accumulators": args.gemm_accumulators,
                    "gemm_ctas_per_sm": 1 if args.gemm_one_cta else (2 if args.gemm_two_cta else "auto"),
                    "l2": "flushed between timed steps (256 MB write)",
@@ -427,6 +436,8 @@ def run_batch(args, wl):
         pb.set_option(L.GJ_OPT_CHOL_FP64, 0)
     if args.chol_cpw:
         pb.set_option(L.GJ_OPT_CHOL_CHAINS_PER_WARP, args.chol_cpw)
+    if args.no_refine:
+        pb.set_option(L.GJ_OPT_REFINE_ITERATES, 0)
     del data
     g0 = torch.Generator().manual_seed(rank)
     state = pb.init([0.01 * torch.randn(C, int(d), generator=g0) for d in ds])
@@ -501,6 +512,7 @@ def run_batch(args, wl):
                                "one CUDA graph per transition of grouped launches: every stage "
                                "one grid over a bucket of posteriors, each bucket a branch")),
                    "cholesky": args.cholesky,
+                   "refine_iterates": not args.no_refine and args.cholesky == "fp64",
                    "chol_chains_per_warp": args.chol_cpw or "auto",
                    "buckets": None if (args.batch_branches or args.batch_pool) else
                               (args.batch_buckets or "auto"),
@@ -1124,6 +1136,9 @@ def main():
     ap.add_argument("--no-fuse-r2x", action="store_true",
                     help="store r2 and contract it by its own GEMM in the momentum evaluations "
                          "(default: r2·X inside the S GEMM's epilogue)")
+    ap.add_argument("--no-refine", action="store_true",
+                    help="factor the generalized leapfrog's position iterates in FP64 (default: "
+                         "FP32 factor, solve refined with FP64 residuals)")
     ap.add_argument("--pdl", action="store_true",
                     help="launch the batched pipeline's kernels with programmatic dependent launch")
     ap.add_argument("--groups", type=int, default=0,

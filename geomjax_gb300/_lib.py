@@ -28,6 +28,7 @@ GJ_OPT_BATCH_GRAPH = 9
 GJ_OPT_MONGE_WARP = 10
 GJ_OPT_FUSE_R2X = 11
 GJ_OPT_BATCH_BUCKETS = 12
+GJ_OPT_REFINE_ITERATES = 13
 
 
 class GjTarget(ctypes.Structure):

@@ -96,6 +96,7 @@ struct gj_ctx {
   int ksplit;     // GJ_OPT_GEMM_KSPLIT (0 = automatic)
   int monge_warp; // GJ_OPT_MONGE_WARP
   int fuse_r2x;   // GJ_OPT_FUSE_R2X
+  int refine;     // GJ_OPT_REFINE_ITERATES
   // batched dense-Fisher path: one context per chain group; in graph mode
   // the groups' transitions run on their own streams, forked from and joined
   // to the caller's stream by events, so one group's factorisation can share
@@ -164,6 +165,7 @@ int ensure_groups(gj_ctx* ctx, const gj::TargetDev& t) {
     gj::logreg_batched_set_pdl(lb, ctx->pdl);
     gj::logreg_batched_set_gemm_ksplit(lb, ctx->ksplit);
     gj::logreg_batched_set_fuse_r2x(lb, ctx->fuse_r2x);
+    gj::logreg_batched_set_refine_iterates(lb, ctx->refine);
     // every group makes the automatic choices of the whole context, so that
     // results do not depend on the group count
     gj::logreg_batched_set_auto_chains(lb, ctx->C);
@@ -224,6 +226,7 @@ int32_t gj_create(const gj_target* target, int32_t sampler, int32_t precision,
   c->ksplit = 0;
   c->monge_warp = 1;
   c->fuse_r2x = 1;
+  c->refine = 1;
   *out = c;
   return GJ_OK;
 }
@@ -276,6 +279,12 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value) {
     if (value < 0 || value > 1) return fail(GJ_EINVAL, "fused r2·X flag must be 0 or 1");
     ctx->fuse_r2x = (int)value;
     for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_fuse_r2x(lb, ctx->fuse_r2x);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_REFINE_ITERATES) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "refined iterate flag must be 0 or 1");
+    ctx->refine = (int)value;
+    for (gj::LogregBatched* lb : ctx->lbs) gj::logreg_batched_set_refine_iterates(lb, ctx->refine);
     return GJ_OK;
   }
   if (key == GJ_OPT_MONGE_WARP) {
@@ -528,7 +537,7 @@ int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s
 
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n < 0) return fail(GJ_EINVAL, "bad arguments");
-  int64_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (!ctx->lbs.empty()) {
     for (gj::LogregBatched* lb : ctx->lbs) {
       const gj::LogregStats s = gj::logreg_batched_stats(lb);
@@ -540,11 +549,13 @@ int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
       v[5] += s.chol_launches;
       v[6] += (int64_t)s.chol_flops;
       v[7] += (int64_t)s.chol_ns;
+      v[8] += s.refine_launches;
+      v[9] += (int64_t)s.refine_ns;
     }
   } else {
     v[2] = 1;  // the per-chain and warp-per-chain paths launch one kernel per step
   }
-  const int m = n < 8 ? n : 8;
+  const int m = n < 10 ? n : 10;
   for (int i = 0; i < m; ++i) out[i] = v[i];
   return m;
 }
@@ -841,6 +852,11 @@ int32_t gj_batch_set_option(gj_batch* b, int32_t key, int64_t value) {
   if (key == GJ_OPT_FUSE_R2X) {
     if (value < 0 || value > 1) return fail(GJ_EINVAL, "fused r2·X flag must be 0 or 1");
     for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_fuse_r2x(lb, (int)value);
+    return GJ_OK;
+  }
+  if (key == GJ_OPT_REFINE_ITERATES) {
+    if (value < 0 || value > 1) return fail(GJ_EINVAL, "refined iterate flag must be 0 or 1");
+    for (gj::LogregBatched* lb : b->lbs) gj::logreg_batched_set_refine_iterates(lb, (int)value);
     return GJ_OK;
   }
   if (key == GJ_OPT_BATCH_BUCKETS) {

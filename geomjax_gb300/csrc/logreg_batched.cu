@@ -103,6 +103,10 @@ struct CholArgs {
   double* Lout;        // DRAW / EVAL: the packed factor, kept for later solves (may be NULL)
   float* Lout32;       // DRAW / EVAL: the same in FP32 (may be NULL)
   int no_inverse;      // EVAL: stop after u = G⁻¹p (no L⁻¹, no packed G⁻¹)
+  // EVAL with no_inverse (FP64, LPC <= 32, d >= 3): u by an FP32 factor and
+  // FP64-residual refinement (refined_solve), the FP64 factorisation only
+  // for the chains whose refinement does not converge
+  int refine;
   // EVAL with no_inverse: the generalized leapfrog's position update
   // q' = q0 + h/2 [G⁻¹(q0) + G⁻¹(q_k)] p½ (UP_GLQN of update_kernel) done
   // here with u = G⁻¹(q_k)p½, with its convergence test
@@ -258,6 +262,12 @@ __device__ __forceinline__ double group_max(double v) {
   return v;
 }
 template <int LPC>
+__device__ __forceinline__ float group_maxf(float v) {
+#pragma unroll
+  for (int o = LPC >> 1; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <int LPC>
 __device__ __forceinline__ bool group_any(bool b) {
   int v = b ? 1 : 0;
 #pragma unroll
@@ -313,6 +323,352 @@ __device__ __forceinline__ bool chain_any(bool b) {
   else return __syncthreads_or(b ? 1 : 0) != 0;
 }
 
+// Right-looking Cholesky of one chain's packed matrix L (T = double / float),
+// in place: the strict lower triangle becomes the factor's, rdiag[j] =
+// 1/L_jj, and the diagonal keeps the pivots (DRAW: L_jj).  log det G = log Π
+// pivots is accumulated as mantissa pm · 2^pe (want_ld), so that one
+// logarithm is taken per chain.  With `border` the right-hand side in y
+// rides along as a bordered row: at step j, y_j is scaled with the pivot and
+// y_k (k > j) updated in the same phase as the trailing triangle, so y ends
+// as L⁻¹y without a separate serial forward substitution.  A non-positive
+// or non-finite pivot sets `bad`.
+template <typename T, int LPC>
+__device__ __forceinline__ void factor_packed(T* L, T* rdiag, T* y, const uint32_t* tab, int d,
+                                              int P, int sl, bool border, bool draw,
+                                              bool want_ld, bool& bad, double& pm, int& pe) {
+  constexpr bool kCta = LPC > 32;
+  // The FP64 factorisation takes one column per step: its DFMA count bounds
+  // it, and rank-2 blocking (one pass over the trailing triangle for two
+  // columns) measured no faster for T = double.  For T = float, where
+  // latency bounds the kernel, columns are taken two at a time: pivot j,
+  // scale column j, update column j + 1 with it, pivot j + 1, scale column
+  // j + 1, then one pass applies both columns to the trailing triangle.
+  // pivot(j): 1/L_jj from the current diagonal, log det product, and the
+  // bordered y_j (all lanes compute the same scalars; lane 0 of the chain
+  // writes them)
+  auto pivot = [&](int j, int cj) -> T {
+    if constexpr (kCta) {
+      // a CTA per chain: thread 0 alone takes the pivot (the FP64 pipe issues
+      // each warp's copy of it at full cost) and publishes 1/L_jj; bad, pm
+      // and pe, read only by thread 0 at the end, stay its own
+      if (sl == 0) {
+        const T djj = L[cj];
+        const T inv = pivot_rsqrt(djj, bad);
+        if (want_ld) ld_accumulate(pm, pe, double(djj));
+        if (draw) L[cj] = djj * inv;  // L_jj, read only by p = L z
+        rdiag[j] = inv;
+        if (border) y[j] *= inv;
+      }
+      chain_sync<LPC>();
+      const T inv = rdiag[j];
+      for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
+      chain_sync<LPC>();
+      return inv;
+    }
+    const T djj = L[cj];
+    const T inv = pivot_rsqrt(djj, bad);  // 1/L_jj
+    if (want_ld) ld_accumulate(pm, pe, double(djj));
+    chain_sync<LPC>();
+    if (sl == 0) {
+      if (draw) L[cj] = djj * inv;  // L_jj, read only by p = L z
+      rdiag[j] = inv;
+      if (border) y[j] *= inv;
+    }
+    for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
+    chain_sync<LPC>();
+    return inv;
+  };
+  constexpr bool kRank2 = sizeof(T) == sizeof(float);
+  int cj = 0;  // colstart(j)
+  for (int j = 0; j < d; j += kRank2 ? 2 : 1) {
+    pivot(j, cj);
+    const int cj1 = cj + (d - j);  // colstart(j + 1)
+    if (!kRank2 || j + 1 == d) {
+      // rank-1 step: bordered y and the trailing triangle with column j
+      if (border) {
+        const T yj = y[j];
+        for (int k = j + 1 + sl; k < d; k += LPC) y[k] -= yj * L[cj + k - j];
+      }
+      const T* __restrict__ colj = L + cj - j;  // colj[i] = L(i, j)
+      T* __restrict__ tr = L;
+#pragma unroll 4
+      for (int t = cj1 + sl; t < P; t += LPC) {
+        const uint32_t ik = tab[t];
+        tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
+      }
+      cj = cj1;
+      chain_sync<LPC>();
+      continue;
+    }
+    // column j + 1 (rows j + 1 ..) and y_{j+1} reduced by column j
+    {
+      const T l10 = L[cj + 1];  // L(j + 1, j)
+      for (int i = j + 1 + sl; i < d; i += LPC) L[cj1 + i - j - 1] -= L[cj + i - j] * l10;
+      if (border && sl == 0) y[j + 1] -= y[j] * l10;
+    }
+    chain_sync<LPC>();
+    pivot(j + 1, cj1);
+    // trailing triangle (columns k >= j + 2): both columns are read-only
+    // here and disjoint from the entries written
+    const int cn = cj1 + (d - j - 1);  // colstart(j + 2)
+    const T* __restrict__ c0 = L + cj - j;        // c0[i] = L(i, j)
+    const T* __restrict__ c1 = L + cj1 - j - 1;   // c1[i] = L(i, j + 1)
+    T* __restrict__ tr = L;
+    if (border) {
+      const T y0 = y[j], y1 = y[j + 1];
+      for (int k = j + 2 + sl; k < d; k += LPC) y[k] -= y0 * c0[k] + y1 * c1[k];
+    }
+#pragma unroll 4
+    for (int t = cn + sl; t < P; t += LPC) {
+      const uint32_t ik = tab[t];
+      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+      tr[t] -= c0[i] * c0[k] + c1[i] * c1[k];
+    }
+    cj = cn;
+    chain_sync<LPC>();
+  }
+}
+
+// y ← L⁻¹y on a factor from factor_packed (column-oriented, one column per
+// step)
+template <typename T, int LPC>
+__device__ __forceinline__ void forward_subst(const T* L, const T* rdiag, T* y, int d, int sl) {
+  int cj = 0;  // colstart(j)
+  for (int j = 0; j < d; ++j) {
+    const T yj = y[j] * rdiag[j];
+    chain_sync<LPC>();
+    if (sl == 0) y[j] = yj;
+    for (int i = j + 1 + sl; i < d; i += LPC) y[i] -= L[cj + i - j] * yj;
+    cj += d - j;
+    chain_sync<LPC>();
+  }
+}
+
+// x ← L⁻ᵀx, column-oriented backward substitution (row j of L is L(j, i) at
+// colstart(i) + j − i)
+template <typename T, int LPC>
+__device__ __forceinline__ void backward_subst(const T* L, const T* rdiag, T* x, int d, int sl) {
+  for (int j = d - 1; j >= 0; --j) {
+    const T xj = x[j] * rdiag[j];
+    chain_sync<LPC>();
+    if (sl == 0) x[j] = xj;
+    for (int i = sl; i < j; i += LPC) x[i] -= L[colstart(i, d) + j - i] * xj;
+    chain_sync<LPC>();
+  }
+}
+
+// Most corrections a refined solve applies before it gives the chain back to
+// the FP64 factorisation.
+constexpr int kRefineMax = 4;
+
+// The stopping rule of a refined solve, on norms relative to ‖x₀‖∞ (float32
+// scalars: the rule needs a few bits of them): er = ‖dx_k‖/‖x₀‖, pr = the
+// previous correction's.  Converged once the next step's predicted size
+// er²/pr is below 2⁻⁴⁴ (x then as accurate as an FP64 factorisation's solve,
+// whose own error is about κ(G)·d·2⁻⁵³); failed when a correction is not
+// finite or shrinks by less than half.  Returns 1 = converged (apply dx),
+// 0 = apply dx and go on, −1 = failed.
+__device__ __forceinline__ int refine_verdict(float er, float pr, bool nonfinite) {
+  if (nonfinite) return -1;
+  if (er * er <= 0x1p-44f * pr) return 1;
+  if (er > 0.5f * pr) return -1;
+  return 0;
+}
+
+// x = G⁻¹p for a position iterate of the generalized leapfrog, one chain
+// per sub-group of LPC <= 32 lanes, by mixed-precision iterative refinement
+// (Wilkinson 1963, Moler 1967; Carson and Higham, SIAM J. Sci. Comput. 40,
+// 2018): G = Gram + prior·I is factored in FP32 (Lf, rdf; the first solution
+// from the bordered factorisation), then x += G₃₂⁻¹(p − G·x) with the
+// residual formed in FP64 from the FP64 Gram (G, packed, without the prior)
+// and the prior.  Each correction shrinks the error by about κ(G)·d·2⁻²⁴
+// (refine_verdict stops it).  Returns false (x then unspecified) when the
+// FP32 factorisation breaks down, the corrections fail or kRefineMax of them
+// do not converge: the caller then factors G in FP64.  The loop runs the
+// same number of times for all chains of the warp; a chain that has
+// converged (or failed) applies no further corrections, so its x depends on
+// its own data only.
+template <int LPC>
+__device__ bool refined_solve(const double* G, const float* gv, double prior, float* Lf,
+                              float* rdf, float* wf, double* x, const uint32_t* tab,
+                              const double* p, bool live, int d, int P, int sl) {
+  const float priorf = float(prior);
+  for (int t = sl; t < P; t += LPC) {
+    const uint32_t ik = tab[t];
+    const bool diag = (ik & 0xffffu) == (ik >> 16);
+    Lf[t] = live ? gv[t] + (diag ? priorf : 0.f) : (diag ? 1.f : 0.f);
+  }
+  for (int i = sl; i < d; i += LPC) wf[i] = live ? float(p[i]) : 0.f;
+  chain_sync<LPC>();
+  bool bad = false;
+  double pm = 1.0;
+  int pe = 0;
+  factor_packed<float, LPC>(Lf, rdf, wf, tab, d, P, sl, true, false, false, bad, pm, pe);
+  backward_subst<float, LPC>(Lf, rdf, wf, d, sl);
+  float xm = 0.f;
+  for (int i = sl; i < d; i += LPC) {
+    x[i] = double(wf[i]);
+    bad |= !isfinite(wf[i]);
+    xm = fmaxf(xm, fabsf(wf[i]));
+  }
+  bool ok = !chain_any<LPC>(bad);
+  const float xn = group_maxf<LPC>(xm);  // ‖x₀‖∞
+  bool conv = ok && xn == 0.f;           // p = 0: x = 0 exactly
+  float pr = 1.f;                        // ‖dx₀‖ / ‖x₀‖
+  for (int k = 0; k < kRefineMax && __any_sync(0xffffffffu, ok && !conv); ++k) {
+    chain_sync<LPC>();
+    // r = p − prior·x − Gram·x in FP64, row i walked along the Gram's packed
+    // row: columns m < i down the packed columns, m >= i along column i (one
+    // trip count for every lane)
+    for (int i = sl; i < d; i += LPC) {
+      double s = live ? fma(-prior, x[i], p[i]) : 0.0;
+      const int ci = colstart(i, d) - i;
+      int cm = 0;  // colstart(m)
+      for (int m = 0; m < d; ++m) {
+        s = fma(-G[m < i ? cm + i - m : ci + m], x[m], s);
+        cm += d - m;
+      }
+      wf[i] = float(s);
+    }
+    chain_sync<LPC>();
+    forward_subst<float, LPC>(Lf, rdf, wf, d, sl);
+    backward_subst<float, LPC>(Lf, rdf, wf, d, sl);
+    float em = 0.f;
+    bool nf = false;
+    for (int i = sl; i < d; i += LPC) {
+      nf |= !isfinite(wf[i]);
+      em = fmaxf(em, fabsf(wf[i]));
+    }
+    nf = chain_any<LPC>(nf);
+    const float er = group_maxf<LPC>(em) / xn;
+    if (ok && !conv) {  // uniform over the chain's lanes
+      const int v = refine_verdict(er, pr, nf);
+      if (v < 0) {
+        ok = false;
+      } else {
+        for (int i = sl; i < d; i += LPC) x[i] += double(wf[i]);
+        conv = v > 0;
+        pr = er;
+      }
+    }
+  }
+  chain_sync<LPC>();
+  return ok && conv;
+}
+
+// The same for one chain per warp and d <= 32, on registers: lane i holds
+// row i of the FP32 factor (the column broadcasts of the factorisation and
+// the substitutions are warp shuffles), its component of y, x and the
+// residual; the strict lower triangle is also written by rows to Lrow
+// (packed, d(d−1)/2 floats), from which the backward substitution reads its
+// columns.  The rows of G come from the FP32 Gram gv of the chain (global
+// memory), the residual from its FP64 copy G in shared memory and from x in
+// xs (shared, FP64).  The warp holds one live chain.
+__device__ __forceinline__ bool refined_solve_w32(const double* G, const float* gv, double prior,
+                                                  float* Lrow, double* xs, const double* p, int d,
+                                                  int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  const int i = lane;
+  const bool in = i < d;
+  float row[32];  // row[k] = G₃₂(i, k), then L(i, k), for k <= i
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    float g = 0.f;
+    if (k <= i && in) g = gv[colstart(k, d) + i - k];
+    if (k == i) g += float(prior);
+    row[k] = g;
+  }
+  const double pi = in ? p[i] : 0.0;
+  float y = float(pi);
+  float rinv = 0.f;  // 1 / L_ii
+  bool bad = false;
+  // right-looking, one column per step, with the bordered y = L⁻¹p
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    if (j < d) {  // uniform
+      const float inv = pivot_rsqrt(__shfl_sync(kAll, row[j], j), bad);
+      const float lij = row[j] * inv;  // L(i, j) for i > j
+      const float yj = __shfl_sync(kAll, y, j) * inv;
+      if (i == j) {
+        rinv = inv;
+        y = yj;
+      } else if (i > j) {
+        row[j] = lij;
+        y -= lij * yj;
+      }
+#pragma unroll
+      for (int k = j + 1; k < 32; ++k) {
+        if (k < d) {
+          const float lkj = __shfl_sync(kAll, lij, k);
+          if (i >= k) row[k] -= lij * lkj;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 31; ++k)
+    if (k < i && in) Lrow[i * (i - 1) / 2 + k] = row[k];
+  __syncwarp();
+  auto forward = [&](float v) -> float {  // L⁻¹v
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      if (j < d) {
+        const float vj = __shfl_sync(kAll, v * rinv, j);
+        if (i == j) v = vj;
+        else if (i > j) v -= row[j] * vj;
+      }
+    }
+    return v;
+  };
+  auto backward = [&](float v) -> float {  // L⁻ᵀv, columns of L from Lrow
+#pragma unroll
+    for (int j = 31; j >= 0; --j) {
+      if (j < d) {
+        const float vj = __shfl_sync(kAll, v * rinv, j);
+        if (i == j) v = vj;
+        else if (i < j) v -= Lrow[j * (j - 1) / 2 + i] * vj;
+      }
+    }
+    return v;
+  };
+  const float w = backward(y);  // x₀ = G₃₂⁻¹p
+  double xi = double(w);
+  if (in) xs[i] = xi;
+  bool ok = !__any_sync(kAll, bad || !isfinite(w));
+  const float xn = group_maxf<32>(fabsf(w));
+  bool conv = ok && xn == 0.f;
+  float pr = 1.f;
+  for (int k = 0; k < kRefineMax && ok && !conv; ++k) {  // uniform: one chain
+    __syncwarp();
+    // r_i = p_i − prior·x_i − Σ_m Gram(i, m)·x_m in FP64 (packed row walk as
+    // in refined_solve)
+    double s = fma(-prior, xi, pi);
+    if (in) {
+      const int ci = colstart(i, d) - i;
+      int cm = 0;
+      for (int m = 0; m < d; ++m) {
+        s = fma(-G[m < i ? cm + i - m : ci + m], xs[m], s);
+        cm += d - m;
+      }
+    }
+    const float dx = backward(forward(in ? float(s) : 0.f));
+    const bool nf = __any_sync(kAll, !isfinite(dx));
+    const float er = group_maxf<32>(fabsf(dx)) / xn;
+    const int v = refine_verdict(er, pr, nf);
+    if (v < 0) {
+      ok = false;
+    } else {
+      xi += double(dx);
+      conv = v > 0;
+      pr = er;
+      __syncwarp();
+      if (in) xs[i] = xi;
+    }
+  }
+  __syncwarp();
+  return ok && conv;
+}
+
 // block bx of the factorisation (chol_kernel, or an item of a grouped launch)
 // LPC = 128 / 256: one chain per CTA of four / eight warps (large d, where
 // one warp per chain leaves most of an SM's FP64 units idle); its barrier is
@@ -346,188 +702,131 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   pdl_wait();
   const bool live = c < a.C && !(a.mode == CH_EVAL && a.active && !a.active[c]);
   if (__all_sync(0xffffffffu, !live)) return;  // uniform per warp
-  // G = Gvec + I/s²: the packed layouts coincide; idle slots get the identity
+  // G = Gvec + I/s²: the packed layouts coincide; idle slots get the identity.
+  // The refined solves of the position iterates keep the Gram alone (their
+  // residuals add the prior) and add the prior before an FP64 fallback.
+  constexpr bool kRefinable = !kCta && sizeof(F) == sizeof(double);
+  const bool refine = kRefinable && a.refine;
   for (int t = sl; t < P; t += LPC) {
     const uint32_t ik = tab[t];
     const bool diag = (ik & 0xffffu) == (ik >> 16);
     F g;
     if (live) {
       g = F(a.Gv[(size_t)c * a.gv_ld + t]);
-      if (diag) g += F(a.prior_inv);
+      if (diag && !refine) g += F(a.prior_inv);
     } else {
       g = diag ? F(1) : F(0);
     }
     L[t] = g;
   }
   chain_sync<LPC>();
-  // right-looking Cholesky; log det G = log Π pivots, accumulated as
-  // mantissa · 2^exponent so that one logarithm is taken per chain.  Outside
-  // DRAW the right-hand side p is known, so y = L⁻¹p rides along as a
-  // bordered row: at step j, y_j is scaled with the pivot and y_k (k > j)
-  // updated in the same phase as the trailing triangle (no separate serial
-  // forward substitution).
   const bool border = a.mode != CH_DRAW;
-  if (border) {
-    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
-  }
   bool bad = false;
   // log det G is needed for the energies (DRAW at the start, ENERGY at the
   // proposal); the map evaluations (EVAL) skip it
   const bool want_ld = a.mode != CH_EVAL;
   double pm = 1.0;
   int pe = 0;
-  // The FP64 factorisation takes one column per step: its DFMA count bounds
-  // it, and rank-2 blocking (one pass over the trailing triangle for two
-  // columns) measured no faster for F = double.  For F = float, where
-  // latency bounds the kernel, columns are taken two at a time: pivot j,
-  // scale column j, update column j + 1 with it, pivot j + 1, scale column
-  // j + 1, then one pass applies both columns to the trailing triangle.
-  // pivot(j): 1/L_jj from the current diagonal, log det product, and the
-  // bordered y_j (all lanes compute the same scalars; lane 0 of the chain
-  // writes them)
-  auto pivot = [&](int j, int cj) -> F {
-    if constexpr (kCta) {
-      // a CTA per chain: thread 0 alone takes the pivot (the FP64 pipe issues
-      // each warp's copy of it at full cost) and publishes 1/L_jj; bad, pm
-      // and pe, read only by thread 0 at the end, stay its own
-      if (sl == 0) {
-        const F djj = L[cj];
-        const F inv = pivot_rsqrt(djj, bad);
-        if (want_ld) ld_accumulate(pm, pe, double(djj));
-        if (a.mode == CH_DRAW) L[cj] = djj * inv;  // L_jj, read only by p = L z
-        rdiag[j] = inv;
-        if (border) y[j] *= inv;
+  // The position iterates (a.refine, set with no_inverse for F = double,
+  // LPC <= 32 and d >= 3) solve by mixed-precision refinement: FP32 factor,
+  // FP64 residuals (refined_solve), the result in xv.  A warp factors in
+  // FP64 when one of its chains needs it; the chains already solved park x
+  // in L⁻¹'s area meanwhile (free here; P floats hold d doubles for d >= 3).
+  bool fp64 = true;   // this warp runs the FP64 factorisation
+  bool kept = false;  // this chain's refined x is final
+  if constexpr (kRefinable) {
+    if (refine) {  // uniform
+      const float* gv = live ? a.Gv + (size_t)c * a.gv_ld : nullptr;
+      const double* pc = live ? a.pc + (size_t)c * d : nullptr;
+      bool w32 = false;
+      if constexpr (LPC == 32) w32 = d <= 32;
+      if (w32) {
+        kept = refined_solve_w32(L, gv, a.prior_inv, Li, xv, pc, d, sl);
+      } else {
+        float* rdf = reinterpret_cast<float*>(rdiag);  // 2d floats in rdiag's d doubles
+        kept = refined_solve<LPC>(L, gv, a.prior_inv, Li, rdf, rdf + d, xv, tab, pc, live, d, P,
+                                  sl);
       }
-      chain_sync<LPC>();
-      const F inv = rdiag[j];
-      for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
-      chain_sync<LPC>();
-      return inv;
-    }
-    const F djj = L[cj];
-    const F inv = pivot_rsqrt(djj, bad);  // 1/L_jj
-    if (want_ld) ld_accumulate(pm, pe, double(djj));
-    chain_sync<LPC>();
-    if (sl == 0) {
-      if (a.mode == CH_DRAW) L[cj] = djj * inv;  // L_jj, read only by p = L z
-      rdiag[j] = inv;
-      if (border) y[j] *= inv;
-    }
-    for (int i = j + 1 + sl; i < d; i += LPC) L[cj + i - j] *= inv;
-    chain_sync<LPC>();
-    return inv;
-  };
-  constexpr bool kRank2 = sizeof(F) == sizeof(float);
-  int cj = 0;  // colstart(j)
-  for (int j = 0; j < d; j += kRank2 ? 2 : 1) {
-    pivot(j, cj);
-    const int cj1 = cj + (d - j);  // colstart(j + 1)
-    if (!kRank2 || j + 1 == d) {
-      // rank-1 step: bordered y and the trailing triangle with column j
-      if (border) {
-        const F yj = y[j];
-        for (int k = j + 1 + sl; k < d; k += LPC) y[k] -= yj * L[cj + k - j];
+      fp64 = __any_sync(0xffffffffu, !kept);
+      if (fp64) {
+        if (kept) {
+          double* park = reinterpret_cast<double*>(Li);
+          for (int i = sl; i < d; i += LPC) park[i] = xv[i];
+        }
+        if (live)
+          for (int i = sl; i < d; i += LPC) L[colstart(i, d)] += F(a.prior_inv);
+        chain_sync<LPC>();
       }
-      const F* __restrict__ colj = L + cj - j;  // colj[i] = L(i, j)
-      F* __restrict__ tr = L;
-#pragma unroll 4
-      for (int t = cj1 + sl; t < P; t += LPC) {
-        const uint32_t ik = tab[t];
-        tr[t] -= colj[ik & 0xffffu] * colj[ik >> 16];
-      }
-      cj = cj1;
-      chain_sync<LPC>();
-      continue;
     }
-    // column j + 1 (rows j + 1 ..) and y_{j+1} reduced by column j
-    {
-      const F l10 = L[cj + 1];  // L(j + 1, j)
-      for (int i = j + 1 + sl; i < d; i += LPC) L[cj1 + i - j - 1] -= L[cj + i - j] * l10;
-      if (border && sl == 0) y[j + 1] -= y[j] * l10;
-    }
-    chain_sync<LPC>();
-    pivot(j + 1, cj1);
-    // trailing triangle (columns k >= j + 2): both columns are read-only
-    // here and disjoint from the entries written
-    const int cn = cj1 + (d - j - 1);  // colstart(j + 2)
-    const F* __restrict__ c0 = L + cj - j;        // c0[i] = L(i, j)
-    const F* __restrict__ c1 = L + cj1 - j - 1;   // c1[i] = L(i, j + 1)
-    F* __restrict__ tr = L;
+  }
+  if (fp64) {
     if (border) {
-      const F y0 = y[j], y1 = y[j + 1];
-      for (int k = j + 2 + sl; k < d; k += LPC) y[k] -= y0 * c0[k] + y1 * c1[k];
+      for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.pc[(size_t)c * d + i]) : F(0);
     }
-#pragma unroll 4
-    for (int t = cn + sl; t < P; t += LPC) {
-      const uint32_t ik = tab[t];
-      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
-      tr[t] -= c0[i] * c0[k] + c1[i] * c1[k];
-    }
-    cj = cn;
-    chain_sync<LPC>();
+    factor_packed<F, LPC>(L, rdiag, y, tab, d, P, sl, border, a.mode == CH_DRAW, want_ld, bad,
+                          pm, pe);
   }
   pdl_trigger();  // the factorisation is done; the successor may be scheduled
-  if (sl == 0 && live) {
-    if (want_ld) a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
-    if (bad) a.bad[c] = 1;
-  }
-  if ((a.Lout || a.Lout32) && live) {  // the factor at this position serves the
-    // momentum solves, with 1/L_jj in place of the diagonal (the solves multiply)
-    for (int t = sl; t < P; t += LPC) {
-      const uint32_t ik = tab[t];
-      const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
-      const double v = i == k ? double(rdiag[i]) : double(L[t]);
-      if (a.Lout) a.Lout[(size_t)c * P + t] = v;
-      if (a.Lout32) a.Lout32[(size_t)c * P + t] = float(v);
+  if (fp64) {
+    if (sl == 0 && live) {
+      if (want_ld) a.logdet[c] = bad ? NAN : log(pm) + pe * 0.69314718055994530942;
+      if (bad) a.bad[c] = 1;
     }
-  }
-  // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
-  // column-oriented forward substitution
-  if (a.mode == CH_DRAW) {
-    for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
-    chain_sync<LPC>();
-    double zz = 0.0;
-    for (int i = sl; i < d; i += LPC) {
-      F sacc = 0;
-      int ck = 0;
-      for (int k = 0; k <= i; ++k) {
-        sacc += L[ck + i - k] * y[k];
-        ck += d - k;
+    if ((a.Lout || a.Lout32) && live) {  // the factor at this position serves the
+      // momentum solves, with 1/L_jj in place of the diagonal (the solves multiply)
+      for (int t = sl; t < P; t += LPC) {
+        const uint32_t ik = tab[t];
+        const int i = (int)(ik & 0xffffu), k = (int)(ik >> 16);
+        const double v = i == k ? double(rdiag[i]) : double(L[t]);
+        if (a.Lout) a.Lout[(size_t)c * P + t] = v;
+        if (a.Lout32) a.Lout32[(size_t)c * P + t] = float(v);
       }
-      if (live) {
-        a.p0[(size_t)c * d + i] = double(sacc);
-        a.pc[(size_t)c * d + i] = double(sacc);
-        if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
+    }
+    // right-hand side: DRAW p = L z (and L⁻¹p = z); otherwise y = L⁻¹ p by
+    // column-oriented forward substitution
+    if (a.mode == CH_DRAW) {
+      for (int i = sl; i < d; i += LPC) y[i] = live ? F(a.z[(size_t)c * d + i]) : F(0);
+      chain_sync<LPC>();
+      double zz = 0.0;
+      for (int i = sl; i < d; i += LPC) {
+        F sacc = 0;
+        int ck = 0;
+        for (int k = 0; k <= i; ++k) {
+          sacc += L[ck + i - k] * y[k];
+          ck += d - k;
+        }
+        if (live) {
+          a.p0[(size_t)c * d + i] = double(sacc);
+          a.pc[(size_t)c * d + i] = double(sacc);
+          if (a.mom_info) a.mom_info[(size_t)c * d + i] = float(sacc);
+        }
+        zz += double(y[i]) * double(y[i]);
       }
-      zz += double(y[i]) * double(y[i]);
+      zz = chain_sum<LPC>(zz);
+      if (sl == 0 && live) a.quad[c] = zz;
+    } else {  // y = L⁻¹p was formed with the factor
+      if (a.mode == CH_ENERGY) {
+        double q = 0.0;
+        for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
+        q = chain_sum<LPC>(q);
+        if (sl == 0 && live) a.quad[c] = q;
+        if (!a.vel_info) return;  // uniform: the proposal velocity was not asked for
+      }
     }
-    zz = chain_sum<LPC>(zz);
-    if (sl == 0 && live) a.quad[c] = zz;
-  } else {  // y = L⁻¹p was formed with the factor
-    if (a.mode == CH_ENERGY) {
-      double q = 0.0;
-      for (int i = sl; i < d; i += LPC) q += double(y[i]) * double(y[i]);
-      q = chain_sum<LPC>(q);
-      if (sl == 0 && live) a.quad[c] = q;
-      if (!a.vel_info) return;  // uniform: the proposal velocity was not asked for
+    chain_sync<LPC>();
+    // u = L⁻ᵀ y
+    for (int i = sl; i < d; i += LPC) xv[i] = y[i];
+    chain_sync<LPC>();
+    backward_subst<F, LPC>(L, rdiag, xv, d, sl);
+    if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
+      if (live)
+        for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = float(-xv[i]);
+      return;
     }
-  }
-  chain_sync<LPC>();
-  // u = L⁻ᵀ y, column-oriented backward substitution (row j of L is
-  // L(j, i) at colstart(i) + j − i)
-  for (int i = sl; i < d; i += LPC) xv[i] = y[i];
-  chain_sync<LPC>();
-  for (int j = d - 1; j >= 0; --j) {
-    const F xj = xv[j] * rdiag[j];
-    chain_sync<LPC>();
-    if (sl == 0) xv[j] = xj;
-    for (int i = sl; i < j; i += LPC) xv[i] -= L[colstart(i, d) + j - i] * xj;
-    chain_sync<LPC>();
-  }
-  if (a.mode == CH_ENERGY) {  // flip_momentum: the proposal carries −G⁻¹p
-    if (live)
-      for (int i = sl; i < d; i += LPC) a.vel_info[(size_t)c * d + i] = float(-xv[i]);
-    return;
+    if (kept) {  // this chain's refined x (the warp factored for another chain)
+      const double* park = reinterpret_cast<const double*>(Li);
+      for (int i = sl; i < d; i += LPC) xv[i] = F(park[i]);
+    }
   }
   if (live) {
     for (int i = sl; i < d; i += LPC) {
@@ -1294,6 +1593,7 @@ struct LogregBatched {
   float* G2;
   int g2_tiles;
   int fuse_r2x;  // logreg_batched_set_fuse_r2x
+  int refine;    // logreg_batched_set_refine_iterates
   int *iters, *iters_total, *n_active_d;
   int* n_active_h;  // pinned
   uint8_t *active, *notconv, *bad;
@@ -1331,6 +1631,8 @@ struct LogregBatched {
   size_t ev_used;
   std::vector<cudaEvent_t> cev;  // the same around the factorisations
   size_t cev_used;
+  std::vector<cudaEvent_t> rev;  // the same around the refined iterate solves
+  size_t rev_used;
   LogregStats stats;
 };
 
@@ -1342,6 +1644,7 @@ void logreg_batched_set_chol_cpw(LogregBatched* lb, int cpw) { lb->chol_cpw = cp
 void logreg_batched_set_pdl(LogregBatched* lb, int on) { lb->pdl = on; }
 void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k) { lb->gsplit_req = k; }
 void logreg_batched_set_fuse_r2x(LogregBatched* lb, int on) { lb->fuse_r2x = on ? 1 : 0; }
+void logreg_batched_set_refine_iterates(LogregBatched* lb, int on) { lb->refine = on ? 1 : 0; }
 void logreg_batched_set_auto_chains(LogregBatched* lb, int C) { lb->auto_C = C > 0 ? C : lb->C; }
 
 // K slices of the gradient contractions [r₁; r₂]·X (M = 2C) and r₂·X
@@ -1387,6 +1690,7 @@ void logreg_batched_destroy(LogregBatched* lb) {
   for (void* p : lb->owned) cudaFree(p);
   for (cudaEvent_t e : lb->ev) cudaEventDestroy(e);
   for (cudaEvent_t e : lb->cev) cudaEventDestroy(e);
+  for (cudaEvent_t e : lb->rev) cudaEventDestroy(e);
   for (auto& g : lb->graphs) cudaGraphExecDestroy(g.exec);
   if (lb->cap_main) cudaStreamDestroy(lb->cap_main);
   if (lb->cap_body) cudaStreamDestroy(lb->cap_body);
@@ -1411,6 +1715,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->pdl = 0;
   lb->gsplit_req = 0;
   lb->fuse_r2x = 1;
+  lb->refine = 1;
   lb->auto_C = C;
   lb->sms = 0;
   {
@@ -1421,6 +1726,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->prof = 0;
   lb->ev_used = 0;
   lb->cev_used = 0;
+  lb->rev_used = 0;
   lb->graph_tick = 0;
   lb->cap_main = lb->cap_body = nullptr;
   lb->stats = LogregStats{};
@@ -1770,26 +2076,44 @@ struct Runner {
     a.Lout = Lout;
     a.Lout32 = Lout32;
     a.no_inverse = no_inverse ? 1 : 0;
+    CholCfg cf =
+        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
+    // the position iterates' solves by FP32 factor and FP64 refinement
+    // (the L⁻¹ area parks d doubles: d >= 3)
+    a.refine = (L.refine && no_inverse && q_update && L.chol_fp64 && cf.lpc <= 32 && L.d >= 3)
+                   ? 1 : 0;
+    // The refined solves issue few FP64 instructions (d per row and
+    // correction) and are bound by the latency of their serial column steps,
+    // so they take one chain per warp (four times the warps of the FP64
+    // factorisation's automatic packing) unless the chains per warp are set.
+    // Measured on the generalized leapfrog at N = 1000, d = 25, 4096 chains:
+    // 49 / 53 / 67 µs per launch at 1 / 2 / 4 chains per warp, against 72 µs
+    // for the FP64 factorisation.
+    if (a.refine) cf = chol_config(L.d, sizeof(double), L.chol_cpw ? L.chol_cpw : 1, L.auto_C);
+    std::vector<cudaEvent_t>& evs = a.refine ? L.rev : L.cev;
+    size_t& used = a.refine ? L.rev_used : L.cev_used;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (L.prof) {
-      while (L.cev.size() < L.cev_used + 2) {
+      while (evs.size() < used + 2) {
         cudaEvent_t ev;
         if (cudaEventCreate(&ev) != cudaSuccess) break;
-        L.cev.push_back(ev);
+        evs.push_back(ev);
       }
-      if (L.cev.size() >= L.cev_used + 2) {
-        e0 = L.cev[L.cev_used];
-        e1 = L.cev[L.cev_used + 1];
-        L.cev_used += 2;
+      if (evs.size() >= used + 2) {
+        e0 = evs[used];
+        e1 = evs[used + 1];
+        used += 2;
         cudaEventRecord(e0, st);
       }
     }
     const double dd = L.d;
-    L.stats.chol_launches++;
-    const double solves = (mode == CH_ENERGY && !vel_info) ? 1.0 : 2.0;
-    L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + solves * dd * dd);
-    const CholCfg cf =
-        chol_config(L.d, L.chol_fp64 ? sizeof(double) : sizeof(float), L.chol_cpw, L.auto_C);
+    if (a.refine) {
+      L.stats.refine_launches++;
+    } else {
+      L.stats.chol_launches++;
+      const double solves = (mode == CH_ENERGY && !vel_info) ? 1.0 : 2.0;
+      L.stats.chol_flops += (double)L.C * (dd * dd * dd / 3.0 + solves * dd * dd);
+    }
     const int per_cta = cf.chains;
     const dim3 grid((L.C + per_cta - 1) / per_cta);
     const size_t smem = cf.smem;
@@ -2064,6 +2388,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   lb->stats = LogregStats{};
   lb->ev_used = 0;
   lb->cev_used = 0;
+  lb->rev_used = 0;
   Runner R{lb, gemm_impl, st};
   R.hsp = sp;
   const int C = lb->C, d = lb->d;
@@ -2160,6 +2485,12 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
       if (cudaEventElapsedTime(&ms, lb->cev[i], lb->cev[i + 1]) == cudaSuccess) cns += 1e6 * ms;
     }
     lb->stats.chol_ns = cns;
+    double rns = 0.0;
+    for (size_t i = 0; i + 1 < lb->rev_used; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, lb->rev[i], lb->rev[i + 1]) == cudaSuccess) rns += 1e6 * ms;
+    }
+    lb->stats.refine_ns = rns;
   }
   if (R.err != cudaSuccess) {
     g_err = std::string("batched logistic-regression step: ") + cudaGetErrorString(R.err);
@@ -2197,7 +2528,8 @@ int graph_cfg(const LogregBatched* lb) {
   k = k * 2 + lb->pdl;
   k = k * 128 + gemm_tc_tuning_code();
   k = k * 8 + lb->gsplit_req;
-  return k * 2 + lb->fuse_r2x;
+  k = k * 2 + lb->fuse_r2x;
+  return k * 2 + lb->refine;
 }
 
 // Record one whole transition (all L steps, each fixed-point solve a

@@ -64,6 +64,8 @@ struct LogregStats {
   long long chol_launches;   // metric factorisations launched
   double chol_flops;         // their algorithmic FP64 flops (d³/3 + 2d² per chain)
   double chol_ns;            // their GPU time (profiling on)
+  long long refine_launches; // position-iterate solves by FP32 factor + FP64 refinement
+  double refine_ns;          // their GPU time (profiling on)
 };
 LogregStats logreg_batched_stats(const LogregBatched* lb);
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);
@@ -80,6 +82,9 @@ void logreg_batched_set_gemm_ksplit(LogregBatched* lb, int k);
 // d <= 32), one partial gradient per N tile; 0: r₂ is stored as split BF16
 // planes and contracted by its own GEMM
 void logreg_batched_set_fuse_r2x(LogregBatched* lb, int on);
+// 1 = the generalized leapfrog's position iterates solve G⁻¹p by an FP32
+// factorisation refined with FP64 residuals (default); 0 = FP64 factorisation
+void logreg_batched_set_refine_iterates(LogregBatched* lb, int on);
 // the chain count the automatic rules (K slices of the gradient contraction,
 // chains per warp of the factorisation) size their grids for (default: the
 // context's own; the chain groups of one sampler pass the sampler's total,

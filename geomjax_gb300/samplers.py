@@ -82,7 +82,7 @@ class Kernel:
     def __init__(self, sampler: int, integrator="implicit_midpoint", divergence_threshold=1000.0,
                  max_iters=100, tol=1e-6, alpha2_fix=False, logreg_path="auto", threads_per_block=None,
                  loop="graph", cholesky="fp64", chol_chains_per_warp=0, chain_groups=0,
-                 pdl=False, gemm_ksplit=0, fuse_r2x=True):
+                 pdl=False, gemm_ksplit=0, fuse_r2x=True, refine_iterates=True):
         if integrator not in INTEGRATORS:
             raise ValueError(f"integrator must be one of {sorted(INTEGRATORS)}")
         if logreg_path not in LOGREG_PATHS:
@@ -108,6 +108,7 @@ class Kernel:
         if gemm_ksplit:
             self.options[L.GJ_OPT_GEMM_KSPLIT] = int(gemm_ksplit)
         self.options[L.GJ_OPT_FUSE_R2X] = 1 if fuse_r2x else 0
+        self.options[L.GJ_OPT_REFINE_ITERATES] = 1 if refine_iterates else 0
         if threads_per_block:
             self.options[L.GJ_OPT_THREADS_PER_BLOCK] = int(threads_per_block)
         self._ctx = {}
@@ -240,17 +241,20 @@ class rmhmc:
     def build_kernel(integrator="implicit_midpoint", divergence_threshold=1000.0, max_iters=100,
                      tol=1e-6, logreg_path="auto", loop="graph", cholesky="fp64",
                      chol_chains_per_warp=0, chain_groups=0, pdl=False, gemm_ksplit=0,
-                     fuse_r2x=True):
+                     fuse_r2x=True, refine_iterates=True):
         """``rmhmc.py:110-176``; kernel(rng_key, state, target, step_size,
         num_integration_steps).  ``logreg_path``, ``loop``, ``cholesky``,
         ``chol_chains_per_warp``, ``chain_groups``, ``pdl``, ``gemm_ksplit``
-        (K slices of the gradient contraction, 0 = automatic) and ``fuse_r2x``
-        (the momentum evaluations' r₂·X inside the S GEMM's epilogue) select
+        (K slices of the gradient contraction, 0 = automatic), ``fuse_r2x``
+        (the momentum evaluations' r₂·X inside the S GEMM's epilogue) and
+        ``refine_iterates`` (the generalized leapfrog's position-iterate
+        solves by an FP32 factorisation refined with FP64 residuals) select
         the implementation of the batched dense-Fisher path."""
         return Kernel(L.GJ_SAMPLER_RMHMC, integrator, divergence_threshold, max_iters, tol,
                       logreg_path=logreg_path, loop=loop, cholesky=cholesky,
                       chol_chains_per_warp=chol_chains_per_warp, chain_groups=chain_groups,
-                      pdl=pdl, gemm_ksplit=gemm_ksplit, fuse_r2x=fuse_r2x)
+                      pdl=pdl, gemm_ksplit=gemm_ksplit, fuse_r2x=fuse_r2x,
+                      refine_iterates=refine_iterates)
 
     def __new__(cls, target: Target, step_size: float, num_integration_steps: int, *,
                 divergence_threshold=1000.0, integrator="implicit_midpoint", max_iters=100,

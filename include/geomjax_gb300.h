@@ -281,6 +281,15 @@ int32_t gj_set_option(gj_ctx* ctx, int32_t key, int64_t value);
  * own grouped launches and fixed-point loops, so a bucket waits only for its
  * own slowest chain and the branches overlap */
 #define GJ_OPT_BATCH_BUCKETS 12
+/* batched path, generalized leapfrog: 1 = each position iterate's solve
+ * u = G(q_k)⁻¹p½ by mixed-precision iterative refinement (default): G is
+ * factored in float32 and u corrected with float64 residuals p − G·u until
+ * it is as accurate as a float64 factorisation's solve; a chain whose
+ * refinement does not converge is factored in float64.  The full
+ * evaluations (kept factor, log det) always factor in float64.  0 = every
+ * factorisation in float64.  Applies with GJ_OPT_CHOL_FP64 = 1 for
+ * 3 <= d <= 64 (where a chain's factorisation runs within one warp). */
+#define GJ_OPT_REFINE_ITERATES 13
 
 /* value_and_grad of the log density at state->position; zeroes
  * volume_adjustment when present. */
@@ -314,7 +323,10 @@ int32_t gj_nuts_step(gj_ctx* ctx, const gj_nuts_params* params, gj_chain_state* 
  * nanoseconds (only while profiling is on), out[5] metric factorisations
  * launched, out[6] their algorithmic FP64 flops (d³/3 + 2d² per chain, d³/3
  * + d² for an energy evaluation), out[7] their GPU time in nanoseconds
- * (profiling on).  Returns the number written (<= n, at most 8).  No counterpart in the reference (measurement only). */
+ * (profiling on), out[8] position-iterate solves by FP32 factorisation and
+ * FP64 refinement (GJ_OPT_REFINE_ITERATES; not counted in out[5..7]),
+ * out[9] their GPU time in nanoseconds (profiling on).  Returns the number
+ * written (<= n, at most 10).  No counterpart in the reference (measurement only). */
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n);
 /* FMA throughput of this device's CUDA cores, in TFLOP/s (2 flops per FMA):
  * float64 for GJ_FP64, float32 for GJ_MIXED.  Eight independent FMA chains

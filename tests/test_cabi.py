@@ -95,6 +95,10 @@ def test_argument_checks_without_gpu():
     assert lib.gj_set_option(h, L.GJ_OPT_FUSE_R2X, -1) == L.GJ_EINVAL
     for v in (0, 1):
         assert lib.gj_set_option(h, L.GJ_OPT_FUSE_R2X, v) == L.GJ_OK
+    for v in (-1, 2):
+        assert lib.gj_set_option(h, L.GJ_OPT_REFINE_ITERATES, v) == L.GJ_EINVAL
+    for v in (0, 1):
+        assert lib.gj_set_option(h, L.GJ_OPT_REFINE_ITERATES, v) == L.GJ_OK
     assert lib.gj_set_gemm_tiling(96, 1) == L.GJ_EINVAL
     # batch creation checks its arguments before touching the GPU
     bh = ctypes.c_void_p()

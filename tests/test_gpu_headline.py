@@ -191,11 +191,12 @@ def test_momentum_draw_accuracy_by_path(N, d, path, bound):
 
 @pytest.mark.parametrize("N,d", [(1000, 25), (300, 9), (400, 32), (100, 8)])
 def test_fused_r2x_matches_stored_r2(N, d):
-    """The momentum evaluations' r₂·X formed in the S = U·Xᵀ GEMM's epilogue
-    (FP32 FMAs on the CUDA cores, one partial gradient per N tile, added in
-    tile order) against r₂ stored as three BF16 planes and contracted on the
-    tensor cores: both within 1e-5 of the oracle per step over 10
-    generalized-leapfrog steps, and within 2e-6 of each other."""
+    """The momentum evaluations' r₂·X formed inside the S = U·Xᵀ GEMM (r₂
+    written as three BF16 planes into the kernel's freed operand ring and
+    contracted against the Xᵀ boxes on the tensor cores, one partial gradient
+    per N tile, added in tile order) against r₂ stored in global memory and
+    contracted by a second GEMM: both within 1e-5 of the oracle per step over
+    10 generalized-leapfrog steps, and within 2e-6 of each other."""
     import geomjax_gb300 as gj
     from geomjax_gb300.base import Draws
 
