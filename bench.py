@@ -249,10 +249,10 @@ def run_ours(args, wl):
     acc_sum = torch.zeros(C, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    stats = np.zeros(10, dtype=np.int64)
+    stats = np.zeros(11, dtype=np.int64)
     import ctypes
 
-    buf = (ctypes.c_int64 * 10)()
+    buf = (ctypes.c_int64 * 11)()
     clocks = ClockSampler(local)
     if ws > 1:
         import torch.distributed as dist
@@ -268,21 +268,21 @@ def run_ours(args, wl):
         evs[i][1].record(stream)
         trace[i].copy_(state.position)
         acc_sum += info["acceptance_rate"]
-        n = ctx.lib.gj_stats(ctx.h, buf, 10)
-        stats += np.array(buf[:10], dtype=np.int64)
+        n = ctx.lib.gj_stats(ctx.h, buf, 11)
+        stats += np.array(buf[:11], dtype=np.int64)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     # dominant-kernel timing: the same transitions with CUDA events around every
     # GEMM launch (profiling switches the batched path to its host-driven loop)
-    prof = np.zeros(10, dtype=np.int64)
+    prof = np.zeros(11, dtype=np.int64)
     if wl["sampler"] == "rmhmc":
         L.check(ctx.lib.gj_profile(ctx.h, 1))
         for i in range(min(K, 3)):
             flush.zero_()
             kern.step_inplace(target, state, Z[W + i], U[W + i], info, h, Lsteps, **extra)
-            ctx.lib.gj_stats(ctx.h, buf, 10)
-            prof += np.array(buf[:10], dtype=np.int64)
+            ctx.lib.gj_stats(ctx.h, buf, 11)
+            prof += np.array(buf[:11], dtype=np.int64)
         L.check(ctx.lib.gj_profile(ctx.h, 0))
         torch.cuda.synchronize()
     dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
@@ -358,7 +358,8 @@ def run_ours(args, wl):
             roof["refined_iterate_solves"] = {
                 "kernel": "chol_kernel (FP32 factor, FP64-residual refinement)",
                 "ms_per_transition": round(prof[9] * 1e-6 / min(K, 3), 3),
-                "launches_per_transition": int(prof[8] // min(K, 3))}
+                "launches_per_transition": int(prof[8] // min(K, 3)),
+                "fp64_fallbacks_per_transition": round(float(prof[10]) / min(K, 3), 2)}
     elif wl["sampler"] == "lmcmonge":
         # the warp-per-chain Monge kernel runs on the FP32 pipe: algorithmic
         # flops (MONGE_FLOPS_PER_DIM·D per chain and step) against the FP32

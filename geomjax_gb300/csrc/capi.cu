@@ -537,7 +537,7 @@ int32_t gj_lmcmonge_step(gj_ctx* ctx, const gj_step_params* p, gj_chain_state* s
 
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n < 0) return fail(GJ_EINVAL, "bad arguments");
-  int64_t v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t v[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (!ctx->lbs.empty()) {
     for (gj::LogregBatched* lb : ctx->lbs) {
       const gj::LogregStats s = gj::logreg_batched_stats(lb);
@@ -551,11 +551,12 @@ int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n) {
       v[7] += (int64_t)s.chol_ns;
       v[8] += s.refine_launches;
       v[9] += (int64_t)s.refine_ns;
+      v[10] += s.refine_fallbacks;
     }
   } else {
     v[2] = 1;  // the per-chain and warp-per-chain paths launch one kernel per step
   }
-  const int m = n < 10 ? n : 10;
+  const int m = n < 11 ? n : 11;
   for (int i = 0; i < m; ++i) out[i] = v[i];
   return m;
 }

@@ -107,6 +107,7 @@ struct CholArgs {
   // FP64-residual refinement (refined_solve), the FP64 factorisation only
   // for the chains whose refinement does not converge
   int refine;
+  int* fallbacks;      // refined solves that fell back to FP64 (may be NULL)
   // EVAL with no_inverse: the generalized leapfrog's position update
   // q' = q0 + h/2 [G⁻¹(q0) + G⁻¹(q_k)] p½ (UP_GLQN of update_kernel) done
   // here with u = G⁻¹(q_k)p½, with its convergence test
@@ -458,20 +459,26 @@ __device__ __forceinline__ void backward_subst(const T* L, const T* rdiag, T* x,
 }
 
 // Most corrections a refined solve applies before it gives the chain back to
-// the FP64 factorisation.
-constexpr int kRefineMax = 4;
+// the FP64 factorisation (about as many FP64 instructions as that
+// factorisation at d = 25, one chain per warp).
+constexpr int kRefineMax = 8;
 
 // The stopping rule of a refined solve, on norms relative to ‖x₀‖∞ (float32
 // scalars: the rule needs a few bits of them): er = ‖dx_k‖/‖x₀‖, pr = the
-// previous correction's.  Converged once the next step's predicted size
-// er²/pr is below 2⁻⁴⁴ (x then as accurate as an FP64 factorisation's solve,
-// whose own error is about κ(G)·d·2⁻⁵³); failed when a correction is not
-// finite or shrinks by less than half.  Returns 1 = converged (apply dx),
-// 0 = apply dx and go on, −1 = failed.
+// previous correction's (1 for the first).
+// * Converged once the next step's predicted size er²/pr is below 2⁻⁴⁴: x is
+//   then as accurate as an FP64 factorisation's solve of a well-conditioned G.
+// * Corrections that stop shrinking (by at least half) have reached the
+//   floor set by the FP64 residual's rounding, about κ(G)·d·2⁻⁵³, which is
+//   also the error of an FP64 factorisation's solve: converged when that
+//   floor is below 2⁻³⁶, failed above it (κ(G)·d beyond about 2¹⁷, where the
+//   FP64 factorisation takes over).
+// * Failed when a correction is not finite.
+// Returns 1 = converged (apply dx), 0 = apply dx and go on, −1 = failed.
 __device__ __forceinline__ int refine_verdict(float er, float pr, bool nonfinite) {
   if (nonfinite) return -1;
   if (er * er <= 0x1p-44f * pr) return 1;
-  if (er > 0.5f * pr) return -1;
+  if (er > 0.5f * pr) return er <= 0x1p-36f ? 1 : -1;
   return 0;
 }
 
@@ -575,7 +582,7 @@ __device__ __forceinline__ bool refined_solve_w32(const double* G, const float* 
   for (int k = 0; k < 32; ++k) {
     float g = 0.f;
     if (k <= i && in) g = gv[colstart(k, d) + i - k];
-    if (k == i) g += float(prior);
+    if (k == i && in) g += float(prior);
     row[k] = g;
   }
   const double pi = in ? p[i] : 0.0;
@@ -673,7 +680,10 @@ __device__ __forceinline__ bool refined_solve_w32(const double* G, const float* 
 // LPC = 128 / 256: one chain per CTA of four / eight warps (large d, where
 // one warp per chain leaves most of an SM's FP64 units idle); its barrier is
 // the CTA's.
-template <typename F, int LPC>  // factorisation type (double / float), lanes per chain
+// REF: the instantiation that serves the refined solves (CholArgs::refine;
+// double, LPC = 32: chol_refined_kernel); the others compile without their
+// code, so the FP64 factorisation keeps its registers and occupancy.
+template <typename F, int LPC, bool REF = false>  // factorisation type, lanes per chain
 __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr bool kCta = LPC > 32;
@@ -705,7 +715,7 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   // G = Gvec + I/s²: the packed layouts coincide; idle slots get the identity.
   // The refined solves of the position iterates keep the Gram alone (their
   // residuals add the prior) and add the prior before an FP64 fallback.
-  constexpr bool kRefinable = !kCta && sizeof(F) == sizeof(double);
+  constexpr bool kRefinable = REF && !kCta && sizeof(F) == sizeof(double);
   const bool refine = kRefinable && a.refine;
   for (int t = sl; t < P; t += LPC) {
     const uint32_t ik = tab[t];
@@ -748,6 +758,7 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
                                   sl);
       }
       fp64 = __any_sync(0xffffffffu, !kept);
+      if (!kept && live && sl == 0 && a.fallbacks) atomicAdd(a.fallbacks, 1);
       if (fp64) {
         if (kept) {
           double* park = reinterpret_cast<double*>(Li);
@@ -985,6 +996,11 @@ template <typename F, int LPC>
 __global__ void chol_kernel(CholArgs a, int stride) {
   chol_body<F, LPC>(a, stride, (int)blockIdx.x);
 }
+// The refined solves (CholArgs::refine): one chain per warp, CTAs of four
+// warps.  (A register bound of 64 or 72 per thread made ptxas spill.)
+__global__ void chol_refined_kernel(CholArgs a, int stride) {
+  chol_body<double, 32, true>(a, stride, (int)blockIdx.x);
+}
 
 // a grouped launch of factorisations: one item per posterior
 struct CholItem {
@@ -997,12 +1013,24 @@ __global__ void chol_grouped_kernel(const CholItem* __restrict__ items,
   const int i = group_item(prefix, n, (int)blockIdx.x);
   chol_body<F, LPC>(items[i].a, items[i].stride, (int)blockIdx.x - __ldg(prefix + i));
 }
+__global__ void chol_refined_grouped_kernel(const CholItem* __restrict__ items,
+                                const int* __restrict__ prefix, int n) {
+  const int i = group_item(prefix, n, (int)blockIdx.x);
+  chol_body<double, 32, true>(items[i].a, items[i].stride,
+                              (int)blockIdx.x - __ldg(prefix + i));
+}
 
 template <typename F>
 cudaError_t chol_launch(const CholCfg& cf, size_t smem, dim3 grid, const CholArgs& a, bool pdl,
                         cudaStream_t st) {
   const dim3 th(32 * cf.warps);
   const int stride = (int)cf.stride;
+  if constexpr (sizeof(F) == sizeof(double)) {
+    if (a.refine)  // the host sets it with one chain per warp only
+      return cf.lpc == 32 && cf.warps <= 4
+                 ? launch_k(pdl, chol_refined_kernel, grid, th, smem, st, a, stride)
+                 : cudaErrorInvalidValue;
+  }
   switch (cf.lpc) {
     case 4: return launch_k(pdl, chol_kernel<F, 4>, grid, th, smem, st, a, stride);
     case 8: return launch_k(pdl, chol_kernel<F, 8>, grid, th, smem, st, a, stride);
@@ -1036,6 +1064,14 @@ cudaError_t chol_set_smem(int smax) {
   if (r != cudaSuccess) e = r;
   r = cudaFuncSetAttribute(chol_kernel<F, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
   if (r != cudaSuccess) e = r;
+  if constexpr (sizeof(F) == sizeof(double)) {  // the refined solves' instantiation
+    r = cudaFuncSetAttribute(chol_refined_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smax);
+    if (r != cudaSuccess) e = r;
+    r = cudaFuncSetAttribute(chol_refined_grouped_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (r != cudaSuccess) e = r;
+  }
   return e;
 }
 
@@ -1598,6 +1634,7 @@ struct LogregBatched {
   int* n_active_h;  // pinned
   uint8_t *active, *notconv, *bad;
   int* tc_err;
+  int* refine_fb;  // refined solves that fell back (profiling on)
   TcOperand *tXb, *tXTb, *tZb, *tZt, *tQb, *tUb, *tLam, *tGiv, *tRb;
   bool tc_ok;
   int chol_fp64;
@@ -1772,6 +1809,7 @@ int logreg_batched_create(const TargetDev& t, int C, LogregBatched** out) {
   lb->notconv = dalloc<uint8_t>(C, lb->owned, &ok);
   lb->bad = dalloc<uint8_t>(C, lb->owned, &ok);
   lb->tc_err = dalloc<int>(1, lb->owned, &ok);
+  lb->refine_fb = dalloc<int>(1, lb->owned, &ok);
   lb->spd = dalloc<StepDev>(1, lb->owned, &ok);
   lb->pos_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
   lb->grad_s = dalloc<float>((size_t)C * d, lb->owned, &ok);
@@ -2085,11 +2123,19 @@ struct Runner {
     // The refined solves issue few FP64 instructions (d per row and
     // correction) and are bound by the latency of their serial column steps,
     // so they take one chain per warp (four times the warps of the FP64
-    // factorisation's automatic packing) unless the chains per warp are set.
-    // Measured on the generalized leapfrog at N = 1000, d = 25, 4096 chains:
-    // 49 / 53 / 67 µs per launch at 1 / 2 / 4 chains per warp, against 72 µs
-    // for the FP64 factorisation.
-    if (a.refine) cf = chol_config(L.d, sizeof(double), L.chol_cpw ? L.chol_cpw : 1, L.auto_C);
+    // factorisation's automatic packing; GJ_OPT_CHOL_CHAINS_PER_WARP applies
+    // to the FP64 factorisations), which also gives d <= 32 the register
+    // form.  Measured with the shared-memory form on the generalized leapfrog
+    // at N = 1000, d = 25, 4096 chains: 49 / 53 / 67 µs per launch at 1 / 2 /
+    // 4 chains per warp, against 72 µs for the FP64 factorisation; 43 µs in
+    // the register form.
+    if (a.refine) {
+      const CholCfg rc = chol_config(L.d, sizeof(double), 1, L.auto_C);
+      if (rc.lpc == 32)  // always for d <= 64
+        cf = rc;
+      else
+        a.refine = 0;
+    }
     std::vector<cudaEvent_t>& evs = a.refine ? L.rev : L.cev;
     size_t& used = a.refine ? L.rev_used : L.cev_used;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -2108,6 +2154,7 @@ struct Runner {
     }
     const double dd = L.d;
     if (a.refine) {
+      a.fallbacks = L.prof ? L.refine_fb : nullptr;
       L.stats.refine_launches++;
     } else {
       L.stats.chol_launches++;
@@ -2120,7 +2167,9 @@ struct Runner {
     if (rec) {
       if (a.q_update) a.n_active = rec->flag;
       CholItem it{a, (int)cf.stride};
-      rec->push(OP_CHOL, (L.chol_fp64 ? 100 : 0) + cf.lpc, (int)grid.x, 32 * cf.warps, smem, it);
+      // variants: FP32 lpc, FP64 100 + lpc, refined solves 400 + lpc
+      rec->push(OP_CHOL, (a.refine ? 400 : (L.chol_fp64 ? 100 : 0)) + cf.lpc, (int)grid.x,
+                32 * cf.warps, smem, it);
       return;
     }
     // the dynamic shared-memory limit was raised at context creation
@@ -2389,6 +2438,7 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
   lb->ev_used = 0;
   lb->cev_used = 0;
   lb->rev_used = 0;
+  if (lb->prof) cudaMemsetAsync(lb->refine_fb, 0, sizeof(int), st);
   Runner R{lb, gemm_impl, st};
   R.hsp = sp;
   const int C = lb->C, d = lb->d;
@@ -2491,6 +2541,9 @@ int logreg_batched_rmhmc_step(LogregBatched* lb, const StepDev& sp, float* pos, 
       if (cudaEventElapsedTime(&ms, lb->rev[i], lb->rev[i + 1]) == cudaSuccess) rns += 1e6 * ms;
     }
     lb->stats.refine_ns = rns;
+    int fb = 0;
+    if (cudaMemcpy(&fb, lb->refine_fb, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
+      lb->stats.refine_fallbacks = fb;
   }
   if (R.err != cudaSuccess) {
     g_err = std::string("batched logistic-regression step: ") + cudaGetErrorString(R.err);
@@ -3090,6 +3143,7 @@ cudaError_t launch_group(const GroupLaunch& g, cudaStream_t s) {
         case 108: chol_grouped_kernel<double, 8><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 116: chol_grouped_kernel<double, 16><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 132: chol_grouped_kernel<double, 32><<<grid, th, g.smem, s>>>(it, pf, n); break;
+        case 432: chol_refined_grouped_kernel<<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 228: chol_grouped_kernel<double, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 128: chol_grouped_kernel<float, 128><<<grid, th, g.smem, s>>>(it, pf, n); break;
         case 356: chol_grouped_kernel<double, 256><<<grid, th, g.smem, s>>>(it, pf, n); break;

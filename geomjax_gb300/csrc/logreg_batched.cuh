@@ -66,6 +66,7 @@ struct LogregStats {
   double chol_ns;            // their GPU time (profiling on)
   long long refine_launches; // position-iterate solves by FP32 factor + FP64 refinement
   double refine_ns;          // their GPU time (profiling on)
+  long long refine_fallbacks; // chains of those that fell back to FP64 (profiling on)
 };
 LogregStats logreg_batched_stats(const LogregBatched* lb);
 void logreg_batched_set_chol_fp64(LogregBatched* lb, int on);

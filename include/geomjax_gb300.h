@@ -325,8 +325,9 @@ int32_t gj_nuts_step(gj_ctx* ctx, const gj_nuts_params* params, gj_chain_state* 
  * + d² for an energy evaluation), out[7] their GPU time in nanoseconds
  * (profiling on), out[8] position-iterate solves by FP32 factorisation and
  * FP64 refinement (GJ_OPT_REFINE_ITERATES; not counted in out[5..7]),
- * out[9] their GPU time in nanoseconds (profiling on).  Returns the number
- * written (<= n, at most 10).  No counterpart in the reference (measurement only). */
+ * out[9] their GPU time in nanoseconds (profiling on), out[10] the chains
+ * of those solves that fell back to the FP64 factorisation (profiling on).
+ * Returns the number written (<= n, at most 11).  No counterpart in the reference (measurement only). */
 int32_t gj_stats(gj_ctx* ctx, int64_t* out, int32_t n);
 /* FMA throughput of this device's CUDA cores, in TFLOP/s (2 flops per FMA):
  * float64 for GJ_FP64, float32 for GJ_MIXED.  Eight independent FMA chains

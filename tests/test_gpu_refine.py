@@ -12,9 +12,9 @@ rmhmc/metrics.py's dense Fisher metric):
 * the same with a rank-deficient design (a duplicated column) and prior
   variance 1e5, where G's condition number is about 1e7: the FP32
   factorisation cannot reach an FP64 solve's accuracy there, so the chains
-  fall back to the FP64 factorisation;
+  fall back to the FP64 factorisation (gj_stats out[10] counts them);
 * the refined solves are the ones launched (gj_stats out[8]), and none with
-  the option off.
+  the option off; on the well-conditioned metric none falls back.
 
 The refinement stops when the predicted error of x is below 2⁻⁴⁴‖x‖, under
 an FP64 solve's own error, so the two solves differ in their last bits only.
@@ -98,13 +98,19 @@ def test_refinement_falls_back_on_ill_conditioned_metric():
     q0 = _f32(0.1 * rng.standard_normal((C, d)))
     z = _f32(rng.standard_normal((C, d)))
     u = -np.ones(C)
-    kr, kf = _kernels()
+    kr, kf = _kernels(loop="host")
+    ctx = kr.context(dt, C)
+    assert ctx.lib.gj_profile(ctx.h, 1) == 0  # counts the fallbacks
     st0 = gj.rmhmc.init(q0, dt)
     sr, _ = kr(Draws(z, u), st0, dt, 0.01, 3)
+    buf = (ctypes.c_int64 * 11)()
+    assert ctx.lib.gj_stats(ctx.h, buf, 11) == 11
+    assert ctx.lib.gj_profile(ctx.h, 0) == 0
     sf, _ = kf(Draws(z, u), st0, dt, 0.01, 3)
     pr, pf = _np(sr.position), _np(sf.position)
     assert np.all(np.isfinite(pr))
     assert rel_err(pr, pf) < 2e-7, rel_err(pr, pf)
+    assert buf[10] > 0, list(buf)  # chains fell back to the FP64 factorisation
 
 
 def test_refined_solves_are_launched():
@@ -120,11 +126,14 @@ def test_refined_solves_are_launched():
     z = _f32(rng.standard_normal((C, 9)))
     counts = []
     for kern in _kernels(loop="host"):
-        kern(Draws(z, -np.ones(C)), gj.rmhmc.init(q0, dt), dt, 0.05, 4)
         ctx = kern.context(dt, C)
-        buf = (ctypes.c_int64 * 10)()
-        assert ctx.lib.gj_stats(ctx.h, buf, 10) == 10
-        counts.append((buf[5], buf[8]))
-    (chol_r, ref_r), (chol_f, ref_f) = counts
+        assert ctx.lib.gj_profile(ctx.h, 1) == 0
+        kern(Draws(z, -np.ones(C)), gj.rmhmc.init(q0, dt), dt, 0.05, 4)
+        buf = (ctypes.c_int64 * 11)()
+        assert ctx.lib.gj_stats(ctx.h, buf, 11) == 11
+        assert ctx.lib.gj_profile(ctx.h, 0) == 0
+        counts.append((buf[5], buf[8], buf[10]))
+    (chol_r, ref_r, fb_r), (chol_f, ref_f, fb_f) = counts
     assert ref_r > 0 and ref_f == 0, counts
     assert 0 < chol_r < chol_f, counts  # the full evaluations still factor in FP64
+    assert fb_r == 0 and fb_f == 0, counts
