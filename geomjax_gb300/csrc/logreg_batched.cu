@@ -469,10 +469,10 @@ constexpr int kRefineMax = 8;
 // * Converged once the next step's predicted size er²/pr is below 2⁻⁴⁴: x is
 //   then as accurate as an FP64 factorisation's solve of a well-conditioned G.
 // * Corrections that stop shrinking (by at least half) have reached the
-//   floor set by the FP64 residual's rounding, about κ(G)·d·2⁻⁵³, which is
-//   also the error of an FP64 factorisation's solve: converged when that
-//   floor is below 2⁻³⁶, failed above it (κ(G)·d beyond about 2¹⁷, where the
-//   FP64 factorisation takes over).
+//   floor set by the FP64 residual's rounding, which is also the order of
+//   an FP64 factorisation's solve error: converged when that floor is below
+//   2⁻³⁶, failed above it (then the FP64 factorisation takes over; on
+//   log-spaced spectra at d = 64 that starts between κ(G) = 1e6 and 3e6).
 // * Failed when a correction is not finite.
 // Returns 1 = converged (apply dx), 0 = apply dx and go on, −1 = failed.
 __device__ __forceinline__ int refine_verdict(float er, float pr, bool nonfinite) {
