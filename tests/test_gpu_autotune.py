@@ -26,10 +26,14 @@ def test_autotune_batched_logreg_keeps_state_and_results():
     st = gj.rmhmc.init(q0, dt)
     before = [t.clone() for t in st]
     res = gj.autotune(kern, dt, st, 0.05, 4, transitions=2, tilings=((0, -1), (0, 1)),
-                      chol_chains_per_warp=(0, 2))
+                      chol_chains_per_warp=(0, 2), gemm_ksplit=(0, 2))
     for a, b in zip(before, st):
         assert torch.equal(a, b)  # the state is not advanced
-    assert len(res.table) == 4 and res.best in [c for c, _ in res.table]
+    # four first-stage candidates, then K split 2 with the best of them
+    assert len(res.table) == 5 and res.best in [c for c, _ in res.table]
+    assert res.table[4][0]["gemm_ksplit"] == 2
+    assert {k: v for k, v in res.table[4][0].items() if k != "gemm_ksplit"} == \
+        {k: v for k, v in min(res.table[:4], key=lambda x: x[1])[0].items() if k != "gemm_ksplit"}
     assert res.ms_per_transition == min(ms for _, ms in res.table) > 0
     # the chosen settings are in force and give the same transition as the
     # defaults up to the order of floating-point sums
@@ -63,8 +67,8 @@ def test_autotune_batch():
     pb = PosteriorBatch(data, 64, num_streams=2)
     st = pb.init([0.01 * np.ones((64, 8)), 0.01 * np.ones((64, 21))])
     res = gj.autotune_batch(pb, st, 0.05, 3, transitions=1, tilings=((0, -1), (64, -1)),
-                            chol_chains_per_warp=(0, 2))
-    assert len(res.table) == 4
+                            chol_chains_per_warp=(0, 2), gemm_ksplit=(0, 1))
+    assert len(res.table) == 5
     new, info = pb.step(1, st, 0.05, 3)
     assert np.isfinite(_np(new.position)).all()
     L.check(L.lib().gj_set_gemm_tiling(0, -1))
