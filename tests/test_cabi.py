@@ -99,6 +99,14 @@ def test_argument_checks_without_gpu():
         assert lib.gj_set_option(h, L.GJ_OPT_REFINE_ITERATES, v) == L.GJ_EINVAL
     for v in (0, 1):
         assert lib.gj_set_option(h, L.GJ_OPT_REFINE_ITERATES, v) == L.GJ_OK
+    # gj_stats: at most 11 counters (out[8..10]: refined solves, their time,
+    # their FP64 fallbacks); a context without the batched path reports one
+    # launch per step and nothing else
+    stats = (ctypes.c_int64 * 16)(*([-1] * 16))
+    assert lib.gj_stats(h, stats, 16) == 11
+    assert list(stats[:11]) == [0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0] and stats[11] == -1
+    assert lib.gj_stats(h, stats, 4) == 4
+    assert lib.gj_stats(None, stats, 4) == L.GJ_EINVAL
     assert lib.gj_set_gemm_tiling(96, 1) == L.GJ_EINVAL
     # batch creation checks its arguments before touching the GPU
     bh = ctypes.c_void_p()
