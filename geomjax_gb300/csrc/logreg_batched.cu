@@ -103,9 +103,10 @@ struct CholArgs {
   double* Lout;        // DRAW / EVAL: the packed factor, kept for later solves (may be NULL)
   float* Lout32;       // DRAW / EVAL: the same in FP32 (may be NULL)
   int no_inverse;      // EVAL: stop after u = G⁻¹p (no L⁻¹, no packed G⁻¹)
-  // EVAL with no_inverse (FP64, LPC <= 32, d >= 3): u by an FP32 factor and
-  // FP64-residual refinement (refined_solve), the FP64 factorisation only
-  // for the chains whose refinement does not converge
+  // EVAL with no_inverse, FP64, 3 <= d <= 64, one chain per warp
+  // (chol_refined_kernel): u by an FP32 factor and FP64-residual refinement
+  // (refined_solve_w32 / refined_solve), the FP64 factorisation only for the
+  // chains whose refinement does not converge
   int refine;
   int* fallbacks;      // refined solves that fell back to FP64 (may be NULL)
   // EVAL with no_inverse: the generalized leapfrog's position update
@@ -483,7 +484,8 @@ __device__ __forceinline__ int refine_verdict(float er, float pr, bool nonfinite
 }
 
 // x = G⁻¹p for a position iterate of the generalized leapfrog, one chain
-// per sub-group of LPC <= 32 lanes, by mixed-precision iterative refinement
+// per sub-group of LPC <= 32 lanes (the refined kernels use it with one
+// chain per warp for 32 < d <= 64), by mixed-precision iterative refinement
 // (Wilkinson 1963, Moler 1967; Carson and Higham, SIAM J. Sci. Comput. 40,
 // 2018): G = Gram + prior·I is factored in FP32 (Lf, rdf; the first solution
 // from the bordered factorisation), then x += G₃₂⁻¹(p − G·x) with the
@@ -737,9 +739,10 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   const bool want_ld = a.mode != CH_EVAL;
   double pm = 1.0;
   int pe = 0;
-  // The position iterates (a.refine, set with no_inverse for F = double,
-  // LPC <= 32 and d >= 3) solve by mixed-precision refinement: FP32 factor,
-  // FP64 residuals (refined_solve), the result in xv.  A warp factors in
+  // The position iterates (a.refine: chol_refined_kernel, F = double,
+  // LPC = 32, 3 <= d <= 64) solve by mixed-precision refinement: FP32 factor,
+  // FP64 residuals (refined_solve_w32 for d <= 32, else refined_solve), the
+  // result in xv.  A warp factors in
   // FP64 when one of its chains needs it; the chains already solved park x
   // in L⁻¹'s area meanwhile (free here; P floats hold d doubles for d >= 3).
   bool fp64 = true;   // this warp runs the FP64 factorisation
