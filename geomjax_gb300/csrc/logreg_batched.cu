@@ -742,9 +742,9 @@ __device__ __forceinline__ void chol_body(const CholArgs& a, int stride, int bx)
   // The position iterates (a.refine: chol_refined_kernel, F = double,
   // LPC = 32, 3 <= d <= 64) solve by mixed-precision refinement: FP32 factor,
   // FP64 residuals (refined_solve_w32 for d <= 32, else refined_solve), the
-  // result in xv.  A warp factors in
-  // FP64 when one of its chains needs it; the chains already solved park x
-  // in L⁻¹'s area meanwhile (free here; P floats hold d doubles for d >= 3).
+  // result in xv.  A warp factors in FP64 when one of its chains needs it;
+  // the chains already solved park x in L⁻¹'s area meanwhile (free here; P
+  // floats hold d doubles for d >= 3).
   bool fp64 = true;   // this warp runs the FP64 factorisation
   bool kept = false;  // this chain's refined x is final
   if constexpr (kRefinable) {
