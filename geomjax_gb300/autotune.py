@@ -63,19 +63,21 @@ def _candidates(tilings, cpws, ksplit0):
             for t, c in itertools.product(tilings, cpws)]
 
 
-def _search(cands, ksplits, apply, step, transitions):
+def _search(cands, ksplits, apply, measure):
     """The first stage over ``cands``, then the other K slices with its
-    best settings; every candidate ends up in the table."""
+    best settings; every candidate ends up in the table.  ``apply(c)`` puts
+    candidate c in force, ``measure()`` times the settings in force (ms per
+    transition)."""
     table = []
     for c in cands:
         apply(c)
-        table.append((c, _time(step, transitions)))
+        table.append((c, measure()))
     best = min(table, key=lambda x: x[1])[0]
     if "gemm_ksplit" in best:
         for k in ksplits[1:]:
             c = dict(best, gemm_ksplit=int(k))
             apply(c)
-            table.append((c, _time(step, transitions)))
+            table.append((c, measure()))
     best, ms = min(table, key=lambda x: x[1])
     apply(best)
     return AutotuneResult(best, ms, table)
@@ -118,7 +120,7 @@ def autotune(kernel, target, state, step_size: float, num_integration_steps: int
     def step():
         kernel.step_inplace(target, work, z, u, info, step_size, num_integration_steps)
 
-    return _search(cands, ksplits, apply, step, transitions)
+    return _search(cands, ksplits, apply, lambda: _time(step, transitions))
 
 
 def autotune_batch(batch, state, step_size: float, num_integration_steps: int, *,
@@ -141,5 +143,5 @@ def autotune_batch(batch, state, step_size: float, num_integration_steps: int, *
         batch.step_inplace(work, z, u, info, step_size, num_integration_steps)
 
     ksplits = tuple(gemm_ksplit) or (0,)
-    return _search(_candidates(tilings, chol_chains_per_warp, ksplits[0]), ksplits, apply, step,
-                   transitions)
+    return _search(_candidates(tilings, chol_chains_per_warp, ksplits[0]), ksplits, apply,
+                   lambda: _time(step, transitions))
